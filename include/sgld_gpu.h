@@ -1,0 +1,159 @@
+/*
+ * sgld_gpu.h -- C ABI of the GB300 matrix-free voxel-elasticity MGPCG solver.
+ *
+ * This is the drop-in boundary for SGLDBench's solve path.  Every entry point
+ * replaces one MATLAB function (or MEX kernel) of the reference; the citation
+ * next to each declaration is that function's file:line in SGLDBench.  All
+ * vectors cross the ABI in the reference's own layout:
+ *
+ *   - DOF vectors: numDOFs = 3 * numNodes doubles, node-major interleaved
+ *     [ux uy uz] per node, nodes in the reference's compact order (the active
+ *     nodes of the (resY+1) x (resX+1) x (resZ+1) node grid in column-major
+ *     order, y fastest -- FEA_VoxelBasedDiscretization.m:71,218-222);
+ *   - element vectors: numElements doubles in the reference's compact element
+ *     order (eleMapBack, FEA_VoxelBasedDiscretization.m:200);
+ *   - the voxel grid: resY x resX x resZ bytes, column-major, nonzero = solid
+ *     (the padded voxelizedVolume_ of FEA_VoxelBasedDiscretization.m:163-186).
+ *
+ * Host buffers belong to the caller and are only read or written during the
+ * call.  Functions with the _device suffix take device pointers (same compact
+ * layout) and do not copy through the host.  Device memory belongs to the
+ * context.  A context is not thread-safe; use one per host thread.
+ *
+ * Every function returns SGLD_OK (0) or an error code; sgld_last_error()
+ * gives the message.  No exceptions cross the ABI.
+ */
+#ifndef SGLD_GPU_H
+#define SGLD_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGLD_OK 0
+#define SGLD_ERR_ARG 1       /* invalid argument or size                     */
+#define SGLD_ERR_CUDA 2      /* CUDA runtime failure                         */
+#define SGLD_ERR_STATE 3     /* call out of order (e.g. solve before assemble) */
+#define SGLD_ERR_NUMERIC 4   /* coarsest matrix not positive definite        */
+#define SGLD_ERR_NOMEM 5     /* device allocation failed                     */
+
+#define SGLD_PREC_FP64 0     /* reference form: FP64 PCG, FP64 additive V-cycle            */
+#define SGLD_PREC_MIXED 1    /* FP64 flexible PCG outer, FP32 preconditioner (see DESIGN) */
+
+typedef struct sgld_ctx sgld_ctx;
+
+typedef struct sgld_options {
+    int num_levels;        /* numLevels_ as produced by FEA_VoxelBasedDiscretization.m:169-177 */
+    int non_dyadic;        /* nonDyadic_ (Data_GlobalVariables.m:15): first coarsening 4:1 if
+                              set and num_levels >= 4 (Solving_BuildingMeshHierarchy.m:12-23) */
+    double poisson_ratio;  /* poissonRatio_ (Data_GlobalVariables.m:20) */
+    double cell_size;      /* cellSize_ (Data_GlobalVariables.m:22) */
+    double omega;          /* weightFactorJacobi_ (Data_GlobalVariables.m:12) */
+    int device;            /* CUDA device ordinal */
+} sgld_options;
+
+typedef struct sgld_solve_opts {
+    double tol;            /* relative residual ||r||/||b|| to stop at (tol_) */
+    int maxit;             /* iteration cap (maxIT_) */
+    int use_x0;            /* 1: x holds the initial guess (Solving_CG_GMGS.m:7 warm start) */
+    int precision;         /* SGLD_PREC_* */
+    int inner_its;         /* SGLD_PREC_MIXED: FP32 inner PCG iterations per outer step (0 = default) */
+    double *history;       /* optional host buffer [maxit]: relative residual per iteration */
+} sgld_solve_opts;
+
+typedef struct sgld_solve_info {
+    int iterations;        /* outer iterations, as the reference's `its` */
+    int converged;         /* 1 if relres < tol */
+    double relres;         /* recursive residual norm / ||b|| at exit */
+    double true_relres;    /* ||b - K x|| / ||b|| recomputed in FP64 at exit */
+    int inner_iterations;  /* SGLD_PREC_MIXED: total FP32 inner iterations */
+    double seconds;        /* device time of the solve (CUDA events) */
+} sgld_solve_info;
+
+/* Fills opts with the reference defaults (Data_GlobalVariables.m:10-23). */
+void sgld_default_options(sgld_options *opts);
+
+/* Number of levels FEA_VoxelBasedDiscretization.m:163-177 derives for a voxel
+ * count and coarsestResolutionControl_ (before the nonDyadic adjustment). */
+int sgld_reference_num_levels(int64_t num_voxels, int64_t coarsest_resolution_control);
+
+/* Builds the grid hierarchy for a padded voxel grid.  Replaces
+ * FEA_VoxelBasedDiscretization.m:188-226 (element/node numbering) and
+ * Solving_BuildingMeshHierarchy.m:9-165 (coarse levels). */
+int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_options *opts, sgld_ctx **out);
+void sgld_destroy(sgld_ctx *ctx);
+const char *sgld_last_error(const sgld_ctx *ctx);
+
+/* Sizes of level `level` (1 = finest, as meshHierarchy_(level)). */
+int sgld_level_info(const sgld_ctx *ctx, int level, int res_yxz[3], int *span, int64_t *num_elements,
+                    int64_t *num_nodes);
+int sgld_num_levels(const sgld_ctx *ctx);
+/* 1-based full-grid indices of the compact nodes / elements of a level
+ * (nodMapBack / eleMapBack of that level, in that level's own grid). */
+int sgld_node_map(const sgld_ctx *ctx, int level, int64_t *map);
+int sgld_element_map(const sgld_ctx *ctx, int level, int64_t *map);
+
+/* Element stiffness matrix Ke (24 x 24, column-major).  sgld_create computes it
+ * as FEA_VoxelBasedElementStiffnessMatrix.m:10-23 does; set_ke replaces it
+ * (it must have the isotropic hexahedral structure). */
+int sgld_get_ke(const sgld_ctx *ctx, double *Ke);
+int sgld_set_ke(sgld_ctx *ctx, const double *Ke);
+
+/* Fixed-DOF mask (numDOFs bytes, nonzero = fixed): meshHierarchy_(1).fixedDOFs of
+ * FEA_ApplyBoundaryCondition.m:37-41; also derives the coarse masks as
+ * FEA_SetupVoxelBased.m:13-26 does. */
+int sgld_set_fixed_dofs(sgld_ctx *ctx, const uint8_t *fixed);
+/* Coarse-level free-DOF mask of `level` (numDOFs of that level). */
+int sgld_get_free_dofs(const sgld_ctx *ctx, int level, uint8_t *free_mask);
+
+/* Element moduli (numElements): meshHierarchy_(1).eleModulus
+ * (TopOpti_MaterialInterpolationSIMP.m:5). */
+int sgld_set_modulus(sgld_ctx *ctx, const double *E);
+int sgld_set_modulus_device(sgld_ctx *ctx, const double *d_E);
+
+/* Solving_AssembleFEAstencil.m:7-135: Galerkin coarse element matrices, Jacobi
+ * diagonals, coarsest-level factorization. */
+int sgld_assemble(sgld_ctx *ctx);
+/* Jacobi diagonal diagK of `level` (1..L-1), compact numDOFs. */
+int sgld_get_diag(const sgld_ctx *ctx, int level, double *diag);
+/* Galerkin element matrices Ks of coarse `level` (2..L), 24 x 24 x numElements. */
+int sgld_get_ks(const sgld_ctx *ctx, int level, double *Ks);
+
+/* Solving_KbyU_MatrixFree.m:1-41 (Solving_KbyU_MatrixFree_mex.cpp:6-138): y = K u,
+ * y(fixedDOFs) = 0. */
+int sgld_kbyu(sgld_ctx *ctx, const double *u, double *y);
+int sgld_kbyu_device(sgld_ctx *ctx, const double *d_u, double *d_y);
+
+/* Solving_RestrictResidual.m:1-23 / Solving_InterpolationDeviation.m:1-23 for
+ * MATLAB level index ii (2..L): coarse = R fine, fine = P coarse (compact DOFs). */
+int sgld_restrict(sgld_ctx *ctx, int ii, const double *r_fine, double *r_coarse);
+int sgld_interpolate(sgld_ctx *ctx, int ii, const double *x_coarse, double *x_fine);
+
+/* Solving_Vcycle.m:1-52: z = M^-1 r (additive multilevel Jacobi + coarsest solve). */
+int sgld_vcycle(sgld_ctx *ctx, const double *r, double *z);
+
+/* Solving_PreconditionedConjugateGradientSolver.m:1-37 with AtX = KbyU and
+ * PtV = Vcycle (as Solving_CG_GMGS.m:7 binds them).  x: in = initial guess when
+ * opts->use_x0, out = solution. */
+int sgld_pcg(sgld_ctx *ctx, const double *b, double *x, const sgld_solve_opts *opts, sgld_solve_info *info);
+int sgld_pcg_device(sgld_ctx *ctx, const double *d_b, double *d_x, const sgld_solve_opts *opts,
+                    sgld_solve_info *info);
+
+/* TopOpti_ComputeUnitCompliance.m:1-21 (TopOpti_CmptUnitCompliance_mex.cpp:6-107):
+ * ce = u_e' Ke u_e per element; c = sum(E .* ce) (FEA_ComputeComplianceVoxel.m:20-22).
+ * ce may be NULL. */
+int sgld_compliance(sgld_ctx *ctx, const double *U, double *ce, double *c);
+
+/* FEA_StressAnalysis.m:17-60 and FEA_ComputePerElementVonMisesStress.m:10-19:
+ * nodal Cartesian stress (numNodes x 6, row-major [xx yy zz yz zx xy]), nodal
+ * von Mises and per-element von Mises with the reference's final .^(1/2).
+ * Any output may be NULL. */
+int sgld_stress(sgld_ctx *ctx, const double *U, double *nodal_stress, double *vm_node, double *vm_elem);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SGLD_GPU_H */

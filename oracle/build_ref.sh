@@ -1,0 +1,28 @@
+#!/bin/sh
+# Builds the reference's own C++/OpenMP MEX kernels (from the read-only
+# SGLDBench checkout, unmodified) against the oracle's MEX shim, into
+# oracle/_ref/libref_mex.so.  Each file's mexFunction is renamed to
+# ref_<file stem> so that the eight kernels can live in one library.
+# Test infrastructure only: the product never links or loads this library.
+set -e
+REF=${SGLD_REFERENCE:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+SRC="$REF/src/MEXfuncs"
+[ -d "$SRC" ] || { echo "reference sources not found at $SRC" >&2; exit 2; }
+mkdir -p "$OUT/obj"
+CXX=${CXX:-g++}
+FLAGS="-O3 -fopenmp -fPIC -std=c++17 -w -I$HERE/mexshim"
+OBJS=""
+for f in Solving_KbyU_MatrixFree_mex Solving_Restriction_MatrixFree_mex \
+         Solving_Interpolation_MatrixFree_mex Solving_AssembleCmptStencilFromFinestLevel \
+         Solving_AssembleCmptStencilFromNonFinestLevel TopOpti_CmptUnitCompliance_mex \
+         TopOpti_SetupDensityFilter_mex TopOpti_PerformDensityFiltering_mex \
+         Solving_KbyU_MatrixFree8x8_mex; do
+  $CXX $FLAGS -DmexFunction=ref_$f -c "$SRC/$f.cpp" -o "$OUT/obj/$f.o" &
+  OBJS="$OBJS $OUT/obj/$f.o"
+done
+$CXX $FLAGS -c "$HERE/mexshim/mexshim.cpp" -o "$OUT/obj/mexshim.o" &
+wait
+$CXX -shared -fopenmp -o "$OUT/libref_mex.so" $OBJS "$OUT/obj/mexshim.o"
+echo "built $OUT/libref_mex.so"

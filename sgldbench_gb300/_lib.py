@@ -1,0 +1,91 @@
+"""ctypes binding of ``libsgld_gb300.so`` (the C ABI of ``include/sgld_gpu.h``).
+
+The library is the product: there is no CPU fallback.  ``load()`` raises if
+the shared library is missing or cannot be loaded, so every caller fails
+loudly instead of silently computing something else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsgld_gb300.so")
+
+SGLD_OK = 0
+SGLD_PREC_FP64 = 0
+SGLD_PREC_MIXED = 1
+
+# exported symbols and their signatures (mirrors include/sgld_gpu.h)
+vp, i32, i64, dbl = C.c_void_p, C.c_int, C.c_int64, C.c_double
+
+
+class Options(C.Structure):
+    _fields_ = [("num_levels", i32), ("non_dyadic", i32), ("poisson_ratio", dbl), ("cell_size", dbl),
+                ("omega", dbl), ("device", i32)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("tol", dbl), ("maxit", i32), ("use_x0", i32), ("precision", i32), ("inner_its", i32),
+                ("history", vp)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("iterations", i32), ("converged", i32), ("relres", dbl), ("true_relres", dbl),
+                ("inner_iterations", i32), ("seconds", dbl)]
+
+
+SIGNATURES = {
+    "sgld_default_options": (None, [vp]),
+    "sgld_reference_num_levels": (i32, [i64, i64]),
+    "sgld_create": (i32, [i32, i32, i32, vp, vp, vp]),
+    "sgld_destroy": (None, [vp]),
+    "sgld_last_error": (C.c_char_p, [vp]),
+    "sgld_level_info": (i32, [vp, i32, vp, vp, vp, vp]),
+    "sgld_num_levels": (i32, [vp]),
+    "sgld_node_map": (i32, [vp, i32, vp]),
+    "sgld_element_map": (i32, [vp, i32, vp]),
+    "sgld_get_ke": (i32, [vp, vp]),
+    "sgld_set_ke": (i32, [vp, vp]),
+    "sgld_set_fixed_dofs": (i32, [vp, vp]),
+    "sgld_get_free_dofs": (i32, [vp, i32, vp]),
+    "sgld_set_modulus": (i32, [vp, vp]),
+    "sgld_set_modulus_device": (i32, [vp, vp]),
+    "sgld_assemble": (i32, [vp]),
+    "sgld_get_diag": (i32, [vp, i32, vp]),
+    "sgld_get_ks": (i32, [vp, i32, vp]),
+    "sgld_kbyu": (i32, [vp, vp, vp]),
+    "sgld_kbyu_device": (i32, [vp, vp, vp]),
+    "sgld_restrict": (i32, [vp, i32, vp, vp]),
+    "sgld_interpolate": (i32, [vp, i32, vp, vp]),
+    "sgld_vcycle": (i32, [vp, vp, vp]),
+    "sgld_pcg": (i32, [vp, vp, vp, vp, vp]),
+    "sgld_pcg_device": (i32, [vp, vp, vp, vp, vp]),
+    "sgld_compliance": (i32, [vp, vp, vp, vp]),
+    "sgld_stress": (i32, [vp, vp, vp, vp, vp]),
+}
+
+_lib = None
+
+
+class SgldError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"sgld error {code}: {msg}")
+        self.code = code
+
+
+def load(path: str = LIB_PATH):
+    """Load the CUDA library (raises if it is not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is not built; run sgldbench_gb300.build.build() "
+                          "(or __graft_entry__.build()) first")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib

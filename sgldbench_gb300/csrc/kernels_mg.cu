@@ -1,0 +1,302 @@
+// Multigrid transfer, smoothing and bookkeeping kernels on the full grid.
+//
+// Restriction / prolongation (reference: src/Solving_RestrictResidual.m,
+// src/Solving_InterpolationDeviation.m and their MEX kernels).  The
+// reference builds a per-coarse-element table of the (s+1)^3 fine nodes,
+// scatters RI' r / multiplicity into the coarse nodes and averages RI x over
+// the elements sharing a fine node.  Because trilinear interpolation from a
+// continuous coarse field gives the same value from every element that
+// contains a fine node, that operator is exactly P = trilinear interpolation
+// restricted to active fine nodes and R = P'.  On the structured grid this is
+// a separable tent stencil of half-width s: w(d) = (s - |d|) / s per axis.
+// Inactive nodes carry zeros on every level, so no tables are needed.
+//
+// The additive V-cycle of the reference (src/Solving_Vcycle.m:12-50) is
+//   r_l = R r_{l-1};  x_L = A_L^-1 r_L;
+//   x_{l} = t_l + P x_{l+1} + t_l  with t_l = (omega r_l) ./ D_l,
+// evaluated in that order so the rounding follows the reference.
+#include "sgld_internal.cuh"
+
+namespace sgld {
+
+template <typename T>
+__global__ void k_restrict(const T *__restrict__ rf, T *__restrict__ rc, int nyc, int nxc, int nzc, int s) {
+    const int NYc = nyc + 1, NXc = nxc + 1, NZc = nzc + 1;
+    const int NYf = s * nyc + 1, NXf = s * nxc + 1, NZf = s * nzc + 1;
+    const int64_t nn = (int64_t)NYc * NXc * NZc;
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    const int I = (int)(n % NYc), J = (int)((n / NYc) % NXc), Kz = (int)(n / ((int64_t)NYc * NXc));
+    const T inv = T(1) / T(s);
+    T a0 = T(0), a1 = T(0), a2 = T(0);
+    for (int dz = -s + 1; dz < s; ++dz) {
+        const int fz = s * Kz + dz;
+        if (fz < 0 || fz >= NZf) continue;
+        const T wz = T(s - abs(dz)) * inv;
+        for (int dx = -s + 1; dx < s; ++dx) {
+            const int fx = s * J + dx;
+            if (fx < 0 || fx >= NXf) continue;
+            const T wxz = T(s - abs(dx)) * inv * wz;
+            for (int dy = -s + 1; dy < s; ++dy) {
+                const int fy = s * I + dy;
+                if (fy < 0 || fy >= NYf) continue;
+                const T w = T(s - abs(dy)) * inv * wxz;
+                const int64_t f = (int64_t)fy + (int64_t)NYf * (fx + (int64_t)NXf * fz);
+                a0 += w * rf[3 * f];
+                a1 += w * rf[3 * f + 1];
+                a2 += w * rf[3 * f + 2];
+            }
+        }
+    }
+    rc[3 * n] = a0;
+    rc[3 * n + 1] = a1;
+    rc[3 * n + 2] = a2;
+}
+
+template <typename T>
+void launch_restrict(const Level &fine, const Level &coarse, const T *rf, T *rc, cudaStream_t st) {
+    const int64_t nn = coarse.nnode;
+    k_restrict<T><<<(unsigned)((nn + 127) / 128), 128, 0, st>>>(rf, rc, coarse.ny, coarse.nx, coarse.nz, coarse.span);
+}
+template void launch_restrict<double>(const Level &, const Level &, const double *, double *, cudaStream_t);
+template void launch_restrict<float>(const Level &, const Level &, const float *, float *, cudaStream_t);
+
+__device__ __forceinline__ double warp_block_sum(double v, double *red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
+    return s;
+}
+
+// x_f = t + P x_c + t, t = (omega r_f) ./ D_f on active fine nodes, 0 elsewhere.
+// FINAL (finest level): fixed DOFs set to 0 and partial sums of x_f . r_f.
+template <typename T, bool FINAL>
+__global__ void k_prolong_smooth(const T *__restrict__ xc, const T *__restrict__ rf, const T *__restrict__ D,
+                                 const uint8_t *__restrict__ nflag, T omega, T *__restrict__ xf, int nyc, int nxc,
+                                 int nzc, int s, double *__restrict__ partial) {
+    const int NYc = nyc + 1, NXc = nxc + 1;
+    const int NYf = s * nyc + 1, NXf = s * nxc + 1, NZf = s * nzc + 1;
+    const int64_t nn = (int64_t)NYf * NXf * NZf;
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double dot = 0.0;
+    if (n < nn) {
+        const uint8_t f = nflag[n];
+        T o0 = T(0), o1 = T(0), o2 = T(0);
+        if (f & NF_ACTIVE) {
+            const int iy = (int)(n % NYf), ix = (int)((n / NYf) % NXf), iz = (int)(n / ((int64_t)NYf * NXf));
+            const int I = iy / s, J = ix / s, Kz = iz / s;
+            const int ry = iy - s * I, rx = ix - s * J, rz = iz - s * Kz;
+            const T inv = T(1) / T(s);
+            const T wy[2] = {T(s - ry) * inv, T(ry) * inv};
+            const T wx[2] = {T(s - rx) * inv, T(rx) * inv};
+            const T wz[2] = {T(s - rz) * inv, T(rz) * inv};
+            T p0 = T(0), p1 = T(0), p2 = T(0);
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                if (c && rz == 0) continue;
+#pragma unroll
+                for (int b = 0; b < 2; ++b) {
+                    if (b && rx == 0) continue;
+#pragma unroll
+                    for (int a = 0; a < 2; ++a) {
+                        if (a && ry == 0) continue;
+                        const T w = wy[a] * wx[b] * wz[c];
+                        const int64_t m = (int64_t)(I + a) + (int64_t)NYc * ((J + b) + (int64_t)NXc * (Kz + c));
+                        p0 += w * xc[3 * m];
+                        p1 += w * xc[3 * m + 1];
+                        p2 += w * xc[3 * m + 2];
+                    }
+                }
+            }
+            const T r0 = rf[3 * n], r1 = rf[3 * n + 1], r2 = rf[3 * n + 2];
+            const T t0 = (omega * r0) / D[3 * n], t1 = (omega * r1) / D[3 * n + 1], t2 = (omega * r2) / D[3 * n + 2];
+            o0 = (t0 + p0) + t0;
+            o1 = (t1 + p1) + t1;
+            o2 = (t2 + p2) + t2;
+            if (FINAL) {
+                if (f & NF_FIXX) o0 = T(0);
+                if (f & NF_FIXY) o1 = T(0);
+                if (f & NF_FIXZ) o2 = T(0);
+                dot = (double)o0 * (double)r0 + (double)o1 * (double)r1 + (double)o2 * (double)r2;
+            }
+        }
+        xf[3 * n] = o0;
+        xf[3 * n + 1] = o1;
+        xf[3 * n + 2] = o2;
+    }
+    if (FINAL && partial) {
+        __shared__ double red[8];
+        const double sum = warp_block_sum(dot, red);
+        if (threadIdx.x == 0) partial[blockIdx.x] = sum;
+    }
+}
+
+template <typename T>
+void launch_prolong_smooth(const Level &fine, const Level &coarse, const T *xc, const T *rf, const T *diag, T omega,
+                           T *xf, bool final_level, double *partial_dot, int *nblocks_out, cudaStream_t st) {
+    const int64_t nn = fine.nnode;
+    const unsigned nb = (unsigned)((nn + 255) / 256);
+    if (nblocks_out) *nblocks_out = (int)nb;
+    if (final_level)
+        k_prolong_smooth<T, true><<<nb, 256, 0, st>>>(xc, rf, diag, fine.nflag, omega, xf, coarse.ny, coarse.nx,
+                                                      coarse.nz, coarse.span, partial_dot);
+    else
+        k_prolong_smooth<T, false><<<nb, 256, 0, st>>>(xc, rf, diag, fine.nflag, omega, xf, coarse.ny, coarse.nx,
+                                                       coarse.nz, coarse.span, nullptr);
+}
+template void launch_prolong_smooth<double>(const Level &, const Level &, const double *, const double *,
+                                            const double *, double, double *, bool, double *, int *, cudaStream_t);
+template void launch_prolong_smooth<float>(const Level &, const Level &, const float *, const float *, const float *,
+                                           float, float *, bool, double *, int *, cudaStream_t);
+
+// ---- Jacobi diagonals (src/Solving_AssembleFEAstencil.m:82-121) -------------
+// reference corner order j = 1..8 as offsets (dy, dx, dz)
+__constant__ int c_cdy[8] = {1, 1, 0, 0, 1, 1, 0, 0};
+__constant__ int c_cdx[8] = {0, 1, 1, 0, 0, 1, 1, 0};
+__constant__ int c_cdz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+__constant__ double c_dKe[24];
+
+__global__ void k_diag_finest(const double *__restrict__ E, const uint8_t *__restrict__ nflag, int ny, int nx, int nz,
+                              double *__restrict__ D) {
+    const int NY = ny + 1, NX = nx + 1, NZ = nz + 1;
+    const int64_t nn = (int64_t)NY * NX * NZ;
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    double d0 = 0.0, d1 = 0.0, d2 = 0.0;
+    if (nflag[n] & NF_ACTIVE) {
+        const int iy = (int)(n % NY), ix = (int)((n / NY) % NX), iz = (int)(n / ((int64_t)NY * NX));
+        for (int j = 0; j < 8; ++j) {
+            const int ey = iy - c_cdy[j], ex = ix - c_cdx[j], ez = iz - c_cdz[j];
+            if (ey < 0 || ex < 0 || ez < 0 || ey >= ny || ex >= nx || ez >= nz) continue;
+            const double ev = E[(int64_t)ey + (int64_t)ny * (ex + (int64_t)nx * ez)];
+            d0 += c_dKe[3 * j] * ev;
+            d1 += c_dKe[3 * j + 1] * ev;
+            d2 += c_dKe[3 * j + 2] * ev;
+        }
+    }
+    D[3 * n] = d0;
+    D[3 * n + 1] = d1;
+    D[3 * n + 2] = d2;
+}
+
+void launch_diag_finest(const Level &l0, const double *E, const double *Ke, double *diag, cudaStream_t s) {
+    double dk[24];
+    for (int i = 0; i < 24; ++i) dk[i] = Ke[i + 24 * i];
+    cudaMemcpyToSymbolAsync(c_dKe, dk, sizeof dk, 0, cudaMemcpyHostToDevice, s);
+    k_diag_finest<<<(unsigned)((l0.nnode + 255) / 256), 256, 0, s>>>(E, l0.nflag, l0.ny, l0.nx, l0.nz, diag);
+}
+
+__global__ void k_diag_from_Ks(const double *__restrict__ Ks, const uint8_t *__restrict__ eact,
+                               const uint8_t *__restrict__ nflag, int ny, int nx, int nz, double *__restrict__ D) {
+    const int NY = ny + 1, NX = nx + 1, NZ = nz + 1;
+    const int64_t nn = (int64_t)NY * NX * NZ;
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    double d0 = 0.0, d1 = 0.0, d2 = 0.0;
+    if (nflag[n] & NF_ACTIVE) {
+        const int iy = (int)(n % NY), ix = (int)((n / NY) % NX), iz = (int)(n / ((int64_t)NY * NX));
+        for (int j = 0; j < 8; ++j) {
+            const int ey = iy - c_cdy[j], ex = ix - c_cdx[j], ez = iz - c_cdz[j];
+            if (ey < 0 || ex < 0 || ez < 0 || ey >= ny || ex >= nx || ez >= nz) continue;
+            const int64_t e = (int64_t)ey + (int64_t)ny * (ex + (int64_t)nx * ez);
+            if (!eact[e]) continue;
+            const double *k = Ks + 576 * e;
+            d0 += k[(3 * j) * 25];
+            d1 += k[(3 * j + 1) * 25];
+            d2 += k[(3 * j + 2) * 25];
+        }
+    }
+    D[3 * n] = d0;
+    D[3 * n + 1] = d1;
+    D[3 * n + 2] = d2;
+}
+
+void launch_diag_from_Ks(const Level &l, double *diag, cudaStream_t s) {
+    k_diag_from_Ks<<<(unsigned)((l.nnode + 255) / 256), 256, 0, s>>>(l.Ks, l.eact, l.nflag, l.ny, l.nx, l.nz, diag);
+}
+
+// ---- compact <-> full conversions -------------------------------------------
+__global__ void k_scatter_nodes(const int64_t *__restrict__ map, int64_t n, const double *__restrict__ src,
+                                double *__restrict__ dst) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= 3 * n) return;
+    const int64_t node = i / 3;
+    const int c = (int)(i - 3 * node);
+    dst[3 * map[node] + c] = src[i];
+}
+__global__ void k_gather_nodes(const int64_t *__restrict__ map, int64_t n, const double *__restrict__ src,
+                               double *__restrict__ dst) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= 3 * n) return;
+    const int64_t node = i / 3;
+    const int c = (int)(i - 3 * node);
+    dst[i] = src[3 * map[node] + c];
+}
+__global__ void k_scatter_elems(const int64_t *__restrict__ map, int64_t n, const double *__restrict__ src,
+                                double *__restrict__ dst) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) dst[map[i]] = src[i];
+}
+__global__ void k_gather_elems(const int64_t *__restrict__ map, int64_t n, const double *__restrict__ src,
+                               double *__restrict__ dst) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[map[i]];
+}
+
+void launch_scatter_nodes(const int64_t *map, int64_t n, const double *compact, double *full, cudaStream_t s) {
+    if (n > 0) k_scatter_nodes<<<(unsigned)((3 * n + 255) / 256), 256, 0, s>>>(map, n, compact, full);
+}
+void launch_gather_nodes(const int64_t *map, int64_t n, const double *full, double *compact, cudaStream_t s) {
+    if (n > 0) k_gather_nodes<<<(unsigned)((3 * n + 255) / 256), 256, 0, s>>>(map, n, full, compact);
+}
+void launch_scatter_elems(const int64_t *map, int64_t n, const double *compact, double *full, cudaStream_t s) {
+    if (n > 0) k_scatter_elems<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(map, n, compact, full);
+}
+void launch_gather_elems(const int64_t *map, int64_t n, const double *full, double *compact, cudaStream_t s) {
+    if (n > 0) k_gather_elems<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(map, n, full, compact);
+}
+
+// ---- fixed-DOF bookkeeping (src/FEA_SetupVoxelBased.m:13-26) ----------------
+__global__ void k_fixed_indicator(const uint8_t *__restrict__ nflag, int64_t nn, double *__restrict__ v) {
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    const uint8_t f = nflag[n];
+    v[3 * n] = (f & NF_FIXX) ? 1.0 : 0.0;
+    v[3 * n + 1] = (f & NF_FIXY) ? 1.0 : 0.0;
+    v[3 * n + 2] = (f & NF_FIXZ) ? 1.0 : 0.0;
+}
+void launch_fixed_indicator(const Level &l, double *v, cudaStream_t s) {
+    k_fixed_indicator<<<(unsigned)((l.nnode + 255) / 256), 256, 0, s>>>(l.nflag, l.nnode, v);
+}
+// a coarse DOF is fixed iff the restricted fixed indicator is nonzero
+__global__ void k_mark_fixed(uint8_t *__restrict__ nflag, int64_t nn, const double *__restrict__ v) {
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    uint8_t f = nflag[n] & NF_ACTIVE;
+    if (v[3 * n] != 0.0) f |= NF_FIXX;
+    if (v[3 * n + 1] != 0.0) f |= NF_FIXY;
+    if (v[3 * n + 2] != 0.0) f |= NF_FIXZ;
+    nflag[n] = f;
+}
+void launch_mark_fixed(Level &l, const double *restricted, cudaStream_t s) {
+    k_mark_fixed<<<(unsigned)((l.nnode + 255) / 256), 256, 0, s>>>(l.nflag, l.nnode, restricted);
+}
+
+__global__ void k_mask_fixed(const uint8_t *__restrict__ nflag, int64_t nn, double *__restrict__ v) {
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    const uint8_t f = nflag[n];
+    if (f & NF_FIXX) v[3 * n] = 0.0;
+    if (f & NF_FIXY) v[3 * n + 1] = 0.0;
+    if (f & NF_FIXZ) v[3 * n + 2] = 0.0;
+}
+void launch_mask_fixed(const Level &l0, double *v, cudaStream_t s) {
+    k_mask_fixed<<<(unsigned)((l0.nnode + 255) / 256), 256, 0, s>>>(l0.nflag, l0.nnode, v);
+}
+
+}  // namespace sgld

@@ -1,0 +1,396 @@
+// Element-stencil kernels on the finest level: matrix-free K*u, unit
+// compliance and the stress recovery of the solution.
+//
+// K*u (reference: src/MEXfuncs/Solving_KbyU_MatrixFree_mex.cpp:53-138) is
+// restated for a structured grid without colouring.  A CTA owns a tile of
+// (TY-1) x (TX-1) node columns and marches through z one element layer at a
+// time: the two node layers an element layer touches are staged in shared
+// memory, every thread applies E_e*Ke to one element of the (TY x TX)
+// element tile (which includes a one-element halo), writes the 24 results to
+// shared memory, and every node thread then sums the contributions of its 8
+// neighbouring elements.  No atomics, deterministic, every node written once.
+//
+// The element product uses the 8-corner Hadamard basis in which the
+// isotropic hexahedral Ke has 45 nonzeros (instead of 576): forward
+// butterflies (72 adds), 45 FMAs, E scaling, inverse butterflies (72 adds).
+// FP64 arithmetic is the scarce resource on GB300, so this is the form that
+// matters for the FP64 operator.
+#include "sgld_internal.cuh"
+
+namespace sgld {
+
+__constant__ double c_Kh[KH_NNZ];
+__constant__ float c_Kh32[KH_NNZ];
+__constant__ double c_M[48 * 24];   // stress: corner stresses = M * u_e (reference corner order)
+
+void upload_kh(const double *Kh, cudaStream_t s) {
+    float f[KH_NNZ];
+    for (int i = 0; i < KH_NNZ; ++i) f[i] = (float)Kh[i];
+    cudaMemcpyToSymbolAsync(c_Kh, Kh, sizeof(double) * KH_NNZ, 0, cudaMemcpyHostToDevice, s);
+    cudaMemcpyToSymbolAsync(c_Kh32, f, sizeof(float) * KH_NNZ, 0, cudaMemcpyHostToDevice, s);
+    cudaStreamSynchronize(s);
+}
+
+template <typename T> __device__ __forceinline__ T khv(int i);
+template <> __device__ __forceinline__ double khv<double>(int i) { return c_Kh[i]; }
+template <> __device__ __forceinline__ float khv<float>(int i) { return c_Kh32[i]; }
+
+// u[3*k + c]: corner bit index k = ks | kt<<1 | kp<<2.  On return u holds
+// e * Ke * u in the same layout.
+template <typename T>
+__device__ __forceinline__ void hex_apply(T (&u)[24], T e) {
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if (k & (1 << ax)) continue;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const T lo = u[3 * k + c], hi = u[3 * (k | (1 << ax)) + c];
+                u[3 * k + c] = lo + hi;
+                u[3 * (k | (1 << ax)) + c] = hi - lo;
+            }
+        }
+    }
+    T g[24];
+    g[0] = g[1] = g[2] = T(0);
+#define KH3(i, j, k, o)                                                          \
+    {                                                                            \
+        const T a = u[i], b = u[j], d = u[k];                                    \
+        g[i] = khv<T>(o) * a + khv<T>(o + 1) * b + khv<T>(o + 2) * d;            \
+        g[j] = khv<T>(o + 3) * a + khv<T>(o + 4) * b + khv<T>(o + 5) * d;        \
+        g[k] = khv<T>(o + 6) * a + khv<T>(o + 7) * b + khv<T>(o + 8) * d;        \
+    }
+#define KH2(i, j, o)                                     \
+    {                                                    \
+        const T a = u[i], b = u[j];                      \
+        g[i] = khv<T>(o) * a + khv<T>(o + 1) * b;        \
+        g[j] = khv<T>(o + 2) * a + khv<T>(o + 3) * b;    \
+    }
+    KH3(3, 7, 14, 0)
+    KH2(4, 6, 9)
+    KH2(5, 12, 13)
+    KH2(8, 13, 17)
+    KH2(9, 20, 21)
+    KH2(10, 17, 25)
+    KH3(11, 16, 18, 29)
+    KH2(15, 19, 38)
+    g[21] = khv<T>(42) * u[21];
+    g[22] = khv<T>(43) * u[22];
+    g[23] = khv<T>(44) * u[23];
+#undef KH3
+#undef KH2
+#pragma unroll
+    for (int i = 3; i < 24; ++i) g[i] *= e;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if (k & (1 << ax)) continue;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const T a = g[3 * k + c], d = g[3 * (k | (1 << ax)) + c];
+                g[3 * k + c] = a - d;
+                g[3 * (k | (1 << ax)) + c] = a + d;
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 24; ++i) u[i] = g[i];
+}
+
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T *red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    T s = T(0);
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
+    }
+    return s;
+}
+
+constexpr int KT_Y = 32, KT_X = 8, KT_THREADS = KT_Y * KT_X;
+constexpr int KT_NL = (KT_Y + 1) * (KT_X + 1);   // staged nodes per layer
+constexpr int KT_ZC = 16;                        // node layers per CTA
+
+template <typename T>
+__device__ __forceinline__ void stage_layer(const T *__restrict__ u, T *dst, int z, int y0, int x0, int NY, int NX,
+                                            int NZ) {
+    for (int i = threadIdx.x; i < KT_NL * 3; i += KT_THREADS) {
+        const int node = i / 3, c = i - 3 * node;
+        const int ly = node % (KT_Y + 1), lx = node / (KT_Y + 1);
+        const int gy = y0 - 1 + ly, gx = x0 - 1 + lx;
+        T v = T(0);
+        if (z >= 0 && z < NZ && gy >= 0 && gy < NY && gx >= 0 && gx < NX)
+            v = u[3 * ((int64_t)gy + (int64_t)NY * (gx + (int64_t)NX * z)) + c];
+        dst[i] = v;
+    }
+}
+
+// y = K u on the full grid; y at fixed DOFs is 0.  When DOT, also writes
+// sum(u .* y) of this CTA's nodes to partial[block].
+template <typename T, bool DOT>
+__global__ void __launch_bounds__(KT_THREADS) k_kbyu(const T *__restrict__ u, T *__restrict__ y,
+                                                     const T *__restrict__ E, const uint8_t *__restrict__ nflag,
+                                                     int ny, int nx, int nz, double *__restrict__ partial) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *su = reinterpret_cast<T *>(smem_raw);      // [2][KT_NL*3]
+    T *so = su + 2 * KT_NL * 3;                   // [24][KT_THREADS]
+    const int tid = threadIdx.x;
+    const int ty = tid % KT_Y, tx = tid / KT_Y;
+    const int NY = ny + 1, NX = nx + 1, NZ = nz + 1;
+    const int y0 = blockIdx.x * (KT_Y - 1), x0 = blockIdx.y * (KT_X - 1), z0 = blockIdx.z * KT_ZC;
+    const int zend = min(z0 + KT_ZC, NZ);
+    const int gny = y0 + ty, gnx = x0 + tx;
+    const bool owner = (ty < KT_Y - 1) && (tx < KT_X - 1) && gny < NY && gnx < NX;
+    const int ey = y0 - 1 + ty, ex = x0 - 1 + tx;
+    const bool ein = ey >= 0 && ey < ny && ex >= 0 && ex < nx;
+    T acc0 = T(0), acc1 = T(0), acc2 = T(0);
+    double dot = 0.0;
+
+    stage_layer(u, su + ((z0 + 1) & 1) * KT_NL * 3, z0 - 1, y0, x0, NY, NX, NZ);
+    for (int ez = z0 - 1; ez < zend; ++ez) {
+        const int s0 = ez & 1, s1 = (ez + 1) & 1;
+        stage_layer(u, su + s1 * KT_NL * 3, ez + 1, y0, x0, NY, NX, NZ);
+        __syncthreads();
+        T ev = T(0);
+        if (ein && ez >= 0 && ez < nz) ev = E[(int64_t)ey + (int64_t)ny * (ex + (int64_t)nx * ez)];
+        T ue[24];
+        if (ev != T(0)) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int dx = k & 1, dy = 1 - ((k >> 1) & 1), kp = k >> 2;
+                const T *src = su + (kp ? s1 : s0) * KT_NL * 3 + 3 * ((ty + dy) + (KT_Y + 1) * (tx + dx));
+                ue[3 * k + 0] = src[0];
+                ue[3 * k + 1] = src[1];
+                ue[3 * k + 2] = src[2];
+            }
+            hex_apply<T>(ue, ev);
+        } else {
+#pragma unroll
+            for (int i = 0; i < 24; ++i) ue[i] = T(0);
+        }
+#pragma unroll
+        for (int i = 0; i < 24; ++i) so[i * KT_THREADS + tid] = ue[i];
+        __syncthreads();
+        if (owner) {
+            // lower corners (kp = 0) of element layer ez complete node layer ez
+#pragma unroll
+            for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+                for (int dx = 0; dx < 2; ++dx) {
+                    const int k = dx | ((1 - dy) << 1);
+                    const int t = (ty + 1 - dy) + KT_Y * (tx + 1 - dx);
+                    acc0 += so[(3 * k + 0) * KT_THREADS + t];
+                    acc1 += so[(3 * k + 1) * KT_THREADS + t];
+                    acc2 += so[(3 * k + 2) * KT_THREADS + t];
+                }
+            if (ez >= z0) {
+                const int64_t node = (int64_t)gny + (int64_t)NY * (gnx + (int64_t)NX * ez);
+                const uint8_t f = nflag[node];
+                const T o0 = (f & NF_FIXX) ? T(0) : acc0;
+                const T o1 = (f & NF_FIXY) ? T(0) : acc1;
+                const T o2 = (f & NF_FIXZ) ? T(0) : acc2;
+                y[3 * node + 0] = o0;
+                y[3 * node + 1] = o1;
+                y[3 * node + 2] = o2;
+                if (DOT) {
+                    const T *un = su + s0 * KT_NL * 3 + 3 * ((ty + 1) + (KT_Y + 1) * (tx + 1));
+                    dot += (double)un[0] * (double)o0 + (double)un[1] * (double)o1 + (double)un[2] * (double)o2;
+                }
+            }
+            acc0 = acc1 = acc2 = T(0);
+#pragma unroll
+            for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+                for (int dx = 0; dx < 2; ++dx) {
+                    const int k = 4 | dx | ((1 - dy) << 1);
+                    const int t = (ty + 1 - dy) + KT_Y * (tx + 1 - dx);
+                    acc0 += so[(3 * k + 0) * KT_THREADS + t];
+                    acc1 += so[(3 * k + 1) * KT_THREADS + t];
+                    acc2 += so[(3 * k + 2) * KT_THREADS + t];
+                }
+        }
+        __syncthreads();
+    }
+    if (DOT) {
+        __shared__ double red[KT_THREADS / 32];
+        const double s = block_sum<double>(dot, red);
+        if (tid == 0) partial[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s;
+    }
+}
+
+static dim3 kbyu_grid(const Level &l) {
+    return dim3((l.ny + 1 + KT_Y - 2) / (KT_Y - 1), (l.nx + 1 + KT_X - 2) / (KT_X - 1), (l.nz + 1 + KT_ZC - 1) / KT_ZC);
+}
+
+template <typename T, bool DOT>
+static void kbyu_launch(const Level &l0, const T *E, const T *u, T *y, double *partial, int *nb, cudaStream_t s) {
+    const size_t smem = sizeof(T) * (2 * KT_NL * 3 + 24 * KT_THREADS);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_kbyu<T, DOT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_set = true;
+    }
+    dim3 g = kbyu_grid(l0);
+    if (nb) *nb = (int)(g.x * g.y * g.z);
+    k_kbyu<T, DOT><<<g, KT_THREADS, smem, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, partial);
+}
+
+void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *y, double *partial_dot,
+                     int *nblocks_out, cudaStream_t s) {
+    if (partial_dot)
+        kbyu_launch<double, true>(l0, E, u, y, partial_dot, nblocks_out, s);
+    else
+        kbyu_launch<double, false>(l0, E, u, y, nullptr, nblocks_out, s);
+}
+
+void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, cudaStream_t s) {
+    kbyu_launch<float, false>(l0, E, u, y, nullptr, nullptr, s);
+}
+
+int kbyu_num_blocks(const Level &l0) {
+    dim3 g = kbyu_grid(l0);
+    return (int)(g.x * g.y * g.z);
+}
+
+// ---------------------------------------------------------------------------
+// unit compliance ce_e = u_e' Ke u_e (TopOpti_CmptUnitCompliance_mex.cpp:40-107)
+// and the weighted sum c = sum E_e ce_e (FEA_ComputeComplianceVoxel.m:20-22).
+// One thread per element; in the Hadamard basis u'Ke u = h' Kh h with h = H u.
+// ---------------------------------------------------------------------------
+__global__ void k_unit_compliance(const double *__restrict__ u, const double *__restrict__ E,
+                                  const uint8_t *__restrict__ eact, int ny, int nx, int nz,
+                                  double *__restrict__ ce, double *__restrict__ partial) {
+    const int64_t nel = (int64_t)ny * nx * nz;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double cs = 0.0;
+    if (e < nel && eact[e]) {
+        const int ey = (int)(e % ny), ex = (int)((e / ny) % nx), ez = (int)(e / ((int64_t)ny * nx));
+        const int NY = ny + 1, NX = nx + 1;
+        double ue[24], h[24];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int dx = k & 1, dy = 1 - ((k >> 1) & 1), dz = k >> 2;
+            const int64_t n = (int64_t)(ey + dy) + (int64_t)NY * ((ex + dx) + (int64_t)NX * (ez + dz));
+            ue[3 * k] = u[3 * n];
+            ue[3 * k + 1] = u[3 * n + 1];
+            ue[3 * k + 2] = u[3 * n + 2];
+            h[3 * k] = ue[3 * k];
+            h[3 * k + 1] = ue[3 * k + 1];
+            h[3 * k + 2] = ue[3 * k + 2];
+        }
+        hex_apply<double>(h, 1.0);
+        double q = 0.0;
+#pragma unroll
+        for (int i = 0; i < 24; ++i) q += ue[i] * h[i];
+        ce[e] = q;
+        cs = E[e] * q;
+    } else if (e < nel) {
+        ce[e] = 0.0;
+    }
+    __shared__ double red[8];
+    const double s = block_sum<double>(cs, red);
+    if (threadIdx.x == 0 && partial) partial[blockIdx.x] = s;
+}
+
+void launch_unit_compliance(const Level &l0, const double *u, const double *E, double *ce_full, double *partial,
+                            int *nblocks_out, cudaStream_t s) {
+    const int64_t nel = l0.nel;
+    const int nb = (int)((nel + 255) / 256);
+    if (nblocks_out) *nblocks_out = nb;
+    k_unit_compliance<<<nb, 256, 0, s>>>(u, E, l0.eact, l0.ny, l0.nx, l0.nz, ce_full, partial);
+}
+
+// ---------------------------------------------------------------------------
+// stress recovery (src/FEA_StressAnalysis.m:29-60): per element, corner
+// stresses = E_e * inv(sFM) * D * B * u_e (48 values); nodal stress = sum
+// over the elements sharing the node / their count; nodal von Mises.
+// Node-centric gather: each node thread recomputes the corner stresses of its
+// (at most 8) elements restricted to its own corner -> deterministic.
+// ---------------------------------------------------------------------------
+__global__ void k_nodal_stress(const double *__restrict__ u, const double *__restrict__ E,
+                               const uint8_t *__restrict__ nflag, const uint8_t *__restrict__ eact, int ny, int nx,
+                               int nz, double *__restrict__ s6,
+                               double *__restrict__ vm) {
+    const int NY = ny + 1, NX = nx + 1, NZ = nz + 1;
+    const int64_t nn = (int64_t)NY * NX * NZ;
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    const int iy = (int)(n % NY), ix = (int)((n / NY) % NX), iz = (int)(n / ((int64_t)NY * NX));
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    int cnt = 0;
+    if (nflag[n] & NF_ACTIVE) {
+        // reference corner order j: offsets (dy, dx, dz)
+        const int cdy[8] = {1, 1, 0, 0, 1, 1, 0, 0}, cdx[8] = {0, 1, 1, 0, 0, 1, 1, 0},
+                  cdz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+        for (int j = 0; j < 8; ++j) {
+            const int ey = iy - cdy[j], ex = ix - cdx[j], ez = iz - cdz[j];
+            if (ey < 0 || ex < 0 || ez < 0 || ey >= ny || ex >= nx || ez >= nz) continue;
+            const int64_t eidx = (int64_t)ey + (int64_t)ny * (ex + (int64_t)nx * ez);
+            if (!eact[eidx]) continue;
+            const double ev = E[eidx];
+            ++cnt;
+            double ue[24];
+            for (int k = 0; k < 8; ++k) {
+                const int64_t m = (int64_t)(ey + cdy[k]) + (int64_t)NY * ((ex + cdx[k]) + (int64_t)NX * (ez + cdz[k]));
+                ue[3 * k] = u[3 * m];
+                ue[3 * k + 1] = u[3 * m + 1];
+                ue[3 * k + 2] = u[3 * m + 2];
+            }
+            for (int c = 0; c < 6; ++c) {
+                const double *row = c_M + (6 * j + c);   // column-major 48 x 24
+                double sacc = 0.0;
+                for (int i = 0; i < 24; ++i) sacc += row[48 * i] * ue[i];
+                acc[c] += sacc * ev;
+            }
+        }
+    }
+    double v[6];
+    for (int c = 0; c < 6; ++c) v[c] = cnt ? acc[c] / (double)cnt : 0.0;
+    for (int c = 0; c < 6; ++c) s6[6 * n + c] = v[c];
+    const double a = v[0] - v[1], b = v[1] - v[2], d = v[2] - v[0];
+    vm[n] = cnt ? sqrt(0.5 * (a * a + b * b + d * d) + 3.0 * (v[5] * v[5] + v[3] * v[3] + v[4] * v[4])) : 0.0;
+}
+
+void launch_stress(const Level &l0, const double *E, const double *u, const double *M48x24, double *nodal6,
+                   double *vm_node, cudaStream_t s) {
+    cudaMemcpyToSymbolAsync(c_M, M48x24, sizeof(double) * 48 * 24, 0, cudaMemcpyHostToDevice, s);
+    const int64_t nn = l0.nnode;
+    k_nodal_stress<<<(unsigned)((nn + 127) / 128), 128, 0, s>>>(u, E, l0.nflag, l0.eact, l0.ny, l0.nx, l0.nz, nodal6, vm_node);
+}
+
+// per-element: centroid stress = mean of the 8 nodal stresses, von Mises,
+// then the reference's extra square root (FEA_ComputePerElementVonMisesStress.m:10-19).
+__global__ void k_elem_vm(const double *__restrict__ s6, const uint8_t *__restrict__ eact, int ny, int nx, int nz,
+                          double *__restrict__ vme) {
+    const int64_t nel = (int64_t)ny * nx * nz;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= nel) return;
+    if (!eact[e]) {
+        vme[e] = 0.0;
+        return;
+    }
+    const int ey = (int)(e % ny), ex = (int)((e / ny) % nx), ez = (int)(e / ((int64_t)ny * nx));
+    const int NY = ny + 1, NX = nx + 1;
+    const int cdy[8] = {1, 1, 0, 0, 1, 1, 0, 0}, cdx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, cdz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 8; ++k) {
+        const int64_t m = (int64_t)(ey + cdy[k]) + (int64_t)NY * ((ex + cdx[k]) + (int64_t)NX * (ez + cdz[k]));
+        for (int c = 0; c < 6; ++c) v[c] += 0.125 * s6[6 * m + c];
+    }
+    const double a = v[0] - v[1], b = v[1] - v[2], d = v[2] - v[0];
+    vme[e] = sqrt(sqrt(0.5 * (a * a + b * b + d * d) + 3.0 * (v[5] * v[5] + v[3] * v[3] + v[4] * v[4])));
+}
+
+void launch_elem_vm(const Level &l0, const double *nodal6, double *vm_elem_full, cudaStream_t s) {
+    const int64_t nel = l0.nel;
+    k_elem_vm<<<(unsigned)((nel + 255) / 256), 256, 0, s>>>(nodal6, l0.eact, l0.ny, l0.nx, l0.nz, vm_elem_full);
+}
+
+}  // namespace sgld

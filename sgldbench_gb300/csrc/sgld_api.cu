@@ -1,0 +1,973 @@
+// Host side of the C ABI (include/sgld_gpu.h): grid hierarchy, element
+// matrices, assembly and the PCG driver.  Every entry point mirrors one
+// function of the reference's solve path (cited in the header).
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/sgld_gpu.h"
+#include "sgld_internal.cuh"
+
+using namespace sgld;
+
+struct sgld_ctx {
+    Ctx c;
+    // lazily allocated stress buffers
+    double *d_s6 = nullptr, *d_vmn = nullptr, *d_vme = nullptr;
+    int *d_rowspos = nullptr;
+    std::vector<std::vector<int64_t>> nodemaps, elemaps;   // per level, 0-based full indices
+    std::vector<int> h_rows;                               // coarsest free DOFs (full DOF index)
+    bool have_mixed = false;
+};
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// element matrices (FEA_VoxelBasedElementStiffnessMatrix.m:10-23 and helpers)
+// ---------------------------------------------------------------------------
+const double kGauss = 0.577350269189626;   // FEA_GaussianIntegral.m:10-15
+const double kGs[8] = {-kGauss, kGauss, kGauss, -kGauss, -kGauss, kGauss, kGauss, -kGauss};
+const double kGt[8] = {-kGauss, -kGauss, kGauss, kGauss, -kGauss, -kGauss, kGauss, kGauss};
+const double kGp[8] = {-kGauss, -kGauss, -kGauss, -kGauss, kGauss, kGauss, kGauss, kGauss};
+// natural coordinates of the 8 nodes (FEA_ShapeFunction.m:11-18)
+const double kNs[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
+const double kNt[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+const double kNp[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+// reference corner j -> offsets (dy, dx, dz) on the grid (FEA_VoxelBasedDiscretization.m:72-79)
+const int kCdy[8] = {1, 1, 0, 0, 1, 1, 0, 0};
+const int kCdx[8] = {0, 1, 1, 0, 0, 1, 1, 0};
+const int kCdz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+
+void hooke(double nu, double S[6][6]) {   // FEA_HookeLaw.m:4-13 (E = 1)
+    memset(S, 0, sizeof(double) * 36);
+    const double c1 = (1 + nu) * (1 - 2 * nu), c2 = 2 * (1 + nu);
+    S[0][0] = S[1][1] = S[2][2] = (1 - nu) / c1;
+    S[0][1] = S[0][2] = S[1][0] = S[1][2] = S[2][0] = S[2][1] = nu / c1;
+    S[3][3] = S[4][4] = S[5][5] = 1.0 / c2;
+}
+
+// strain-displacement matrix at Gauss point g: 6 x 24 (FEA_ElementStrainMatrix.m)
+void strain_at(int g, double h, double B[6][24]) {
+    const double s = kGs[g], t = kGt[g], p = kGp[g];
+    memset(B, 0, sizeof(double) * 144);
+    for (int n = 0; n < 8; ++n) {
+        const double ds = 0.125 * kNs[n] * (1 + kNt[n] * t) * (1 + kNp[n] * p) * (2.0 / h);
+        const double dt = 0.125 * kNt[n] * (1 + kNs[n] * s) * (1 + kNp[n] * p) * (2.0 / h);
+        const double dp = 0.125 * kNp[n] * (1 + kNs[n] * s) * (1 + kNt[n] * t) * (2.0 / h);
+        B[0][3 * n] = ds;
+        B[1][3 * n + 1] = dt;
+        B[2][3 * n + 2] = dp;
+        B[3][3 * n + 1] = dp;
+        B[3][3 * n + 2] = dt;
+        B[4][3 * n] = dp;
+        B[4][3 * n + 2] = ds;
+        B[5][3 * n] = dt;
+        B[5][3 * n + 1] = ds;
+    }
+}
+
+void element_stiffness(double nu, double h, double Ke[576]) {
+    double S[6][6], B[6][24];
+    hooke(nu, S);
+    const double w = h * h * h / 8.0;
+    memset(Ke, 0, sizeof(double) * 576);
+    for (int g = 0; g < 8; ++g) {
+        strain_at(g, h, B);
+        double SB[6][24];
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 24; ++j) {
+                double v = 0;
+                for (int k = 0; k < 6; ++k) v += S[i][k] * B[k][j];
+                SB[i][j] = v * w;
+            }
+        for (int r = 0; r < 24; ++r)
+            for (int c = 0; c < 24; ++c) {
+                double v = 0;
+                for (int k = 0; k < 6; ++k) v += B[k][r] * SB[k][c];
+                Ke[r + 24 * c] += v;
+            }
+    }
+}
+
+// stress matrix M (48 x 24, column-major): corner stresses = M u_e
+// (FEA_StressAnalysis.m:43-45: inv(sFM) * D * B).
+void stress_matrix(double nu, double h, double M[48 * 24]) {
+    double N[8][8];   // N[g][n] shape function n at Gauss point g
+    for (int g = 0; g < 8; ++g)
+        for (int n = 0; n < 8; ++n)
+            N[g][n] = 0.125 * (1 + kNs[n] * kGs[g]) * (1 + kNt[n] * kGt[g]) * (1 + kNp[n] * kGp[g]);
+    // invert N (8x8) by Gauss-Jordan with partial pivoting
+    double A[8][16];
+    for (int i = 0; i < 8; ++i)
+        for (int j = 0; j < 16; ++j) A[i][j] = j < 8 ? N[i][j] : (j - 8 == i ? 1.0 : 0.0);
+    for (int c = 0; c < 8; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < 8; ++r)
+            if (fabs(A[r][c]) > fabs(A[piv][c])) piv = r;
+        for (int j = 0; j < 16; ++j) std::swap(A[c][j], A[piv][j]);
+        const double d = A[c][c];
+        for (int j = 0; j < 16; ++j) A[c][j] /= d;
+        for (int r = 0; r < 8; ++r)
+            if (r != c) {
+                const double f = A[r][c];
+                for (int j = 0; j < 16; ++j) A[r][j] -= f * A[c][j];
+            }
+    }
+    double S[6][6], B[6][24], SB[8][6][24];
+    hooke(nu, S);
+    for (int g = 0; g < 8; ++g) {
+        strain_at(g, h, B);
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 24; ++j) {
+                double v = 0;
+                for (int k = 0; k < 6; ++k) v += S[i][k] * B[k][j];
+                SB[g][i][j] = v;
+            }
+    }
+    for (int n = 0; n < 8; ++n)
+        for (int k = 0; k < 6; ++k)
+            for (int j = 0; j < 24; ++j) {
+                double v = 0;
+                for (int g = 0; g < 8; ++g) v += A[n][8 + g] * SB[g][k][j];
+                M[(6 * n + k) + 48 * j] = v;
+            }
+}
+
+// Ke in the Hadamard basis: verify the isotropic block structure and extract
+// the 45 values in the kernels' block order.
+const int kBlk[11][3] = {{3, 7, 14}, {4, 6, -1}, {5, 12, -1}, {8, 13, -1}, {9, 20, -1}, {10, 17, -1},
+                         {11, 16, 18}, {15, 19, -1}, {21, -1, -1}, {22, -1, -1}, {23, -1, -1}};
+
+bool hadamard_blocks(const double *Ke, double Kh45[KH_NNZ], std::string &why) {
+    const int kmap[8] = {0, 1, 3, 2, 4, 5, 7, 6};   // reference corner -> bit index (ks | kt<<1 | kp<<2)
+    double Kb[24][24];
+    for (int j = 0; j < 8; ++j)
+        for (int c = 0; c < 3; ++c)
+            for (int jj = 0; jj < 8; ++jj)
+                for (int cc = 0; cc < 3; ++cc)
+                    Kb[3 * kmap[j] + c][3 * kmap[jj] + cc] = Ke[(3 * j + c) + 24 * (3 * jj + cc)];
+    double H[8][8];
+    for (int m = 0; m < 8; ++m)
+        for (int k = 0; k < 8; ++k) {
+            double v = 1;
+            for (int ax = 0; ax < 3; ++ax)
+                if ((m >> ax) & 1) v *= (((k >> ax) & 1) ? 1.0 : -1.0);
+            H[m][k] = v;
+        }
+    double T[24][24], Kh[24][24];
+    for (int r = 0; r < 24; ++r)
+        for (int c = 0; c < 24; ++c) {
+            double v = 0;
+            for (int k = 0; k < 8; ++k) v += H[r / 3][k] * Kb[3 * k + r % 3][c];
+            T[r][c] = v;
+        }
+    double mx = 0;
+    for (int r = 0; r < 24; ++r)
+        for (int c = 0; c < 24; ++c) {
+            double v = 0;
+            for (int k = 0; k < 8; ++k) v += T[r][3 * k + c % 3] * H[c / 3][k];
+            Kh[r][c] = v / 64.0;
+            mx = std::max(mx, fabs(Kh[r][c]));
+        }
+    bool in[24][24] = {};
+    int o = 0;
+    for (auto &b : kBlk) {
+        int n = 0;
+        while (n < 3 && b[n] >= 0) ++n;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                in[b[i]][b[j]] = true;
+                Kh45[o++] = Kh[b[i]][b[j]];
+            }
+    }
+    for (int r = 0; r < 24; ++r)
+        for (int c = 0; c < 24; ++c) {
+            if (!in[r][c] && fabs(Kh[r][c]) > 1e-12 * mx) {
+                why = "element matrix does not have the isotropic hexahedral structure";
+                return false;
+            }
+            if (fabs(Kh[r][c] - Kh[c][r]) > 1e-12 * mx) {
+                why = "element matrix is not symmetric";
+                return false;
+            }
+        }
+    return true;
+}
+
+// level-2 templates H_q = P_q' Ke P_q for span s (column-major, q = child index, y fastest)
+void make_templates(const double *Ke, int s, std::vector<double> &H) {
+    const int nq = s * s * s;
+    H.assign((size_t)nq * 576, 0.0);
+    for (int q = 0; q < nq; ++q) {
+        const int oy = q % s, ox = (q / s) % s, oz = q / (s * s);
+        double W[8][8];
+        for (int j = 0; j < 8; ++j) {
+            const double py = oy + kCdy[j], px = ox + kCdx[j], pz = oz + kCdz[j];
+            const double sn = -1.0 + 2.0 * px / s, tn = 1.0 - 2.0 * py / s, pn = -1.0 + 2.0 * pz / s;
+            for (int a = 0; a < 8; ++a) W[j][a] = 0.125 * (1 + kNs[a] * sn) * (1 + kNt[a] * tn) * (1 + kNp[a] * pn);
+        }
+        double KP[24][24];   // Ke P_q
+        for (int r = 0; r < 24; ++r)
+            for (int a = 0; a < 8; ++a)
+                for (int d = 0; d < 3; ++d) {
+                    double v = 0;
+                    for (int k = 0; k < 8; ++k) v += Ke[r + 24 * (3 * k + d)] * W[k][a];
+                    KP[r][3 * a + d] = v;
+                }
+        double *h = H.data() + 576 * (size_t)q;
+        for (int b = 0; b < 8; ++b)
+            for (int c = 0; c < 3; ++c)
+                for (int col = 0; col < 24; ++col) {
+                    double v = 0;
+                    for (int j = 0; j < 8; ++j) v += W[j][b] * KP[3 * j + c][col];
+                    h[(3 * b + c) + 24 * col] = v;
+                }
+    }
+}
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    return cudaMalloc((void **)p, n * sizeof(T));
+}
+
+int fail(sgld_ctx *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->c.err = msg;
+    return code;
+}
+
+#define CK(x)                                                                                            \
+    do {                                                                                                 \
+        cudaError_t e_ = (x);                                                                            \
+        if (e_ != cudaSuccess) return fail(ctx, e_ == cudaErrorMemoryAllocation ? SGLD_ERR_NOMEM : SGLD_ERR_CUDA, \
+                                           std::string(#x) + ": " + cudaGetErrorString(e_));             \
+    } while (0)
+#define CKL()                                                                                            \
+    do {                                                                                                 \
+        cudaError_t e_ = cudaGetLastError();                                                             \
+        if (e_ != cudaSuccess) return fail(ctx, SGLD_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+int setup_templates(sgld_ctx *ctx) {
+    Ctx &c = ctx->c;
+    std::vector<double> H;
+    const int s = c.lv[1].span;
+    make_templates(c.Ke, s, H);
+    if (c.d_H) cudaFree(c.d_H);
+    CK(dalloc(&c.d_H, H.size()));
+    CK(cudaMemcpy(c.d_H, H.data(), H.size() * sizeof(double), cudaMemcpyHostToDevice));
+    upload_kh(c.Kh, c.stream);
+    return SGLD_OK;
+}
+
+// device V-cycle on full-grid vectors (Solving_Vcycle.m:12-50); partial dot z.r
+int vcycle_dev(sgld_ctx *ctx, const double *r, double *z, double *partial, int *nb) {
+    Ctx &c = ctx->c;
+    const int L = c.L;
+    const double *rf = r;
+    for (int l = 1; l < L; ++l) {
+        launch_restrict<double>(c.lv[l - 1], c.lv[l], rf, c.lv[l].r, c.stream);
+        rf = c.lv[l].r;
+    }
+    launch_coarse_apply_f64(c, c.lv[L - 1].r, c.lv[L - 1].x, c.stream);
+    for (int l = L - 2; l >= 0; --l) {
+        const double *rl = (l == 0) ? r : c.lv[l].r;
+        double *xl = (l == 0) ? z : c.lv[l].x;
+        launch_prolong_smooth<double>(c.lv[l], c.lv[l + 1], c.lv[l + 1].x, rl, c.lv[l].diag, c.omega, xl, l == 0,
+                                      l == 0 ? partial : nullptr, l == 0 ? nb : nullptr, c.stream);
+    }
+    CKL();
+    return SGLD_OK;
+}
+
+int check_ready(sgld_ctx *ctx) {
+    if (!ctx) return SGLD_ERR_ARG;
+    if (!ctx->c.have_fixed) return fail(ctx, SGLD_ERR_STATE, "fixed DOFs not set (sgld_set_fixed_dofs)");
+    if (!ctx->c.have_E) return fail(ctx, SGLD_ERR_STATE, "element moduli not set (sgld_set_modulus)");
+    return SGLD_OK;
+}
+
+int check_assembled(sgld_ctx *ctx) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!ctx->c.assembled) return fail(ctx, SGLD_ERR_STATE, "stencil not assembled (sgld_assemble)");
+    return SGLD_OK;
+}
+
+// host compact -> device full (zeroed first)
+int upload_nodes(sgld_ctx *ctx, const double *h, double *d_full) {
+    Ctx &c = ctx->c;
+    const int64_t n = (int64_t)c.h_nodemap.size();
+    CK(cudaMemsetAsync(d_full, 0, sizeof(double) * 3 * c.lv[0].nnode, c.stream));
+    CK(cudaMemcpyAsync(c.d_tmp, h, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c.stream));
+    launch_scatter_nodes(c.d_nodemap, n, c.d_tmp, d_full, c.stream);
+    CKL();
+    return SGLD_OK;
+}
+
+int download_nodes(sgld_ctx *ctx, const double *d_full, double *h) {
+    Ctx &c = ctx->c;
+    const int64_t n = (int64_t)c.h_nodemap.size();
+    launch_gather_nodes(c.d_nodemap, n, d_full, c.d_tmp, c.stream);
+    CKL();
+    CK(cudaMemcpyAsync(h, c.d_tmp, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    return SGLD_OK;
+}
+
+int pcg_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info);
+
+}  // namespace
+
+// =============================================================================
+extern "C" {
+
+void sgld_default_options(sgld_options *o) {
+    if (!o) return;
+    o->num_levels = 0;
+    o->non_dyadic = 1;
+    o->poisson_ratio = 0.3;
+    o->cell_size = 1.0;
+    o->omega = 0.35;
+    o->device = 0;
+}
+
+int sgld_reference_num_levels(int64_t num_voxels, int64_t crc) {
+    // FEA_VoxelBasedDiscretization.m:168-177 (MATLAB round = half away from zero)
+    auto mround = [](double x) { return (int64_t)floor(x + 0.5); };
+    crc = std::min<int64_t>(crc, mround((double)mround(num_voxels / 8.0) / 8.0));
+    if (crc <= 0) return -1;
+    int L = 0;
+    int64_t nv = num_voxels;
+    while (nv >= crc) {
+        ++L;
+        nv = mround(nv / 8.0);
+    }
+    return L + 1;
+}
+
+const char *sgld_last_error(const sgld_ctx *ctx) { return ctx ? ctx->c.err.c_str() : "null context"; }
+
+int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_options *opts, sgld_ctx **out) {
+    if (!out || !solid || resX <= 0 || resY <= 0 || resZ <= 0) return SGLD_ERR_ARG;
+    *out = nullptr;
+    sgld_options o;
+    sgld_default_options(&o);
+    if (opts) o = *opts;
+    auto *ctx = new sgld_ctx;
+    Ctx &c = ctx->c;
+    c.nu = o.poisson_ratio;
+    c.cell = o.cell_size;
+    c.omega = o.omega;
+    c.device = o.device;
+    int L = o.num_levels;
+    int nd = o.non_dyadic;
+    if (nd == 1 && L >= 4)
+        L -= 1;
+    else
+        nd = 0;
+    if (L < 2) {
+        int rc = fail(ctx, SGLD_ERR_ARG, "at least two multigrid levels are required");
+        *out = ctx;
+        return rc;
+    }
+    c.L = L;
+    c.non_dyadic = nd;
+    c.lv.resize(L);
+    int ny = resY, nx = resX, nz = resZ;
+    for (int l = 0; l < L; ++l) {
+        const int s = (l == 0) ? 1 : ((l == 1 && nd) ? 4 : 2);
+        if (l > 0) {
+            if (ny % s || nx % s || nz % s) {
+                int rc = fail(ctx, SGLD_ERR_ARG, "grid resolution is not divisible by the coarsening factors");
+                *out = ctx;
+                return rc;
+            }
+            ny /= s;
+            nx /= s;
+            nz /= s;
+        }
+        Level &lv = c.lv[l];
+        lv.nx = nx;
+        lv.ny = ny;
+        lv.nz = nz;
+        lv.span = s;
+        lv.nel = (int64_t)nx * ny * nz;
+        lv.nnode = (int64_t)(nx + 1) * (ny + 1) * (nz + 1);
+    }
+    *out = ctx;
+    if (cudaSetDevice(c.device) != cudaSuccess) return fail(ctx, SGLD_ERR_CUDA, "cudaSetDevice failed");
+    CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    // element / node activity per level (host)
+    ctx->nodemaps.resize(L);
+    ctx->elemaps.resize(L);
+    for (int l = 0; l < L; ++l) {
+        Level &lv = c.lv[l];
+        lv.h_eact.assign(lv.nel, 0);
+        if (l == 0) {
+            for (int64_t e = 0; e < lv.nel; ++e) lv.h_eact[e] = solid[e] ? 1 : 0;
+        } else {
+            const Level &f = c.lv[l - 1];
+            const int s = lv.span;
+            for (int64_t fz = 0; fz < f.nz; ++fz)
+                for (int64_t fx = 0; fx < f.nx; ++fx)
+                    for (int64_t fy = 0; fy < f.ny; ++fy)
+                        if (f.h_eact[fy + f.ny * (fx + f.nx * fz)])
+                            lv.h_eact[(fy / s) + lv.ny * ((fx / s) + lv.nx * (fz / s))] = 1;
+        }
+        lv.h_nflag.assign(lv.nnode, 0);
+        const int64_t NY = lv.ny + 1, NX = lv.nx + 1;
+        for (int64_t ez = 0; ez < lv.nz; ++ez)
+            for (int64_t ex = 0; ex < lv.nx; ++ex)
+                for (int64_t ey = 0; ey < lv.ny; ++ey)
+                    if (lv.h_eact[ey + lv.ny * (ex + lv.nx * ez)])
+                        for (int j = 0; j < 8; ++j)
+                            lv.h_nflag[(ey + kCdy[j]) + NY * ((ex + kCdx[j]) + NX * (ez + kCdz[j]))] = NF_ACTIVE;
+        auto &nm = ctx->nodemaps[l];
+        auto &em = ctx->elemaps[l];
+        for (int64_t n = 0; n < lv.nnode; ++n)
+            if (lv.h_nflag[n]) nm.push_back(n);
+        for (int64_t e = 0; e < lv.nel; ++e)
+            if (lv.h_eact[e]) em.push_back(e);
+        lv.nel_active = (int64_t)em.size();
+        lv.nnode_active = (int64_t)nm.size();
+        CK(dalloc(&lv.eact, lv.nel));
+        CK(dalloc(&lv.nflag, lv.nnode));
+        CK(cudaMemcpy(lv.eact, lv.h_eact.data(), lv.nel, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(lv.nflag, lv.h_nflag.data(), lv.nnode, cudaMemcpyHostToDevice));
+        if (l < L - 1) {
+            CK(dalloc(&lv.diag, 3 * lv.nnode));
+            CK(dalloc(&lv.diag32, 3 * lv.nnode));
+        }
+        if (l > 0) {
+            CK(dalloc(&lv.Ks, 576 * (size_t)lv.nel));
+            CK(dalloc(&lv.r, 3 * lv.nnode));
+            CK(dalloc(&lv.x, 3 * lv.nnode));
+            CK(dalloc(&lv.r32, 3 * lv.nnode));
+            CK(dalloc(&lv.x32, 3 * lv.nnode));
+        }
+    }
+    if (c.lv[0].nel_active == 0) return fail(ctx, SGLD_ERR_ARG, "the voxel grid has no solid voxel");
+    c.h_nodemap = ctx->nodemaps[0];
+    c.h_elemap = ctx->elemaps[0];
+    CK(dalloc(&c.d_nodemap, c.h_nodemap.size()));
+    CK(dalloc(&c.d_elemap, c.h_elemap.size()));
+    CK(cudaMemcpy(c.d_nodemap, c.h_nodemap.data(), c.h_nodemap.size() * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c.d_elemap, c.h_elemap.data(), c.h_elemap.size() * 8, cudaMemcpyHostToDevice));
+    const Level &l0 = c.lv[0];
+    const size_t nv = 3 * (size_t)l0.nnode;
+    CK(dalloc(&c.E, l0.nel));
+    CK(cudaMemset(c.E, 0, sizeof(double) * l0.nel));
+    CK(dalloc(&c.d_E32, l0.nel));
+    for (double **p : {&c.d_b, &c.d_x, &c.d_r, &c.d_z, &c.d_p, &c.d_q, &c.d_tmp}) CK(dalloc(p, nv));
+    CK(dalloc(&c.d_r32, nv));
+    CK(dalloc(&c.d_z32, nv));
+    c.npart = (int)std::max<int64_t>({(int64_t)152 * 8, (l0.nel + 255) / 256 + 1, (l0.nnode + 255) / 256 + 1,
+                                      (int64_t)((l0.ny + 31) / 31 + 1) * ((l0.nx + 7) / 7 + 1) * ((l0.nz + 16) / 16 + 1)});
+    CK(dalloc(&c.d_part, c.npart));
+    CK(dalloc(&c.d_scal, 64));
+    CK(dalloc(&c.d_iflag, 64));
+    CK(cudaMemset(c.d_iflag, 0, 64 * sizeof(int)));
+    element_stiffness(c.nu, c.cell, c.Ke);
+    std::string why;
+    if (!hadamard_blocks(c.Ke, c.Kh, why)) return fail(ctx, SGLD_ERR_ARG, why);
+    return setup_templates(ctx);
+}
+
+void sgld_destroy(sgld_ctx *ctx) {
+    if (!ctx) return;
+    Ctx &c = ctx->c;
+    for (Level &l : c.lv) {
+        for (void *p : {(void *)l.eact, (void *)l.nflag, (void *)l.diag, (void *)l.diag32, (void *)l.Ks, (void *)l.r,
+                        (void *)l.x, (void *)l.r32, (void *)l.x32})
+            if (p) cudaFree(p);
+    }
+    for (void *p : {(void *)c.d_nodemap, (void *)c.d_elemap, (void *)c.E, (void *)c.d_E32, (void *)c.d_b,
+                    (void *)c.d_x, (void *)c.d_r, (void *)c.d_z, (void *)c.d_p, (void *)c.d_q, (void *)c.d_tmp,
+                    (void *)c.d_r32, (void *)c.d_z32, (void *)c.d_part, (void *)c.d_scal, (void *)c.d_iflag,
+                    (void *)c.d_Ac, (void *)c.d_Ainv, (void *)c.d_Ainv32, (void *)c.d_cpart, (void *)c.d_cfree,
+                    (void *)c.d_H, (void *)ctx->d_s6, (void *)ctx->d_vmn, (void *)ctx->d_vme})
+        if (p) cudaFree(p);
+    if (c.stream) cudaStreamDestroy(c.stream);
+    delete ctx;
+}
+
+int sgld_num_levels(const sgld_ctx *ctx) { return ctx ? ctx->c.L : -1; }
+
+int sgld_level_info(const sgld_ctx *ctx, int level, int res[3], int *span, int64_t *ne, int64_t *nn) {
+    if (!ctx || level < 1 || level > ctx->c.L) return SGLD_ERR_ARG;
+    const Level &l = ctx->c.lv[level - 1];
+    if (res) {
+        res[0] = l.ny;
+        res[1] = l.nx;
+        res[2] = l.nz;
+    }
+    if (span) *span = l.span;
+    if (ne) *ne = l.nel_active;
+    if (nn) *nn = l.nnode_active;
+    return SGLD_OK;
+}
+
+int sgld_node_map(const sgld_ctx *ctx, int level, int64_t *map) {
+    if (!ctx || !map || level < 1 || level > ctx->c.L) return SGLD_ERR_ARG;
+    const auto &m = ctx->nodemaps[level - 1];
+    for (size_t i = 0; i < m.size(); ++i) map[i] = m[i] + 1;
+    return SGLD_OK;
+}
+
+int sgld_element_map(const sgld_ctx *ctx, int level, int64_t *map) {
+    if (!ctx || !map || level < 1 || level > ctx->c.L) return SGLD_ERR_ARG;
+    const auto &m = ctx->elemaps[level - 1];
+    for (size_t i = 0; i < m.size(); ++i) map[i] = m[i] + 1;
+    return SGLD_OK;
+}
+
+int sgld_get_ke(const sgld_ctx *ctx, double *Ke) {
+    if (!ctx || !Ke) return SGLD_ERR_ARG;
+    memcpy(Ke, ctx->c.Ke, sizeof(double) * 576);
+    return SGLD_OK;
+}
+
+int sgld_set_ke(sgld_ctx *ctx, const double *Ke) {
+    if (!ctx || !Ke) return SGLD_ERR_ARG;
+    double Kh[KH_NNZ];
+    std::string why;
+    if (!hadamard_blocks(Ke, Kh, why)) return fail(ctx, SGLD_ERR_ARG, why);
+    memcpy(ctx->c.Ke, Ke, sizeof(double) * 576);
+    memcpy(ctx->c.Kh, Kh, sizeof Kh);
+    ctx->c.assembled = false;
+    return setup_templates(ctx);
+}
+
+int sgld_set_fixed_dofs(sgld_ctx *ctx, const uint8_t *fixed) {
+    if (!ctx || !fixed) return SGLD_ERR_ARG;
+    Ctx &c = ctx->c;
+    Level &l0 = c.lv[0];
+    for (int64_t n = 0; n < l0.nnode; ++n) l0.h_nflag[n] &= NF_ACTIVE;
+    for (size_t i = 0; i < c.h_nodemap.size(); ++i)
+        for (int d = 0; d < 3; ++d)
+            if (fixed[3 * i + d]) l0.h_nflag[c.h_nodemap[i]] |= (uint8_t)(NF_FIXX << d);
+    CK(cudaMemcpy(l0.nflag, l0.h_nflag.data(), l0.nnode, cudaMemcpyHostToDevice));
+    // coarse masks: restrict the fixed indicator level by level (FEA_SetupVoxelBased.m:13-26)
+    launch_fixed_indicator(l0, c.d_tmp, c.stream);
+    const double *v = c.d_tmp;
+    for (int l = 1; l < c.L; ++l) {
+        launch_restrict<double>(c.lv[l - 1], c.lv[l], v, c.lv[l].r, c.stream);
+        launch_mark_fixed(c.lv[l], c.lv[l].r, c.stream);
+        v = c.lv[l].r;
+    }
+    CKL();
+    for (int l = 1; l < c.L; ++l)
+        CK(cudaMemcpyAsync(c.lv[l].h_nflag.data(), c.lv[l].nflag, c.lv[l].nnode, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    // coarsest free DOFs in a bandwidth-reducing order: slowest axis = longest
+    const Level &lc = c.lv[c.L - 1];
+    const int64_t NY = lc.ny + 1, NX = lc.nx + 1, NZ = lc.nz + 1;
+    int ax[3] = {0, 1, 2};                    // 0 = y, 1 = x, 2 = z
+    const int64_t dimn[3] = {NY, NX, NZ};
+    std::sort(ax, ax + 3, [&](int a, int b) { return dimn[a] < dimn[b]; });   // fastest first
+    std::vector<std::pair<int64_t, int>> order;   // (key, dof)
+    for (int64_t n = 0; n < lc.nnode; ++n) {
+        const uint8_t f = lc.h_nflag[n];
+        if (!(f & NF_ACTIVE)) continue;
+        const int64_t co[3] = {n % NY, (n / NY) % NX, n / (NY * NX)};
+        const int64_t key = co[ax[0]] + dimn[ax[0]] * (co[ax[1]] + dimn[ax[1]] * co[ax[2]]);
+        for (int d = 0; d < 3; ++d)
+            if (!(f & (NF_FIXX << d))) order.push_back({3 * key + d, (int)(3 * n + d)});
+    }
+    std::sort(order.begin(), order.end());
+    const int ncf = (int)order.size();
+    std::vector<int> rows(ncf), pos(3 * lc.nnode, -1);
+    for (int i = 0; i < ncf; ++i) {
+        rows[i] = order[i].second;
+        pos[rows[i]] = i;
+    }
+    // half bandwidth over the element connectivity
+    int band = 0;
+    for (int64_t ez = 0; ez < lc.nz; ++ez)
+        for (int64_t ex = 0; ex < lc.nx; ++ex)
+            for (int64_t ey = 0; ey < lc.ny; ++ey) {
+                if (!lc.h_eact[ey + lc.ny * (ex + lc.nx * ez)]) continue;
+                int lo = ncf, hi = -1;
+                for (int j = 0; j < 8; ++j) {
+                    const int64_t m = (ey + kCdy[j]) + NY * ((ex + kCdx[j]) + NX * (ez + kCdz[j]));
+                    for (int d = 0; d < 3; ++d) {
+                        const int p = pos[3 * m + d];
+                        if (p >= 0) {
+                            lo = std::min(lo, p);
+                            hi = std::max(hi, p);
+                        }
+                    }
+                }
+                if (hi >= lo) band = std::max(band, hi - lo);
+            }
+    ctx->h_rows = rows;
+    if (ncf != c.ncf) {
+        for (void *p : {(void *)c.d_Ac, (void *)c.d_Ainv, (void *)c.d_Ainv32, (void *)c.d_cpart, (void *)c.d_cfree})
+            if (p) cudaFree(p);
+        c.d_Ac = c.d_Ainv = nullptr;
+        c.d_Ainv32 = nullptr;
+        c.d_cpart = nullptr;
+        c.d_cfree = nullptr;
+        c.ncf = ncf;
+        CK(dalloc(&c.d_Ac, (size_t)ncf * ncf));
+        CK(dalloc(&c.d_Ainv, (size_t)ncf * ncf));
+        CK(dalloc(&c.d_Ainv32, (size_t)ncf * ncf));
+        CK(dalloc(&c.d_cpart, (size_t)CSPLIT * ncf));
+    }
+    if (!c.d_cfree) CK(dalloc(&c.d_cfree, (size_t)ncf + 3 * lc.nnode));
+    CK(cudaMemcpy(c.d_cfree, rows.data(), sizeof(int) * ncf, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c.d_cfree + ncf, pos.data(), sizeof(int) * 3 * lc.nnode, cudaMemcpyHostToDevice));
+    c.cband = band;
+    c.have_fixed = true;
+    c.assembled = false;
+    return SGLD_OK;
+}
+
+int sgld_get_free_dofs(const sgld_ctx *ctx, int level, uint8_t *free_mask) {
+    if (!ctx || !free_mask || level < 1 || level > ctx->c.L) return SGLD_ERR_ARG;
+    const Level &l = ctx->c.lv[level - 1];
+    const auto &m = ctx->nodemaps[level - 1];
+    for (size_t i = 0; i < m.size(); ++i)
+        for (int d = 0; d < 3; ++d) free_mask[3 * i + d] = (l.h_nflag[m[i]] & (NF_FIXX << d)) ? 0 : 1;
+    return SGLD_OK;
+}
+
+int sgld_set_modulus_device(sgld_ctx *ctx, const double *d_E) {
+    if (!ctx || !d_E) return SGLD_ERR_ARG;
+    Ctx &c = ctx->c;
+    CK(cudaMemsetAsync(c.E, 0, sizeof(double) * c.lv[0].nel, c.stream));
+    launch_scatter_elems(c.d_elemap, (int64_t)c.h_elemap.size(), d_E, c.E, c.stream);
+    CKL();
+    CK(cudaStreamSynchronize(c.stream));
+    c.have_E = true;
+    c.assembled = false;
+    return SGLD_OK;
+}
+
+int sgld_set_modulus(sgld_ctx *ctx, const double *E) {
+    if (!ctx || !E) return SGLD_ERR_ARG;
+    Ctx &c = ctx->c;
+    CK(cudaMemcpyAsync(c.d_tmp, E, sizeof(double) * c.h_elemap.size(), cudaMemcpyHostToDevice, c.stream));
+    return sgld_set_modulus_device(ctx, c.d_tmp);
+}
+
+int sgld_assemble(sgld_ctx *ctx) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    Ctx &c = ctx->c;
+    const int L = c.L;
+    launch_diag_finest(c.lv[0], c.E, c.Ke, c.lv[0].diag, c.stream);
+    for (int l = 1; l < L; ++l) {
+        if (l == 1)
+            launch_asm_finest(c.lv[1], c.lv[0], c.E, c.d_H, c.lv[1].Ks, c.stream);
+        else
+            launch_asm_coarse(c.lv[l], c.lv[l - 1], c.lv[l].Ks, c.stream);
+        if (l < L - 1) launch_diag_from_Ks(c.lv[l], c.lv[l].diag, c.stream);
+    }
+    CKL();
+    launch_coarse_dense(c.lv[L - 1], c.ncf, c.d_cfree, c.d_Ac, c.stream);
+    CKL();
+    const int info = coarse_factor_invert(c);
+    CKL();
+    CK(cudaStreamSynchronize(c.stream));
+    if (info != 0)
+        return fail(ctx, SGLD_ERR_NUMERIC,
+                    "coarsest-level matrix is not positive definite (pivot " + std::to_string(info) + ")");
+    for (int l = 0; l < L - 1; ++l) launch_cast_f32(c.lv[l].diag, c.lv[l].diag32, 3 * c.lv[l].nnode, c.stream);
+    launch_cast_f32(c.E, c.d_E32, c.lv[0].nel, c.stream);
+    CKL();
+    CK(cudaStreamSynchronize(c.stream));
+    c.assembled = true;
+    return SGLD_OK;
+}
+
+int sgld_get_diag(const sgld_ctx *cctx, int level, double *diag) {
+    auto *ctx = const_cast<sgld_ctx *>(cctx);
+    if (!ctx || !diag || level < 1 || level >= ctx->c.L) return SGLD_ERR_ARG;
+    const Level &l = ctx->c.lv[level - 1];
+    std::vector<double> full(3 * l.nnode);
+    CK(cudaMemcpy(full.data(), l.diag, sizeof(double) * full.size(), cudaMemcpyDeviceToHost));
+    const auto &m = ctx->nodemaps[level - 1];
+    for (size_t i = 0; i < m.size(); ++i)
+        for (int d = 0; d < 3; ++d) diag[3 * i + d] = full[3 * m[i] + d];
+    return SGLD_OK;
+}
+
+int sgld_get_ks(const sgld_ctx *cctx, int level, double *Ks) {
+    auto *ctx = const_cast<sgld_ctx *>(cctx);
+    if (!ctx || !Ks || level < 2 || level > ctx->c.L) return SGLD_ERR_ARG;
+    const Level &l = ctx->c.lv[level - 1];
+    const auto &m = ctx->elemaps[level - 1];
+    for (size_t i = 0; i < m.size(); ++i)
+        CK(cudaMemcpy(Ks + 576 * i, l.Ks + 576 * m[i], sizeof(double) * 576, cudaMemcpyDeviceToHost));
+    return SGLD_OK;
+}
+
+int sgld_kbyu_device(sgld_ctx *ctx, const double *d_u, double *d_y) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    Ctx &c = ctx->c;
+    const int64_t n = (int64_t)c.h_nodemap.size();
+    CK(cudaMemsetAsync(c.d_p, 0, sizeof(double) * 3 * c.lv[0].nnode, c.stream));
+    launch_scatter_nodes(c.d_nodemap, n, d_u, c.d_p, c.stream);
+    launch_kbyu_f64(c.lv[0], c.E, c.d_p, c.d_q, nullptr, nullptr, c.stream);
+    launch_gather_nodes(c.d_nodemap, n, c.d_q, d_y, c.stream);
+    CKL();
+    CK(cudaStreamSynchronize(c.stream));
+    return SGLD_OK;
+}
+
+int sgld_kbyu(sgld_ctx *ctx, const double *u, double *y) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!u || !y) return fail(ctx, SGLD_ERR_ARG, "null vector");
+    Ctx &c = ctx->c;
+    if ((rc = upload_nodes(ctx, u, c.d_p))) return rc;
+    launch_kbyu_f64(c.lv[0], c.E, c.d_p, c.d_q, nullptr, nullptr, c.stream);
+    CKL();
+    return download_nodes(ctx, c.d_q, y);
+}
+
+static int level_vec_to_dev(sgld_ctx *ctx, int l, const double *h, double *d_full) {
+    Ctx &c = ctx->c;
+    const Level &lv = c.lv[l];
+    std::vector<double> full(3 * lv.nnode, 0.0);
+    const auto &m = ctx->nodemaps[l];
+    for (size_t i = 0; i < m.size(); ++i)
+        for (int d = 0; d < 3; ++d) full[3 * m[i] + d] = h[3 * i + d];
+    CK(cudaMemcpy(d_full, full.data(), sizeof(double) * full.size(), cudaMemcpyHostToDevice));
+    return SGLD_OK;
+}
+
+static int level_vec_to_host(sgld_ctx *ctx, int l, const double *d_full, double *h) {
+    Ctx &c = ctx->c;
+    const Level &lv = c.lv[l];
+    CK(cudaStreamSynchronize(c.stream));
+    std::vector<double> full(3 * lv.nnode);
+    CK(cudaMemcpy(full.data(), d_full, sizeof(double) * full.size(), cudaMemcpyDeviceToHost));
+    const auto &m = ctx->nodemaps[l];
+    for (size_t i = 0; i < m.size(); ++i)
+        for (int d = 0; d < 3; ++d) h[3 * i + d] = full[3 * m[i] + d];
+    return SGLD_OK;
+}
+
+int sgld_restrict(sgld_ctx *ctx, int ii, const double *rf, double *rc_out) {
+    if (!ctx || !rf || !rc_out || ii < 2 || ii > ctx->c.L) return SGLD_ERR_ARG;
+    Ctx &c = ctx->c;
+    const int l = ii - 1;
+    int rc;
+    double *fin = (l - 1 == 0) ? c.d_r : c.lv[l - 1].x;
+    if ((rc = level_vec_to_dev(ctx, l - 1, rf, fin))) return rc;
+    launch_restrict<double>(c.lv[l - 1], c.lv[l], fin, c.lv[l].r, c.stream);
+    CKL();
+    return level_vec_to_host(ctx, l, c.lv[l].r, rc_out);
+}
+
+int sgld_interpolate(sgld_ctx *ctx, int ii, const double *xc, double *xf) {
+    if (!ctx || !xc || !xf || ii < 2 || ii > ctx->c.L) return SGLD_ERR_ARG;
+    Ctx &c = ctx->c;
+    const int l = ii - 1;
+    int rc;
+    if ((rc = level_vec_to_dev(ctx, l, xc, c.lv[l].x))) return rc;
+    // P x with t = 0: zero residual, unit diagonal
+    const Level &f = c.lv[l - 1];
+    double *rzero = c.d_tmp, *ones = c.d_q, *out = c.d_z;
+    CK(cudaMemsetAsync(rzero, 0, sizeof(double) * 3 * f.nnode, c.stream));
+    std::vector<double> one(3 * f.nnode, 1.0);
+    CK(cudaMemcpy(ones, one.data(), sizeof(double) * one.size(), cudaMemcpyHostToDevice));
+    launch_prolong_smooth<double>(f, c.lv[l], c.lv[l].x, rzero, ones, 0.0, out, false, nullptr, nullptr, c.stream);
+    CKL();
+    return level_vec_to_host(ctx, l - 1, out, xf);
+}
+
+int sgld_vcycle(sgld_ctx *ctx, const double *r, double *z) {
+    int rc = check_assembled(ctx);
+    if (rc) return rc;
+    if (!r || !z) return fail(ctx, SGLD_ERR_ARG, "null vector");
+    Ctx &c = ctx->c;
+    if ((rc = upload_nodes(ctx, r, c.d_r))) return rc;
+    if ((rc = vcycle_dev(ctx, c.d_r, c.d_z, nullptr, nullptr))) return rc;
+    return download_nodes(ctx, c.d_z, z);
+}
+
+int sgld_pcg_device(sgld_ctx *ctx, const double *d_b, double *d_x, const sgld_solve_opts *o, sgld_solve_info *info) {
+    int rc = check_assembled(ctx);
+    if (rc) return rc;
+    if (!d_b || !d_x || !o) return fail(ctx, SGLD_ERR_ARG, "null argument");
+    Ctx &c = ctx->c;
+    const int64_t n = (int64_t)c.h_nodemap.size();
+    const size_t nv = 3 * (size_t)c.lv[0].nnode;
+    CK(cudaMemsetAsync(c.d_b, 0, sizeof(double) * nv, c.stream));
+    CK(cudaMemsetAsync(c.d_x, 0, sizeof(double) * nv, c.stream));
+    launch_scatter_nodes(c.d_nodemap, n, d_b, c.d_b, c.stream);
+    if (o->use_x0) launch_scatter_nodes(c.d_nodemap, n, d_x, c.d_x, c.stream);
+    CKL();
+    if ((rc = pcg_dev(ctx, o, info))) return rc;
+    launch_gather_nodes(c.d_nodemap, n, c.d_x, d_x, c.stream);
+    CKL();
+    CK(cudaStreamSynchronize(c.stream));
+    return SGLD_OK;
+}
+
+int sgld_pcg(sgld_ctx *ctx, const double *b, double *x, const sgld_solve_opts *o, sgld_solve_info *info) {
+    int rc = check_assembled(ctx);
+    if (rc) return rc;
+    if (!b || !x || !o) return fail(ctx, SGLD_ERR_ARG, "null argument");
+    Ctx &c = ctx->c;
+    if ((rc = upload_nodes(ctx, b, c.d_b))) return rc;
+    if (o->use_x0) {
+        if ((rc = upload_nodes(ctx, x, c.d_x))) return rc;
+    } else {
+        CK(cudaMemsetAsync(c.d_x, 0, sizeof(double) * 3 * c.lv[0].nnode, c.stream));
+    }
+    if ((rc = pcg_dev(ctx, o, info))) return rc;
+    return download_nodes(ctx, c.d_x, x);
+}
+
+int sgld_compliance(sgld_ctx *ctx, const double *U, double *ce, double *cval) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!U) return fail(ctx, SGLD_ERR_ARG, "null vector");
+    Ctx &c = ctx->c;
+    if ((rc = upload_nodes(ctx, U, c.d_z))) return rc;
+    int nb = 0;
+    launch_unit_compliance(c.lv[0], c.d_z, c.E, c.d_q, c.d_part, &nb, c.stream);
+    launch_finalize_sum(c.d_part, nb, c.d_scal + 16, c.stream);
+    CKL();
+    if (cval) CK(cudaMemcpyAsync(cval, c.d_scal + 16, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    if (ce) {
+        const int64_t ne = (int64_t)c.h_elemap.size();
+        launch_gather_elems(c.d_elemap, ne, c.d_q, c.d_tmp, c.stream);
+        CKL();
+        CK(cudaMemcpyAsync(ce, c.d_tmp, sizeof(double) * ne, cudaMemcpyDeviceToHost, c.stream));
+    }
+    CK(cudaStreamSynchronize(c.stream));
+    return SGLD_OK;
+}
+
+int sgld_stress(sgld_ctx *ctx, const double *U, double *nodal, double *vmn, double *vme) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!U) return fail(ctx, SGLD_ERR_ARG, "null vector");
+    Ctx &c = ctx->c;
+    const Level &l0 = c.lv[0];
+    if (!ctx->d_s6) {
+        CK(dalloc(&ctx->d_s6, 6 * (size_t)l0.nnode));
+        CK(dalloc(&ctx->d_vmn, (size_t)l0.nnode));
+        CK(dalloc(&ctx->d_vme, (size_t)l0.nel));
+    }
+    if ((rc = upload_nodes(ctx, U, c.d_z))) return rc;
+    double M[48 * 24];
+    stress_matrix(c.nu, c.cell, M);
+    launch_stress(l0, c.E, c.d_z, M, ctx->d_s6, ctx->d_vmn, c.stream);
+    launch_elem_vm(l0, ctx->d_s6, ctx->d_vme, c.stream);
+    CKL();
+    CK(cudaStreamSynchronize(c.stream));
+    const auto &nm = c.h_nodemap;
+    if (nodal || vmn) {
+        std::vector<double> s6(6 * l0.nnode), v(l0.nnode);
+        CK(cudaMemcpy(s6.data(), ctx->d_s6, sizeof(double) * s6.size(), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(v.data(), ctx->d_vmn, sizeof(double) * v.size(), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < nm.size(); ++i) {
+            if (nodal)
+                for (int k = 0; k < 6; ++k) nodal[6 * i + k] = s6[6 * nm[i] + k];
+            if (vmn) vmn[i] = v[nm[i]];
+        }
+    }
+    if (vme) {
+        const int64_t ne = (int64_t)c.h_elemap.size();
+        launch_gather_elems(c.d_elemap, ne, ctx->d_vme, c.d_tmp, c.stream);
+        CKL();
+        CK(cudaMemcpyAsync(vme, c.d_tmp, sizeof(double) * ne, cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaStreamSynchronize(c.stream));
+    }
+    return SGLD_OK;
+}
+
+}  // extern "C"
+
+// =============================================================================
+namespace {
+
+// FP64 PCG on the full-grid vectors in ctx (Solving_PreconditionedConjugateGradientSolver.m:7-36)
+int pcg_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
+    Ctx &c = ctx->c;
+    const Level &l0 = c.lv[0];
+    const int64_t nv = 3 * l0.nnode;
+    const int nbv = reduce_blocks(nv);
+    const double tol = o->tol;
+    const int maxit = o->maxit;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, c.stream));
+    int nb = 0;
+    launch_pcg_scalar(5, c.d_scal, c.d_iflag, c.d_part, 1, tol, maxit, c.stream);
+    launch_dot(c.d_b, c.d_b, nv, c.d_part, nbv, c.stream);
+    launch_pcg_scalar(0, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
+    if (o->use_x0) {
+        launch_kbyu_f64(l0, c.E, c.d_x, c.d_q, nullptr, nullptr, c.stream);
+        launch_residual(c.d_r, c.d_b, c.d_q, nv, c.stream);
+    } else {
+        CK(cudaMemcpyAsync(c.d_r, c.d_b, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c.stream));
+    }
+    int rc = vcycle_dev(ctx, c.d_r, c.d_z, c.d_part, &nb);
+    if (rc) return rc;
+    launch_pcg_scalar(1, c.d_scal, c.d_iflag, c.d_part, nb, tol, maxit, c.stream);
+    CK(cudaMemcpyAsync(c.d_p, c.d_z, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c.stream));
+    int h_flag[4] = {0, 0, 0, 0};
+    int its = 0;
+    const int poll = 1;
+    for (int k = 1; k <= maxit; ++k) {
+        launch_kbyu_f64(l0, c.E, c.d_p, c.d_q, c.d_part, &nb, c.stream);
+        launch_pcg_scalar(2, c.d_scal, c.d_iflag, c.d_part, nb, tol, maxit, c.stream);
+        launch_pcg_update(c.d_x, c.d_r, c.d_p, c.d_q, nv, c.d_scal, c.d_iflag, c.d_part, nbv, c.stream);
+        launch_pcg_scalar(3, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
+        if (o->history || (k % poll) == 0 || k == maxit) {
+            CK(cudaMemcpyAsync(h_flag, c.d_iflag, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.stream));
+            if (o->history) CK(cudaMemcpyAsync(o->history + (k - 1), c.d_scal + 3, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            CK(cudaStreamSynchronize(c.stream));
+            if (h_flag[2]) break;
+        }
+        if ((rc = vcycle_dev(ctx, c.d_r, c.d_z, c.d_part, &nb))) return rc;
+        launch_pcg_scalar(4, c.d_scal, c.d_iflag, c.d_part, nb, tol, maxit, c.stream);
+        launch_pcg_pupdate(c.d_p, c.d_z, nv, c.d_scal, c.d_iflag, c.stream);
+        CKL();
+    }
+    CK(cudaEventRecord(e1, c.stream));
+    CK(cudaMemcpyAsync(h_flag, c.d_iflag, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.stream));
+    double sc[8];
+    CK(cudaMemcpyAsync(sc, c.d_scal, sizeof(double) * 8, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    its = h_flag[0];
+    // true residual in FP64
+    launch_kbyu_f64(l0, c.E, c.d_x, c.d_q, nullptr, nullptr, c.stream);
+    launch_residual(c.d_tmp, c.d_b, c.d_q, nv, c.stream);
+    launch_dot(c.d_tmp, c.d_tmp, nv, c.d_part, nbv, c.stream);
+    launch_finalize_sum(c.d_part, nbv, c.d_scal + 17, c.stream);
+    CKL();
+    double rr = 0;
+    CK(cudaMemcpyAsync(&rr, c.d_scal + 17, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    if (info) {
+        info->iterations = its;
+        info->converged = h_flag[1];
+        info->relres = sc[3];
+        info->true_relres = sc[0] > 0 ? sqrt(rr) / sc[0] : 0.0;
+        info->inner_iterations = 0;
+        info->seconds = ms * 1e-3;
+    }
+    return SGLD_OK;
+}
+
+}  // namespace

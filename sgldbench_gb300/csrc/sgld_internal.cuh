@@ -1,0 +1,133 @@
+// Internal declarations shared by the CUDA translation units of the GB300
+// MGPCG voxel-elasticity solver.  Nothing here crosses the C ABI.
+//
+// Device data layout (every level, every vector):
+//   * structured full grid: elements (ny, nx, nz), nodes (ny+1, nx+1, nz+1),
+//     linear index y + NY*(x + NX*z) with y fastest -- the reference's own
+//     column-major node numbering (src/FEA_VoxelBasedDiscretization.m:71),
+//     so the reference's compact numbering is this order with the inactive
+//     nodes removed;
+//   * nodal vectors node-major interleaved: v[3*node + c], c = x, y, z;
+//   * inactive nodes hold exact zeros, inactive elements have modulus 0.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace sgld {
+
+// node flag bits
+enum : uint8_t { NF_ACTIVE = 1, NF_FIXX = 2, NF_FIXY = 4, NF_FIXZ = 8 };
+
+// The isotropic hexahedral element matrix in the 8-corner Hadamard basis has
+// 45 nonzeros in 11 symmetric blocks (index = 3*mode + component, mode bits:
+// bit0 = x/s, bit1 = y/t, bit2 = z/p).  KH_BLOCKS lists the blocks; the values
+// sit in constant memory in the same order (row-major within each block).
+constexpr int KH_NNZ = 45;
+
+struct Level {
+    int nx = 0, ny = 0, nz = 0;   // elements
+    int span = 1;                 // coarsening factor from the next finer level
+    int64_t nel = 0, nnode = 0;   // full-grid counts
+    int64_t nel_active = 0, nnode_active = 0;
+    uint8_t *eact = nullptr;      // [nel] element non-empty
+    uint8_t *nflag = nullptr;     // [nnode] NF_* bits
+    double *diag = nullptr;       // [3*nnode] Jacobi diagonal (levels 1..L-1)
+    float *diag32 = nullptr;
+    double *Ks = nullptr;         // [576*nel] Galerkin element matrices (coarse levels)
+    double *r = nullptr, *x = nullptr;      // [3*nnode] V-cycle work (coarse levels)
+    float *r32 = nullptr, *x32 = nullptr;
+    std::vector<uint8_t> h_eact, h_nflag;
+};
+
+struct Ctx {
+    int L = 0;
+    int non_dyadic = 0;
+    std::vector<Level> lv;
+    double nu = 0.3, cell = 1.0;
+    double omega = 0.35;
+    double Ke[576];       // column-major 24x24, reference DOF order
+    double Kh[KH_NNZ];
+    // finest-level compact <-> full maps (host + device)
+    std::vector<int64_t> h_nodemap, h_elemap;   // compact -> full (0-based)
+    int64_t *d_nodemap = nullptr, *d_elemap = nullptr;
+    double *E = nullptr;            // [nel] modulus on the full grid (0 = void)
+    bool have_fixed = false, have_E = false, assembled = false;
+    // coarsest direct solve
+    int ncf = 0;                    // free DOFs on the coarsest level
+    int cband = 0;                  // half bandwidth of the permuted coarse matrix
+    int *d_cfree = nullptr;         // [ncf] full-grid DOF index (3*node + c), permuted order
+    double *d_Ac = nullptr;         // [ncf*ncf] dense matrix / Cholesky factor
+    double *d_Ainv = nullptr;       // [ncf*ncf] inverse (symmetric)
+    float *d_Ainv32 = nullptr;
+    double *d_cpart = nullptr;      // [CSPLIT*ncf] GEMV partials
+    // templates for the level-2 Galerkin assembly
+    double *d_H = nullptr;          // [span^3 * 576]
+    // PCG vectors (full grid, FP64)
+    double *d_b = nullptr, *d_x = nullptr, *d_r = nullptr, *d_z = nullptr, *d_p = nullptr, *d_q = nullptr;
+    double *d_tmp = nullptr;
+    double *d_part = nullptr;       // reduction partials
+    double *d_scal = nullptr;       // device scalars
+    int *d_iflag = nullptr;         // device int scalars (iteration, done)
+    int npart = 0;
+    // mixed-precision work
+    float *d_r32 = nullptr, *d_z32 = nullptr, *d_E32 = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int device = 0;
+};
+
+constexpr int CSPLIT = 16;   // column chunks of the coarse GEMV
+
+// ---- launchers (kernels_*.cu) ------------------------------------------------
+void upload_kh(const double *Kh, cudaStream_t s);
+void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *y, double *partial_dot,
+                     int *nblocks_out, cudaStream_t s);
+void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, cudaStream_t s);
+void launch_unit_compliance(const Level &l0, const double *u, const double *E, double *ce_full,
+                            double *partial, int *nblocks_out, cudaStream_t s);
+void launch_stress(const Level &l0, const double *E, const double *u, const double *M48x24,
+                   double *nodal6, double *vm_node, cudaStream_t s);
+void launch_elem_vm(const Level &l0, const double *nodal6, double *vm_elem_full, cudaStream_t s);
+
+template <typename T>
+void launch_restrict(const Level &fine, const Level &coarse, const T *rf, T *rc, cudaStream_t s);
+template <typename T>
+void launch_prolong_smooth(const Level &fine, const Level &coarse, const T *xc, const T *rf, const T *diag,
+                           T omega, T *xf, bool final_level, double *partial_dot, int *nblocks_out,
+                           cudaStream_t s);
+void launch_diag_finest(const Level &l0, const double *E, const double *Ke, double *diag, cudaStream_t s);
+void launch_diag_from_Ks(const Level &l, double *diag, cudaStream_t s);
+void launch_scatter_nodes(const int64_t *map, int64_t n, const double *compact, double *full, cudaStream_t s);
+void launch_gather_nodes(const int64_t *map, int64_t n, const double *full, double *compact, cudaStream_t s);
+void launch_scatter_elems(const int64_t *map, int64_t n, const double *compact, double *full, cudaStream_t s);
+void launch_gather_elems(const int64_t *map, int64_t n, const double *full, double *compact, cudaStream_t s);
+void launch_fixed_indicator(const Level &l, double *v, cudaStream_t s);
+void launch_mark_fixed(Level &l, const double *restricted, cudaStream_t s);
+
+void launch_asm_finest(const Level &coarse, const Level &fine, const double *E, const double *H, double *Ks,
+                       cudaStream_t s);
+void launch_asm_coarse(const Level &coarse, const Level &fine, double *Ks, cudaStream_t s);
+void launch_coarse_dense(const Level &lc, int ncf, const int *cfree_pos_of_dof, double *A, cudaStream_t s);
+int coarse_factor_invert(Ctx &c);  // returns 0 or error
+void launch_coarse_apply_f64(const Ctx &c, const double *rc, double *xc, cudaStream_t s);
+void launch_coarse_apply_f32(const Ctx &c, const float *rc, float *xc, cudaStream_t s);
+
+// vector ops (FP64 PCG)
+int reduce_blocks(int64_t n);
+void launch_dot(const double *a, const double *b, int64_t n, double *partial, int nb, cudaStream_t s);
+void launch_finalize_sum(const double *partial, int nb, double *out, cudaStream_t s);
+void launch_pcg_update(double *x, double *r, const double *p, const double *q, int64_t n, const double *scal,
+                       int *iflag, double *partial, int nb, cudaStream_t s);
+void launch_pcg_pupdate(double *p, const double *z, int64_t n, const double *scal, const int *iflag,
+                        cudaStream_t s);
+void launch_residual(double *r, const double *b, const double *Ax, int64_t n, cudaStream_t s);
+void launch_pcg_scalar(int op, double *scal, int *iflag, const double *partial, int nb, double tol, int maxit,
+                       cudaStream_t s);
+void launch_mask_fixed(const Level &l0, double *v, cudaStream_t s);
+void launch_cast_f32(const double *a, float *b, int64_t n, cudaStream_t s);
+void launch_cast_f64(const float *a, double *b, int64_t n, cudaStream_t s);
+
+}  // namespace sgld

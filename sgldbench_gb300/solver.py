@@ -1,0 +1,282 @@
+"""Python host interface over the C ABI, mirroring SGLDBench's solve path.
+
+``VoxelSolver`` owns one device context (``sgld_ctx``).  Its methods carry
+the reference's function names and argument meaning:
+
+==========================================  =====================================================
+reference (SGLDBench)                       here
+==========================================  =====================================================
+FEA_VoxelBasedDiscretization.m + Solving_   ``VoxelSolver(voxels, ...)``
+BuildingMeshHierarchy.m
+FEA_ApplyBoundaryCondition.m (fixedDOFs)    ``set_fixed_dofs(mask)``
+  + FEA_SetupVoxelBased.m (coarse masks)
+TopOpti_MaterialInterpolationSIMP.m         ``set_modulus(E)``  (``simp_modulus`` computes E)
+Solving_AssembleFEAstencil.m                ``Solving_AssembleFEAstencil()``
+Solving_KbyU_MatrixFree.m                   ``Solving_KbyU_MatrixFree(u)``
+Solving_RestrictResidual.m                  ``Solving_RestrictResidual(r, ii)``
+Solving_InterpolationDeviation.m            ``Solving_InterpolationDeviation(x, ii)``
+Solving_Vcycle.m                            ``Solving_Vcycle(r)``
+Solving_PreconditionedConjugate...m         ``Solving_PreconditionedConjugateGradientSolver(...)``
+Solving_CG_GMGS.m                           ``Solving_CG_GMGS(F, U0)``
+TopOpti_ComputeUnitCompliance.m             ``TopOpti_ComputeUnitCompliance(U)``
+FEA_StressAnalysis.m /                      ``FEA_StressAnalysis(U)``
+FEA_ComputePerElementVonMisesStress.m
+==========================================  =====================================================
+
+Vectors use the reference's compact layout: DOF vectors of length
+3 * numNodes (node-major [ux uy uz]), element vectors of length numElements.
+All computation happens in the CUDA library; errors raise ``SgldError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import warnings
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def reference_num_levels(num_voxels: int, coarsest_resolution_control: int = 50000) -> int:
+    """Level count of FEA_VoxelBasedDiscretization.m:168-177 (before nonDyadic)."""
+    return int(L.load().sgld_reference_num_levels(int(num_voxels), int(coarsest_resolution_control)))
+
+
+def pad_voxels(voxels: np.ndarray, num_levels: int) -> np.ndarray:
+    """Pads the (ny, nx, nz) grid to multiples of 2^(num_levels-1) with void,
+    as FEA_VoxelBasedDiscretization.m:174-186 does."""
+    m = 2 ** (num_levels - 1)
+    ny, nx, nz = voxels.shape
+    out = np.zeros((int(math.ceil(ny / m) * m), int(math.ceil(nx / m) * m), int(math.ceil(nz / m) * m)), bool)
+    out[:ny, :nx, :nz] = voxels
+    return out
+
+
+def simp_modulus(x, E0: float = 1.0, Emin: float = 1e-6, p: float = 3.0) -> np.ndarray:
+    """TopOpti_MaterialInterpolationSIMP.m:5: E = Emin + x^p (E0 - Emin)."""
+    return Emin + np.asarray(x, dtype=np.float64).reshape(-1) ** p * (E0 - Emin)
+
+
+class VoxelSolver:
+    """One GB300 solver context for a padded voxel grid (ny, nx, nz)."""
+
+    def __init__(self, voxels: np.ndarray, num_levels: int | None = None, non_dyadic: int = 1,
+                 coarsest_resolution_control: int = 50000, poisson_ratio: float = 0.3,
+                 cell_size: float = 1.0, omega: float = 0.35, device: int = 0, pad: bool = True):
+        self.lib = L.load()
+        vox = np.asarray(voxels, dtype=bool)
+        if num_levels is None:
+            num_levels = reference_num_levels(int(vox.sum()), coarsest_resolution_control)
+            if num_levels < 0:
+                raise ValueError("domain too small to build a mesh hierarchy")
+        if pad:
+            vox = pad_voxels(vox, num_levels)
+        self.voxels = vox
+        self.resY, self.resX, self.resZ = vox.shape
+        opts = L.Options()
+        self.lib.sgld_default_options(C.byref(opts))
+        opts.num_levels, opts.non_dyadic = int(num_levels), int(non_dyadic)
+        opts.poisson_ratio, opts.cell_size, opts.omega, opts.device = poisson_ratio, cell_size, omega, device
+        buf = np.ascontiguousarray(vox.flatten(order="F").astype(np.uint8))
+        ctx = C.c_void_p()
+        rc = self.lib.sgld_create(self.resY, self.resX, self.resZ, _p(buf), C.byref(opts), C.byref(ctx))
+        self.ctx = ctx
+        if rc != L.SGLD_OK:
+            msg = self.lib.sgld_last_error(ctx).decode() if ctx else "create failed"
+            if ctx:
+                self.lib.sgld_destroy(ctx)
+                self.ctx = None
+            raise L.SgldError(rc, msg)
+        self.numLevels = int(self.lib.sgld_num_levels(ctx))
+        self.levels = [self.level_info(i + 1) for i in range(self.numLevels)]
+        self.numElements = self.levels[0]["numElements"]
+        self.numNodes = self.levels[0]["numNodes"]
+        self.numDOFs = 3 * self.numNodes
+        self.omega = omega
+
+    # -- housekeeping -------------------------------------------------------
+    def _check(self, rc: int):
+        if rc != L.SGLD_OK:
+            raise L.SgldError(rc, self.lib.sgld_last_error(self.ctx).decode())
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.sgld_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def level_info(self, level: int) -> dict:
+        res = (C.c_int * 3)()
+        span = C.c_int()
+        ne, nn = C.c_int64(), C.c_int64()
+        self._check(self.lib.sgld_level_info(self.ctx, level, res, C.byref(span), C.byref(ne), C.byref(nn)))
+        return {"resY": res[0], "resX": res[1], "resZ": res[2], "spanWidth": span.value,
+                "numElements": ne.value, "numNodes": nn.value, "numDOFs": 3 * nn.value}
+
+    def nodMapBack(self, level: int = 1) -> np.ndarray:
+        out = np.zeros(self.levels[level - 1]["numNodes"], np.int64)
+        self._check(self.lib.sgld_node_map(self.ctx, level, _p(out)))
+        return out
+
+    def eleMapBack(self, level: int = 1) -> np.ndarray:
+        out = np.zeros(self.levels[level - 1]["numElements"], np.int64)
+        self._check(self.lib.sgld_element_map(self.ctx, level, _p(out)))
+        return out
+
+    @property
+    def Ke(self) -> np.ndarray:
+        k = np.zeros(576)
+        self._check(self.lib.sgld_get_ke(self.ctx, _p(k)))
+        return k.reshape(24, 24, order="F")
+
+    def set_ke(self, Ke: np.ndarray):
+        k = np.asfortranarray(np.asarray(Ke, dtype=np.float64)).reshape(-1, order="F").copy()
+        self._check(self.lib.sgld_set_ke(self.ctx, _p(k)))
+
+    # -- setup ----------------------------------------------------------------
+    def set_fixed_dofs(self, fixed_mask: np.ndarray):
+        m = np.ascontiguousarray(np.asarray(fixed_mask, dtype=bool).reshape(-1).astype(np.uint8))
+        if m.size != self.numDOFs:
+            raise ValueError("fixed mask must have numDOFs entries")
+        self._check(self.lib.sgld_set_fixed_dofs(self.ctx, _p(m)))
+
+    def free_dofs(self, level: int) -> np.ndarray:
+        out = np.zeros(self.levels[level - 1]["numDOFs"], np.uint8)
+        self._check(self.lib.sgld_get_free_dofs(self.ctx, level, _p(out)))
+        return out.astype(bool)
+
+    def set_modulus(self, E: np.ndarray):
+        e = np.ascontiguousarray(np.asarray(E, dtype=np.float64).reshape(-1))
+        if e.size != self.numElements:
+            raise ValueError("modulus must have numElements entries")
+        self._check(self.lib.sgld_set_modulus(self.ctx, _p(e)))
+
+    def set_modulus_device(self, ptr: int):
+        self._check(self.lib.sgld_set_modulus_device(self.ctx, C.c_void_p(ptr)))
+
+    def Solving_AssembleFEAstencil(self):
+        self._check(self.lib.sgld_assemble(self.ctx))
+
+    def diagK(self, level: int) -> np.ndarray:
+        out = np.zeros(self.levels[level - 1]["numDOFs"])
+        self._check(self.lib.sgld_get_diag(self.ctx, level, _p(out)))
+        return out
+
+    def Ks(self, level: int) -> np.ndarray:
+        ne = self.levels[level - 1]["numElements"]
+        out = np.zeros(576 * ne)
+        self._check(self.lib.sgld_get_ks(self.ctx, level, _p(out)))
+        return out.reshape(ne, 24, 24).transpose(2, 1, 0).copy(order="F")  # (24, 24, ne), column-major pages
+
+    # -- operators ----------------------------------------------------------------
+    def _vec(self, v, n):
+        a = np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(-1))
+        if a.size != n:
+            raise ValueError(f"vector must have {n} entries, got {a.size}")
+        return a
+
+    def Solving_KbyU_MatrixFree(self, uVec) -> np.ndarray:
+        u = self._vec(uVec, self.numDOFs)
+        y = np.zeros_like(u)
+        self._check(self.lib.sgld_kbyu(self.ctx, _p(u), _p(y)))
+        return y
+
+    def Solving_RestrictResidual(self, rFiner, ii: int) -> np.ndarray:
+        r = self._vec(rFiner, self.levels[ii - 2]["numDOFs"])
+        out = np.zeros(self.levels[ii - 1]["numDOFs"])
+        self._check(self.lib.sgld_restrict(self.ctx, ii, _p(r), _p(out)))
+        return out
+
+    def Solving_InterpolationDeviation(self, xCoarser, ii: int) -> np.ndarray:
+        x = self._vec(xCoarser, self.levels[ii - 1]["numDOFs"])
+        out = np.zeros(self.levels[ii - 2]["numDOFs"])
+        self._check(self.lib.sgld_interpolate(self.ctx, ii, _p(x), _p(out)))
+        return out
+
+    def Solving_Vcycle(self, r) -> np.ndarray:
+        rv = self._vec(r, self.numDOFs)
+        z = np.zeros_like(rv)
+        self._check(self.lib.sgld_vcycle(self.ctx, _p(rv), _p(z)))
+        return z
+
+    def pcg(self, b, tol: float = 1e-3, maxIT: int = 500, x0=None, precision: str = "fp64",
+            inner_its: int = 0, history: bool = False):
+        """Runs the whole PCG on the device.  Returns (x, info dict)."""
+        bv = self._vec(b, self.numDOFs)
+        x = np.zeros_like(bv) if x0 is None else self._vec(x0, self.numDOFs).copy()
+        hist = np.zeros(maxIT) if history else None
+        o = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=int(x0 is not None),
+                        precision=L.SGLD_PREC_MIXED if precision == "mixed" else L.SGLD_PREC_FP64,
+                        inner_its=inner_its, history=hist.ctypes.data if history else None)
+        info = L.SolveInfo()
+        self._check(self.lib.sgld_pcg(self.ctx, _p(bv), _p(x), C.byref(o), C.byref(info)))
+        d = {"its": info.iterations, "converged": bool(info.converged), "relres": info.relres,
+             "true_relres": info.true_relres, "inner_its": info.inner_iterations, "seconds": info.seconds}
+        if history:
+            d["history"] = hist[: info.iterations].copy()
+        return x, d
+
+    def pcg_device(self, b_ptr: int, x_ptr: int, tol: float, maxIT: int, use_x0: bool = False,
+                   precision: str = "fp64", inner_its: int = 0) -> dict:
+        o = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=int(use_x0),
+                        precision=L.SGLD_PREC_MIXED if precision == "mixed" else L.SGLD_PREC_FP64,
+                        inner_its=inner_its, history=None)
+        info = L.SolveInfo()
+        self._check(self.lib.sgld_pcg_device(self.ctx, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(o),
+                                             C.byref(info)))
+        return {"its": info.iterations, "converged": bool(info.converged), "relres": info.relres,
+                "true_relres": info.true_relres, "inner_its": info.inner_iterations, "seconds": info.seconds}
+
+    def Solving_PreconditionedConjugateGradientSolver(self, AtX, PtV, b, tol, maxIT, printP="printP_OFF",
+                                                      x0=None):
+        """Solving_PreconditionedConjugateGradientSolver.m:1-37.  With this
+        solver's own operators (AtX = Solving_KbyU_MatrixFree, PtV =
+        Solving_Vcycle) the whole loop runs on the device; other callables are
+        not supported (the reference's function-handle form is a MATLAB
+        feature)."""
+        if AtX != self.Solving_KbyU_MatrixFree or PtV != self.Solving_Vcycle:
+            raise NotImplementedError("only this solver's KbyU / Vcycle operators are supported")
+        x, info = self.pcg(b, tol, maxIT, x0=x0, history=(printP == "printP_ON"))
+        if printP == "printP_ON":
+            for k, r in enumerate(info["history"], 1):
+                print(f" It.: {k:4d} Res.: {r:16.6e}")
+        if info["converged"]:
+            print(f"CG solver converged at iteration{info['its']:5d} to a solution with relative residual"
+                  f"{info['relres']:16.6e}")
+        else:
+            warnings.warn("Exceed the maximum iterate numbers")
+            print(f"The iterative process stops at residual = {info['relres']:10.4f}")
+        return x, info["its"]
+
+    def Solving_CG_GMGS(self, F, U0, tol: float, maxIT: int, printP="printP_OFF"):
+        """Solving_CG_GMGS.m:7: PCG warm-started from the previous U."""
+        return self.Solving_PreconditionedConjugateGradientSolver(
+            self.Solving_KbyU_MatrixFree, self.Solving_Vcycle, F, tol, maxIT, printP, U0)
+
+    def TopOpti_ComputeUnitCompliance(self, U):
+        """Returns (ceList, c) with c = sum(E .* ce) (FEA_ComputeComplianceVoxel.m:20-22)."""
+        u = self._vec(U, self.numDOFs)
+        ce = np.zeros(self.numElements)
+        c = C.c_double()
+        self._check(self.lib.sgld_compliance(self.ctx, _p(u), _p(ce), C.byref(c)))
+        return ce, c.value
+
+    def FEA_StressAnalysis(self, U):
+        """Returns (cartesianStressField numNodes x 6, vonMises per node,
+        per-element von Mises with the reference's extra square root)."""
+        u = self._vec(U, self.numDOFs)
+        s6 = np.zeros(6 * self.numNodes)
+        vmn = np.zeros(self.numNodes)
+        vme = np.zeros(self.numElements)
+        self._check(self.lib.sgld_stress(self.ctx, _p(u), _p(s6), _p(vmn), _p(vme)))
+        return s6.reshape(self.numNodes, 6), vmn, vme

@@ -1,0 +1,162 @@
+"""GPU parity: every operator of the solve path, through the C ABI, against
+the oracle (CPU restatement of the reference, pinned to the reference's own
+compiled MEX kernels by the CPU tests).
+
+Tolerances (relative, max-norm unless stated):
+  K*u, restriction, interpolation, Jacobi diagonals   1e-13
+  Galerkin element matrices Ks                          1e-12
+  V-cycle (coarsest solve through an explicit inverse)  1e-9
+  PCG: iteration count equal to the oracle's (+-1); displacement relative L2
+  vs the oracle's solve at the same tolerance 1e-6; against an FP64 solve to
+  1e-10: displacement relative L2 <= 1e-5 and compliance <= 1e-6.
+"""
+import numpy as np
+import pytest
+
+from oracle import glue as G
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def make_pair(vox, non_dyadic=1, omega=0.6, E=None, seed=0, crc=50000):
+    from sgldbench_gb300 import VoxelSolver
+
+    m = G.build_model(vox, coarsest_control=crc, non_dyadic=non_dyadic, omega=omega)
+    s = VoxelSolver(vox, non_dyadic=non_dyadic, omega=omega, coarsest_resolution_control=crc)
+    l1 = m.levels[0]
+    if E is None:
+        E = np.random.default_rng(seed).uniform(0.05, 1.0, l1.numElements)
+    G.set_modulus(m, E)
+    s.set_fixed_dofs(l1.fixedDOFs)
+    s.set_modulus(E)
+    G.assemble_stencil(m)
+    s.Solving_AssembleFEAstencil()
+    return m, s
+
+
+@pytest.fixture(scope="module", params=["solid_nondyadic", "irregular", "solid_dyadic"])
+def pair(request, built_lib):
+    rng = np.random.default_rng(7)
+    if request.param == "solid_nondyadic":
+        vox = np.ones((8, 16, 8), bool)
+        return make_pair(vox, non_dyadic=1)
+    if request.param == "irregular":
+        vox = rng.random((16, 24, 16)) < 0.7
+        return make_pair(vox, non_dyadic=1, seed=3)
+    vox = np.ones((16, 32, 16), bool)
+    return make_pair(vox, non_dyadic=0, seed=5)
+
+
+def test_hierarchy_matches(pair):
+    m, s = pair
+    assert s.numLevels == m.numLevels
+    for i, lv in enumerate(m.levels, 1):
+        info = s.levels[i - 1]
+        assert (info["resX"], info["resY"], info["resZ"]) == (lv.resX, lv.resY, lv.resZ)
+        assert info["numElements"] == lv.numElements
+        assert info["numNodes"] == lv.numNodes
+        assert np.array_equal(s.eleMapBack(i), lv.eleMapBack.astype(np.int64))
+    assert np.array_equal(s.nodMapBack(1), m.levels[0].nodMapBack.astype(np.int64))
+
+
+def test_coarse_free_dofs(pair):
+    m, s = pair
+    for ii in range(2, m.numLevels + 1):
+        assert np.array_equal(s.free_dofs(ii), m.levels[ii - 1].freeDOFs)
+
+
+def test_kbyu(pair):
+    m, s = pair
+    u = np.random.default_rng(1).standard_normal(m.levels[0].numDOFs)
+    assert _rel(s.Solving_KbyU_MatrixFree(u), G.kbyu(m, u)) <= 1e-13
+
+
+def test_restrict_interpolate(pair):
+    m, s = pair
+    rng = np.random.default_rng(2)
+    for ii in range(2, m.numLevels + 1):
+        rf = rng.standard_normal(m.levels[ii - 2].numDOFs)
+        assert _rel(s.Solving_RestrictResidual(rf, ii), G.restrict(m.levels, rf, ii)) <= 1e-13
+        xc = rng.standard_normal(m.levels[ii - 1].numDOFs)
+        assert _rel(s.Solving_InterpolationDeviation(xc, ii), G.interpolate(m.levels, xc, ii)) <= 1e-13
+
+
+def test_diag_and_stencils(pair):
+    m, s = pair
+    for ii in range(1, m.numLevels):
+        assert _rel(s.diagK(ii), m.levels[ii - 1].diagK) <= 1e-13
+    for ii in range(2, m.numLevels + 1):
+        assert _rel(s.Ks(ii), m.levels[ii - 1].Ks) <= 1e-12
+
+
+def test_vcycle(pair):
+    m, s = pair
+    r = np.random.default_rng(4).standard_normal(m.levels[0].numDOFs)
+    r[m.levels[0].fixedDOFs] = 0.0
+    assert _rel(s.Solving_Vcycle(r), G.vcycle(m, r)) <= 1e-9
+
+
+def test_compliance_and_stress(pair):
+    m, s = pair
+    u = np.random.default_rng(5).standard_normal(m.levels[0].numDOFs)
+    ce, c = s.TopOpti_ComputeUnitCompliance(u)
+    ce_o = G.unit_compliance(m, u)
+    assert _rel(ce, ce_o) <= 1e-13
+    assert abs(c - G.compliance(m, u)) <= 1e-12 * abs(c)
+    s6, vmn, vme = s.FEA_StressAnalysis(u)
+    s6_o, vmn_o = G.stress_analysis(m, u)
+    assert _rel(s6, s6_o) <= 1e-12
+    assert _rel(vmn, vmn_o) <= 1e-12
+    assert _rel(vme, G.per_element_von_mises(m, s6_o)) <= 1e-12
+
+
+@pytest.fixture(scope="module")
+def config0(built_lib):
+    """Config 0: solid 64x32x32 cantilever, 3 levels (4:1 then 2:1), omega 0.6."""
+    vox = np.ones((32, 64, 32), bool)
+    m = G.build_model(vox, omega=0.6)
+    from sgldbench_gb300 import VoxelSolver
+
+    s = VoxelSolver(vox, omega=0.6)
+    E = np.ones(m.levels[0].numElements)
+    G.set_modulus(m, E)
+    s.set_fixed_dofs(m.levels[0].fixedDOFs)
+    s.set_modulus(E)
+    G.assemble_stencil(m)
+    s.Solving_AssembleFEAstencil()
+    return m, s
+
+
+def test_pcg_config0_matches_oracle(config0):
+    m, s = config0
+    U_o, its_o = G.solve(m, tol=1e-6, maxIT=500)
+    U, info = s.pcg(m.F, tol=1e-6, maxIT=500)
+    assert info["converged"]
+    assert abs(info["its"] - its_o) <= 1, (info["its"], its_o)
+    assert np.linalg.norm(U - U_o) / np.linalg.norm(U_o) <= 1e-8
+    assert info["true_relres"] < 1.01e-6
+
+
+def test_pcg_config0_vs_converged_fp64(config0):
+    m, s = config0
+    U_ref, _ = G.solve(m, tol=1e-10, maxIT=1000)
+    U, info = s.pcg(m.F, tol=1e-6, maxIT=500)
+    c_ref = G.compliance(m, U_ref)
+    _, c = s.TopOpti_ComputeUnitCompliance(U)
+    assert abs(c - c_ref) / abs(c_ref) <= 1e-6
+    U10, _ = s.pcg(m.F, tol=1e-10, maxIT=1000)
+    assert np.linalg.norm(U10 - U_ref) / np.linalg.norm(U_ref) <= 1e-5
+
+
+def test_pcg_warm_start(config0):
+    m, s = config0
+    U1, info1 = s.pcg(m.F, tol=1e-6, maxIT=500)
+    U2, info2 = s.pcg(m.F, tol=1e-6, maxIT=500, x0=U1)
+    assert info2["its"] <= 2
+    y_o, its_o = G.pcg(lambda u: G.kbyu(m, u), lambda r: G.vcycle(m, r), m.F, 1e-6, 500, x0=U1)
+    assert abs(info2["its"] - its_o) <= 1

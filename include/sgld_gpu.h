@@ -62,6 +62,8 @@ typedef struct sgld_solve_opts {
     int precision;         /* SGLD_PREC_* */
     int inner_its;         /* SGLD_PREC_MIXED: FP32 inner PCG iterations per outer step (0 = default) */
     double *history;       /* optional host buffer [maxit]: relative residual per iteration */
+    int profile;           /* 1: time the K*u and preconditioner launches with CUDA events
+                              (the SpMV / PtV split of QuickAccess/zTmp_Benchmarking_SpMV.m:63-111) */
 } sgld_solve_opts;
 
 typedef struct sgld_solve_info {
@@ -71,7 +73,17 @@ typedef struct sgld_solve_info {
     double true_relres;    /* ||b - K x|| / ||b|| recomputed in FP64 at exit */
     int inner_iterations;  /* SGLD_PREC_MIXED: total FP32 inner iterations */
     double seconds;        /* device time of the solve (CUDA events) */
+    double kbyu_seconds;   /* profile: summed device time of the outer K*u launches */
+    int kbyu_launches;     /* profile: number of those launches */
+    double precond_seconds;/* profile: summed device time of the preconditioner applications */
 } sgld_solve_info;
+
+/* The CUDA stream every call of this context runs on (a cudaStream_t). */
+void *sgld_get_stream(const sgld_ctx *ctx);
+
+/* Total number of CUDA kernels this library has launched in the process
+ * (a host-side counter; no counterpart in the reference, used for accounting). */
+int64_t sgld_kernel_launches(void);
 
 /* Fills opts with the reference defaults (Data_GlobalVariables.m:10-23). */
 void sgld_default_options(sgld_options *opts);

@@ -251,20 +251,25 @@ def _discretize_level(lv: Level):
     return full
 
 
-def voxel_discretization(vox, coarsest_control=50000):
+def voxel_discretization(vox, coarsest_control=50000, num_levels=None):
     """src/FEA_VoxelBasedDiscretization.m:26-106 (node coordinate caches excluded).
-    vox: bool (ny, nx, nz).  Returns (level1, numLevels, padded vox, (nely, nelx, nelz))."""
+    vox: bool (ny, nx, nz).  Returns (level1, numLevels, padded vox, (nely, nelx, nelz)).
+    num_levels, when given, replaces the level-count heuristic (:168-173), as
+    setting the global numLevels_ would."""
     vox = np.asarray(vox, dtype=bool)
     nely, nelx, nelz = vox.shape
     num_voxels = int(vox.sum())
-    crc = min(coarsest_control, mround(mround(num_voxels / 8) / 8))
-    if crc <= 0:
-        raise ValueError("domain too small to build a mesh hierarchy")
-    L = 0
-    nv = num_voxels
-    while nv >= crc:
-        L += 1
-        nv = mround(nv / 8)
+    if num_levels is not None:
+        L = int(num_levels) - 1
+    else:
+        crc = min(coarsest_control, mround(mround(num_voxels / 8) / 8))
+        if crc <= 0:
+            raise ValueError("domain too small to build a mesh hierarchy")
+        L = 0
+        nv = num_voxels
+        while nv >= crc:
+            L += 1
+            nv = mround(nv / 8)
     ax = int(math.ceil(nelx / 2 ** L) * 2 ** L)
     ay = int(math.ceil(nely / 2 ** L) * 2 ** L)
     az = int(math.ceil(nelz / 2 ** L) * 2 ** L)
@@ -645,10 +650,10 @@ def per_element_von_mises(model: Model, cartesian):
 # end-to-end helpers
 # ---------------------------------------------------------------------------
 def build_model(vox, coarsest_control=50000, non_dyadic=1, nu=0.3, omega=0.35,
-                bc="cantilever3", fixing=None, loading=None):
+                bc="cantilever3", fixing=None, loading=None, num_levels=None):
     """Discretize, apply boundary conditions and set up the hierarchy, as
     QuickAccess/QuickAccess_Mtd0_StressAnalysis.m:24-25 does."""
-    l1, nlev, pad, (nely, nelx, nelz) = voxel_discretization(vox, coarsest_control)
+    l1, nlev, pad, (nely, nelx, nelz) = voxel_discretization(vox, coarsest_control, num_levels)
     levels, nlev, nd = build_hierarchy(l1, nlev, non_dyadic)
     if bc == "cantilever3":
         fixing, loading = cantilever3(l1, nelx)

@@ -27,12 +27,13 @@ class Options(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("tol", dbl), ("maxit", i32), ("use_x0", i32), ("precision", i32), ("inner_its", i32),
-                ("history", vp)]
+                ("history", vp), ("profile", i32)]
 
 
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", i32), ("converged", i32), ("relres", dbl), ("true_relres", dbl),
-                ("inner_iterations", i32), ("seconds", dbl)]
+                ("inner_iterations", i32), ("seconds", dbl), ("kbyu_seconds", dbl), ("kbyu_launches", i32),
+                ("precond_seconds", dbl)]
 
 
 SIGNATURES = {
@@ -63,6 +64,8 @@ SIGNATURES = {
     "sgld_pcg_device": (i32, [vp, vp, vp, vp, vp]),
     "sgld_compliance": (i32, [vp, vp, vp, vp]),
     "sgld_stress": (i32, [vp, vp, vp, vp, vp]),
+    "sgld_get_stream": (vp, [vp]),
+    "sgld_kernel_launches": (i64, []),
 }
 
 _lib = None

@@ -59,6 +59,7 @@ void launch_asm_finest(const Level &coarse, const Level &fine, const double *E, 
     const int64_t nel = coarse.nel;
     const unsigned gx = (unsigned)(nel < 65535 ? nel : 65535);
     const unsigned gy = (unsigned)((nel + gx - 1) / gx);
+    ++g_launches;
     k_asm_finest<<<dim3(gx, gy), 192, 0, s>>>(E, coarse.eact, H, coarse.ny, coarse.nx, coarse.nz, coarse.span, Ks);
 }
 
@@ -137,6 +138,7 @@ void launch_asm_coarse(const Level &coarse, const Level &fine, double *Ks, cudaS
     const int64_t nel = coarse.nel;
     const unsigned gx = (unsigned)(nel < 65535 ? nel : 65535);
     const unsigned gy = (unsigned)((nel + gx - 1) / gx);
+    ++g_launches;
     k_asm_coarse<<<dim3(gx, gy), 192, 0, s>>>(fine.Ks, fine.eact, coarse.eact, coarse.ny, coarse.nx, coarse.nz, Ks);
 }
 
@@ -175,6 +177,7 @@ void launch_coarse_dense(const Level &lc, int ncf, const int *rows_and_pos, doub
     const int *rows = rows_and_pos;
     const int *pos = rows_and_pos + ncf;
     cudaMemsetAsync(A, 0, sizeof(double) * (size_t)ncf * ncf, s);
+    ++g_launches;
     k_coarse_dense<<<(ncf + 127) / 128, 128, 0, s>>>(lc.Ks, lc.eact, lc.ny, lc.nx, lc.nz, rows, pos, ncf, A);
 }
 
@@ -384,20 +387,30 @@ int coarse_factor_invert(Ctx &c) {
     double *A = c.d_Ac;
     for (int kb = 0; kb < nblk; ++kb) {
         const int k0 = kb * NB;
+        ++g_launches;
         k_potrf_tile<<<1, NB * NB, 0, c.stream>>>(A, n, k0, d_info);
         const int kend = min(nblk - 1, kb + bw);
         const int nbelow = kend - kb;
         if (nbelow > 0) {
+            ++g_launches;
             k_trsm_panel<<<nbelow, NB, 0, c.stream>>>(A, n, k0, kb + 1);
             const int npairs = nbelow * (nbelow + 1) / 2;
+            ++g_launches;
             k_syrk_update<<<npairs, 256, 0, c.stream>>>(A, n, k0, kb + 1, nbelow);
         }
     }
     // inverse: Y = L^-1 then X = L^-T Y (in d_Ainv)
     cudaMemsetAsync(c.d_Ainv, 0, sizeof(double) * (size_t)n * n, c.stream);
-    for (int bi = 0; bi < nblk; ++bi) k_trsm_fwd<<<bi + 1, NB, 0, c.stream>>>(A, c.d_Ainv, n, bi, bw);
-    for (int bi = nblk - 1; bi >= 0; --bi) k_trsm_bwd<<<nblk, NB, 0, c.stream>>>(A, c.d_Ainv, n, bi, bw, nblk);
+    for (int bi = 0; bi < nblk; ++bi) {
+        ++g_launches;
+        k_trsm_fwd<<<bi + 1, NB, 0, c.stream>>>(A, c.d_Ainv, n, bi, bw);
+    }
+    for (int bi = nblk - 1; bi >= 0; --bi) {
+        ++g_launches;
+        k_trsm_bwd<<<nblk, NB, 0, c.stream>>>(A, c.d_Ainv, n, bi, bw, nblk);
+    }
     const int64_t nn = (int64_t)n * n;
+    ++g_launches;
     k_to_f32<<<(unsigned)((nn + 255) / 256), 256, 0, c.stream>>>(c.d_Ainv, c.d_Ainv32, nn);
     int info = 0;
     cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
@@ -432,7 +445,9 @@ void launch_coarse_apply_f64(const Ctx &c, const double *rc, double *xc, cudaStr
     cudaMemsetAsync(xc, 0, sizeof(double) * 3 * lc.nnode, s);
     if (c.ncf == 0) return;
     dim3 g((c.ncf + 127) / 128, CSPLIT);
+    ++g_launches;
     k_coarse_gemv<double><<<g, 128, 0, s>>>(c.d_Ainv, c.d_cfree, rc, c.ncf, c.d_cpart);
+    ++g_launches;
     k_coarse_finish<double><<<(c.ncf + 127) / 128, 128, 0, s>>>(c.d_cpart, c.d_cfree, c.ncf, xc);
 }
 
@@ -441,7 +456,9 @@ void launch_coarse_apply_f32(const Ctx &c, const float *rc, float *xc, cudaStrea
     cudaMemsetAsync(xc, 0, sizeof(float) * 3 * lc.nnode, s);
     if (c.ncf == 0) return;
     dim3 g((c.ncf + 127) / 128, CSPLIT);
+    ++g_launches;
     k_coarse_gemv<float><<<g, 128, 0, s>>>(c.d_Ainv32, c.d_cfree, rc, c.ncf, c.d_cpart);
+    ++g_launches;
     k_coarse_finish<float><<<(c.ncf + 127) / 128, 128, 0, s>>>(c.d_cpart, c.d_cfree, c.ncf, xc);
 }
 

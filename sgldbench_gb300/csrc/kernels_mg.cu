@@ -56,6 +56,7 @@ __global__ void k_restrict(const T *__restrict__ rf, T *__restrict__ rc, int nyc
 template <typename T>
 void launch_restrict(const Level &fine, const Level &coarse, const T *rf, T *rc, cudaStream_t st) {
     const int64_t nn = coarse.nnode;
+    ++g_launches;
     k_restrict<T><<<(unsigned)((nn + 127) / 128), 128, 0, st>>>(rf, rc, coarse.ny, coarse.nx, coarse.nz, coarse.span);
 }
 template void launch_restrict<double>(const Level &, const Level &, const double *, double *, cudaStream_t);
@@ -142,6 +143,7 @@ void launch_prolong_smooth(const Level &fine, const Level &coarse, const T *xc, 
     const int64_t nn = fine.nnode;
     const unsigned nb = (unsigned)((nn + 255) / 256);
     if (nblocks_out) *nblocks_out = (int)nb;
+    ++g_launches;
     if (final_level)
         k_prolong_smooth<T, true><<<nb, 256, 0, st>>>(xc, rf, diag, fine.nflag, omega, xf, coarse.ny, coarse.nx,
                                                       coarse.nz, coarse.span, partial_dot);
@@ -188,6 +190,7 @@ void launch_diag_finest(const Level &l0, const double *E, const double *Ke, doub
     double dk[24];
     for (int i = 0; i < 24; ++i) dk[i] = Ke[i + 24 * i];
     cudaMemcpyToSymbolAsync(c_dKe, dk, sizeof dk, 0, cudaMemcpyHostToDevice, s);
+    ++g_launches;
     k_diag_finest<<<(unsigned)((l0.nnode + 255) / 256), 256, 0, s>>>(E, l0.nflag, l0.ny, l0.nx, l0.nz, diag);
 }
 
@@ -217,6 +220,7 @@ __global__ void k_diag_from_Ks(const double *__restrict__ Ks, const uint8_t *__r
 }
 
 void launch_diag_from_Ks(const Level &l, double *diag, cudaStream_t s) {
+    ++g_launches;
     k_diag_from_Ks<<<(unsigned)((l.nnode + 255) / 256), 256, 0, s>>>(l.Ks, l.eact, l.nflag, l.ny, l.nx, l.nz, diag);
 }
 
@@ -249,16 +253,28 @@ __global__ void k_gather_elems(const int64_t *__restrict__ map, int64_t n, const
 }
 
 void launch_scatter_nodes(const int64_t *map, int64_t n, const double *compact, double *full, cudaStream_t s) {
-    if (n > 0) k_scatter_nodes<<<(unsigned)((3 * n + 255) / 256), 256, 0, s>>>(map, n, compact, full);
+    if (n > 0) {
+        ++g_launches;
+        k_scatter_nodes<<<(unsigned)((3 * n + 255) / 256), 256, 0, s>>>(map, n, compact, full);
+    }
 }
 void launch_gather_nodes(const int64_t *map, int64_t n, const double *full, double *compact, cudaStream_t s) {
-    if (n > 0) k_gather_nodes<<<(unsigned)((3 * n + 255) / 256), 256, 0, s>>>(map, n, full, compact);
+    if (n > 0) {
+        ++g_launches;
+        k_gather_nodes<<<(unsigned)((3 * n + 255) / 256), 256, 0, s>>>(map, n, full, compact);
+    }
 }
 void launch_scatter_elems(const int64_t *map, int64_t n, const double *compact, double *full, cudaStream_t s) {
-    if (n > 0) k_scatter_elems<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(map, n, compact, full);
+    if (n > 0) {
+        ++g_launches;
+        k_scatter_elems<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(map, n, compact, full);
+    }
 }
 void launch_gather_elems(const int64_t *map, int64_t n, const double *full, double *compact, cudaStream_t s) {
-    if (n > 0) k_gather_elems<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(map, n, full, compact);
+    if (n > 0) {
+        ++g_launches;
+        k_gather_elems<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(map, n, full, compact);
+    }
 }
 
 // ---- fixed-DOF bookkeeping (src/FEA_SetupVoxelBased.m:13-26) ----------------
@@ -271,6 +287,7 @@ __global__ void k_fixed_indicator(const uint8_t *__restrict__ nflag, int64_t nn,
     v[3 * n + 2] = (f & NF_FIXZ) ? 1.0 : 0.0;
 }
 void launch_fixed_indicator(const Level &l, double *v, cudaStream_t s) {
+    ++g_launches;
     k_fixed_indicator<<<(unsigned)((l.nnode + 255) / 256), 256, 0, s>>>(l.nflag, l.nnode, v);
 }
 // a coarse DOF is fixed iff the restricted fixed indicator is nonzero
@@ -284,6 +301,7 @@ __global__ void k_mark_fixed(uint8_t *__restrict__ nflag, int64_t nn, const doub
     nflag[n] = f;
 }
 void launch_mark_fixed(Level &l, const double *restricted, cudaStream_t s) {
+    ++g_launches;
     k_mark_fixed<<<(unsigned)((l.nnode + 255) / 256), 256, 0, s>>>(l.nflag, l.nnode, restricted);
 }
 
@@ -296,6 +314,7 @@ __global__ void k_mask_fixed(const uint8_t *__restrict__ nflag, int64_t nn, doub
     if (f & NF_FIXZ) v[3 * n + 2] = 0.0;
 }
 void launch_mask_fixed(const Level &l0, double *v, cudaStream_t s) {
+    ++g_launches;
     k_mask_fixed<<<(unsigned)((l0.nnode + 255) / 256), 256, 0, s>>>(l0.nflag, l0.nnode, v);
 }
 

@@ -239,6 +239,7 @@ static void kbyu_launch(const Level &l0, const T *E, const T *u, T *y, double *p
     }
     dim3 g = kbyu_grid(l0);
     if (nb) *nb = (int)(g.x * g.y * g.z);
+    ++g_launches;
     k_kbyu<T, DOT><<<g, KT_THREADS, smem, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, partial);
 }
 
@@ -304,6 +305,7 @@ void launch_unit_compliance(const Level &l0, const double *u, const double *E, d
     const int64_t nel = l0.nel;
     const int nb = (int)((nel + 255) / 256);
     if (nblocks_out) *nblocks_out = nb;
+    ++g_launches;
     k_unit_compliance<<<nb, 256, 0, s>>>(u, E, l0.eact, l0.ny, l0.nx, l0.nz, ce_full, partial);
 }
 
@@ -362,6 +364,7 @@ void launch_stress(const Level &l0, const double *E, const double *u, const doub
                    double *vm_node, cudaStream_t s) {
     cudaMemcpyToSymbolAsync(c_M, M48x24, sizeof(double) * 48 * 24, 0, cudaMemcpyHostToDevice, s);
     const int64_t nn = l0.nnode;
+    ++g_launches;
     k_nodal_stress<<<(unsigned)((nn + 127) / 128), 128, 0, s>>>(u, E, l0.nflag, l0.eact, l0.ny, l0.nx, l0.nz, nodal6, vm_node);
 }
 
@@ -390,6 +393,7 @@ __global__ void k_elem_vm(const double *__restrict__ s6, const uint8_t *__restri
 
 void launch_elem_vm(const Level &l0, const double *nodal6, double *vm_elem_full, cudaStream_t s) {
     const int64_t nel = l0.nel;
+    ++g_launches;
     k_elem_vm<<<(unsigned)((nel + 255) / 256), 256, 0, s>>>(nodal6, l0.eact, l0.ny, l0.nx, l0.nz, vm_elem_full);
 }
 

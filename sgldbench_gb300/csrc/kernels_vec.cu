@@ -37,6 +37,7 @@ __global__ void k_dot(const double *__restrict__ a, const double *__restrict__ b
 }
 
 void launch_dot(const double *a, const double *b, int64_t n, double *partial, int nb, cudaStream_t s) {
+    ++g_launches;
     k_dot<<<nb, VB, 0, s>>>(a, b, n, partial);
 }
 
@@ -52,6 +53,7 @@ __global__ void k_finalize_sum(const double *__restrict__ part, int nb, double *
     if (threadIdx.x == 0) out[0] = s;
 }
 void launch_finalize_sum(const double *partial, int nb, double *out, cudaStream_t s) {
+    ++g_launches;
     k_finalize_sum<<<1, VB, 0, s>>>(partial, nb, out);
 }
 
@@ -104,6 +106,7 @@ __global__ void k_pcg_scalar(int op, double *__restrict__ scal, int *__restrict_
 
 void launch_pcg_scalar(int op, double *scal, int *iflag, const double *partial, int nb, double tol, int maxit,
                        cudaStream_t s) {
+    ++g_launches;
     k_pcg_scalar<<<1, VB, 0, s>>>(op, scal, iflag, partial, nb, tol, maxit);
 }
 
@@ -126,6 +129,7 @@ __global__ void k_pcg_update(double *__restrict__ x, double *__restrict__ r, con
 
 void launch_pcg_update(double *x, double *r, const double *p, const double *q, int64_t n, const double *scal,
                        int *iflag, double *partial, int nb, cudaStream_t s) {
+    ++g_launches;
     k_pcg_update<<<nb, VB, 0, s>>>(x, r, p, q, n, scal, iflag, partial);
 }
 
@@ -139,6 +143,7 @@ __global__ void k_pcg_pupdate(double *__restrict__ p, const double *__restrict__
 }
 
 void launch_pcg_pupdate(double *p, const double *z, int64_t n, const double *scal, const int *iflag, cudaStream_t s) {
+    ++g_launches;
     k_pcg_pupdate<<<reduce_blocks(n), VB, 0, s>>>(p, z, n, scal, iflag);
 }
 
@@ -148,6 +153,7 @@ __global__ void k_residual(double *__restrict__ r, const double *__restrict__ b,
     for (int64_t i = blockIdx.x * (int64_t)VB + threadIdx.x; i < n; i += (int64_t)gridDim.x * VB) r[i] = b[i] - Ax[i];
 }
 void launch_residual(double *r, const double *b, const double *Ax, int64_t n, cudaStream_t s) {
+    ++g_launches;
     k_residual<<<reduce_blocks(n), VB, 0, s>>>(r, b, Ax, n);
 }
 
@@ -158,9 +164,11 @@ __global__ void k_cast_f64(const float *__restrict__ a, double *__restrict__ b, 
     for (int64_t i = blockIdx.x * (int64_t)VB + threadIdx.x; i < n; i += (int64_t)gridDim.x * VB) b[i] = (double)a[i];
 }
 void launch_cast_f32(const double *a, float *b, int64_t n, cudaStream_t s) {
+    ++g_launches;
     k_cast_f32<<<reduce_blocks(n), VB, 0, s>>>(a, b, n);
 }
 void launch_cast_f64(const float *a, double *b, int64_t n, cudaStream_t s) {
+    ++g_launches;
     k_cast_f64<<<reduce_blocks(n), VB, 0, s>>>(a, b, n);
 }
 

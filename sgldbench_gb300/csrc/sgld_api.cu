@@ -14,6 +14,8 @@
 
 using namespace sgld;
 
+int64_t sgld::g_launches = 0;
+
 struct sgld_ctx {
     Ctx c;
     // lazily allocated stress buffers
@@ -352,6 +354,10 @@ int sgld_reference_num_levels(int64_t num_voxels, int64_t crc) {
 }
 
 const char *sgld_last_error(const sgld_ctx *ctx) { return ctx ? ctx->c.err.c_str() : "null context"; }
+
+void *sgld_get_stream(const sgld_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }
+
+int64_t sgld_kernel_launches(void) { return g_launches; }
 
 int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_options *opts, sgld_ctx **out) {
     if (!out || !solid || resX <= 0 || resY <= 0 || resZ <= 0) return SGLD_ERR_ARG;
@@ -924,8 +930,17 @@ int pcg_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
     int h_flag[4] = {0, 0, 0, 0};
     int its = 0;
     const int poll = 1;
+    const bool prof = o->profile != 0;
+    cudaEvent_t pe[4] = {nullptr, nullptr, nullptr, nullptr};   // K*u start/end, precond start/end
+    if (prof)
+        for (auto &e : pe) CK(cudaEventCreate(&e));
+    double kb_ms = 0.0, pc_ms = 0.0;
+    int kb_n = 0;
+    bool pc_pending = false;
     for (int k = 1; k <= maxit; ++k) {
+        if (prof) CK(cudaEventRecord(pe[0], c.stream));
         launch_kbyu_f64(l0, c.E, c.d_p, c.d_q, c.d_part, &nb, c.stream);
+        if (prof) CK(cudaEventRecord(pe[1], c.stream));
         launch_pcg_scalar(2, c.d_scal, c.d_iflag, c.d_part, nb, tol, maxit, c.stream);
         launch_pcg_update(c.d_x, c.d_r, c.d_p, c.d_q, nv, c.d_scal, c.d_iflag, c.d_part, nbv, c.stream);
         launch_pcg_scalar(3, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
@@ -933,14 +948,39 @@ int pcg_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
             CK(cudaMemcpyAsync(h_flag, c.d_iflag, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.stream));
             if (o->history) CK(cudaMemcpyAsync(o->history + (k - 1), c.d_scal + 3, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
             CK(cudaStreamSynchronize(c.stream));
+            if (prof) {
+                float t = 0.f;
+                cudaEventElapsedTime(&t, pe[0], pe[1]);
+                kb_ms += t;
+                ++kb_n;
+                if (pc_pending) {
+                    cudaEventElapsedTime(&t, pe[2], pe[3]);
+                    pc_ms += t;
+                    pc_pending = false;
+                }
+            }
             if (h_flag[2]) break;
         }
+        if (prof) CK(cudaEventRecord(pe[2], c.stream));
         if ((rc = vcycle_dev(ctx, c.d_r, c.d_z, c.d_part, &nb))) return rc;
+        if (prof) {
+            CK(cudaEventRecord(pe[3], c.stream));
+            pc_pending = true;
+        }
         launch_pcg_scalar(4, c.d_scal, c.d_iflag, c.d_part, nb, tol, maxit, c.stream);
         launch_pcg_pupdate(c.d_p, c.d_z, nv, c.d_scal, c.d_iflag, c.stream);
         CKL();
     }
     CK(cudaEventRecord(e1, c.stream));
+    if (prof) {
+        CK(cudaStreamSynchronize(c.stream));
+        if (pc_pending) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, pe[2], pe[3]);
+            pc_ms += t;
+        }
+        for (auto &e : pe) cudaEventDestroy(e);
+    }
     CK(cudaMemcpyAsync(h_flag, c.d_iflag, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.stream));
     double sc[8];
     CK(cudaMemcpyAsync(sc, c.d_scal, sizeof(double) * 8, cudaMemcpyDeviceToHost, c.stream));
@@ -966,6 +1006,9 @@ int pcg_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
         info->true_relres = sc[0] > 0 ? sqrt(rr) / sc[0] : 0.0;
         info->inner_iterations = 0;
         info->seconds = ms * 1e-3;
+        info->kbyu_seconds = kb_ms * 1e-3;
+        info->kbyu_launches = kb_n;
+        info->precond_seconds = pc_ms * 1e-3;
     }
     return SGLD_OK;
 }

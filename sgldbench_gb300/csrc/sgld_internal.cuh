@@ -81,6 +81,9 @@ struct Ctx {
 
 constexpr int CSPLIT = 16;   // column chunks of the coarse GEMV
 
+// number of kernels this library has launched (host-side counter, one per launch)
+extern int64_t g_launches;
+
 // ---- launchers (kernels_*.cu) ------------------------------------------------
 void upload_kh(const double *Kh, cudaStream_t s);
 void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *y, double *partial_dot,

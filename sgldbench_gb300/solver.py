@@ -57,6 +57,18 @@ def pad_voxels(voxels: np.ndarray, num_levels: int) -> np.ndarray:
     return out
 
 
+def _info_dict(info) -> dict:
+    return {"its": info.iterations, "converged": bool(info.converged), "relres": info.relres,
+            "true_relres": info.true_relres, "inner_its": info.inner_iterations, "seconds": info.seconds,
+            "kbyu_seconds": info.kbyu_seconds, "kbyu_launches": info.kbyu_launches,
+            "precond_seconds": info.precond_seconds}
+
+
+def kernel_launches() -> int:
+    """Kernels the CUDA library has launched so far in this process."""
+    return int(L.load().sgld_kernel_launches())
+
+
 def simp_modulus(x, E0: float = 1.0, Emin: float = 1e-6, p: float = 3.0) -> np.ndarray:
     """TopOpti_MaterialInterpolationSIMP.m:5: E = Emin + x^p (E0 - Emin)."""
     return Emin + np.asarray(x, dtype=np.float64).reshape(-1) ** p * (E0 - Emin)
@@ -220,22 +232,25 @@ class VoxelSolver:
                         inner_its=inner_its, history=hist.ctypes.data if history else None)
         info = L.SolveInfo()
         self._check(self.lib.sgld_pcg(self.ctx, _p(bv), _p(x), C.byref(o), C.byref(info)))
-        d = {"its": info.iterations, "converged": bool(info.converged), "relres": info.relres,
-             "true_relres": info.true_relres, "inner_its": info.inner_iterations, "seconds": info.seconds}
+        d = _info_dict(info)
         if history:
             d["history"] = hist[: info.iterations].copy()
         return x, d
 
     def pcg_device(self, b_ptr: int, x_ptr: int, tol: float, maxIT: int, use_x0: bool = False,
-                   precision: str = "fp64", inner_its: int = 0) -> dict:
+                   precision: str = "fp64", inner_its: int = 0, profile: bool = False) -> dict:
         o = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=int(use_x0),
                         precision=L.SGLD_PREC_MIXED if precision == "mixed" else L.SGLD_PREC_FP64,
-                        inner_its=inner_its, history=None)
+                        inner_its=inner_its, history=None, profile=int(profile))
         info = L.SolveInfo()
         self._check(self.lib.sgld_pcg_device(self.ctx, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(o),
                                              C.byref(info)))
-        return {"its": info.iterations, "converged": bool(info.converged), "relres": info.relres,
-                "true_relres": info.true_relres, "inner_its": info.inner_iterations, "seconds": info.seconds}
+        return _info_dict(info)
+
+    @property
+    def stream(self) -> int:
+        """cudaStream_t of this context (every call runs on it)."""
+        return int(self.lib.sgld_get_stream(self.ctx) or 0)
 
     def Solving_PreconditionedConjugateGradientSolver(self, AtX, PtV, b, tol, maxIT, printP="printP_OFF",
                                                       x0=None):

@@ -85,6 +85,14 @@ void *sgld_get_stream(const sgld_ctx *ctx);
  * (a host-side counter; no counterpart in the reference, used for accounting). */
 int64_t sgld_kernel_launches(void);
 
+/* Times `reps` back-to-back applications of one internal operator on the
+ * context's own (already set up) device buffers with CUDA events and returns
+ * the mean milliseconds per application.  No counterpart in the reference:
+ * it is the kernel-level measurement hook used for rooflines and profiling.
+ *   op 0: FP64 K*u   op 1: FP32 K*u   op 2: FP64 V-cycle   op 3: FP32 V-cycle
+ *   op 4: assembly (Galerkin levels + coarsest factorization) */
+int sgld_time_op(sgld_ctx *ctx, int op, int reps, double *ms_per_op);
+
 /* Fills opts with the reference defaults (Data_GlobalVariables.m:10-23). */
 void sgld_default_options(sgld_options *opts);
 

@@ -66,6 +66,7 @@ SIGNATURES = {
     "sgld_stress": (i32, [vp, vp, vp, vp, vp]),
     "sgld_get_stream": (vp, [vp]),
     "sgld_kernel_launches": (i64, []),
+    "sgld_time_op": (i32, [vp, i32, i32, vp]),
 }
 
 _lib = None

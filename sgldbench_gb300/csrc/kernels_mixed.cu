@@ -1,3 +1,143 @@
-// Mixed-precision preconditioner kernels (FP32 V-cycle).  Filled in with the
-// mixed solve path.
+// Kernels of the mixed-precision solve (SGLD_PREC_MIXED).
+//
+// The outer loop is the reference's PCG in FP64 made flexible (Polak-Ribiere
+// beta = -lambda z_new'q / z'r), so that the preconditioner may change from
+// one application to the next.  The preconditioner is a fixed number of FP32
+// CG iterations on K e = r, each preconditioned by the reference's additive
+// V-cycle in FP32.  The inner loop runs entirely on the device (scalars in
+// device memory) and is captured once into a CUDA graph.
 #include "sgld_internal.cuh"
+
+namespace sgld {
+
+constexpr int MB = 256;
+
+__device__ __forceinline__ double mblock_reduce(double v) {
+    __shared__ double red[MB / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < MB / 32; ++i) s += red[i];
+    return s;
+}
+
+__device__ double msum_partials(const double *__restrict__ part, int nb) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nb; i += MB) s += part[i];
+    return mblock_reduce(s);
+}
+
+// inner scalars (FP64 storage): [0] rho, [1] alpha, [2] beta, [3] rho_new
+enum { IS_RHO = 0, IS_ALPHA = 1, IS_BETA = 2 };
+
+// op 0: rho = sum; op 1: alpha = rho / sum; op 2: beta = sum / rho, rho = sum
+__global__ void k_icg_scalar(int op, double *__restrict__ sc, const double *__restrict__ part, int nb) {
+    const double s = msum_partials(part, nb);
+    if (threadIdx.x != 0) return;
+    if (op == 0) {
+        sc[IS_RHO] = s;
+    } else if (op == 1) {
+        sc[IS_ALPHA] = (s != 0.0) ? sc[IS_RHO] / s : 0.0;
+    } else {
+        sc[IS_BETA] = (sc[IS_RHO] != 0.0) ? s / sc[IS_RHO] : 0.0;
+        sc[IS_RHO] = s;
+    }
+}
+
+void launch_icg_scalar(int op, double *sc, const double *part, int nb, cudaStream_t s) {
+    ++g_launches;
+    k_icg_scalar<<<1, MB, 0, s>>>(op, sc, part, nb);
+}
+
+// e += alpha d; s -= alpha t
+__global__ void k_icg_update(float *__restrict__ e, float *__restrict__ s, const float *__restrict__ d,
+                             const float *__restrict__ t, int64_t n, const double *__restrict__ sc) {
+    const float a = (float)sc[IS_ALPHA];
+    for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n; i += (int64_t)gridDim.x * MB) {
+        e[i] = fmaf(a, d[i], e[i]);
+        s[i] = fmaf(-a, t[i], s[i]);
+    }
+}
+
+void launch_icg_update(float *e, float *s, const float *d, const float *t, int64_t n, const double *sc,
+                       cudaStream_t st) {
+    ++g_launches;
+    k_icg_update<<<reduce_blocks(n), MB, 0, st>>>(e, s, d, t, n, sc);
+}
+
+// d = w + beta d
+__global__ void k_icg_dupdate(float *__restrict__ d, const float *__restrict__ w, int64_t n,
+                              const double *__restrict__ sc) {
+    const float b = (float)sc[IS_BETA];
+    for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n; i += (int64_t)gridDim.x * MB)
+        d[i] = fmaf(b, d[i], w[i]);
+}
+
+void launch_icg_dupdate(float *d, const float *w, int64_t n, const double *sc, cudaStream_t st) {
+    ++g_launches;
+    k_icg_dupdate<<<reduce_blocks(n), MB, 0, st>>>(d, w, n, sc);
+}
+
+// z64 = e32 (masked at fixed DOFs by construction), partials of z.r and z.q
+__global__ void k_widen_dots(const float *__restrict__ e, double *__restrict__ z, const double *__restrict__ r,
+                             const double *__restrict__ q, int64_t n, double *__restrict__ p1,
+                             double *__restrict__ p2) {
+    double a = 0.0, b = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n; i += (int64_t)gridDim.x * MB) {
+        const double zi = (double)e[i];
+        z[i] = zi;
+        a += zi * r[i];
+        b += zi * q[i];
+    }
+    a = mblock_reduce(a);
+    b = mblock_reduce(b);
+    if (threadIdx.x == 0) {
+        p1[blockIdx.x] = a;
+        p2[blockIdx.x] = b;
+    }
+}
+
+void launch_widen_dots(const float *e, double *z, const double *r, const double *q, int64_t n, double *p1,
+                       double *p2, int nb, cudaStream_t st) {
+    ++g_launches;
+    k_widen_dots<<<nb, MB, 0, st>>>(e, z, r, q, n, p1, p2);
+}
+
+// outer flexible-PCG scalars after the preconditioner: beta = -lambda zq / x1, x1 = zr
+// (slots as in kernels_vec.cu: S_X1 = 1, S_LAM = 2, S_BETA = 4)
+__global__ void k_flex_beta(double *__restrict__ scal, const int *__restrict__ iflag, const double *__restrict__ p1,
+                            const double *__restrict__ p2, int nb, int first) {
+    const double zr = msum_partials(p1, nb);
+    const double zq = msum_partials(p2, nb);
+    if (threadIdx.x != 0) return;
+    if (first) {
+        scal[1] = zr;
+        return;
+    }
+    if (iflag[2]) return;
+    scal[4] = -scal[2] * zq / scal[1];
+    scal[1] = zr;
+}
+
+void launch_flex_beta(double *scal, const int *iflag, const double *p1, const double *p2, int nb, int first,
+                      cudaStream_t st) {
+    ++g_launches;
+    k_flex_beta<<<1, MB, 0, st>>>(scal, iflag, p1, p2, nb, first);
+}
+
+// r32 = (float) r64
+__global__ void k_narrow(const double *__restrict__ a, float *__restrict__ b, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n; i += (int64_t)gridDim.x * MB) b[i] = (float)a[i];
+}
+
+void launch_narrow(const double *a, float *b, int64_t n, cudaStream_t st) {
+    ++g_launches;
+    k_narrow<<<reduce_blocks(n), MB, 0, st>>>(a, b, n);
+}
+
+}  // namespace sgld

@@ -229,14 +229,23 @@ static dim3 kbyu_grid(const Level &l) {
     return dim3((l.ny + 1 + KT_Y - 2) / (KT_Y - 1), (l.nx + 1 + KT_X - 2) / (KT_X - 1), (l.nz + 1 + KT_ZC - 1) / KT_ZC);
 }
 
+template <typename T>
+static constexpr size_t kbyu_smem() {
+    return sizeof(T) * (2 * KT_NL * 3 + 24 * KT_THREADS);
+}
+
+// opt-in shared memory sizes; called once per context before any launch or
+// graph capture
+void init_kernel_attributes() {
+    cudaFuncSetAttribute(k_kbyu<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<double>());
+    cudaFuncSetAttribute(k_kbyu<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<double>());
+    cudaFuncSetAttribute(k_kbyu<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<float>());
+    cudaFuncSetAttribute(k_kbyu<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<float>());
+}
+
 template <typename T, bool DOT>
 static void kbyu_launch(const Level &l0, const T *E, const T *u, T *y, double *partial, int *nb, cudaStream_t s) {
-    const size_t smem = sizeof(T) * (2 * KT_NL * 3 + 24 * KT_THREADS);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_kbyu<T, DOT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr_set = true;
-    }
+    const size_t smem = kbyu_smem<T>();
     dim3 g = kbyu_grid(l0);
     if (nb) *nb = (int)(g.x * g.y * g.z);
     ++g_launches;
@@ -251,8 +260,12 @@ void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *
         kbyu_launch<double, false>(l0, E, u, y, nullptr, nblocks_out, s);
 }
 
-void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, cudaStream_t s) {
-    kbyu_launch<float, false>(l0, E, u, y, nullptr, nullptr, s);
+void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
+                     int *nblocks_out, cudaStream_t s) {
+    if (partial_dot)
+        kbyu_launch<float, true>(l0, E, u, y, partial_dot, nblocks_out, s);
+    else
+        kbyu_launch<float, false>(l0, E, u, y, nullptr, nblocks_out, s);
 }
 
 int kbyu_num_blocks(const Level &l0) {

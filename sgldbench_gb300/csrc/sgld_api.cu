@@ -287,6 +287,73 @@ int vcycle_dev(sgld_ctx *ctx, const double *r, double *z, double *partial, int *
     return SGLD_OK;
 }
 
+// the same additive V-cycle in FP32 (mixed-precision preconditioner)
+int vcycle_dev32(sgld_ctx *ctx, const float *r, float *z, double *partial, int *nb) {
+    Ctx &c = ctx->c;
+    const int L = c.L;
+    const float *rf = r;
+    for (int l = 1; l < L; ++l) {
+        launch_restrict<float>(c.lv[l - 1], c.lv[l], rf, c.lv[l].r32, c.stream);
+        rf = c.lv[l].r32;
+    }
+    launch_coarse_apply_f32(c, c.lv[L - 1].r32, c.lv[L - 1].x32, c.stream);
+    for (int l = L - 2; l >= 0; --l) {
+        const float *rl = (l == 0) ? r : c.lv[l].r32;
+        float *xl = (l == 0) ? z : c.lv[l].x32;
+        launch_prolong_smooth<float>(c.lv[l], c.lv[l + 1], c.lv[l + 1].x32, rl, c.lv[l].diag32, (float)c.omega, xl,
+                                     l == 0, l == 0 ? partial : nullptr, l == 0 ? nb : nullptr, c.stream);
+    }
+    return SGLD_OK;
+}
+
+// k FP32 CG iterations on K e = r32 from e = 0, preconditioned by the FP32
+// V-cycle; result in d_e32.  Enqueue only (no host synchronisation), so the
+// sequence can be captured into a graph.
+void inner_enqueue(sgld_ctx *ctx, int k) {
+    Ctx &c = ctx->c;
+    const Level &l0 = c.lv[0];
+    const int64_t nv = 3 * l0.nnode;
+    int nb = 0;
+    cudaMemcpyAsync(c.d_s32, c.d_r32, sizeof(float) * nv, cudaMemcpyDeviceToDevice, c.stream);
+    cudaMemsetAsync(c.d_e32, 0, sizeof(float) * nv, c.stream);
+    vcycle_dev32(ctx, c.d_s32, c.d_z32, c.d_part2, &nb);
+    launch_icg_scalar(0, c.d_isc, c.d_part2, nb, c.stream);
+    cudaMemcpyAsync(c.d_d32, c.d_z32, sizeof(float) * nv, cudaMemcpyDeviceToDevice, c.stream);
+    for (int j = 1; j <= k; ++j) {
+        launch_kbyu_f32(l0, c.d_E32, c.d_d32, c.d_t32, c.d_part2, &nb, c.stream);
+        launch_icg_scalar(1, c.d_isc, c.d_part2, nb, c.stream);
+        launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.stream);
+        if (j == k) break;
+        vcycle_dev32(ctx, c.d_s32, c.d_z32, c.d_part2, &nb);
+        launch_icg_scalar(2, c.d_isc, c.d_part2, nb, c.stream);
+        launch_icg_dupdate(c.d_d32, c.d_z32, nv, c.d_isc, c.stream);
+    }
+}
+
+// runs the inner solve through a CUDA graph captured once per (context, k)
+int inner_run(sgld_ctx *ctx, int k) {
+    Ctx &c = ctx->c;
+    if (!c.inner_graph || c.inner_graph_k != k) {
+        if (c.inner_graph) {
+            cudaGraphExecDestroy(c.inner_graph);
+            c.inner_graph = nullptr;
+        }
+        const int64_t before = g_launches;
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+        inner_enqueue(ctx, k);
+        CK(cudaStreamEndCapture(c.stream, &g));
+        c.inner_graph_launches = g_launches - before;
+        g_launches = before;
+        CK(cudaGraphInstantiate(&c.inner_graph, g, 0));
+        cudaGraphDestroy(g);
+        c.inner_graph_k = k;
+    }
+    CK(cudaGraphLaunch(c.inner_graph, c.stream));
+    g_launches += c.inner_graph_launches;
+    return SGLD_OK;
+}
+
 int check_ready(sgld_ctx *ctx) {
     if (!ctx) return SGLD_ERR_ARG;
     if (!ctx->c.have_fixed) return fail(ctx, SGLD_ERR_STATE, "fixed DOFs not set (sgld_set_fixed_dofs)");
@@ -323,6 +390,14 @@ int download_nodes(sgld_ctx *ctx, const double *d_full, double *h) {
 }
 
 int pcg_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info);
+int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info);
+
+int solve_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
+    if (o->maxit < 1 || !(o->tol >= 0.0)) return fail(ctx, SGLD_ERR_ARG, "maxit must be >= 1 and tol >= 0");
+    if (o->precision == SGLD_PREC_MIXED) return pcg_mixed_dev(ctx, o, info);
+    if (o->precision != SGLD_PREC_FP64) return fail(ctx, SGLD_ERR_ARG, "unknown precision mode");
+    return pcg_dev(ctx, o, info);
+}
 
 }  // namespace
 
@@ -473,9 +548,13 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
     for (double **p : {&c.d_b, &c.d_x, &c.d_r, &c.d_z, &c.d_p, &c.d_q, &c.d_tmp}) CK(dalloc(p, nv));
     CK(dalloc(&c.d_r32, nv));
     CK(dalloc(&c.d_z32, nv));
+    for (float **p : {&c.d_e32, &c.d_s32, &c.d_d32, &c.d_t32}) CK(dalloc(p, nv));
+    CK(dalloc(&c.d_isc, 16));
+    init_kernel_attributes();
     c.npart = (int)std::max<int64_t>({(int64_t)152 * 8, (l0.nel + 255) / 256 + 1, (l0.nnode + 255) / 256 + 1,
                                       (int64_t)((l0.ny + 31) / 31 + 1) * ((l0.nx + 7) / 7 + 1) * ((l0.nz + 16) / 16 + 1)});
     CK(dalloc(&c.d_part, c.npart));
+    CK(dalloc(&c.d_part2, c.npart));
     CK(dalloc(&c.d_scal, 64));
     CK(dalloc(&c.d_iflag, 64));
     CK(cudaMemset(c.d_iflag, 0, 64 * sizeof(int)));
@@ -497,8 +576,10 @@ void sgld_destroy(sgld_ctx *ctx) {
                     (void *)c.d_x, (void *)c.d_r, (void *)c.d_z, (void *)c.d_p, (void *)c.d_q, (void *)c.d_tmp,
                     (void *)c.d_r32, (void *)c.d_z32, (void *)c.d_part, (void *)c.d_scal, (void *)c.d_iflag,
                     (void *)c.d_Ac, (void *)c.d_Ainv, (void *)c.d_Ainv32, (void *)c.d_cpart, (void *)c.d_cfree,
-                    (void *)c.d_H, (void *)ctx->d_s6, (void *)ctx->d_vmn, (void *)ctx->d_vme})
+                    (void *)c.d_H, (void *)ctx->d_s6, (void *)ctx->d_vmn, (void *)ctx->d_vme, (void *)c.d_e32,
+                    (void *)c.d_s32, (void *)c.d_d32, (void *)c.d_t32, (void *)c.d_isc, (void *)c.d_part2})
         if (p) cudaFree(p);
+    if (c.inner_graph) cudaGraphExecDestroy(c.inner_graph);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete ctx;
 }
@@ -814,7 +895,7 @@ int sgld_pcg_device(sgld_ctx *ctx, const double *d_b, double *d_x, const sgld_so
     launch_scatter_nodes(c.d_nodemap, n, d_b, c.d_b, c.stream);
     if (o->use_x0) launch_scatter_nodes(c.d_nodemap, n, d_x, c.d_x, c.stream);
     CKL();
-    if ((rc = pcg_dev(ctx, o, info))) return rc;
+    if ((rc = solve_dev(ctx, o, info))) return rc;
     launch_gather_nodes(c.d_nodemap, n, c.d_x, d_x, c.stream);
     CKL();
     CK(cudaStreamSynchronize(c.stream));
@@ -832,7 +913,7 @@ int sgld_pcg(sgld_ctx *ctx, const double *b, double *x, const sgld_solve_opts *o
     } else {
         CK(cudaMemsetAsync(c.d_x, 0, sizeof(double) * 3 * c.lv[0].nnode, c.stream));
     }
-    if ((rc = pcg_dev(ctx, o, info))) return rc;
+    if ((rc = solve_dev(ctx, o, info))) return rc;
     return download_nodes(ctx, c.d_x, x);
 }
 
@@ -1013,4 +1094,157 @@ int pcg_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
     return SGLD_OK;
 }
 
+// Mixed precision: FP64 flexible PCG whose preconditioner is k FP32 CG
+// iterations with the FP32 additive V-cycle (graph-captured).  The FP64
+// residual recurrence, dot products, stopping test and K*p stay in FP64, so
+// the outer solve reaches the same tolerance on the true residual.
+int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
+    Ctx &c = ctx->c;
+    const Level &l0 = c.lv[0];
+    const int64_t nv = 3 * l0.nnode;
+    const int nbv = reduce_blocks(nv);
+    const double tol = o->tol;
+    const int maxit = o->maxit;
+    const int k = o->inner_its > 0 ? o->inner_its : 12;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, c.stream));
+    int nb = 0, rc;
+    launch_pcg_scalar(5, c.d_scal, c.d_iflag, c.d_part, 1, tol, maxit, c.stream);
+    launch_dot(c.d_b, c.d_b, nv, c.d_part, nbv, c.stream);
+    launch_pcg_scalar(0, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
+    if (o->use_x0) {
+        launch_kbyu_f64(l0, c.E, c.d_x, c.d_q, nullptr, nullptr, c.stream);
+        launch_residual(c.d_r, c.d_b, c.d_q, nv, c.stream);
+    } else {
+        CK(cudaMemcpyAsync(c.d_r, c.d_b, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c.stream));
+    }
+    launch_narrow(c.d_r, c.d_r32, nv, c.stream);
+    if ((rc = inner_run(ctx, k))) return rc;
+    launch_widen_dots(c.d_e32, c.d_z, c.d_r, c.d_r, nv, c.d_part, c.d_part2, nbv, c.stream);
+    launch_flex_beta(c.d_scal, c.d_iflag, c.d_part, c.d_part2, nbv, 1, c.stream);
+    CK(cudaMemcpyAsync(c.d_p, c.d_z, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c.stream));
+    int h_flag[4] = {0, 0, 0, 0};
+    const bool prof = o->profile != 0;
+    cudaEvent_t pe[4] = {nullptr, nullptr, nullptr, nullptr};
+    if (prof)
+        for (auto &e : pe) CK(cudaEventCreate(&e));
+    double kb_ms = 0.0, pc_ms = 0.0;
+    int kb_n = 0, outer = 0;
+    bool pc_pending = false;
+    for (int it = 1; it <= maxit; ++it) {
+        if (prof) CK(cudaEventRecord(pe[0], c.stream));
+        launch_kbyu_f64(l0, c.E, c.d_p, c.d_q, c.d_part, &nb, c.stream);
+        if (prof) CK(cudaEventRecord(pe[1], c.stream));
+        launch_pcg_scalar(2, c.d_scal, c.d_iflag, c.d_part, nb, tol, maxit, c.stream);
+        launch_pcg_update(c.d_x, c.d_r, c.d_p, c.d_q, nv, c.d_scal, c.d_iflag, c.d_part, nbv, c.stream);
+        launch_pcg_scalar(3, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
+        CK(cudaMemcpyAsync(h_flag, c.d_iflag, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.stream));
+        if (o->history) CK(cudaMemcpyAsync(o->history + (it - 1), c.d_scal + 3, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaStreamSynchronize(c.stream));
+        outer = it;
+        if (prof) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, pe[0], pe[1]);
+            kb_ms += t;
+            ++kb_n;
+            if (pc_pending) {
+                cudaEventElapsedTime(&t, pe[2], pe[3]);
+                pc_ms += t;
+                pc_pending = false;
+            }
+        }
+        if (h_flag[2]) break;
+        if (prof) CK(cudaEventRecord(pe[2], c.stream));
+        launch_narrow(c.d_r, c.d_r32, nv, c.stream);
+        if ((rc = inner_run(ctx, k))) return rc;
+        launch_widen_dots(c.d_e32, c.d_z, c.d_r, c.d_q, nv, c.d_part, c.d_part2, nbv, c.stream);
+        if (prof) {
+            CK(cudaEventRecord(pe[3], c.stream));
+            pc_pending = true;
+        }
+        launch_flex_beta(c.d_scal, c.d_iflag, c.d_part, c.d_part2, nbv, 0, c.stream);
+        launch_pcg_pupdate(c.d_p, c.d_z, nv, c.d_scal, c.d_iflag, c.stream);
+        CKL();
+    }
+    CK(cudaEventRecord(e1, c.stream));
+    double sc[8];
+    CK(cudaMemcpyAsync(h_flag, c.d_iflag, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaMemcpyAsync(sc, c.d_scal, sizeof(double) * 8, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    if (prof) {
+        if (pc_pending) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, pe[2], pe[3]);
+            pc_ms += t;
+        }
+        for (auto &e : pe) cudaEventDestroy(e);
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    launch_kbyu_f64(l0, c.E, c.d_x, c.d_q, nullptr, nullptr, c.stream);
+    launch_residual(c.d_tmp, c.d_b, c.d_q, nv, c.stream);
+    launch_dot(c.d_tmp, c.d_tmp, nv, c.d_part, nbv, c.stream);
+    launch_finalize_sum(c.d_part, nbv, c.d_scal + 17, c.stream);
+    CKL();
+    double rr = 0;
+    CK(cudaMemcpyAsync(&rr, c.d_scal + 17, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    if (info) {
+        info->iterations = h_flag[0];
+        info->converged = h_flag[1];
+        info->relres = sc[3];
+        info->true_relres = sc[0] > 0 ? sqrt(rr) / sc[0] : 0.0;
+        info->inner_iterations = k * outer;
+        info->seconds = ms * 1e-3;
+        info->kbyu_seconds = kb_ms * 1e-3;
+        info->kbyu_launches = kb_n;
+        info->precond_seconds = pc_ms * 1e-3;
+    }
+    return SGLD_OK;
+}
+
 }  // namespace
+
+extern "C" int sgld_time_op(sgld_ctx *ctx, int op, int reps, double *ms_per_op) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!ms_per_op || reps < 1 || op < 0 || op > 4) return fail(ctx, SGLD_ERR_ARG, "bad op / reps");
+    if ((op == 2 || op == 3) && !ctx->c.assembled) return fail(ctx, SGLD_ERR_STATE, "stencil not assembled");
+    Ctx &c = ctx->c;
+    const Level &l0 = c.lv[0];
+    const int64_t nv = 3 * l0.nnode;
+    if (op == 1 || op == 3) {
+        launch_cast_f32(c.E, c.d_E32, l0.nel, c.stream);
+        launch_narrow(c.d_p, c.d_r32, nv, c.stream);
+    }
+    auto once = [&]() -> int {
+        switch (op) {
+            case 0: launch_kbyu_f64(l0, c.E, c.d_p, c.d_q, nullptr, nullptr, c.stream); break;
+            case 1: launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, c.stream); break;
+            case 2: return vcycle_dev(ctx, c.d_p, c.d_z, nullptr, nullptr);
+            case 3: return vcycle_dev32(ctx, c.d_r32, c.d_z32, nullptr, nullptr);
+            case 4: return sgld_assemble(ctx);
+        }
+        return SGLD_OK;
+    };
+    if ((rc = once())) return rc;   // warm-up
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaEventRecord(a, c.stream));
+    for (int i = 0; i < reps; ++i)
+        if ((rc = once())) return rc;
+    CK(cudaEventRecord(b, c.stream));
+    CK(cudaEventSynchronize(b));
+    CKL();
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms_per_op = ms / reps;
+    return SGLD_OK;
+}

@@ -74,6 +74,12 @@ struct Ctx {
     int npart = 0;
     // mixed-precision work
     float *d_r32 = nullptr, *d_z32 = nullptr, *d_E32 = nullptr;
+    float *d_e32 = nullptr, *d_s32 = nullptr, *d_d32 = nullptr, *d_t32 = nullptr;
+    double *d_part2 = nullptr;      // second partial-sum buffer
+    double *d_isc = nullptr;        // inner CG scalars
+    cudaGraphExec_t inner_graph = nullptr;
+    int inner_graph_k = 0;
+    int64_t inner_graph_launches = 0;
     cudaStream_t stream = nullptr;
     std::string err;
     int device = 0;
@@ -88,7 +94,19 @@ extern int64_t g_launches;
 void upload_kh(const double *Kh, cudaStream_t s);
 void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *y, double *partial_dot,
                      int *nblocks_out, cudaStream_t s);
-void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, cudaStream_t s);
+void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
+                     int *nblocks_out, cudaStream_t s);
+void init_kernel_attributes();
+// mixed-precision solve (kernels_mixed.cu)
+void launch_icg_scalar(int op, double *sc, const double *part, int nb, cudaStream_t s);
+void launch_icg_update(float *e, float *s, const float *d, const float *t, int64_t n, const double *sc,
+                       cudaStream_t st);
+void launch_icg_dupdate(float *d, const float *w, int64_t n, const double *sc, cudaStream_t st);
+void launch_widen_dots(const float *e, double *z, const double *r, const double *q, int64_t n, double *p1,
+                       double *p2, int nb, cudaStream_t st);
+void launch_flex_beta(double *scal, const int *iflag, const double *p1, const double *p2, int nb, int first,
+                      cudaStream_t st);
+void launch_narrow(const double *a, float *b, int64_t n, cudaStream_t st);
 void launch_unit_compliance(const Level &l0, const double *u, const double *E, double *ce_full,
                             double *partial, int *nblocks_out, cudaStream_t s);
 void launch_stress(const Level &l0, const double *E, const double *u, const double *M48x24,

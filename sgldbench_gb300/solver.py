@@ -247,6 +247,14 @@ class VoxelSolver:
                                              C.byref(info)))
         return _info_dict(info)
 
+    OPS = {"kbyu64": 0, "kbyu32": 1, "vcycle64": 2, "vcycle32": 3, "assemble": 4}
+
+    def time_op(self, op: str, reps: int = 10) -> float:
+        """Mean device milliseconds of one internal operator (CUDA events)."""
+        ms = C.c_double()
+        self._check(self.lib.sgld_time_op(self.ctx, self.OPS[op], int(reps), C.byref(ms)))
+        return ms.value
+
     @property
     def stream(self) -> int:
         """cudaStream_t of this context (every call runs on it)."""

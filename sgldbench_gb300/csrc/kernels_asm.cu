@@ -269,112 +269,44 @@ __global__ void k_syrk_update(double *A, int n, int k0, int jb0, int nbt) {
     }
 }
 
-// forward block substitution for Y = L^-1 (Y lower triangular), block row bi,
-// all column tiles bj <= bi in parallel (one CTA each, NB threads = columns).
-__global__ void k_trsm_fwd(const double *L, double *Y, int n, int bi, int bw) {
-    const int bj = blockIdx.x;
-    __shared__ double Ld[NB][NB + 1];
-    __shared__ double Lo[NB][NB + 1];
-    __shared__ double Yt[NB][NB + 1];
-    const int t = threadIdx.x;
-    const int i0 = bi * NB, j0 = bj * NB;
-    const int mi = min(NB, n - i0);
-    for (int idx = t; idx < NB * NB; idx += NB) {
-        const int r = idx % NB, c = idx / NB;
-        Ld[r][c] = (r < mi && c < mi) ? L[(int64_t)(i0 + r) + (int64_t)n * (i0 + c)] : 0.0;
-    }
-    // rhs: identity block on the diagonal, else 0
-    double acc[NB];
-#pragma unroll
-    for (int r = 0; r < NB; ++r) acc[r] = (bi == bj && r == t) ? 1.0 : 0.0;
-    const int kb0 = max(bj, bi - bw);
-    for (int kb = kb0; kb < bi; ++kb) {
-        const int k0 = kb * NB;
-        __syncthreads();
-        for (int idx = t; idx < NB * NB; idx += NB) {
-            const int r = idx % NB, c = idx / NB;
-            Lo[r][c] = (r < mi && k0 + c < n) ? L[(int64_t)(i0 + r) + (int64_t)n * (k0 + c)] : 0.0;
-            Yt[r][c] = (k0 + r < n && j0 + c < n) ? Y[(int64_t)(k0 + r) + (int64_t)n * (j0 + c)] : 0.0;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < NB; ++r) {
-            double v = 0.0;
-#pragma unroll 8
-            for (int q = 0; q < NB; ++q) v += Lo[r][q] * Yt[q][t];
-            acc[r] -= v;
-        }
-    }
-    __syncthreads();
-    // solve Ld * y = acc (column t)
-#pragma unroll
-    for (int r = 0; r < NB; ++r) {
-        if (r < mi) {
-            double v = acc[r];
-            for (int q = 0; q < r; ++q) v -= Ld[r][q] * acc[q];
-            acc[r] = v / Ld[r][r];
-        }
-    }
-    if (j0 + t < n)
-#pragma unroll
-        for (int r = 0; r < NB; ++r)
-            if (r < mi) Y[(int64_t)(i0 + r) + (int64_t)n * (j0 + t)] = acc[r];
-}
-
-// backward block substitution X = L^-T Y, block row bi (descending), all
-// column tiles; X overwrites Y in place.
-__global__ void k_trsm_bwd(const double *L, double *Y, int n, int bi, int bw, int nblk) {
-    const int bj = blockIdx.x;
-    __shared__ double Ld[NB][NB + 1];
-    __shared__ double Lo[NB][NB + 1];
-    __shared__ double Xt[NB][NB + 1];
-    const int t = threadIdx.x;
-    const int i0 = bi * NB, j0 = bj * NB;
-    const int mi = min(NB, n - i0);
-    for (int idx = t; idx < NB * NB; idx += NB) {
-        const int r = idx % NB, c = idx / NB;
-        Ld[r][c] = (r < mi && c < mi) ? L[(int64_t)(i0 + r) + (int64_t)n * (i0 + c)] : 0.0;
-    }
-    double acc[NB];
-#pragma unroll
-    for (int r = 0; r < NB; ++r) acc[r] = (r < mi && j0 + t < n) ? Y[(int64_t)(i0 + r) + (int64_t)n * (j0 + t)] : 0.0;
-    const int kb1 = min(nblk - 1, bi + bw);
-    for (int kb = bi + 1; kb <= kb1; ++kb) {
-        const int k0 = kb * NB;
-        __syncthreads();
-        for (int idx = t; idx < NB * NB; idx += NB) {
-            const int r = idx % NB, c = idx / NB;
-            // Lo[r][c] = L[k0 + c, i0 + r]  (transpose of the sub-diagonal tile)
-            Lo[r][c] = (r < mi && k0 + c < n) ? L[(int64_t)(k0 + c) + (int64_t)n * (i0 + r)] : 0.0;
-            Xt[r][c] = (k0 + r < n && j0 + c < n) ? Y[(int64_t)(k0 + r) + (int64_t)n * (j0 + c)] : 0.0;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < NB; ++r) {
-            double v = 0.0;
-#pragma unroll 8
-            for (int q = 0; q < NB; ++q) v += Lo[r][q] * Xt[q][t];
-            acc[r] -= v;
-        }
-    }
-    __syncthreads();
-    // solve Ld' x = acc
-    for (int r = NB - 1; r >= 0; --r) {
-        if (r < mi) {
-            double v = acc[r];
-            for (int q = r + 1; q < mi; ++q) v -= Ld[q][r] * acc[q];
-            acc[r] = v / Ld[r][r];
-        }
-    }
-    if (j0 + t < n)
-#pragma unroll
-        for (int r = 0; r < NB; ++r)
-            if (r < mi) Y[(int64_t)(i0 + r) + (int64_t)n * (j0 + t)] = acc[r];
-}
-
 __global__ void k_to_f32(const double *a, float *b, int64_t n) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) b[i] = (float)a[i];
+}
+
+// LB[i*(b+1) + d] = L[i, i-b+d], d = 0..b (0 outside the matrix)
+__global__ void k_band_rows(const double *__restrict__ L, int n, int b, double *__restrict__ LB) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)n * (b + 1)) return;
+    const int i = (int)(t / (b + 1)), d = (int)(t % (b + 1));
+    const int k = i - b + d;
+    LB[t] = (k >= 0) ? L[(int64_t)i + (int64_t)n * k] : 0.0;
+}
+
+// M = L^-1: warp w of the CTA owns column c; for rows i = c..n-1
+//   M[i,c] = (delta_ic - sum_{k=max(c,i-b)}^{i-1} L[i,k] M[k,c]) / L[i,i],
+// with the last R values of the column kept in a shared ring (R a power of
+// two > b, dynamic shared memory of warps * R doubles).
+__global__ void k_trinv_cols(const double *__restrict__ LB, int n, int b, int R, double *__restrict__ M) {
+    extern __shared__ double ringmem[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = blockIdx.x * (blockDim.x >> 5) + w;
+    if (c >= n) return;
+    double *ring = ringmem + (int64_t)w * R;
+    for (int i = c; i < n; ++i) {
+        const int k0 = max(c, i - b);
+        const double *row = LB + (int64_t)i * (b + 1) - (i - b);   // row[k] = L[i,k]
+        double s = 0.0;
+        for (int k = k0 + lane; k < i; k += 32) s += row[k] * ring[k & (R - 1)];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        const double v = ((i == c ? 1.0 : 0.0) - s) / row[i];
+        if (lane == 0) {
+            ring[i & (R - 1)] = v;
+            M[(int64_t)i + (int64_t)n * c] = v;
+        }
+        __syncwarp();
+    }
 }
 
 int coarse_factor_invert(Ctx &c) {
@@ -399,16 +331,21 @@ int coarse_factor_invert(Ctx &c) {
             k_syrk_update<<<npairs, 256, 0, c.stream>>>(A, n, k0, kb + 1, nbelow);
         }
     }
-    // inverse: Y = L^-1 then X = L^-T Y (in d_Ainv)
+    // M = L^-1 (dense lower triangular) column by column: one warp per column,
+    // rows in order, the band of L read as contiguous rows
+    const int b = c.cband;
+    ++g_launches;
+    k_band_rows<<<(unsigned)(((int64_t)n * (b + 1) + 255) / 256), 256, 0, c.stream>>>(A, n, b, c.d_LB);
     cudaMemsetAsync(c.d_Ainv, 0, sizeof(double) * (size_t)n * n, c.stream);
-    for (int bi = 0; bi < nblk; ++bi) {
-        ++g_launches;
-        k_trsm_fwd<<<bi + 1, NB, 0, c.stream>>>(A, c.d_Ainv, n, bi, bw);
-    }
-    for (int bi = nblk - 1; bi >= 0; --bi) {
-        ++g_launches;
-        k_trsm_bwd<<<nblk, NB, 0, c.stream>>>(A, c.d_Ainv, n, bi, bw, nblk);
-    }
+    int R = 32;
+    while (R < b + 1) R <<= 1;
+    int warps = 8;
+    while (warps > 1 && (size_t)warps * R * sizeof(double) > 200 * 1024) warps >>= 1;
+    const size_t smem = (size_t)warps * R * sizeof(double);
+    if (smem > 220 * 1024) return -2;   // band too wide for the shared ring
+    cudaFuncSetAttribute(k_trinv_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    ++g_launches;
+    k_trinv_cols<<<(n + warps - 1) / warps, 32 * warps, smem, c.stream>>>(c.d_LB, n, b, R, c.d_Ainv);
     const int64_t nn = (int64_t)n * n;
     ++g_launches;
     k_to_f32<<<(unsigned)((nn + 255) / 256), 256, 0, c.stream>>>(c.d_Ainv, c.d_Ainv32, nn);
@@ -418,48 +355,64 @@ int coarse_factor_invert(Ctx &c) {
     return info;
 }
 
-// ---- coarse apply: x_L[free] = A^-1 r_L[free] ------------------------------------
+// ---- coarse apply: x_L[free] = A^-1 r_L[free] = M' (M r) -------------------------
+// y = M r (M lower triangular): rows in threads, columns split into CSPLIT chunks
 template <typename T>
-__global__ void k_coarse_gemv(const T *__restrict__ Ainv, const int *__restrict__ rows, const T *__restrict__ r, int n,
-                              double *__restrict__ part) {
+__global__ void k_coarse_lower(const T *__restrict__ M, const int *__restrict__ rows, const T *__restrict__ r, int n,
+                               double *__restrict__ part) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int chunk = (n + CSPLIT - 1) / CSPLIT;
-    const int j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+    const int j0 = blockIdx.y * chunk, j1 = min(min(n, j0 + chunk), i + 1);
     if (i >= n) return;
     T acc = T(0);
-    for (int j = j0; j < j1; ++j) acc += Ainv[(int64_t)i + (int64_t)n * j] * r[rows[j]];
+    for (int j = j0; j < j1; ++j) acc += M[(int64_t)i + (int64_t)n * j] * r[rows[j]];
     part[(int64_t)blockIdx.y * n + i] = (double)acc;
 }
 
 template <typename T>
-__global__ void k_coarse_finish(const double *__restrict__ part, const int *__restrict__ rows, int n, T *__restrict__ x) {
+__global__ void k_coarse_sum(const double *__restrict__ part, int n, T *__restrict__ y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double s = 0.0;
     for (int k = 0; k < CSPLIT; ++k) s += part[(int64_t)k * n + i];
-    x[rows[i]] = (T)s;
+    y[i] = (T)s;
+}
+
+// x_j = sum_{i >= j} M[i,j] y_i: one warp per column (coalesced column reads)
+template <typename T>
+__global__ void k_coarse_upper(const T *__restrict__ M, const int *__restrict__ rows, const T *__restrict__ y, int n,
+                               T *__restrict__ x) {
+    const int j = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (j >= n) return;
+    const T *col = M + (int64_t)n * j;
+    T acc = T(0);
+    for (int i = j + lane; i < n; i += 32) acc += col[i] * y[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) x[rows[j]] = acc;
+}
+
+template <typename T>
+static void coarse_apply(const Ctx &c, const T *M, const T *rc, T *xc, T *ybuf, cudaStream_t s) {
+    const Level &lc = c.lv[c.L - 1];
+    cudaMemsetAsync(xc, 0, sizeof(T) * 3 * lc.nnode, s);
+    if (c.ncf == 0) return;
+    dim3 g((c.ncf + 127) / 128, CSPLIT);
+    ++g_launches;
+    k_coarse_lower<T><<<g, 128, 0, s>>>(M, c.d_cfree, rc, c.ncf, c.d_cpart);
+    ++g_launches;
+    k_coarse_sum<T><<<(c.ncf + 127) / 128, 128, 0, s>>>(c.d_cpart, c.ncf, ybuf);
+    ++g_launches;
+    k_coarse_upper<T><<<(unsigned)(((int64_t)c.ncf * 32 + 255) / 256), 256, 0, s>>>(M, c.d_cfree, ybuf, c.ncf, xc);
 }
 
 void launch_coarse_apply_f64(const Ctx &c, const double *rc, double *xc, cudaStream_t s) {
-    const Level &lc = c.lv[c.L - 1];
-    cudaMemsetAsync(xc, 0, sizeof(double) * 3 * lc.nnode, s);
-    if (c.ncf == 0) return;
-    dim3 g((c.ncf + 127) / 128, CSPLIT);
-    ++g_launches;
-    k_coarse_gemv<double><<<g, 128, 0, s>>>(c.d_Ainv, c.d_cfree, rc, c.ncf, c.d_cpart);
-    ++g_launches;
-    k_coarse_finish<double><<<(c.ncf + 127) / 128, 128, 0, s>>>(c.d_cpart, c.d_cfree, c.ncf, xc);
+    coarse_apply<double>(c, c.d_Ainv, rc, xc, c.d_cy, s);
 }
 
 void launch_coarse_apply_f32(const Ctx &c, const float *rc, float *xc, cudaStream_t s) {
-    const Level &lc = c.lv[c.L - 1];
-    cudaMemsetAsync(xc, 0, sizeof(float) * 3 * lc.nnode, s);
-    if (c.ncf == 0) return;
-    dim3 g((c.ncf + 127) / 128, CSPLIT);
-    ++g_launches;
-    k_coarse_gemv<float><<<g, 128, 0, s>>>(c.d_Ainv32, c.d_cfree, rc, c.ncf, c.d_cpart);
-    ++g_launches;
-    k_coarse_finish<float><<<(c.ncf + 127) / 128, 128, 0, s>>>(c.d_cpart, c.d_cfree, c.ncf, xc);
+    coarse_apply<float>(c, c.d_Ainv32, rc, xc, reinterpret_cast<float *>(c.d_cy + c.ncf), s);
 }
 
 }  // namespace sgld

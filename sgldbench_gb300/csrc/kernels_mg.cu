@@ -14,7 +14,9 @@
 // The additive V-cycle of the reference (src/Solving_Vcycle.m:12-50) is
 //   r_l = R r_{l-1};  x_L = A_L^-1 r_L;
 //   x_{l} = t_l + P x_{l+1} + t_l  with t_l = (omega r_l) ./ D_l,
-// evaluated in that order so the rounding follows the reference.
+// summed in that order.  1 ./ D_l is formed once per assembly (the division
+// is the most expensive FP64 operation of the cycle), so t_l may differ from
+// the reference's (omega r_l) ./ D_l in the last bit.
 #include "sgld_internal.cuh"
 
 namespace sgld {
@@ -74,7 +76,8 @@ __device__ __forceinline__ double warp_block_sum(double v, double *red) {
     return s;
 }
 
-// x_f = t + P x_c + t, t = (omega r_f) ./ D_f on active fine nodes, 0 elsewhere.
+// x_f = t + P x_c + t, t = (omega r_f) .* D on active fine nodes, 0 elsewhere,
+// where D holds the reciprocal Jacobi diagonal.
 // FINAL (finest level): fixed DOFs set to 0 and partial sums of x_f . r_f.
 template <typename T, bool FINAL>
 __global__ void k_prolong_smooth(const T *__restrict__ xc, const T *__restrict__ rf, const T *__restrict__ D,
@@ -115,7 +118,7 @@ __global__ void k_prolong_smooth(const T *__restrict__ xc, const T *__restrict__
                 }
             }
             const T r0 = rf[3 * n], r1 = rf[3 * n + 1], r2 = rf[3 * n + 2];
-            const T t0 = (omega * r0) / D[3 * n], t1 = (omega * r1) / D[3 * n + 1], t2 = (omega * r2) / D[3 * n + 2];
+            const T t0 = (omega * r0) * D[3 * n], t1 = (omega * r1) * D[3 * n + 1], t2 = (omega * r2) * D[3 * n + 2];
             o0 = (t0 + p0) + t0;
             o1 = (t1 + p1) + t1;
             o2 = (t2 + p2) + t2;
@@ -222,6 +225,20 @@ __global__ void k_diag_from_Ks(const double *__restrict__ Ks, const uint8_t *__r
 void launch_diag_from_Ks(const Level &l, double *diag, cudaStream_t s) {
     ++g_launches;
     k_diag_from_Ks<<<(unsigned)((l.nnode + 255) / 256), 256, 0, s>>>(l.Ks, l.eact, l.nflag, l.ny, l.nx, l.nz, diag);
+}
+
+__global__ void k_inverse_diag(const double *__restrict__ D, const uint8_t *__restrict__ nflag, int64_t nn,
+                               double *__restrict__ iD, float *__restrict__ iD32) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= 3 * nn) return;
+    const double v = (nflag[i / 3] & NF_ACTIVE) ? 1.0 / D[i] : 0.0;
+    iD[i] = v;
+    iD32[i] = (float)v;
+}
+
+void launch_inverse_diag(const Level &l, cudaStream_t s) {
+    ++g_launches;
+    k_inverse_diag<<<(unsigned)((3 * l.nnode + 255) / 256), 256, 0, s>>>(l.diag, l.nflag, l.nnode, l.idiag, l.idiag32);
 }
 
 // ---- compact <-> full conversions -------------------------------------------

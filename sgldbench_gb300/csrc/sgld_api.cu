@@ -280,7 +280,7 @@ int vcycle_dev(sgld_ctx *ctx, const double *r, double *z, double *partial, int *
     for (int l = L - 2; l >= 0; --l) {
         const double *rl = (l == 0) ? r : c.lv[l].r;
         double *xl = (l == 0) ? z : c.lv[l].x;
-        launch_prolong_smooth<double>(c.lv[l], c.lv[l + 1], c.lv[l + 1].x, rl, c.lv[l].diag, c.omega, xl, l == 0,
+        launch_prolong_smooth<double>(c.lv[l], c.lv[l + 1], c.lv[l + 1].x, rl, c.lv[l].idiag, c.omega, xl, l == 0,
                                       l == 0 ? partial : nullptr, l == 0 ? nb : nullptr, c.stream);
     }
     CKL();
@@ -300,7 +300,7 @@ int vcycle_dev32(sgld_ctx *ctx, const float *r, float *z, double *partial, int *
     for (int l = L - 2; l >= 0; --l) {
         const float *rl = (l == 0) ? r : c.lv[l].r32;
         float *xl = (l == 0) ? z : c.lv[l].x32;
-        launch_prolong_smooth<float>(c.lv[l], c.lv[l + 1], c.lv[l + 1].x32, rl, c.lv[l].diag32, (float)c.omega, xl,
+        launch_prolong_smooth<float>(c.lv[l], c.lv[l + 1], c.lv[l + 1].x32, rl, c.lv[l].idiag32, (float)c.omega, xl,
                                      l == 0, l == 0 ? partial : nullptr, l == 0 ? nb : nullptr, c.stream);
     }
     return SGLD_OK;
@@ -523,7 +523,8 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
         CK(cudaMemcpy(lv.nflag, lv.h_nflag.data(), lv.nnode, cudaMemcpyHostToDevice));
         if (l < L - 1) {
             CK(dalloc(&lv.diag, 3 * lv.nnode));
-            CK(dalloc(&lv.diag32, 3 * lv.nnode));
+            CK(dalloc(&lv.idiag, 3 * lv.nnode));
+            CK(dalloc(&lv.idiag32, 3 * lv.nnode));
         }
         if (l > 0) {
             CK(dalloc(&lv.Ks, 576 * (size_t)lv.nel));
@@ -568,7 +569,7 @@ void sgld_destroy(sgld_ctx *ctx) {
     if (!ctx) return;
     Ctx &c = ctx->c;
     for (Level &l : c.lv) {
-        for (void *p : {(void *)l.eact, (void *)l.nflag, (void *)l.diag, (void *)l.diag32, (void *)l.Ks, (void *)l.r,
+        for (void *p : {(void *)l.eact, (void *)l.nflag, (void *)l.diag, (void *)l.idiag, (void *)l.idiag32, (void *)l.Ks, (void *)l.r,
                         (void *)l.x, (void *)l.r32, (void *)l.x32})
             if (p) cudaFree(p);
     }
@@ -577,7 +578,8 @@ void sgld_destroy(sgld_ctx *ctx) {
                     (void *)c.d_r32, (void *)c.d_z32, (void *)c.d_part, (void *)c.d_scal, (void *)c.d_iflag,
                     (void *)c.d_Ac, (void *)c.d_Ainv, (void *)c.d_Ainv32, (void *)c.d_cpart, (void *)c.d_cfree,
                     (void *)c.d_H, (void *)ctx->d_s6, (void *)ctx->d_vmn, (void *)ctx->d_vme, (void *)c.d_e32,
-                    (void *)c.d_s32, (void *)c.d_d32, (void *)c.d_t32, (void *)c.d_isc, (void *)c.d_part2})
+                    (void *)c.d_s32, (void *)c.d_d32, (void *)c.d_t32, (void *)c.d_isc, (void *)c.d_part2, (void *)c.d_LB,
+                    (void *)c.d_cy})
         if (p) cudaFree(p);
     if (c.inner_graph) cudaGraphExecDestroy(c.inner_graph);
     if (c.stream) cudaStreamDestroy(c.stream);
@@ -694,23 +696,29 @@ int sgld_set_fixed_dofs(sgld_ctx *ctx, const uint8_t *fixed) {
                 if (hi >= lo) band = std::max(band, hi - lo);
             }
     ctx->h_rows = rows;
-    if (ncf != c.ncf) {
-        for (void *p : {(void *)c.d_Ac, (void *)c.d_Ainv, (void *)c.d_Ainv32, (void *)c.d_cpart, (void *)c.d_cfree})
+    if (ncf != c.ncf || band != c.cband || !c.d_cfree) {
+        for (void *p : {(void *)c.d_Ac, (void *)c.d_Ainv, (void *)c.d_Ainv32, (void *)c.d_cpart, (void *)c.d_cfree,
+                        (void *)c.d_LB, (void *)c.d_cy})
             if (p) cudaFree(p);
-        c.d_Ac = c.d_Ainv = nullptr;
+        c.d_Ac = c.d_Ainv = c.d_LB = c.d_cy = c.d_cpart = nullptr;
         c.d_Ainv32 = nullptr;
-        c.d_cpart = nullptr;
         c.d_cfree = nullptr;
         c.ncf = ncf;
+        c.cband = band;
         CK(dalloc(&c.d_Ac, (size_t)ncf * ncf));
         CK(dalloc(&c.d_Ainv, (size_t)ncf * ncf));
         CK(dalloc(&c.d_Ainv32, (size_t)ncf * ncf));
         CK(dalloc(&c.d_cpart, (size_t)CSPLIT * ncf));
+        CK(dalloc(&c.d_LB, (size_t)ncf * (band + 1)));
+        CK(dalloc(&c.d_cy, 2 * (size_t)ncf));
+        CK(dalloc(&c.d_cfree, (size_t)ncf + 3 * lc.nnode));
+        if (c.inner_graph) {   // the captured inner solve holds the old coarse buffers
+            cudaGraphExecDestroy(c.inner_graph);
+            c.inner_graph = nullptr;
+        }
     }
-    if (!c.d_cfree) CK(dalloc(&c.d_cfree, (size_t)ncf + 3 * lc.nnode));
     CK(cudaMemcpy(c.d_cfree, rows.data(), sizeof(int) * ncf, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c.d_cfree + ncf, pos.data(), sizeof(int) * 3 * lc.nnode, cudaMemcpyHostToDevice));
-    c.cband = band;
     c.have_fixed = true;
     c.assembled = false;
     return SGLD_OK;
@@ -763,10 +771,11 @@ int sgld_assemble(sgld_ctx *ctx) {
     const int info = coarse_factor_invert(c);
     CKL();
     CK(cudaStreamSynchronize(c.stream));
+    if (info == -2) return fail(ctx, SGLD_ERR_ARG, "coarsest-level band too wide; use more multigrid levels");
     if (info != 0)
         return fail(ctx, SGLD_ERR_NUMERIC,
                     "coarsest-level matrix is not positive definite (pivot " + std::to_string(info) + ")");
-    for (int l = 0; l < L - 1; ++l) launch_cast_f32(c.lv[l].diag, c.lv[l].diag32, 3 * c.lv[l].nnode, c.stream);
+    for (int l = 0; l < L - 1; ++l) launch_inverse_diag(c.lv[l], c.stream);
     launch_cast_f32(c.E, c.d_E32, c.lv[0].nel, c.stream);
     CKL();
     CK(cudaStreamSynchronize(c.stream));

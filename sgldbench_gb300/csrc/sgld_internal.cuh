@@ -35,7 +35,8 @@ struct Level {
     uint8_t *eact = nullptr;      // [nel] element non-empty
     uint8_t *nflag = nullptr;     // [nnode] NF_* bits
     double *diag = nullptr;       // [3*nnode] Jacobi diagonal (levels 1..L-1)
-    float *diag32 = nullptr;
+    double *idiag = nullptr;      // [3*nnode] 1 / diag on active nodes, 0 elsewhere
+    float *idiag32 = nullptr;
     double *Ks = nullptr;         // [576*nel] Galerkin element matrices (coarse levels)
     double *r = nullptr, *x = nullptr;      // [3*nnode] V-cycle work (coarse levels)
     float *r32 = nullptr, *x32 = nullptr;
@@ -62,6 +63,8 @@ struct Ctx {
     double *d_Ac = nullptr;         // [ncf*ncf] dense matrix / Cholesky factor
     double *d_Ainv = nullptr;       // [ncf*ncf] inverse (symmetric)
     float *d_Ainv32 = nullptr;
+    double *d_LB = nullptr;         // [ncf*(cband+1)] rows of the Cholesky factor's band
+    double *d_cy = nullptr;         // [2*ncf] intermediate of the coarse apply
     double *d_cpart = nullptr;      // [CSPLIT*ncf] GEMV partials
     // templates for the level-2 Galerkin assembly
     double *d_H = nullptr;          // [span^3 * 576]
@@ -121,6 +124,7 @@ void launch_prolong_smooth(const Level &fine, const Level &coarse, const T *xc, 
                            cudaStream_t s);
 void launch_diag_finest(const Level &l0, const double *E, const double *Ke, double *diag, cudaStream_t s);
 void launch_diag_from_Ks(const Level &l, double *diag, cudaStream_t s);
+void launch_inverse_diag(const Level &l, cudaStream_t s);   // l.idiag, l.idiag32 from l.diag
 void launch_scatter_nodes(const int64_t *map, int64_t n, const double *compact, double *full, cudaStream_t s);
 void launch_gather_nodes(const int64_t *map, int64_t n, const double *full, double *compact, cudaStream_t s);
 void launch_scatter_elems(const int64_t *map, int64_t n, const double *compact, double *full, cudaStream_t s);

@@ -8,11 +8,12 @@
 //  * level l>2: Ks_E = sum_q P_q' Ks_q P_q with P_q = W_q (x) I3, W_q the 8x8
 //    trilinear weights of the parent's corners at child q's corners;
 //  * coarsest: dense K on the free DOFs (in a bandwidth-reducing order),
-//    blocked band Cholesky K = L L', explicit inverse A^-1 = L^-T L^-1
-//    (two band TRSMs), applied per V-cycle as one dense GEMV.  The reference
+//    blocked band Cholesky K = L L' and the explicit triangular inverse
+//    M = L^-1, captured once into a CUDA graph; each V-cycle applies
+//    K^-1 r = M' (M r) as two dense triangular mat-vecs.  The reference
 //    applies its sparse Cholesky factor with two triangular solves
-//    (src/Solving_Vcycle.m:116-118); the inverse gives the same numbers to
-//    rounding and turns a sequential solve into a parallel mat-vec.
+//    (src/Solving_Vcycle.m:116-118); M' M gives the same numbers to rounding
+//    and turns two sequential solves into parallel mat-vecs.
 #include <math.h>
 
 #include <vector>
@@ -21,8 +22,28 @@
 
 namespace sgld {
 
+// Element matrices are symmetric: the kernels form the 300 entries of the
+// upper triangle (row <= col) and mirror them.
+__constant__ unsigned char c_pr[300], c_pc[300];
+
+static void upload_pairs(cudaStream_t s) {
+    static bool done = false;
+    if (done) return;
+    unsigned char pr[300], pc[300];
+    int k = 0;
+    for (int col = 0; col < 24; ++col)
+        for (int row = 0; row <= col; ++row) {
+            pr[k] = (unsigned char)row;
+            pc[k] = (unsigned char)col;
+            ++k;
+        }
+    cudaMemcpyToSymbolAsync(c_pr, pr, sizeof pr, 0, cudaMemcpyHostToDevice, s);
+    cudaMemcpyToSymbolAsync(c_pc, pc, sizeof pc, 0, cudaMemcpyHostToDevice, s);
+    done = true;
+}
+
 // ---- level 2 from the finest level ------------------------------------------
-__global__ void __launch_bounds__(192) k_asm_finest(const double *__restrict__ E, const uint8_t *__restrict__ eact_c,
+__global__ void __launch_bounds__(320) k_asm_finest(const double *__restrict__ E, const uint8_t *__restrict__ eact_c,
                                                     const double *__restrict__ H, int nyc, int nxc, int nzc, int s,
                                                     double *__restrict__ Ks) {
     const int64_t e = blockIdx.x + (int64_t)gridDim.x * blockIdx.y;
@@ -37,36 +58,40 @@ __global__ void __launch_bounds__(192) k_asm_finest(const double *__restrict__ E
         ev[q] = E[(int64_t)(s * cy + oy) + (int64_t)nyf * ((s * cx + ox) + (int64_t)nxf * (s * cz + oz))];
     }
     __syncthreads();
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
     const int t = threadIdx.x;
+    if (t >= 300) return;
+    const int r = c_pr[t], c = c_pc[t];
+    const int off = r + 24 * c;
+    double a = 0.0;
     for (int q = 0; q < nq; ++q) {
         const double w = ev[q];
-        if (w == 0.0) continue;
-        const double *h = H + 576 * q;
-        a0 += w * h[t];
-        a1 += w * h[t + 192];
-        a2 += w * h[t + 384];
+        if (w != 0.0) a += w * H[576 * q + off];
     }
     double *o = Ks + 576 * e;
-    o[t] = a0;
-    o[t + 192] = a1;
-    o[t + 384] = a2;
+    o[off] = a;
+    o[c + 24 * r] = a;
 }
 
 void launch_asm_finest(const Level &coarse, const Level &fine, const double *E, const double *H, double *Ks,
                        cudaStream_t s) {
     (void)fine;
+    upload_pairs(s);
     const int64_t nel = coarse.nel;
     const unsigned gx = (unsigned)(nel < 65535 ? nel : 65535);
     const unsigned gy = (unsigned)((nel + gx - 1) / gx);
     ++g_launches;
-    k_asm_finest<<<dim3(gx, gy), 192, 0, s>>>(E, coarse.eact, H, coarse.ny, coarse.nx, coarse.nz, coarse.span, Ks);
+    k_asm_finest<<<dim3(gx, gy), 320, 0, s>>>(E, coarse.eact, H, coarse.ny, coarse.nx, coarse.nz, coarse.span, Ks);
 }
 
 // ---- deeper levels: P_q' Ks_q P_q ---------------------------------------------
-__constant__ double c_W[8 * 64];   // W_q[j][a] at c_W[64 q + 8 j + a]
+// W_q[i][a] = trilinear weight of parent corner a at child q's corner i
+// (span 2, reference corner order, child q = oy + 2 ox + 4 oz).  Only 27 of
+// its 64 entries are nonzero; the kernel walks the nonzeros of each column.
+__constant__ unsigned char c_wn[8][8];      // nonzeros in column a of W_q
+__constant__ unsigned char c_wi[8][8][8];   // their row indices i
+__constant__ double c_ww[8][8][8];          // and weights
 
-__global__ void __launch_bounds__(192) k_asm_coarse(const double *__restrict__ Kf, const uint8_t *__restrict__ eact_f,
+__global__ void __launch_bounds__(320) k_asm_coarse(const double *__restrict__ Kf, const uint8_t *__restrict__ eact_f,
                                                     const uint8_t *__restrict__ eact_c, int nyc, int nxc, int nzc,
                                                     double *__restrict__ Ks) {
     const int64_t e = blockIdx.x + (int64_t)gridDim.x * blockIdx.y;
@@ -76,70 +101,76 @@ __global__ void __launch_bounds__(192) k_asm_coarse(const double *__restrict__ K
     const int cy = (int)(e % nyc), cx = (int)((e / nyc) % nxc), cz = (int)(e / ((int64_t)nyc * nxc));
     const int nyf = 2 * nyc, nxf = 2 * nxc;
     const int t = threadIdx.x;
-    double acc[3] = {0.0, 0.0, 0.0};
+    double acc = 0.0;
     for (int q = 0; q < 8; ++q) {
         const int oy = q & 1, ox = (q >> 1) & 1, oz = q >> 2;
         const int64_t f = (int64_t)(2 * cy + oy) + (int64_t)nyf * ((2 * cx + ox) + (int64_t)nxf * (2 * cz + oz));
         if (!eact_f[f]) continue;   // uniform per CTA
         const double *src = Kf + 576 * f;
-        for (int i = t; i < 576; i += 192) sk[i] = src[i];
+        for (int i = t; i < 576; i += blockDim.x) sk[i] = src[i];
         __syncthreads();
-        const double *W = c_W + 64 * q;
         // st[r + 24*(3a+d)] = sum_i sk[r + 24*(3i+d)] W[i][a]
-        for (int idx = t; idx < 576; idx += 192) {
+        for (int idx = t; idx < 576; idx += blockDim.x) {
             const int r = idx % 24, col = idx / 24, a = col / 3, d = col % 3;
             double v = 0.0;
-#pragma unroll
-            for (int i = 0; i < 8; ++i) v += sk[r + 24 * (3 * i + d)] * W[8 * i + a];
+            const int nz = c_wn[q][a];
+            for (int k = 0; k < nz; ++k) v += sk[r + 24 * (3 * c_wi[q][a][k] + d)] * c_ww[q][a][k];
             st[idx] = v;
         }
         __syncthreads();
-        // out[(3b+e) + 24*col] += sum_j W[j][b] st[(3j+e) + 24*col]
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const int idx = t + 192 * k;
-            const int row = idx % 24, col = idx / 24, b = row / 3, ec = row % 3;
+        // upper triangle of W' st: out[(3b+e), col] = sum_j W[j][b] st[(3j+e) + 24 col]
+        if (t < 300) {
+            const int row = c_pr[t], col = c_pc[t], b = row / 3, ec = row % 3;
             double v = 0.0;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) v += W[8 * j + b] * st[(3 * j + ec) + 24 * col];
-            acc[k] += v;
+            const int nz = c_wn[q][b];
+            for (int k = 0; k < nz; ++k) v += c_ww[q][b][k] * st[(3 * c_wi[q][b][k] + ec) + 24 * col];
+            acc += v;
         }
         __syncthreads();
     }
-    double *o = Ks + 576 * e;
-    o[t] = acc[0];
-    o[t + 192] = acc[1];
-    o[t + 384] = acc[2];
+    if (t < 300) {
+        double *o = Ks + 576 * e;
+        o[c_pr[t] + 24 * c_pc[t]] = acc;
+        o[c_pc[t] + 24 * c_pr[t]] = acc;
+    }
 }
 
 void launch_asm_coarse(const Level &coarse, const Level &fine, double *Ks, cudaStream_t s) {
-    // W_q for span 2, reference corner order, child order y fastest
     static bool uploaded = false;
+    upload_pairs(s);
     if (!uploaded) {
         const int cdy[8] = {1, 1, 0, 0, 1, 1, 0, 0}, cdx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, cdz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
-        double W[8 * 64];
+        unsigned char wn[8][8] = {}, wi[8][8][8] = {};
+        double ww[8][8][8] = {};
         for (int q = 0; q < 8; ++q) {
             const int oy = q & 1, ox = (q >> 1) & 1, oz = q >> 2;
-            for (int j = 0; j < 8; ++j) {
-                // child corner position in the 3x3x3 local block (units of fine cells)
-                const int py = oy + cdy[j], px = ox + cdx[j], pz = oz + cdz[j];
-                // natural coordinates in the parent: s = -1 + px, t = 1 - py, p = -1 + pz
-                const double sn = -1.0 + px, tn = 1.0 - py, pn = -1.0 + pz;
+            for (int i = 0; i < 8; ++i) {
+                // child corner position in parent units: natural coordinates
+                const double sn = -1.0 + (ox + cdx[i]), tn = 1.0 - (oy + cdy[i]), pn = -1.0 + (oz + cdz[i]);
                 const double N[8] = {(1 - sn) * (1 - tn) * (1 - pn), (1 + sn) * (1 - tn) * (1 - pn),
                                      (1 + sn) * (1 + tn) * (1 - pn), (1 - sn) * (1 + tn) * (1 - pn),
                                      (1 - sn) * (1 - tn) * (1 + pn), (1 + sn) * (1 - tn) * (1 + pn),
                                      (1 + sn) * (1 + tn) * (1 + pn), (1 - sn) * (1 + tn) * (1 + pn)};
-                for (int a = 0; a < 8; ++a) W[64 * q + 8 * j + a] = 0.125 * N[a];
+                for (int a = 0; a < 8; ++a) {
+                    const double w = 0.125 * N[a];
+                    if (w != 0.0) {
+                        const int k = wn[q][a]++;
+                        wi[q][a][k] = (unsigned char)i;
+                        ww[q][a][k] = w;
+                    }
+                }
             }
         }
-        cudaMemcpyToSymbolAsync(c_W, W, sizeof W, 0, cudaMemcpyHostToDevice, s);
+        cudaMemcpyToSymbolAsync(c_wn, wn, sizeof wn, 0, cudaMemcpyHostToDevice, s);
+        cudaMemcpyToSymbolAsync(c_wi, wi, sizeof wi, 0, cudaMemcpyHostToDevice, s);
+        cudaMemcpyToSymbolAsync(c_ww, ww, sizeof ww, 0, cudaMemcpyHostToDevice, s);
         uploaded = true;
     }
     const int64_t nel = coarse.nel;
     const unsigned gx = (unsigned)(nel < 65535 ? nel : 65535);
     const unsigned gy = (unsigned)((nel + gx - 1) / gx);
     ++g_launches;
-    k_asm_coarse<<<dim3(gx, gy), 192, 0, s>>>(fine.Ks, fine.eact, coarse.eact, coarse.ny, coarse.nx, coarse.nz, Ks);
+    k_asm_coarse<<<dim3(gx, gy), 320, 0, s>>>(fine.Ks, fine.eact, coarse.eact, coarse.ny, coarse.nx, coarse.nz, Ks);
 }
 
 // ---- coarsest level: dense matrix on the free DOFs ---------------------------
@@ -184,59 +215,51 @@ void launch_coarse_dense(const Level &lc, int ncf, const int *rows_and_pos, doub
 // ---- blocked band Cholesky, NB x NB tiles, column-major n x n ------------------
 constexpr int NB = 32;
 
-// factor the diagonal tile in place (lower), one CTA of NB*NB threads
-__global__ void k_potrf_tile(double *A, int n, int k0, int *info) {
-    __shared__ double T[NB][NB + 1];
-    const int tx = threadIdx.x % NB, ty = threadIdx.x / NB;   // tx = row, ty = col
+// Factors one block column of the band in place: the NB x NB diagonal tile
+// and the rows below it inside the band (prow rows in all, one thread per
+// row, the row's NB entries in registers).  Right-looking within the panel:
+// for each column j the diagonal thread forms sqrt, every row below scales,
+// and the trailing columns of the panel are updated with column j.
+__global__ void __launch_bounds__(384) k_potrf_panel(double *A, int n, int k0, int prow, int *info) {
+    __shared__ double col[NB];
+    __shared__ double dsh;
+    const int t = threadIdx.x;
+    const int r = k0 + t;
     const int m = min(NB, n - k0);
-    T[tx][ty] = (tx < m && ty < m) ? A[(int64_t)(k0 + tx) + (int64_t)n * (k0 + ty)] : (tx == ty ? 1.0 : 0.0);
-    __syncthreads();
-    for (int j = 0; j < m; ++j) {
-        if (tx == j && ty == j) {
-            const double d = T[j][j];
-            if (!(d > 0.0)) {
-                if (info) atomicExch(info, k0 + j + 1);
-                T[j][j] = 1.0;
-            } else {
-                T[j][j] = sqrt(d);
-            }
-        }
-        __syncthreads();
-        if (ty == j && tx > j) T[tx][j] /= T[j][j];
-        __syncthreads();
-        if (tx > j && ty > j && ty <= tx) T[tx][ty] -= T[tx][j] * T[ty][j];
-        __syncthreads();
-    }
-    if (tx < m && ty < m) A[(int64_t)(k0 + tx) + (int64_t)n * (k0 + ty)] = (ty <= tx) ? T[tx][ty] : 0.0;
-}
-
-// A[i-tile, k-tile] <- A[i-tile, k-tile] * L_kk^-T for tiles i = k+1 .. kend
-__global__ void k_trsm_panel(double *A, int n, int k0, int iblk0) {
-    __shared__ double L[NB][NB + 1];
-    const int t = threadIdx.x;   // NB threads: one per row of the panel tile
-    const int m = min(NB, n - k0);
-    for (int idx = t; idx < NB * NB; idx += NB) {
-        const int r = idx % NB, c = idx / NB;
-        L[r][c] = (r < m && c < m) ? A[(int64_t)(k0 + r) + (int64_t)n * (k0 + c)] : 0.0;
-    }
-    __syncthreads();
-    const int i0 = (iblk0 + blockIdx.x) * NB;
-    const int row = i0 + t;
-    if (row >= n) return;
+    const bool act = t < prow && r < n;
     double x[NB];
 #pragma unroll
-    for (int j = 0; j < NB; ++j) x[j] = (j < m) ? A[(int64_t)row + (int64_t)n * (k0 + j)] : 0.0;
+    for (int j = 0; j < NB; ++j) x[j] = (act && j < m) ? A[(int64_t)r + (int64_t)n * (k0 + j)] : 0.0;
 #pragma unroll
     for (int j = 0; j < NB; ++j) {
-        if (j < m) {
-            double v = x[j];
-            for (int q = 0; q < j; ++q) v -= x[q] * L[j][q];
-            x[j] = v / L[j][j];
+        if (j >= m) break;
+        if (t == j) {
+            double d = x[j];
+            if (!(d > 0.0)) {
+                if (info) atomicExch(info, k0 + j + 1);
+                d = 1.0;
+            }
+            dsh = sqrt(d);
+        }
+        __syncthreads();
+        const double d = dsh;
+        const double rd = 1.0 / d;
+        if (t == j)
+            x[j] = d;
+        else if (t > j)
+            x[j] *= rd;
+        if (t < NB) col[t] = x[j];
+        __syncthreads();
+        if (t > j) {
+#pragma unroll
+            for (int q = j + 1; q < NB; ++q) x[q] -= x[j] * col[q];
         }
     }
+    if (act) {
 #pragma unroll
-    for (int j = 0; j < NB; ++j)
-        if (j < m) A[(int64_t)row + (int64_t)n * (k0 + j)] = x[j];
+        for (int j = 0; j < NB; ++j)
+            if (j < m) A[(int64_t)r + (int64_t)n * (k0 + j)] = (t < NB && j > t) ? 0.0 : x[j];
+    }
 }
 
 // trailing update A[i,j] -= A[i,k] A[j,k]' for k < j <= i <= kend (tile pairs)
@@ -283,25 +306,42 @@ __global__ void k_band_rows(const double *__restrict__ L, int n, int b, double *
     LB[t] = (k >= 0) ? L[(int64_t)i + (int64_t)n * k] : 0.0;
 }
 
-// M = L^-1: warp w of the CTA owns column c; for rows i = c..n-1
-//   M[i,c] = (delta_ic - sum_{k=max(c,i-b)}^{i-1} L[i,k] M[k,c]) / L[i,i],
-// with the last R values of the column kept in a shared ring (R a power of
-// two > b, dynamic shared memory of warps * R doubles).
-__global__ void k_trinv_cols(const double *__restrict__ LB, int n, int b, int R, double *__restrict__ M) {
+// M = L^-1: warp w of the CTA owns column c and walks down it 32 rows at a
+// time, lane l holding row i = i0 + l of the block:
+//   1. s_l = sum_{k=max(c,i-b)}^{i0-1} L[i,k] M[k,c]   (rows above the block,
+//      kept in a shared ring of R >= b+1 values), all lanes in parallel;
+//   2. within the block, rows finish in order: lane t forms
+//      M[i0+t,c] = (delta - s_t) / L[i0+t,i0+t], broadcasts it, and the
+//      lanes below subtract its contribution.
+// LB holds the band of L row-wise (LB[i*(b+1)+d] = L[i,i-b+d]), rdiag = 1/diag(L).
+__global__ void k_trinv_cols(const double *__restrict__ LB, const double *__restrict__ rdiag, int n, int b, int R,
+                             double *__restrict__ M) {
     extern __shared__ double ringmem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int c = blockIdx.x * (blockDim.x >> 5) + w;
     if (c >= n) return;
     double *ring = ringmem + (int64_t)w * R;
-    for (int i = c; i < n; ++i) {
-        const int k0 = max(c, i - b);
-        const double *row = LB + (int64_t)i * (b + 1) - (i - b);   // row[k] = L[i,k]
+    const int64_t bs = b + 1;
+    for (int i0 = c; i0 < n; i0 += 32) {
+        const int i = i0 + lane;
+        const bool valid = i < n;
+        const double *row = LB + (int64_t)(valid ? i : i0) * bs;   // row[d] = L[i, i-b+d]
         double s = 0.0;
-        for (int k = k0 + lane; k < i; k += 32) s += row[k] * ring[k & (R - 1)];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        const double v = ((i == c ? 1.0 : 0.0) - s) / row[i];
-        if (lane == 0) {
+        if (valid) {
+            // k = i - b + t runs over [max(c, i-b), i0)
+            const int t0 = max(0, c - (i - b));
+            const int t1 = b - lane;   // k < i0
+            for (int t = t0; t < t1; ++t) s += row[t] * ring[(i - b + t) & (R - 1)];
+        }
+        double v = 0.0;
+#pragma unroll 4
+        for (int t = 0; t < 32; ++t) {
+            if (i0 + t >= n) break;
+            if (lane == t) v = ((i == c ? 1.0 : 0.0) - s) * rdiag[i];
+            const double vt = __shfl_sync(0xffffffffu, v, t);
+            if (lane > t && valid && lane - t <= b) s += row[b - lane + t] * vt;   // L[i, i0+t]
+        }
+        if (valid) {
             ring[i & (R - 1)] = v;
             M[(int64_t)i + (int64_t)n * c] = v;
         }
@@ -309,46 +349,81 @@ __global__ void k_trinv_cols(const double *__restrict__ LB, int n, int b, int R,
     }
 }
 
-int coarse_factor_invert(Ctx &c) {
+__global__ void k_recip_diag(const double *__restrict__ L, int n, double *__restrict__ rd) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) rd[i] = 1.0 / L[(int64_t)i + (int64_t)n * i];
+}
+
+// Enqueues the whole factorization (band Cholesky, L^-1, FP32 copy); no host
+// synchronisation, so the sequence is captured once into a CUDA graph.
+static void factor_enqueue(Ctx &c, int *d_info) {
     const int n = c.ncf;
-    if (n == 0) return 0;
     const int nblk = (n + NB - 1) / NB;
     const int bw = (c.cband + NB - 1) / NB + 1;   // band in tiles (safety margin of one)
-    int *d_info = c.d_iflag + 8;
-    cudaMemsetAsync(d_info, 0, sizeof(int), c.stream);
     double *A = c.d_Ac;
+    cudaMemsetAsync(d_info, 0, sizeof(int), c.stream);
     for (int kb = 0; kb < nblk; ++kb) {
         const int k0 = kb * NB;
-        ++g_launches;
-        k_potrf_tile<<<1, NB * NB, 0, c.stream>>>(A, n, k0, d_info);
         const int kend = min(nblk - 1, kb + bw);
         const int nbelow = kend - kb;
+        ++g_launches;
+        k_potrf_panel<<<1, NB * (1 + bw), 0, c.stream>>>(A, n, k0, NB * (1 + nbelow), d_info);
         if (nbelow > 0) {
-            ++g_launches;
-            k_trsm_panel<<<nbelow, NB, 0, c.stream>>>(A, n, k0, kb + 1);
             const int npairs = nbelow * (nbelow + 1) / 2;
             ++g_launches;
             k_syrk_update<<<npairs, 256, 0, c.stream>>>(A, n, k0, kb + 1, nbelow);
         }
     }
-    // M = L^-1 (dense lower triangular) column by column: one warp per column,
-    // rows in order, the band of L read as contiguous rows
     const int b = c.cband;
+    double *rdiag = c.d_LB + (int64_t)n * (b + 1);
     ++g_launches;
     k_band_rows<<<(unsigned)(((int64_t)n * (b + 1) + 255) / 256), 256, 0, c.stream>>>(A, n, b, c.d_LB);
-    cudaMemsetAsync(c.d_Ainv, 0, sizeof(double) * (size_t)n * n, c.stream);
-    int R = 32;
-    while (R < b + 1) R <<= 1;
-    int warps = 8;
-    while (warps > 1 && (size_t)warps * R * sizeof(double) > 200 * 1024) warps >>= 1;
-    const size_t smem = (size_t)warps * R * sizeof(double);
-    if (smem > 220 * 1024) return -2;   // band too wide for the shared ring
-    cudaFuncSetAttribute(k_trinv_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     ++g_launches;
-    k_trinv_cols<<<(n + warps - 1) / warps, 32 * warps, smem, c.stream>>>(c.d_LB, n, b, R, c.d_Ainv);
+    k_recip_diag<<<(n + 255) / 256, 256, 0, c.stream>>>(A, n, rdiag);
+    cudaMemsetAsync(c.d_Ainv, 0, sizeof(double) * (size_t)n * n, c.stream);
+    ++g_launches;
+    k_trinv_cols<<<(n + c.trinv_warps - 1) / c.trinv_warps, 32 * c.trinv_warps, c.trinv_smem, c.stream>>>(
+        c.d_LB, rdiag, n, b, c.trinv_ring, c.d_Ainv);
     const int64_t nn = (int64_t)n * n;
     ++g_launches;
     k_to_f32<<<(unsigned)((nn + 255) / 256), 256, 0, c.stream>>>(c.d_Ainv, c.d_Ainv32, nn);
+}
+
+// Cholesky of the dense coarsest matrix in d_Ac (lower, in place) and
+// M = L^-1 in d_Ainv / d_Ainv32.  Returns 0, the 1-based failing pivot, -1 on
+// a CUDA error or -2 when the band is too wide for the shared ring.
+int coarse_factor_invert(Ctx &c) {
+    const int n = c.ncf;
+    if (n == 0) return 0;
+    const int bw = (c.cband + NB - 1) / NB + 1;
+    if (NB * (1 + bw) > 384) return -2;
+    int *d_info = c.d_iflag + 8;
+    if (!c.factor_graph) {
+        int R = 32;
+        while (R < c.cband + 1) R <<= 1;
+        int warps = 8;
+        while (warps > 1 && (size_t)warps * R * sizeof(double) > 200 * 1024) warps >>= 1;
+        const size_t smem = (size_t)warps * R * sizeof(double);
+        if (smem > 220 * 1024) return -2;
+        cudaFuncSetAttribute(k_trinv_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        c.trinv_ring = R;
+        c.trinv_warps = warps;
+        c.trinv_smem = smem;
+        const int64_t before = g_launches;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return -1;
+        factor_enqueue(c, d_info);
+        if (cudaStreamEndCapture(c.stream, &g) != cudaSuccess) return -1;
+        c.factor_graph_launches = g_launches - before;
+        g_launches = before;
+        if (cudaGraphInstantiate(&c.factor_graph, g, 0) != cudaSuccess) {
+            cudaGraphDestroy(g);
+            return -1;
+        }
+        cudaGraphDestroy(g);
+    }
+    if (cudaGraphLaunch(c.factor_graph, c.stream) != cudaSuccess) return -1;
+    g_launches += c.factor_graph_launches;
     int info = 0;
     cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
     cudaStreamSynchronize(c.stream);

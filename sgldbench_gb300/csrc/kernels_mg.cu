@@ -25,10 +25,12 @@ template <typename T>
 __global__ void k_restrict(const T *__restrict__ rf, T *__restrict__ rc, int nyc, int nxc, int nzc, int s) {
     const int NYc = nyc + 1, NXc = nxc + 1, NZc = nzc + 1;
     const int NYf = s * nyc + 1, NXf = s * nxc + 1, NZf = s * nzc + 1;
-    const int64_t nn = (int64_t)NYc * NXc * NZc;
-    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (n >= nn) return;
-    const int I = (int)(n % NYc), J = (int)((n / NYc) % NXc), Kz = (int)(n / ((int64_t)NYc * NXc));
+    // grid: x over the (y, x) plane of coarse nodes, y over z (32-bit index math)
+    const int pl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pl >= NYc * NXc) return;
+    const int I = pl % NYc, J = pl / NYc, Kz = blockIdx.y;
+    const int64_t n = (int64_t)pl + (int64_t)NYc * NXc * Kz;
+    (void)NZc;
     const T inv = T(1) / T(s);
     T a0 = T(0), a1 = T(0), a2 = T(0);
     for (int dz = -s + 1; dz < s; ++dz) {
@@ -59,7 +61,9 @@ template <typename T>
 void launch_restrict(const Level &fine, const Level &coarse, const T *rf, T *rc, cudaStream_t st) {
     const int64_t nn = coarse.nnode;
     ++g_launches;
-    k_restrict<T><<<(unsigned)((nn + 127) / 128), 128, 0, st>>>(rf, rc, coarse.ny, coarse.nx, coarse.nz, coarse.span);
+    (void)nn;
+    const dim3 g((unsigned)(((coarse.ny + 1) * (coarse.nx + 1) + 127) / 128), (unsigned)(coarse.nz + 1));
+    k_restrict<T><<<g, 128, 0, st>>>(rf, rc, coarse.ny, coarse.nx, coarse.nz, coarse.span);
 }
 template void launch_restrict<double>(const Level &, const Level &, const double *, double *, cudaStream_t);
 template void launch_restrict<float>(const Level &, const Level &, const float *, float *, cudaStream_t);
@@ -85,14 +89,16 @@ __global__ void k_prolong_smooth(const T *__restrict__ xc, const T *__restrict__
                                  int nzc, int s, double *__restrict__ partial) {
     const int NYc = nyc + 1, NXc = nxc + 1;
     const int NYf = s * nyc + 1, NXf = s * nxc + 1, NZf = s * nzc + 1;
-    const int64_t nn = (int64_t)NYf * NXf * NZf;
-    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    // grid: x over the (y, x) plane of fine nodes, y over z (32-bit index math)
+    const int pl = blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)pl + (int64_t)NYf * NXf * blockIdx.y;
     double dot = 0.0;
-    if (n < nn) {
+    (void)NZf;
+    if (pl < NYf * NXf) {
         const uint8_t f = nflag[n];
         T o0 = T(0), o1 = T(0), o2 = T(0);
         if (f & NF_ACTIVE) {
-            const int iy = (int)(n % NYf), ix = (int)((n / NYf) % NXf), iz = (int)(n / ((int64_t)NYf * NXf));
+            const int iy = pl % NYf, ix = pl / NYf, iz = blockIdx.y;
             const int I = iy / s, J = ix / s, Kz = iz / s;
             const int ry = iy - s * I, rx = ix - s * J, rz = iz - s * Kz;
             const T inv = T(1) / T(s);
@@ -136,7 +142,7 @@ __global__ void k_prolong_smooth(const T *__restrict__ xc, const T *__restrict__
     if (FINAL && partial) {
         __shared__ double red[8];
         const double sum = warp_block_sum(dot, red);
-        if (threadIdx.x == 0) partial[blockIdx.x] = sum;
+        if (threadIdx.x == 0) partial[blockIdx.x + gridDim.x * blockIdx.y] = sum;
     }
 }
 
@@ -144,8 +150,9 @@ template <typename T>
 void launch_prolong_smooth(const Level &fine, const Level &coarse, const T *xc, const T *rf, const T *diag, T omega,
                            T *xf, bool final_level, double *partial_dot, int *nblocks_out, cudaStream_t st) {
     const int64_t nn = fine.nnode;
-    const unsigned nb = (unsigned)((nn + 255) / 256);
-    if (nblocks_out) *nblocks_out = (int)nb;
+    (void)nn;
+    const dim3 nb((unsigned)(((fine.ny + 1) * (fine.nx + 1) + 255) / 256), (unsigned)(fine.nz + 1));
+    if (nblocks_out) *nblocks_out = (int)(nb.x * nb.y);
     ++g_launches;
     if (final_level)
         k_prolong_smooth<T, true><<<nb, 256, 0, st>>>(xc, rf, diag, fine.nflag, omega, xf, coarse.ny, coarse.nx,

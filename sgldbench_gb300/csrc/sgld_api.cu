@@ -552,7 +552,10 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
     for (float **p : {&c.d_e32, &c.d_s32, &c.d_d32, &c.d_t32}) CK(dalloc(p, nv));
     CK(dalloc(&c.d_isc, 16));
     init_kernel_attributes();
-    c.npart = (int)std::max<int64_t>({(int64_t)152 * 8, (l0.nel + 255) / 256 + 1, (l0.nnode + 255) / 256 + 1,
+    // partial-sum slots: the largest grid of any kernel that writes per-CTA partials
+    // (prolongation: ceil(NY*NX/256) CTAs per node plane)
+    c.npart = (int)std::max<int64_t>({(int64_t)152 * 8, (l0.nel + 255) / 256 + 1,
+                                      (int64_t)(((l0.ny + 1) * (l0.nx + 1) + 255) / 256) * (l0.nz + 1),
                                       (int64_t)((l0.ny + 31) / 31 + 1) * ((l0.nx + 7) / 7 + 1) * ((l0.nz + 16) / 16 + 1)});
     CK(dalloc(&c.d_part, c.npart));
     CK(dalloc(&c.d_part2, c.npart));
@@ -582,6 +585,7 @@ void sgld_destroy(sgld_ctx *ctx) {
                     (void *)c.d_cy})
         if (p) cudaFree(p);
     if (c.inner_graph) cudaGraphExecDestroy(c.inner_graph);
+    if (c.factor_graph) cudaGraphExecDestroy(c.factor_graph);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete ctx;
 }
@@ -709,12 +713,16 @@ int sgld_set_fixed_dofs(sgld_ctx *ctx, const uint8_t *fixed) {
         CK(dalloc(&c.d_Ainv, (size_t)ncf * ncf));
         CK(dalloc(&c.d_Ainv32, (size_t)ncf * ncf));
         CK(dalloc(&c.d_cpart, (size_t)CSPLIT * ncf));
-        CK(dalloc(&c.d_LB, (size_t)ncf * (band + 1)));
+        CK(dalloc(&c.d_LB, (size_t)ncf * (band + 1) + ncf));
         CK(dalloc(&c.d_cy, 2 * (size_t)ncf));
         CK(dalloc(&c.d_cfree, (size_t)ncf + 3 * lc.nnode));
-        if (c.inner_graph) {   // the captured inner solve holds the old coarse buffers
+        if (c.inner_graph) {   // the captured graphs hold the old coarse buffers
             cudaGraphExecDestroy(c.inner_graph);
             c.inner_graph = nullptr;
+        }
+        if (c.factor_graph) {
+            cudaGraphExecDestroy(c.factor_graph);
+            c.factor_graph = nullptr;
         }
     }
     CK(cudaMemcpy(c.d_cfree, rows.data(), sizeof(int) * ncf, cudaMemcpyHostToDevice));
@@ -772,6 +780,7 @@ int sgld_assemble(sgld_ctx *ctx) {
     CKL();
     CK(cudaStreamSynchronize(c.stream));
     if (info == -2) return fail(ctx, SGLD_ERR_ARG, "coarsest-level band too wide; use more multigrid levels");
+    if (info == -1) return fail(ctx, SGLD_ERR_CUDA, "coarsest-level factorization could not be captured or launched");
     if (info != 0)
         return fail(ctx, SGLD_ERR_NUMERIC,
                     "coarsest-level matrix is not positive definite (pivot " + std::to_string(info) + ")");

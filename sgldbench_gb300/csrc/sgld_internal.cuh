@@ -63,8 +63,12 @@ struct Ctx {
     double *d_Ac = nullptr;         // [ncf*ncf] dense matrix / Cholesky factor
     double *d_Ainv = nullptr;       // [ncf*ncf] inverse (symmetric)
     float *d_Ainv32 = nullptr;
-    double *d_LB = nullptr;         // [ncf*(cband+1)] rows of the Cholesky factor's band
+    double *d_LB = nullptr;         // [ncf*(cband+1) + ncf] band rows of the Cholesky factor, 1/diag
     double *d_cy = nullptr;         // [2*ncf] intermediate of the coarse apply
+    cudaGraphExec_t factor_graph = nullptr;   // captured factorization of the coarsest matrix
+    int64_t factor_graph_launches = 0;
+    int trinv_ring = 0, trinv_warps = 0;
+    size_t trinv_smem = 0;
     double *d_cpart = nullptr;      // [CSPLIT*ncf] GEMV partials
     // templates for the level-2 Galerkin assembly
     double *d_H = nullptr;          // [span^3 * 576]

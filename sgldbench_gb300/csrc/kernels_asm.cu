@@ -42,45 +42,105 @@ static void upload_pairs(cudaStream_t s) {
     done = true;
 }
 
-// ---- level 2 from the finest level ------------------------------------------
-__global__ void __launch_bounds__(320) k_asm_finest(const double *__restrict__ E, const uint8_t *__restrict__ eact_c,
-                                                    const double *__restrict__ H, int nyc, int nxc, int nzc, int s,
-                                                    double *__restrict__ Ks) {
-    const int64_t e = blockIdx.x + (int64_t)gridDim.x * blockIdx.y;
+// ---- coarse element matrices straight from the finest level ------------------
+// Ks_E = sum_q E_q H_q over the S^3 finest elements q inside coarse element E,
+// with templates H_q = P_q' Ke P_q (P_q: trilinear interpolation from E's
+// corners to q's corners; span S = 2 or 4).  Composed trilinear
+// interpolation is trilinear, so S = 4 gives the same matrices as two
+// Galerkin steps of span 2.  A CTA handles EB consecutive coarse elements;
+// thread t owns one upper-triangle entry and keeps EB accumulators.
+constexpr int EB = 16;
+
+template <int NQ>
+__global__ void __launch_bounds__(320) k_asm_templates(const double *__restrict__ E, const uint8_t *__restrict__ eact_c,
+                                                       const double *__restrict__ H, int nyc, int nxc, int nzc,
+                                                       double *__restrict__ Ks) {
+    constexpr int S = (NQ == 8) ? 2 : 4;
+    __shared__ double ev[EB][NQ];
     const int64_t nel = (int64_t)nyc * nxc * nzc;
-    if (e >= nel || !eact_c[e]) return;
-    __shared__ double ev[64];
-    const int cy = (int)(e % nyc), cx = (int)((e / nyc) % nxc), cz = (int)(e / ((int64_t)nyc * nxc));
-    const int nyf = s * nyc, nxf = s * nxc;
-    const int nq = s * s * s;
-    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-        const int oy = q % s, ox = (q / s) % s, oz = q / (s * s);
-        ev[q] = E[(int64_t)(s * cy + oy) + (int64_t)nyf * ((s * cx + ox) + (int64_t)nxf * (s * cz + oz))];
+    const int64_t e0 = (int64_t)blockIdx.x * EB;
+    const int nyf = S * nyc, nxf = S * nxc;
+    for (int idx = threadIdx.x; idx < EB * NQ; idx += blockDim.x) {
+        const int k = idx / NQ, q = idx % NQ;
+        const int64_t e = e0 + k;
+        double v = 0.0;
+        if (e < nel && eact_c[e]) {
+            const int cy = (int)(e % nyc), cx = (int)((e / nyc) % nxc), cz = (int)(e / ((int64_t)nyc * nxc));
+            const int oy = q % S, ox = (q / S) % S, oz = q / (S * S);
+            v = E[(int64_t)(S * cy + oy) + (int64_t)nyf * ((S * cx + ox) + (int64_t)nxf * (S * cz + oz))];
+        }
+        ev[k][q] = v;
     }
     __syncthreads();
     const int t = threadIdx.x;
     if (t >= 300) return;
     const int r = c_pr[t], c = c_pc[t];
-    const int off = r + 24 * c;
-    double a = 0.0;
-    for (int q = 0; q < nq; ++q) {
-        const double w = ev[q];
-        if (w != 0.0) a += w * H[576 * q + off];
+    const int off = r + 24 * c, offt = c + 24 * r;
+    double acc[EB];
+#pragma unroll
+    for (int k = 0; k < EB; ++k) acc[k] = 0.0;
+    for (int q = 0; q < NQ; ++q) {
+        const double h = H[576 * q + off];
+#pragma unroll
+        for (int k = 0; k < EB; ++k) acc[k] += ev[k][q] * h;
     }
-    double *o = Ks + 576 * e;
-    o[off] = a;
-    o[c + 24 * r] = a;
+#pragma unroll
+    for (int k = 0; k < EB; ++k) {
+        const int64_t e = e0 + k;
+        if (e < nel && eact_c[e]) {
+            Ks[576 * e + off] = acc[k];
+            Ks[576 * e + offt] = acc[k];
+        }
+    }
 }
 
-void launch_asm_finest(const Level &coarse, const Level &fine, const double *E, const double *H, double *Ks,
-                       cudaStream_t s) {
-    (void)fine;
+void launch_asm_templates(const Level &coarse, int S, const double *E, const double *H, double *Ks, cudaStream_t s) {
     upload_pairs(s);
-    const int64_t nel = coarse.nel;
-    const unsigned gx = (unsigned)(nel < 65535 ? nel : 65535);
-    const unsigned gy = (unsigned)((nel + gx - 1) / gx);
+    const unsigned nb = (unsigned)((coarse.nel + EB - 1) / EB);
     ++g_launches;
-    k_asm_finest<<<dim3(gx, gy), 320, 0, s>>>(E, coarse.eact, H, coarse.ny, coarse.nx, coarse.nz, coarse.span, Ks);
+    if (S == 2)
+        k_asm_templates<8><<<nb, 320, 0, s>>>(E, coarse.eact, H, coarse.ny, coarse.nx, coarse.nz, Ks);
+    else
+        k_asm_templates<64><<<nb, 320, 0, s>>>(E, coarse.eact, H, coarse.ny, coarse.nx, coarse.nz, Ks);
+}
+
+// Jacobi diagonal of a span-2 coarse level without its element matrices:
+// diag(N, c) = sum_{coarse elements e around N} sum_q E_q H_q[(3j+c),(3j+c)]
+// with j the corner of e at N.
+__global__ void k_diag_templates(const double *__restrict__ E, const uint8_t *__restrict__ nflag,
+                                 const double *__restrict__ H, int ny, int nx, int nz, double *__restrict__ D) {
+    const int NY = ny + 1, NX = nx + 1;
+    const int pl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pl >= NY * NX) return;
+    const int iy = pl % NY, ix = pl / NY, iz = blockIdx.y;
+    const int64_t n = (int64_t)pl + (int64_t)NY * NX * iz;
+    double d0 = 0.0, d1 = 0.0, d2 = 0.0;
+    if (nflag[n] & NF_ACTIVE) {
+        const int cdy[8] = {1, 1, 0, 0, 1, 1, 0, 0}, cdx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, cdz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+        const int nyf = 2 * ny, nxf = 2 * nx;
+        for (int j = 0; j < 8; ++j) {
+            const int ey = iy - cdy[j], ex = ix - cdx[j], ez = iz - cdz[j];
+            if (ey < 0 || ex < 0 || ez < 0 || ey >= ny || ex >= nx || ez >= nz) continue;
+            for (int q = 0; q < 8; ++q) {
+                const int oy = q & 1, ox = (q >> 1) & 1, oz = q >> 2;
+                const double ev = E[(int64_t)(2 * ey + oy) + (int64_t)nyf * ((2 * ex + ox) + (int64_t)nxf * (2 * ez + oz))];
+                if (ev == 0.0) continue;
+                const double *h = H + 576 * q;
+                d0 += ev * h[(3 * j) * 25];
+                d1 += ev * h[(3 * j + 1) * 25];
+                d2 += ev * h[(3 * j + 2) * 25];
+            }
+        }
+    }
+    D[3 * n] = d0;
+    D[3 * n + 1] = d1;
+    D[3 * n + 2] = d2;
+}
+
+void launch_diag_templates(const Level &coarse, const double *E, const double *H2, double *diag, cudaStream_t s) {
+    const dim3 g((unsigned)(((coarse.ny + 1) * (coarse.nx + 1) + 255) / 256), (unsigned)(coarse.nz + 1));
+    ++g_launches;
+    k_diag_templates<<<g, 256, 0, s>>>(E, coarse.nflag, H2, coarse.ny, coarse.nx, coarse.nz, diag);
 }
 
 // ---- deeper levels: P_q' Ks_q P_q ---------------------------------------------
@@ -215,51 +275,57 @@ void launch_coarse_dense(const Level &lc, int ncf, const int *rows_and_pos, doub
 // ---- blocked band Cholesky, NB x NB tiles, column-major n x n ------------------
 constexpr int NB = 32;
 
-// Factors one block column of the band in place: the NB x NB diagonal tile
-// and the rows below it inside the band (prow rows in all, one thread per
-// row, the row's NB entries in registers).  Right-looking within the panel:
-// for each column j the diagonal thread forms sqrt, every row below scales,
-// and the trailing columns of the panel are updated with column j.
-__global__ void __launch_bounds__(384) k_potrf_panel(double *A, int n, int k0, int prow, int *info) {
-    __shared__ double col[NB];
-    __shared__ double dsh;
-    const int t = threadIdx.x;
-    const int r = k0 + t;
+// One block column of the band Cholesky.  CTA ib (one warp) handles the
+// 32-row tile kb + ib: every CTA first factors the diagonal tile in shared
+// memory (32 x 32, lane = row), CTA 0 writes it back, and CTA ib > 0 then
+// solves its tile rows against it (X = A_ib L_kk^-T, lane = row).  The FP64
+// work of a panel is spread over the tiles instead of one SM.
+__global__ void __launch_bounds__(32) k_chol_panel(double *A, int n, int k0, int *info) {
+    __shared__ double T[NB][NB + 1];
+    __shared__ double rd[NB];
+    const int lane = threadIdx.x;
     const int m = min(NB, n - k0);
-    const bool act = t < prow && r < n;
-    double x[NB];
-#pragma unroll
-    for (int j = 0; j < NB; ++j) x[j] = (act && j < m) ? A[(int64_t)r + (int64_t)n * (k0 + j)] : 0.0;
-#pragma unroll
-    for (int j = 0; j < NB; ++j) {
-        if (j >= m) break;
-        if (t == j) {
-            double d = x[j];
+    for (int j = 0; j < NB; ++j)
+        T[lane][j] = (lane < m && j < m) ? A[(int64_t)(k0 + lane) + (int64_t)n * (k0 + j)] : (lane == j ? 1.0 : 0.0);
+    __syncwarp();
+    for (int j = 0; j < m; ++j) {
+        if (lane == j) {
+            double d = T[j][j];
             if (!(d > 0.0)) {
-                if (info) atomicExch(info, k0 + j + 1);
+                if (info && blockIdx.x == 0) atomicExch(info, k0 + j + 1);
                 d = 1.0;
             }
-            dsh = sqrt(d);
+            d = sqrt(d);
+            T[j][j] = d;
+            rd[j] = 1.0 / d;
         }
-        __syncthreads();
-        const double d = dsh;
-        const double rd = 1.0 / d;
-        if (t == j)
-            x[j] = d;
-        else if (t > j)
-            x[j] *= rd;
-        if (t < NB) col[t] = x[j];
-        __syncthreads();
-        if (t > j) {
-#pragma unroll
-            for (int q = j + 1; q < NB; ++q) x[q] -= x[j] * col[q];
-        }
+        __syncwarp();
+        if (lane > j) T[lane][j] *= rd[j];
+        __syncwarp();
+        if (lane > j)
+            for (int q = j + 1; q <= lane; ++q) T[lane][q] -= T[lane][j] * T[q][j];
+        __syncwarp();
     }
-    if (act) {
-#pragma unroll
-        for (int j = 0; j < NB; ++j)
-            if (j < m) A[(int64_t)r + (int64_t)n * (k0 + j)] = (t < NB && j > t) ? 0.0 : x[j];
+    if (blockIdx.x == 0) {
+        if (lane < m)
+            for (int j = 0; j < m; ++j) A[(int64_t)(k0 + lane) + (int64_t)n * (k0 + j)] = (j <= lane) ? T[lane][j] : 0.0;
+        return;
     }
+    const int row = k0 + NB * blockIdx.x + lane;
+    if (row >= n) return;
+    double x[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) x[j] = (j < m) ? A[(int64_t)row + (int64_t)n * (k0 + j)] : 0.0;
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+        double v = x[j];
+#pragma unroll
+        for (int q = 0; q < j; ++q) v -= x[q] * T[j][q];
+        x[j] = v * rd[j];
+    }
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+        if (j < m) A[(int64_t)row + (int64_t)n * (k0 + j)] = x[j];
 }
 
 // trailing update A[i,j] -= A[i,k] A[j,k]' for k < j <= i <= kend (tile pairs)
@@ -297,11 +363,12 @@ __global__ void k_to_f32(const double *a, float *b, int64_t n) {
     if (i < n) b[i] = (float)a[i];
 }
 
-// LB[i*(b+1) + d] = L[i, i-b+d], d = 0..b (0 outside the matrix)
+// Band of L stored by diagonals: LB[d*n + i] = L[i, i-b+d], d = 0..b (0 outside
+// the matrix), so that lanes holding consecutive rows read consecutive words.
 __global__ void k_band_rows(const double *__restrict__ L, int n, int b, double *__restrict__ LB) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= (int64_t)n * (b + 1)) return;
-    const int i = (int)(t / (b + 1)), d = (int)(t % (b + 1));
+    const int d = (int)(t / n), i = (int)(t % n);
     const int k = i - b + d;
     LB[t] = (k >= 0) ? L[(int64_t)i + (int64_t)n * k] : 0.0;
 }
@@ -313,7 +380,7 @@ __global__ void k_band_rows(const double *__restrict__ L, int n, int b, double *
 //   2. within the block, rows finish in order: lane t forms
 //      M[i0+t,c] = (delta - s_t) / L[i0+t,i0+t], broadcasts it, and the
 //      lanes below subtract its contribution.
-// LB holds the band of L row-wise (LB[i*(b+1)+d] = L[i,i-b+d]), rdiag = 1/diag(L).
+// LB holds the band of L by diagonals (see k_band_rows), rdiag = 1/diag(L).
 __global__ void k_trinv_cols(const double *__restrict__ LB, const double *__restrict__ rdiag, int n, int b, int R,
                              double *__restrict__ M) {
     extern __shared__ double ringmem[];
@@ -321,25 +388,30 @@ __global__ void k_trinv_cols(const double *__restrict__ LB, const double *__rest
     const int c = blockIdx.x * (blockDim.x >> 5) + w;
     if (c >= n) return;
     double *ring = ringmem + (int64_t)w * R;
-    const int64_t bs = b + 1;
     for (int i0 = c; i0 < n; i0 += 32) {
         const int i = i0 + lane;
         const bool valid = i < n;
-        const double *row = LB + (int64_t)(valid ? i : i0) * bs;   // row[d] = L[i, i-b+d]
-        double s = 0.0;
+        const double *col = LB + (valid ? i : i0);   // col[d*n] = L[i, i-b+d]
+        double s0 = 0.0, s1 = 0.0;
         if (valid) {
             // k = i - b + t runs over [max(c, i-b), i0)
             const int t0 = max(0, c - (i - b));
             const int t1 = b - lane;   // k < i0
-            for (int t = t0; t < t1; ++t) s += row[t] * ring[(i - b + t) & (R - 1)];
+            int t = t0;
+            for (; t + 1 < t1; t += 2) {
+                s0 += col[(int64_t)t * n] * ring[(i - b + t) & (R - 1)];
+                s1 += col[(int64_t)(t + 1) * n] * ring[(i - b + t + 1) & (R - 1)];
+            }
+            if (t < t1) s0 += col[(int64_t)t * n] * ring[(i - b + t) & (R - 1)];
         }
+        double s = s0 + s1;
         double v = 0.0;
 #pragma unroll 4
         for (int t = 0; t < 32; ++t) {
             if (i0 + t >= n) break;
             if (lane == t) v = ((i == c ? 1.0 : 0.0) - s) * rdiag[i];
             const double vt = __shfl_sync(0xffffffffu, v, t);
-            if (lane > t && valid && lane - t <= b) s += row[b - lane + t] * vt;   // L[i, i0+t]
+            if (lane > t && valid && lane - t <= b) s += col[(int64_t)(b - lane + t) * n] * vt;   // L[i, i0+t]
         }
         if (valid) {
             ring[i & (R - 1)] = v;
@@ -367,7 +439,7 @@ static void factor_enqueue(Ctx &c, int *d_info) {
         const int kend = min(nblk - 1, kb + bw);
         const int nbelow = kend - kb;
         ++g_launches;
-        k_potrf_panel<<<1, NB * (1 + bw), 0, c.stream>>>(A, n, k0, NB * (1 + nbelow), d_info);
+        k_chol_panel<<<1 + nbelow, NB, 0, c.stream>>>(A, n, k0, d_info);
         if (nbelow > 0) {
             const int npairs = nbelow * (nbelow + 1) / 2;
             ++g_launches;
@@ -395,8 +467,6 @@ static void factor_enqueue(Ctx &c, int *d_info) {
 int coarse_factor_invert(Ctx &c) {
     const int n = c.ncf;
     if (n == 0) return 0;
-    const int bw = (c.cband + NB - 1) / NB + 1;
-    if (NB * (1 + bw) > 384) return -2;
     int *d_info = c.d_iflag + 8;
     if (!c.factor_graph) {
         int R = 32;

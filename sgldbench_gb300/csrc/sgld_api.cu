@@ -257,15 +257,23 @@ int fail(sgld_ctx *ctx, int code, const std::string &msg) {
 
 int setup_templates(sgld_ctx *ctx) {
     Ctx &c = ctx->c;
-    std::vector<double> H;
-    const int s = c.lv[1].span;
-    make_templates(c.Ke, s, H);
+    std::vector<double> H2, H4;
+    make_templates(c.Ke, 2, H2);
+    make_templates(c.Ke, 4, H4);
     if (c.d_H) cudaFree(c.d_H);
-    CK(dalloc(&c.d_H, H.size()));
-    CK(cudaMemcpy(c.d_H, H.data(), H.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(dalloc(&c.d_H, H2.size() + H4.size()));
+    CK(cudaMemcpy(c.d_H, H2.data(), H2.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c.d_H + H2.size(), H4.data(), H4.size() * sizeof(double), cudaMemcpyHostToDevice));
     upload_kh(c.Kh, c.stream);
     return SGLD_OK;
 }
+
+const double *templates(const Ctx &c, int S) { return S == 2 ? c.d_H : c.d_H + 8 * 576; }
+
+// A dyadic hierarchy with more than two levels never needs the element
+// matrices of level 2 (MATLAB index): its diagonal comes from the span-2
+// templates and level 3 from the span-4 templates.
+bool skip_level2_ks(const Ctx &c) { return c.L > 2 && c.lv[1].span == 2; }
 
 // device V-cycle on full-grid vectors (Solving_Vcycle.m:12-50); partial dot z.r
 int vcycle_dev(sgld_ctx *ctx, const double *r, double *z, double *partial, int *nb) {
@@ -527,7 +535,7 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
             CK(dalloc(&lv.idiag32, 3 * lv.nnode));
         }
         if (l > 0) {
-            CK(dalloc(&lv.Ks, 576 * (size_t)lv.nel));
+            if (!(l == 1 && skip_level2_ks(c))) CK(dalloc(&lv.Ks, 576 * (size_t)lv.nel));
             CK(dalloc(&lv.r, 3 * lv.nnode));
             CK(dalloc(&lv.x, 3 * lv.nnode));
             CK(dalloc(&lv.r32, 3 * lv.nnode));
@@ -766,9 +774,16 @@ int sgld_assemble(sgld_ctx *ctx) {
     Ctx &c = ctx->c;
     const int L = c.L;
     launch_diag_finest(c.lv[0], c.E, c.Ke, c.lv[0].diag, c.stream);
+    const bool skip2 = skip_level2_ks(c);
     for (int l = 1; l < L; ++l) {
+        if (l == 1 && skip2) {
+            launch_diag_templates(c.lv[1], c.E, templates(c, 2), c.lv[1].diag, c.stream);
+            continue;
+        }
         if (l == 1)
-            launch_asm_finest(c.lv[1], c.lv[0], c.E, c.d_H, c.lv[1].Ks, c.stream);
+            launch_asm_templates(c.lv[1], c.lv[1].span, c.E, templates(c, c.lv[1].span), c.lv[1].Ks, c.stream);
+        else if (l == 2 && skip2)
+            launch_asm_templates(c.lv[2], 4, c.E, templates(c, 4), c.lv[2].Ks, c.stream);
         else
             launch_asm_coarse(c.lv[l], c.lv[l - 1], c.lv[l].Ks, c.stream);
         if (l < L - 1) launch_diag_from_Ks(c.lv[l], c.lv[l].diag, c.stream);
@@ -807,7 +822,15 @@ int sgld_get_diag(const sgld_ctx *cctx, int level, double *diag) {
 int sgld_get_ks(const sgld_ctx *cctx, int level, double *Ks) {
     auto *ctx = const_cast<sgld_ctx *>(cctx);
     if (!ctx || !Ks || level < 2 || level > ctx->c.L) return SGLD_ERR_ARG;
-    const Level &l = ctx->c.lv[level - 1];
+    Ctx &c = ctx->c;
+    if (!c.assembled) return fail(ctx, SGLD_ERR_STATE, "stencil not assembled (sgld_assemble)");
+    Level &l = c.lv[level - 1];
+    if (!l.Ks) {   // level 2 of a dyadic hierarchy: formed on request only
+        CK(dalloc(&l.Ks, 576 * (size_t)l.nel));
+        launch_asm_templates(l, 2, c.E, templates(c, 2), l.Ks, c.stream);
+        CKL();
+        CK(cudaStreamSynchronize(c.stream));
+    }
     const auto &m = ctx->elemaps[level - 1];
     for (size_t i = 0; i < m.size(); ++i)
         CK(cudaMemcpy(Ks + 576 * i, l.Ks + 576 * m[i], sizeof(double) * 576, cudaMemcpyDeviceToHost));

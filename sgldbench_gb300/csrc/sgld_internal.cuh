@@ -71,7 +71,7 @@ struct Ctx {
     size_t trinv_smem = 0;
     double *d_cpart = nullptr;      // [CSPLIT*ncf] GEMV partials
     // templates for the level-2 Galerkin assembly
-    double *d_H = nullptr;          // [span^3 * 576]
+    double *d_H = nullptr;          // [(8 + 64) * 576] templates for span 2, then span 4
     // PCG vectors (full grid, FP64)
     double *d_b = nullptr, *d_x = nullptr, *d_r = nullptr, *d_z = nullptr, *d_p = nullptr, *d_q = nullptr;
     double *d_tmp = nullptr;
@@ -136,8 +136,8 @@ void launch_gather_elems(const int64_t *map, int64_t n, const double *full, doub
 void launch_fixed_indicator(const Level &l, double *v, cudaStream_t s);
 void launch_mark_fixed(Level &l, const double *restricted, cudaStream_t s);
 
-void launch_asm_finest(const Level &coarse, const Level &fine, const double *E, const double *H, double *Ks,
-                       cudaStream_t s);
+void launch_asm_templates(const Level &coarse, int S, const double *E, const double *H, double *Ks, cudaStream_t s);
+void launch_diag_templates(const Level &coarse, const double *E, const double *H2, double *diag, cudaStream_t s);
 void launch_asm_coarse(const Level &coarse, const Level &fine, double *Ks, cudaStream_t s);
 void launch_coarse_dense(const Level &lc, int ncf, const int *cfree_pos_of_dof, double *A, cudaStream_t s);
 int coarse_factor_invert(Ctx &c);  // returns 0 or error

@@ -16,16 +16,6 @@ using namespace sgld;
 
 int64_t sgld::g_launches = 0;
 
-struct sgld_ctx {
-    Ctx c;
-    // lazily allocated stress buffers
-    double *d_s6 = nullptr, *d_vmn = nullptr, *d_vme = nullptr;
-    int *d_rowspos = nullptr;
-    std::vector<std::vector<int64_t>> nodemaps, elemaps;   // per level, 0-based full indices
-    std::vector<int> h_rows;                               // coarsest free DOFs (full DOF index)
-    bool have_mixed = false;
-};
-
 namespace {
 
 // ---------------------------------------------------------------------------

@@ -92,6 +92,19 @@ struct Ctx {
     int device = 0;
 };
 
+}  // namespace sgld
+
+// The opaque handle of the C ABI.
+struct sgld_ctx {
+    sgld::Ctx c;
+    // lazily allocated stress buffers
+    double *d_s6 = nullptr, *d_vmn = nullptr, *d_vme = nullptr;
+    std::vector<std::vector<int64_t>> nodemaps, elemaps;   // per level, 0-based full indices
+    std::vector<int> h_rows;                               // coarsest free DOFs (full DOF index)
+};
+
+namespace sgld {
+
 constexpr int CSPLIT = 16;   // column chunks of the coarse GEMV
 
 // number of kernels this library has launched (host-side counter, one per launch)

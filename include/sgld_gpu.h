@@ -93,6 +93,29 @@ int64_t sgld_kernel_launches(void);
  *   op 4: assembly (Galerkin levels + coarsest factorization) */
 int sgld_time_op(sgld_ctx *ctx, int op, int reps, double *ms_per_op);
 
+/* Allocation-free K*u with its dot product (no counterpart in the reference).
+ *
+ * For callers that must not allocate device memory when they apply the
+ * operator: a stream being captured into a CUDA graph, a real-time loop whose
+ * device memory budget is fixed at start-up, or a plugin in a process whose
+ * device memory belongs to another framework's caching allocator.  Enqueues,
+ * on `stream` (a cudaStream_t; NULL = the legacy default stream),
+ *     d_y = K d_u (fixed DOFs of d_y set to 0)   and   *d_dot = d_u . d_y,
+ * for the context's current moduli.  d_u and d_y are device arrays in the
+ * full-grid layout: 3 * (resY+1) * (resX+1) * (resZ+1) doubles, node-major,
+ * nodes in column-major grid order, zeros at inactive nodes; d_dot is one
+ * device double.  The call allocates nothing: its scratch is a static device
+ * array of SGLD_NOALLOC_MAX_CTAS doubles (256 KiB) that every GPU loading this
+ * library holds until the process exits.  The first call on a device looks up
+ * that array's address (once per device, the context's device must be
+ * current); make that first call before any stream capture.  Every call
+ * shares the array, so calls that overlap on the GPU (other streams, other
+ * contexts on the same device) race; serialise them.  Grids needing more than
+ * SGLD_NOALLOC_MAX_CTAS CTAs (on the order of 1e8 nodes; each CTA covers a
+ * 31 x 7 x 16 node block) are rejected with SGLD_ERR_ARG. */
+#define SGLD_NOALLOC_MAX_CTAS 32768
+int sgld_kbyu_dot_noalloc(sgld_ctx *ctx, const double *d_u, double *d_y, double *d_dot, void *stream);
+
 /* Fills opts with the reference defaults (Data_GlobalVariables.m:10-23). */
 void sgld_default_options(sgld_options *opts);
 

@@ -509,9 +509,18 @@ __global__ void k_coarse_lower(const T *__restrict__ M, const int *__restrict__ 
     const int chunk = (n + CSPLIT - 1) / CSPLIT;
     const int j0 = blockIdx.y * chunk, j1 = min(min(n, j0 + chunk), i + 1);
     if (i >= n) return;
-    T acc = T(0);
-    for (int j = j0; j < j1; ++j) acc += M[(int64_t)i + (int64_t)n * j] * r[rows[j]];
-    part[(int64_t)blockIdx.y * n + i] = (double)acc;
+    // four independent accumulators: the chain of one would be latency-bound
+    T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+    const T *col = M + i;
+    int j = j0;
+    for (; j + 3 < j1; j += 4) {
+        a0 += col[(int64_t)n * j] * r[rows[j]];
+        a1 += col[(int64_t)n * (j + 1)] * r[rows[j + 1]];
+        a2 += col[(int64_t)n * (j + 2)] * r[rows[j + 2]];
+        a3 += col[(int64_t)n * (j + 3)] * r[rows[j + 3]];
+    }
+    for (; j < j1; ++j) a0 += col[(int64_t)n * j] * r[rows[j]];
+    part[(int64_t)blockIdx.y * n + i] = (double)((a0 + a1) + (a2 + a3));
 }
 
 template <typename T>

@@ -68,11 +68,13 @@ void launch_restrict(const Level &fine, const Level &coarse, const T *rf, T *rc,
 template void launch_restrict<double>(const Level &, const Level &, const double *, double *, cudaStream_t);
 template void launch_restrict<float>(const Level &, const Level &, const float *, float *, cudaStream_t);
 
-__device__ __forceinline__ double warp_block_sum(double v, double *red) {
+// warp stage in the kernel's precision T, the warp sums added in FP64
+template <typename T>
+__device__ __forceinline__ double warp_block_sum(T v, double *red) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) red[w] = v;
+    if (l == 0) red[w] = (double)v;
     __syncthreads();
     double s = 0.0;
     if (threadIdx.x == 0)
@@ -92,7 +94,7 @@ __global__ void k_prolong_smooth(const T *__restrict__ xc, const T *__restrict__
     // grid: x over the (y, x) plane of fine nodes, y over z (32-bit index math)
     const int pl = blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t n = (int64_t)pl + (int64_t)NYf * NXf * blockIdx.y;
-    double dot = 0.0;
+    T dot = T(0);
     (void)NZf;
     if (pl < NYf * NXf) {
         const uint8_t f = nflag[n];
@@ -132,7 +134,7 @@ __global__ void k_prolong_smooth(const T *__restrict__ xc, const T *__restrict__
                 if (f & NF_FIXX) o0 = T(0);
                 if (f & NF_FIXY) o1 = T(0);
                 if (f & NF_FIXZ) o2 = T(0);
-                dot = (double)o0 * (double)r0 + (double)o1 * (double)r1 + (double)o2 * (double)r2;
+                dot = o0 * r0 + o1 * r1 + o2 * r2;
             }
         }
         xf[3 * n] = o0;
@@ -141,7 +143,7 @@ __global__ void k_prolong_smooth(const T *__restrict__ xc, const T *__restrict__
     }
     if (FINAL && partial) {
         __shared__ double red[8];
-        const double sum = warp_block_sum(dot, red);
+        const double sum = warp_block_sum<T>(dot, red);
         if (threadIdx.x == 0) partial[blockIdx.x + gridDim.x * blockIdx.y] = sum;
     }
 }

@@ -99,6 +99,23 @@ __device__ __forceinline__ void hex_apply(T (&u)[24], T e) {
     for (int i = 0; i < 24; ++i) u[i] = g[i];
 }
 
+// Per-CTA sum of a per-thread partial: the warp stage runs in the kernel's own
+// precision T (FP64 issue is scarce on GB300, so FP32 kernels must not do
+// their reductions in FP64), the 8 warp sums are added in FP64.
+template <typename T>
+__device__ __forceinline__ double block_sum_to_double(T v, double *red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = (double)v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
+    return s;
+}
+
 template <typename T>
 __device__ __forceinline__ T block_sum(T v, T *red) {
 #pragma unroll
@@ -118,19 +135,22 @@ constexpr int KT_Y = 32, KT_X = 8, KT_THREADS = KT_Y * KT_X;
 constexpr int KT_NL = (KT_Y + 1) * (KT_X + 1);   // staged nodes per layer
 constexpr int KT_ZC = 16;                        // node layers per CTA
 
+constexpr int KT_SV = (KT_NL * 3 + KT_THREADS - 1) / KT_THREADS;   // staged words per thread and layer
+
+// node layer z lives in ring slot z mod 3 (z may be -1)
+__device__ __forceinline__ int kslot(int z) { return (z + 3) % 3; }
+
+// asynchronous global -> shared word copy (cp.async, completes at async_wait_all)
 template <typename T>
-__device__ __forceinline__ void stage_layer(const T *__restrict__ u, T *dst, int z, int y0, int x0, int NY, int NX,
-                                            int NZ) {
-    for (int i = threadIdx.x; i < KT_NL * 3; i += KT_THREADS) {
-        const int node = i / 3, c = i - 3 * node;
-        const int ly = node % (KT_Y + 1), lx = node / (KT_Y + 1);
-        const int gy = y0 - 1 + ly, gx = x0 - 1 + lx;
-        T v = T(0);
-        if (z >= 0 && z < NZ && gy >= 0 && gy < NY && gx >= 0 && gx < NX)
-            v = u[3 * ((int64_t)gy + (int64_t)NY * (gx + (int64_t)NX * z)) + c];
-        dst[i] = v;
-    }
+__device__ __forceinline__ void async_copy(T *dst, const T *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if (sizeof(T) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src));
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src));
 }
+__device__ __forceinline__ void async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // y = K u on the full grid; y at fixed DOFs is 0.  When DOT, also writes
 // sum(u .* y) of this CTA's nodes to partial[block].
@@ -139,8 +159,8 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu(const T *__restrict__ u, T 
                                                      const T *__restrict__ E, const uint8_t *__restrict__ nflag,
                                                      int ny, int nx, int nz, double *__restrict__ partial) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *su = reinterpret_cast<T *>(smem_raw);      // [2][KT_NL*3]
-    T *so = su + 2 * KT_NL * 3;                   // [24][KT_THREADS]
+    T *su = reinterpret_cast<T *>(smem_raw);      // [3][KT_NL*3] ring of node layers
+    T *so = su + 3 * KT_NL * 3;                   // [24][KT_THREADS]
     const int tid = threadIdx.x;
     const int ty = tid % KT_Y, tx = tid / KT_Y;
     const int NY = ny + 1, NX = nx + 1, NZ = nz + 1;
@@ -151,13 +171,45 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu(const T *__restrict__ u, T 
     const int ey = y0 - 1 + ty, ex = x0 - 1 + tx;
     const bool ein = ey >= 0 && ey < ny && ex >= 0 && ex < nx;
     T acc0 = T(0), acc1 = T(0), acc2 = T(0);
-    double dot = 0.0;
+    T dot = T(0);
 
-    stage_layer(u, su + ((z0 + 1) & 1) * KT_NL * 3, z0 - 1, y0, x0, NY, NX, NZ);
+    // staging plan: this thread copies up to KT_SV words of every node layer;
+    // the in-layer source offsets are fixed, only the layer stride changes
+    int soff[KT_SV];
+#pragma unroll
+    for (int k = 0; k < KT_SV; ++k) {
+        const int i = tid + k * KT_THREADS;
+        soff[k] = -2;
+        if (i < KT_NL * 3) {
+            const int node = i / 3, c = i - 3 * node;
+            const int ly = node % (KT_Y + 1), lx = node / (KT_Y + 1);
+            const int gy = y0 - 1 + ly, gx = x0 - 1 + lx;
+            soff[k] = (gy >= 0 && gy < NY && gx >= 0 && gx < NX) ? 3 * (gy + NY * gx) + c : -1;
+        }
+    }
+    const int64_t lstride = 3 * (int64_t)NY * NX;
+    auto stage = [&](int z) {
+        T *dst = su + kslot(z) * KT_NL * 3;
+        const bool zin = z >= 0 && z < NZ;
+#pragma unroll
+        for (int k = 0; k < KT_SV; ++k) {
+            const int i = tid + k * KT_THREADS;
+            if (soff[k] == -2) continue;
+            if (zin && soff[k] >= 0)
+                async_copy(dst + i, u + ((int64_t)z * lstride + soff[k]));
+            else
+                dst[i] = T(0);
+        }
+        async_commit();
+    };
+
+    stage(z0 - 1);
+    stage(z0);
+    async_wait_all();
+    __syncthreads();
     for (int ez = z0 - 1; ez < zend; ++ez) {
-        const int s0 = ez & 1, s1 = (ez + 1) & 1;
-        stage_layer(u, su + s1 * KT_NL * 3, ez + 1, y0, x0, NY, NX, NZ);
-        __syncthreads();
+        const int s0 = kslot(ez), s1 = kslot(ez + 1);
+        if (ez + 2 <= zend) stage(ez + 2);   // prefetch, overlaps the element work below
         T ev = T(0);
         if (ein && ez >= 0 && ez < nz) ev = E[(int64_t)ey + (int64_t)ny * (ex + (int64_t)nx * ez)];
         T ue[24];
@@ -201,7 +253,7 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu(const T *__restrict__ u, T 
                 y[3 * node + 2] = o2;
                 if (DOT) {
                     const T *un = su + s0 * KT_NL * 3 + 3 * ((ty + 1) + (KT_Y + 1) * (tx + 1));
-                    dot += (double)un[0] * (double)o0 + (double)un[1] * (double)o1 + (double)un[2] * (double)o2;
+                    dot += un[0] * o0 + un[1] * o1 + un[2] * o2;
                 }
             }
             acc0 = acc1 = acc2 = T(0);
@@ -216,11 +268,12 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu(const T *__restrict__ u, T 
                     acc2 += so[(3 * k + 2) * KT_THREADS + t];
                 }
         }
+        async_wait_all();
         __syncthreads();
     }
     if (DOT) {
         __shared__ double red[KT_THREADS / 32];
-        const double s = block_sum<double>(dot, red);
+        const double s = block_sum_to_double<T>(dot, red);
         if (tid == 0) partial[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s;
     }
 }
@@ -231,7 +284,7 @@ static dim3 kbyu_grid(const Level &l) {
 
 template <typename T>
 static constexpr size_t kbyu_smem() {
-    return sizeof(T) * (2 * KT_NL * 3 + 24 * KT_THREADS);
+    return sizeof(T) * (3 * KT_NL * 3 + 24 * KT_THREADS);
 }
 
 // opt-in shared memory sizes; called once per context before any launch or

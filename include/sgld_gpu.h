@@ -190,6 +190,41 @@ int sgld_pcg_device(sgld_ctx *ctx, const double *d_b, double *d_x, const sgld_so
  * ce may be NULL. */
 int sgld_compliance(sgld_ctx *ctx, const double *U, double *ce, double *c);
 
+/* Cone density filter (TopOpti_PerformDensityFiltering_mex.cpp:8-52; with x ==
+ * NULL the weight sums Hs of TopOpti_SetupDensityFilter_mex.cpp:9-51):
+ * y_e = sum over solid e2 in the (2 ceil(rmin) - 1)^3 box of max(0, rmin - |e - e2|) x_e2.
+ * Compact element vectors (numElements). */
+int sgld_density_filter(sgld_ctx *ctx, double rmin, const double *x, double *y);
+
+/* SIMP loop with a global volume constraint (TopOpti_GlobalVolumeConstraint_Tmp.m:26-120,
+ * ft = 2): per iteration E = SIMP(xPhys), assembly, warm-started MGPCG, unit
+ * compliance, sensitivities, filtered sensitivities, OC bisection on the
+ * linearised volume constraint, filtered densities.  Defaults (0 fields) follow
+ * Data_GlobalVariables.m / the reference. */
+typedef struct sgld_topopt_opts {
+    double volfrac;        /* V_ */
+    double rmin;           /* rMin_ */
+    double move;           /* move_ (0 = 0.1) */
+    int n_loop;            /* nLoop_ */
+    double min_change;     /* minChange_ (0 = 1e-4) */
+    double max_sharpness;  /* maxSharpness_ (0 = 0.05) */
+    double penalty;        /* SIMPpenalty_ (0 = 3) */
+    double E0, Emin;       /* modulus_, modulusMin_ (0 = 1, 1e-6) */
+    sgld_solve_opts solve; /* tol_, maxIT_, precision of every MGPCG solve (warm-started) */
+} sgld_topopt_opts;
+
+typedef struct sgld_topopt_iter {
+    int loop, cg_iterations;
+    double compliance, volume, sharpness, change, constraint;   /* cHist_, volHist_, sharpHist_, change, consHist_ */
+    double t_assemble, t_solve, t_opt, t_filter;                 /* tHist_ columns (device seconds) */
+} sgld_topopt_iter;
+
+/* x0: initial design (NULL = volfrac everywhere, TopOpti_CallTopOpti.m:34);
+ * xphys: final filtered design (numElements); hist: n_loop records; *n_iter:
+ * iterations run.  Leaves the last displacement in the context. */
+int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const double *F, const double *x0, double *xphys,
+                sgld_topopt_iter *hist, int *n_iter);
+
 /* FEA_StressAnalysis.m:17-60 and FEA_ComputePerElementVonMisesStress.m:10-19:
  * nodal Cartesian stress (numNodes x 6, row-major [xx yy zz yz zx xy]), nodal
  * von Mises and per-element von Mises with the reference's final .^(1/2).

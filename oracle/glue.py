@@ -673,3 +673,67 @@ def set_modulus(model: Model, E):
 def solve(model: Model, tol=1e-6, maxIT=500, x0=None, history=None):
     return pcg(lambda u: kbyu(model, u), lambda r: vcycle(model, r), model.F, tol, maxIT,
                x0=x0, history=history)
+
+
+# ---------------------------------------------------------------------------
+# SIMP loop (src/TopOpti_GlobalVolumeConstraint_Tmp.m:26-120, ft = 2 branch)
+# ---------------------------------------------------------------------------
+@dataclass
+class TopOptOptions:
+    volfrac: float = 0.3          # V_
+    rmin: float = 1.5             # rMin_
+    move: float = 0.1             # move_ (Data_GlobalVariables.m:65)
+    n_loop: int = 60              # nLoop_
+    min_change: float = 1.0e-4    # minChange_ (Data_GlobalVariables.m:68)
+    max_sharpness: float = 0.05   # maxSharpness_ (Data_GlobalVariables.m:67)
+    penalty: float = 3.0          # SIMPpenalty_ / penalty_
+    E0: float = 1.0               # modulus_
+    Emin: float = 1.0e-9          # modulusMin_
+    tol: float = 1.0e-6           # tol_
+    maxit: int = 500              # maxIT_
+
+
+def topopt_global_volume(model: Model, opt: TopOptOptions, history=None):
+    """TopOpti_GlobalVolumeConstraint_Tmp.m:26-120 with ft = 2 (density filter on
+    sensitivities and densities), OC bisection on the linearised volume
+    constraint, warm-started MGPCG (Solving_CG_GMGS.m:7).  Returns xPhys and a
+    list of per-iteration records (compliance, volume, sharpness, change, its)."""
+    l1 = model.levels[0]
+    n = l1.numElements
+    emf, (rx, ry, rz) = l1.eleMapForward, (l1.resX, l1.resY, l1.resZ)
+    Hs = K.density_filter(None, opt.rmin, emf, rx, ry, rz)                    # :35
+    x = np.full(n, opt.volfrac)                                               # TopOpti_CallTopOpti.m:34
+    xPhys = x.copy()
+    U = np.zeros(l1.numDOFs)
+    loop, change, sharp = 0, 1.0, 1.0
+    hist = [] if history is None else history
+    while loop < opt.n_loop and change > opt.min_change and sharp > opt.max_sharpness:   # :47
+        loop += 1
+        E = simp_modulus(xPhys, opt.E0, opt.Emin, opt.penalty)               # :52
+        set_modulus(model, E)
+        assemble_stencil(model)                                              # :54
+        U, its = pcg(lambda u: kbyu(model, u), lambda r: vcycle(model, r), model.F, opt.tol, opt.maxit, x0=U)
+        ce = unit_compliance(model, U)                                       # :59
+        c = float(E @ ce)                                                    # :63 (complianceSolid_ = 1)
+        vol = float(xPhys.sum() / n)                                         # :65
+        dc = -(opt.penalty * (opt.E0 - opt.Emin) * xPhys ** (opt.penalty - 1)) * ce   # :66, TopOpti_DeMaterialInterpolation.m:5
+        dv = np.ones(n)
+        dc = K.density_filter(dc / Hs, opt.rmin, emf, rx, ry, rz)            # :76
+        dv = K.density_filter(dv / Hs, opt.rmin, emf, rx, ry, rz)            # :77
+        g = float(xPhys.mean() - opt.volfrac)                                # :83
+        lo, hi = 0.0, 1e9                                                    # :84
+        while (hi - lo) / (lo + hi) > 1e-6:                                  # :85-90
+            lmid = 0.5 * (hi + lo)
+            xnew = np.maximum(0.0, np.maximum(x - opt.move, np.minimum(1.0, np.minimum(x + opt.move,
+                                                                                      x * np.sqrt(-dc / dv / lmid)))))
+            gt = g + float(np.sum(dv * (xnew - x)))
+            if gt > 0:
+                lo = lmid
+            else:
+                hi = lmid
+        change = float(np.abs(xnew - x).max())                              # :91
+        x = xnew
+        xPhys = K.density_filter(xnew, opt.rmin, emf, rx, ry, rz) / Hs       # :99
+        sharp = float(4.0 * np.sum(xPhys * (1.0 - xPhys)) / n)               # :102
+        hist.append({"loop": loop, "c": c, "vol": vol, "sharp": sharp, "change": change, "g": g, "its": its})
+    return xPhys, hist

@@ -36,6 +36,17 @@ class SolveInfo(C.Structure):
                 ("precond_seconds", dbl)]
 
 
+class TopOptOpts(C.Structure):
+    _fields_ = [("volfrac", dbl), ("rmin", dbl), ("move", dbl), ("n_loop", i32), ("min_change", dbl),
+                ("max_sharpness", dbl), ("penalty", dbl), ("E0", dbl), ("Emin", dbl), ("solve", SolveOpts)]
+
+
+class TopOptIter(C.Structure):
+    _fields_ = [("loop", i32), ("cg_iterations", i32), ("compliance", dbl), ("volume", dbl), ("sharpness", dbl),
+                ("change", dbl), ("constraint", dbl), ("t_assemble", dbl), ("t_solve", dbl), ("t_opt", dbl),
+                ("t_filter", dbl)]
+
+
 SIGNATURES = {
     "sgld_default_options": (None, [vp]),
     "sgld_reference_num_levels": (i32, [i64, i64]),
@@ -68,6 +79,8 @@ SIGNATURES = {
     "sgld_kernel_launches": (i64, []),
     "sgld_time_op": (i32, [vp, i32, i32, vp]),
     "sgld_kbyu_dot_noalloc": (i32, [vp, vp, vp, vp, vp]),
+    "sgld_density_filter": (i32, [vp, dbl, vp, vp]),
+    "sgld_topopt": (i32, [vp, vp, vp, vp, vp, vp, vp]),
 }
 
 _lib = None

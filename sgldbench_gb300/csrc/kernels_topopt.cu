@@ -1,0 +1,272 @@
+// SIMP topology-optimisation kernels around the solve
+// (reference: src/TopOpti_GlobalVolumeConstraint_Tmp.m:26-120 with the cone
+// density filter of src/MEXfuncs/TopOpti_SetupDensityFilter_mex.cpp:23-50 and
+// TopOpti_PerformDensityFiltering_mex.cpp:75-102).
+//
+// Element fields live on the finest level's full element grid (inactive = 0).
+// The filter weights max(0, rmin - |d|) depend only on the offset d, so they
+// are formed once on the host with the reference's expression and kept in
+// constant memory; the kernel sums over the box in the reference's loop
+// order (z outer, x, y inner).
+#include <math.h>
+
+#include "sgld_internal.cuh"
+
+namespace sgld {
+
+constexpr int FW_MAX = 7;   // box side up to 7 (rmin <= 4)
+__constant__ double c_fw[FW_MAX * FW_MAX * FW_MAX];
+
+void upload_filter_weights(double rmin, int *radius, cudaStream_t s) {
+    const int r = (int)ceil(rmin) - 1;
+    const int side = 2 * r + 1;
+    double w[FW_MAX * FW_MAX * FW_MAX];
+    for (int dz = -r; dz <= r; ++dz)
+        for (int dx = -r; dx <= r; ++dx)
+            for (int dy = -r; dy <= r; ++dy) {
+                const double d = rmin - sqrt((double)(dx * dx + dy * dy + dz * dz));
+                w[(dz + r) * side * side + (dx + r) * side + (dy + r)] = d > 0.0 ? d : 0.0;
+            }
+    cudaMemcpyToSymbolAsync(c_fw, w, sizeof(double) * side * side * side, 0, cudaMemcpyHostToDevice, s);
+    *radius = r;
+}
+
+// y_e = sum_{e2 in box, active} w(e - e2) x_e2   (x == nullptr: the weight sums Hs)
+__global__ void k_density_filter(const double *__restrict__ x, const uint8_t *__restrict__ eact, int ny, int nx,
+                                 int nz, int r, double *__restrict__ y) {
+    const int pl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pl >= ny * nx) return;
+    const int jj = pl % ny, ii = pl / ny, kk = blockIdx.y;
+    const int64_t e = (int64_t)pl + (int64_t)ny * nx * kk;
+    if (!eact[e]) {
+        y[e] = 0.0;
+        return;
+    }
+    const int side = 2 * r + 1;
+    double acc = 0.0;
+    for (int k2 = max(kk - r, 0); k2 <= min(kk + r, nz - 1); ++k2)
+        for (int i2 = max(ii - r, 0); i2 <= min(ii + r, nx - 1); ++i2)
+            for (int j2 = max(jj - r, 0); j2 <= min(jj + r, ny - 1); ++j2) {
+                const int64_t e2 = (int64_t)j2 + (int64_t)ny * (i2 + (int64_t)nx * k2);
+                if (!eact[e2]) continue;
+                const double w = c_fw[(k2 - kk + r) * side * side + (i2 - ii + r) * side + (j2 - jj + r)];
+                acc += x ? w * x[e2] : w;
+            }
+    y[e] = acc;
+}
+
+void launch_density_filter(const Level &l0, const double *x, int r, double *y, cudaStream_t s) {
+    const dim3 g((unsigned)((l0.ny * l0.nx + 255) / 256), (unsigned)l0.nz);
+    ++g_launches;
+    k_density_filter<<<g, 256, 0, s>>>(x, l0.eact, l0.ny, l0.nx, l0.nz, r, y);
+}
+
+constexpr int TB = 256;
+
+__device__ __forceinline__ double tblock_sum(double v) {
+    __shared__ double red[TB / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < TB / 32; ++i) s += red[i];
+    return s;
+}
+
+__device__ __forceinline__ double tblock_max(double v) {
+    __shared__ double red[TB / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < TB / 32; ++i) s = fmax(s, red[i]);
+    return s;
+}
+
+// E = Emin + xPhys^p (E0 - Emin) on active elements (TopOpti_MaterialInterpolationSIMP.m:5);
+// partial sums of xPhys (volume) and of 4 xPhys (1 - xPhys) (sharpness, :102)
+__global__ void k_topo_modulus(const double *__restrict__ xp, const uint8_t *__restrict__ eact, int64_t n, double p,
+                               double E0, double Emin, double *__restrict__ E, double *__restrict__ part_v,
+                               double *__restrict__ part_s) {
+    double sv = 0.0, ss = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB) {
+        if (!eact[e]) {
+            E[e] = 0.0;
+            continue;
+        }
+        const double v = xp[e];
+        E[e] = Emin + pow(v, p) * (E0 - Emin);
+        sv += v;
+        ss += 4.0 * v * (1.0 - v);
+    }
+    sv = tblock_sum(sv);
+    ss = tblock_sum(ss);
+    if (threadIdx.x == 0) {
+        part_v[blockIdx.x] = sv;
+        part_s[blockIdx.x] = ss;
+    }
+}
+
+// dc/Hs and dv/Hs (TopOpti_GlobalVolumeConstraint_Tmp.m:66-77, ft = 2):
+// dc = -p (E0 - Emin) xPhys^(p-1) ce (TopOpti_DeMaterialInterpolation.m:5)
+__global__ void k_topo_sens(const double *__restrict__ xp, const double *__restrict__ ce,
+                            const double *__restrict__ Hs, const uint8_t *__restrict__ eact, int64_t n, double p,
+                            double E0, double Emin, double *__restrict__ dcs, double *__restrict__ dvs) {
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB) {
+        if (!eact[e]) {
+            dcs[e] = 0.0;
+            dvs[e] = 0.0;
+            continue;
+        }
+        const double dc = -(p * (E0 - Emin) * pow(xp[e], p - 1.0)) * ce[e];
+        dcs[e] = dc / Hs[e];
+        dvs[e] = 1.0 / Hs[e];
+    }
+}
+
+// q = x sqrt(-dc/dv) once per update, so that a bisection step needs one
+// multiply per element: x sqrt(-dc/dv/lmid) = q / sqrt(lmid)
+__global__ void k_topo_q(const double *__restrict__ x, const double *__restrict__ dc, const double *__restrict__ dv,
+                         const uint8_t *__restrict__ eact, int64_t n, double *__restrict__ q) {
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB)
+        q[e] = eact[e] ? x[e] * sqrt(-dc[e] / dv[e]) : 0.0;
+}
+
+// bisection state (device): [0] lo [1] hi [2] lmid [3] g [4] done [5] steps
+enum { OC_LO = 0, OC_HI = 1, OC_MID = 2, OC_G = 3, OC_DONE = 4, OC_STEPS = 5 };
+
+__device__ __forceinline__ double oc_new(double xe, double qe, double rs, double move) {
+    // max(0, max(x - move, min(1, min(x + move, x sqrt(-dc/dv/lmid)))))   (:87)
+    return fmax(0.0, fmax(xe - move, fmin(1.0, fmin(xe + move, qe * rs))));
+}
+
+__global__ void k_oc_step(const double *__restrict__ x, const double *__restrict__ q, const double *__restrict__ dv,
+                          const uint8_t *__restrict__ eact, int64_t n, double move, const double *__restrict__ st,
+                          double *__restrict__ part) {
+    if (st[OC_DONE] != 0.0) return;
+    const double lmid = 0.5 * (st[OC_HI] + st[OC_LO]);
+    const double rs = 1.0 / sqrt(lmid);
+    double s = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB) {
+        if (!eact[e]) continue;
+        s += dv[e] * (oc_new(x[e], q[e], rs, move) - x[e]);
+    }
+    s = tblock_sum(s);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__device__ double tsum_partials(const double *__restrict__ part, int nb) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nb; i += TB) s += part[i];
+    return tblock_sum(s);
+}
+
+// op 0: init (g = sum_v / n - V, lo = 0, hi = 1e9); op 1: bisection update (:88-89)
+__global__ void k_oc_scalar(int op, double *__restrict__ st, const double *__restrict__ part, int nb, double nact,
+                            double volfrac) {
+    const double s = tsum_partials(part, nb);
+    if (threadIdx.x != 0) return;
+    if (op == 0) {
+        st[OC_G] = s / nact - volfrac;
+        st[OC_LO] = 0.0;
+        st[OC_HI] = 1e9;
+        st[OC_DONE] = 0.0;
+        st[OC_STEPS] = 0.0;
+        st[OC_MID] = 0.5e9;
+        return;
+    }
+    if (st[OC_DONE] != 0.0) return;
+    const double lmid = 0.5 * (st[OC_HI] + st[OC_LO]);
+    st[OC_MID] = lmid;
+    const double gt = st[OC_G] + s;
+    if (gt > 0.0)
+        st[OC_LO] = lmid;
+    else
+        st[OC_HI] = lmid;
+    st[OC_STEPS] += 1.0;
+    if (!((st[OC_HI] - st[OC_LO]) / (st[OC_LO] + st[OC_HI]) > 1e-6)) st[OC_DONE] = 1.0;
+}
+
+// x <- xnew(lmid of the last bisection step); partial max |xnew - x| (:91-92)
+__global__ void k_oc_apply(double *__restrict__ x, const double *__restrict__ q, const uint8_t *__restrict__ eact,
+                           int64_t n, double move, const double *__restrict__ st, double *__restrict__ part) {
+    const double rs = 1.0 / sqrt(st[OC_MID]);
+    double m = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB) {
+        if (!eact[e]) continue;
+        const double xn = oc_new(x[e], q[e], rs, move);
+        m = fmax(m, fabs(xn - x[e]));
+        x[e] = xn;
+    }
+    m = tblock_max(m);
+    if (threadIdx.x == 0) part[blockIdx.x] = m;
+}
+
+__global__ void k_max_partials(const double *__restrict__ part, int nb, double *__restrict__ out) {
+    double m = 0.0;
+    for (int i = threadIdx.x; i < nb; i += TB) m = fmax(m, part[i]);
+    m = tblock_max(m);
+    if (threadIdx.x == 0) out[0] = m;
+}
+
+__global__ void k_div(const double *__restrict__ a, const double *__restrict__ b, const uint8_t *__restrict__ eact,
+                      int64_t n, double *__restrict__ y) {
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB)
+        y[e] = eact[e] ? a[e] / b[e] : 0.0;
+}
+
+__global__ void k_fill_active(double *__restrict__ y, const uint8_t *__restrict__ eact, int64_t n, double v) {
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB)
+        y[e] = eact[e] ? v : 0.0;
+}
+
+// ---- launchers ----------------------------------------------------------------
+void launch_topo_modulus(const Level &l0, const double *xp, double p, double E0, double Emin, double *E,
+                         double *pv, double *ps, int nb, cudaStream_t s) {
+    ++g_launches;
+    k_topo_modulus<<<nb, TB, 0, s>>>(xp, l0.eact, l0.nel, p, E0, Emin, E, pv, ps);
+}
+void launch_topo_sens(const Level &l0, const double *xp, const double *ce, const double *Hs, double p, double E0,
+                      double Emin, double *dcs, double *dvs, int nb, cudaStream_t s) {
+    ++g_launches;
+    k_topo_sens<<<nb, TB, 0, s>>>(xp, ce, Hs, l0.eact, l0.nel, p, E0, Emin, dcs, dvs);
+}
+void launch_topo_q(const Level &l0, const double *x, const double *dc, const double *dv, double *q, int nb,
+                   cudaStream_t s) {
+    ++g_launches;
+    k_topo_q<<<nb, TB, 0, s>>>(x, dc, dv, l0.eact, l0.nel, q);
+}
+void launch_oc_step(const Level &l0, const double *x, const double *q, const double *dv, double move,
+                    const double *st, double *part, int nb, cudaStream_t s) {
+    ++g_launches;
+    k_oc_step<<<nb, TB, 0, s>>>(x, q, dv, l0.eact, l0.nel, move, st, part);
+}
+void launch_oc_scalar(int op, double *st, const double *part, int nb, double nact, double volfrac, cudaStream_t s) {
+    ++g_launches;
+    k_oc_scalar<<<1, TB, 0, s>>>(op, st, part, nb, nact, volfrac);
+}
+void launch_oc_apply(const Level &l0, double *x, const double *q, double move, const double *st, double *part,
+                     int nb, cudaStream_t s) {
+    ++g_launches;
+    k_oc_apply<<<nb, TB, 0, s>>>(x, q, l0.eact, l0.nel, move, st, part);
+}
+void launch_max_partials(const double *part, int nb, double *out, cudaStream_t s) {
+    ++g_launches;
+    k_max_partials<<<1, TB, 0, s>>>(part, nb, out);
+}
+void launch_div(const Level &l0, const double *a, const double *b, double *y, int nb, cudaStream_t s) {
+    ++g_launches;
+    k_div<<<nb, TB, 0, s>>>(a, b, l0.eact, l0.nel, y);
+}
+void launch_fill_active(const Level &l0, double *y, double v, int nb, cudaStream_t s) {
+    ++g_launches;
+    k_fill_active<<<nb, TB, 0, s>>>(y, l0.eact, l0.nel, v);
+}
+
+}  // namespace sgld

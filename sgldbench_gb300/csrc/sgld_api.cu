@@ -1240,6 +1240,14 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
 
 }  // namespace
 
+// PCG on the context's own full-grid vectors (b in d_b, x in d_x), used by the
+// SIMP driver (sgld_topopt_api.cu)
+int sgld::solve_on_device(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
+    int rc = check_assembled(ctx);
+    if (rc) return rc;
+    return solve_dev(ctx, o, info);
+}
+
 extern "C" int sgld_time_op(sgld_ctx *ctx, int op, int reps, double *ms_per_op) {
     int rc = check_ready(ctx);
     if (rc) return rc;

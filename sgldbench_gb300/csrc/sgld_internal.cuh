@@ -65,6 +65,10 @@ struct Ctx {
     float *d_Ainv32 = nullptr;
     double *d_LB = nullptr;         // [ncf*(cband+1) + ncf] band rows of the Cholesky factor, 1/diag
     double *d_cy = nullptr;         // [2*ncf] intermediate of the coarse apply
+    // SIMP loop fields on the finest element grid (allocated on first use)
+    double *t_x = nullptr, *t_xp = nullptr, *t_hs = nullptr, *t_ce = nullptr, *t_dcs = nullptr, *t_dvs = nullptr,
+           *t_dc = nullptr, *t_dv = nullptr, *t_q = nullptr, *t_tmp = nullptr, *t_st = nullptr;
+    double t_rmin = -1.0;
     cudaGraphExec_t factor_graph = nullptr;   // captured factorization of the coarsest matrix
     int64_t factor_graph_launches = 0;
     int trinv_ring = 0, trinv_warps = 0;
@@ -127,6 +131,29 @@ void launch_widen_dots(const float *e, double *z, const double *r, const double 
 void launch_flex_beta(double *scal, const int *iflag, const double *p1, const double *p2, int nb, int first,
                       cudaStream_t st);
 void launch_narrow(const double *a, float *b, int64_t n, cudaStream_t st);
+}  // namespace sgld
+struct sgld_solve_opts;
+struct sgld_solve_info;
+namespace sgld {
+// PCG on the context's own full-grid vectors d_b / d_x (sgld_api.cu)
+int solve_on_device(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info);
+// SIMP loop (kernels_topopt.cu)
+void upload_filter_weights(double rmin, int *radius, cudaStream_t s);
+void launch_density_filter(const Level &l0, const double *x, int r, double *y, cudaStream_t s);
+void launch_topo_modulus(const Level &l0, const double *xp, double p, double E0, double Emin, double *E,
+                         double *pv, double *ps, int nb, cudaStream_t s);
+void launch_topo_sens(const Level &l0, const double *xp, const double *ce, const double *Hs, double p, double E0,
+                      double Emin, double *dcs, double *dvs, int nb, cudaStream_t s);
+void launch_topo_q(const Level &l0, const double *x, const double *dc, const double *dv, double *q, int nb,
+                   cudaStream_t s);
+void launch_oc_step(const Level &l0, const double *x, const double *q, const double *dv, double move,
+                    const double *st, double *part, int nb, cudaStream_t s);
+void launch_oc_scalar(int op, double *st, const double *part, int nb, double nact, double volfrac, cudaStream_t s);
+void launch_oc_apply(const Level &l0, double *x, const double *q, double move, const double *st, double *part,
+                     int nb, cudaStream_t s);
+void launch_max_partials(const double *part, int nb, double *out, cudaStream_t s);
+void launch_div(const Level &l0, const double *a, const double *b, double *y, int nb, cudaStream_t s);
+void launch_fill_active(const Level &l0, double *y, double v, int nb, cudaStream_t s);
 void launch_unit_compliance(const Level &l0, const double *u, const double *E, double *ce_full,
                             double *partial, int *nblocks_out, cudaStream_t s);
 void launch_stress(const Level &l0, const double *E, const double *u, const double *M48x24,

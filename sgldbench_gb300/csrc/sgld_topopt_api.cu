@@ -1,0 +1,210 @@
+// C ABI of the SIMP loop and the density filter (include/sgld_gpu.h):
+// TopOpti_GlobalVolumeConstraint_Tmp.m:26-120 driven from the host, every
+// field operation on the device.
+#include <math.h>
+#include <string.h>
+
+#include <string>
+
+#include "../../include/sgld_gpu.h"
+#include "sgld_internal.cuh"
+
+using namespace sgld;
+
+namespace {
+
+int tfail(sgld_ctx *ctx, int code, const std::string &m) {
+    ctx->c.err = m;
+    return code;
+}
+
+#define TCK(x)                                                                                  \
+    do {                                                                                        \
+        cudaError_t e_ = (x);                                                                   \
+        if (e_ != cudaSuccess) return tfail(ctx, SGLD_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+enum { OC_MID = 2, OC_G = 3, OC_DONE = 4, OC_STEPS = 5, T_SHARP = 8, T_C = 9, T_CHANGE = 10, T_VOL = 11 };
+
+int ensure_topo(sgld_ctx *ctx) {
+    Ctx &c = ctx->c;
+    if (c.t_x) return SGLD_OK;
+    const size_t n = (size_t)c.lv[0].nel;
+    for (double **p : {&c.t_x, &c.t_xp, &c.t_hs, &c.t_ce, &c.t_dcs, &c.t_dvs, &c.t_dc, &c.t_dv, &c.t_q, &c.t_tmp}) {
+        cudaError_t e = cudaMalloc((void **)p, n * sizeof(double));
+        if (e != cudaSuccess) return tfail(ctx, SGLD_ERR_NOMEM, "SIMP-loop buffers: out of device memory");
+    }
+    TCK(cudaMalloc((void **)&c.t_st, 16 * sizeof(double)));
+    return SGLD_OK;
+}
+
+// weights for this rmin and the weight sums Hs in t_hs
+int setup_filter(sgld_ctx *ctx, double rmin, int *radius) {
+    Ctx &c = ctx->c;
+    if (!(rmin > 0.0) || (int)ceil(rmin) - 1 > 3) return tfail(ctx, SGLD_ERR_ARG, "rmin must be in (0, 4]");
+    int r = 0;
+    upload_filter_weights(rmin, &r, c.stream);
+    if (c.t_rmin != rmin) {
+        launch_density_filter(c.lv[0], nullptr, r, c.t_hs, c.stream);
+        c.t_rmin = rmin;
+    }
+    *radius = r;
+    return SGLD_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+}  // namespace
+
+extern "C" int sgld_density_filter(sgld_ctx *ctx, double rmin, const double *x, double *y) {
+    if (!ctx || !y) return SGLD_ERR_ARG;
+    Ctx &c = ctx->c;
+    int rc = ensure_topo(ctx);
+    if (rc) return rc;
+    int r = 0;
+    if ((rc = setup_filter(ctx, rmin, &r))) return rc;
+    const int64_t ne = (int64_t)c.h_elemap.size();
+    const Level &l0 = c.lv[0];
+    if (x) {
+        TCK(cudaMemcpyAsync(c.d_tmp, x, sizeof(double) * ne, cudaMemcpyHostToDevice, c.stream));
+        TCK(cudaMemsetAsync(c.t_tmp, 0, sizeof(double) * l0.nel, c.stream));
+        launch_scatter_elems(c.d_elemap, ne, c.d_tmp, c.t_tmp, c.stream);
+        launch_density_filter(l0, c.t_tmp, r, c.t_q, c.stream);
+        launch_gather_elems(c.d_elemap, ne, c.t_q, c.d_tmp, c.stream);
+    } else {
+        launch_gather_elems(c.d_elemap, ne, c.t_hs, c.d_tmp, c.stream);
+    }
+    TCK(cudaGetLastError());
+    TCK(cudaMemcpyAsync(y, c.d_tmp, sizeof(double) * ne, cudaMemcpyDeviceToHost, c.stream));
+    TCK(cudaStreamSynchronize(c.stream));
+    return SGLD_OK;
+}
+
+extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const double *F, const double *x0,
+                           double *xphys, sgld_topopt_iter *hist, int *n_iter) {
+    if (!ctx || !opts || !F) return SGLD_ERR_ARG;
+    Ctx &c = ctx->c;
+    if (!c.have_fixed) return tfail(ctx, SGLD_ERR_STATE, "fixed DOFs not set (sgld_set_fixed_dofs)");
+    sgld_topopt_opts o = *opts;
+    if (o.move == 0) o.move = 0.1;
+    if (o.min_change == 0) o.min_change = 1e-4;
+    if (o.max_sharpness == 0) o.max_sharpness = 0.05;
+    if (o.penalty == 0) o.penalty = 3.0;
+    if (o.E0 == 0) o.E0 = 1.0;
+    if (o.Emin == 0) o.Emin = 1e-6;
+    if (o.n_loop < 1 || !(o.volfrac > 0.0 && o.volfrac <= 1.0))
+        return tfail(ctx, SGLD_ERR_ARG, "n_loop >= 1 and volfrac in (0, 1] required");
+    int rc = ensure_topo(ctx);
+    if (rc) return rc;
+    int r = 0;
+    if ((rc = setup_filter(ctx, o.rmin, &r))) return rc;
+    const Level &l0 = c.lv[0];
+    const int64_t ne = (int64_t)c.h_elemap.size(), nn = (int64_t)c.h_nodemap.size();
+    const size_t nv = 3 * (size_t)l0.nnode;
+    const int nb = reduce_blocks(l0.nel);
+    const double nact = (double)ne;
+    cudaStream_t s = c.stream;
+    // loads: F -> d_b, U = 0 (TopOpti_CallTopOpti.m:15), x = x0 or volfrac
+    TCK(cudaMemsetAsync(c.d_b, 0, sizeof(double) * nv, s));
+    TCK(cudaMemsetAsync(c.d_x, 0, sizeof(double) * nv, s));
+    TCK(cudaMemcpyAsync(c.d_tmp, F, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, s));
+    launch_scatter_nodes(c.d_nodemap, nn, c.d_tmp, c.d_b, s);
+    if (x0) {
+        TCK(cudaMemsetAsync(c.t_x, 0, sizeof(double) * l0.nel, s));
+        TCK(cudaMemcpyAsync(c.d_tmp, x0, sizeof(double) * ne, cudaMemcpyHostToDevice, s));
+        launch_scatter_elems(c.d_elemap, ne, c.d_tmp, c.t_x, s);
+    } else {
+        launch_fill_active(l0, c.t_x, o.volfrac, nb, s);
+    }
+    TCK(cudaMemcpyAsync(c.t_xp, c.t_x, sizeof(double) * l0.nel, cudaMemcpyDeviceToDevice, s));
+    launch_topo_modulus(l0, c.t_xp, o.penalty, o.E0, o.Emin, c.E, c.d_part, c.d_part2, nb, s);
+    launch_finalize_sum(c.d_part, nb, c.t_st + T_VOL, s);
+    launch_finalize_sum(c.d_part2, nb, c.t_st + T_SHARP, s);
+    c.have_E = true;
+    TCK(cudaGetLastError());
+    cudaEvent_t ev[5];
+    for (auto &e : ev) TCK(cudaEventCreate(&e));
+    sgld_solve_opts so = o.solve;
+    so.use_x0 = 1;
+    so.history = nullptr;
+    double change = 1.0, sharp = 1.0;
+    int loop = 0;
+    while (loop < o.n_loop && change > o.min_change && sharp > o.max_sharpness) {   // :47
+        ++loop;
+        double vol = 0.0;
+        TCK(cudaMemcpyAsync(&vol, c.t_st + T_VOL, sizeof(double), cudaMemcpyDeviceToHost, s));
+        launch_oc_scalar(0, c.t_st, c.t_st + T_VOL, 1, nact, o.volfrac, s);        // g (:83), bisection bounds
+        TCK(cudaEventRecord(ev[0], s));
+        if ((rc = sgld_assemble(ctx))) return rc;                                  // :54
+        TCK(cudaEventRecord(ev[1], s));
+        sgld_solve_info si;
+        if ((rc = solve_on_device(ctx, &so, &si))) return rc;                      // :57
+        TCK(cudaEventRecord(ev[2], s));
+        int nbc = 0;
+        launch_unit_compliance(l0, c.d_x, c.E, c.t_ce, c.d_part, &nbc, s);        // :59, :63
+        launch_finalize_sum(c.d_part, nbc, c.t_st + T_C, s);
+        launch_topo_sens(l0, c.t_xp, c.t_ce, c.t_hs, o.penalty, o.E0, o.Emin, c.t_dcs, c.t_dvs, nb, s);   // :66
+        TCK(cudaEventRecord(ev[3], s));
+        launch_density_filter(l0, c.t_dcs, r, c.t_dc, s);                          // :76
+        launch_density_filter(l0, c.t_dvs, r, c.t_dv, s);                          // :77
+        cudaEvent_t evf;
+        TCK(cudaEventCreate(&evf));
+        TCK(cudaEventRecord(evf, s));
+        launch_topo_q(l0, c.t_x, c.t_dc, c.t_dv, c.t_q, nb, s);
+        double done = 0.0;
+        for (int round = 0; round < 8 && done == 0.0; ++round) {                   // :85-90
+            for (int k = 0; k < 32; ++k) {
+                launch_oc_step(l0, c.t_x, c.t_q, c.t_dv, o.move, c.t_st, c.d_part, nb, s);
+                launch_oc_scalar(1, c.t_st, c.d_part, nb, nact, o.volfrac, s);
+            }
+            TCK(cudaMemcpyAsync(&done, c.t_st + OC_DONE, sizeof(double), cudaMemcpyDeviceToHost, s));
+            TCK(cudaStreamSynchronize(s));
+        }
+        launch_oc_apply(l0, c.t_x, c.t_q, o.move, c.t_st, c.d_part, nb, s);       // :91-92
+        launch_max_partials(c.d_part, nb, c.t_st + T_CHANGE, s);
+        cudaEvent_t evo;
+        TCK(cudaEventCreate(&evo));
+        TCK(cudaEventRecord(evo, s));
+        launch_density_filter(l0, c.t_x, r, c.t_tmp, s);                           // :99
+        launch_div(l0, c.t_tmp, c.t_hs, c.t_xp, nb, s);
+        TCK(cudaEventRecord(ev[4], s));
+        launch_topo_modulus(l0, c.t_xp, o.penalty, o.E0, o.Emin, c.E, c.d_part, c.d_part2, nb, s);   // :52, :102
+        launch_finalize_sum(c.d_part, nb, c.t_st + T_VOL, s);
+        launch_finalize_sum(c.d_part2, nb, c.t_st + T_SHARP, s);
+        TCK(cudaGetLastError());
+        double st[16];
+        TCK(cudaMemcpyAsync(st, c.t_st, sizeof st, cudaMemcpyDeviceToHost, s));
+        TCK(cudaStreamSynchronize(s));
+        change = st[T_CHANGE];
+        sharp = st[T_SHARP] / nact;
+        if (hist) {
+            sgld_topopt_iter &h = hist[loop - 1];
+            h.loop = loop;
+            h.cg_iterations = si.iterations;
+            h.compliance = st[T_C];
+            h.volume = vol / nact;
+            h.sharpness = sharp;
+            h.change = change;
+            h.constraint = st[OC_G];
+            h.t_assemble = elapsed(ev[0], ev[1]) * 1e-3;
+            h.t_solve = elapsed(ev[1], ev[2]) * 1e-3;
+            h.t_opt = (elapsed(ev[2], ev[3]) + elapsed(evf, evo)) * 1e-3;
+            h.t_filter = (elapsed(ev[3], evf) + elapsed(evo, ev[4])) * 1e-3;
+        }
+        cudaEventDestroy(evf);
+        cudaEventDestroy(evo);
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (n_iter) *n_iter = loop;
+    if (xphys) {
+        launch_gather_elems(c.d_elemap, ne, c.t_xp, c.d_tmp, s);
+        TCK(cudaMemcpyAsync(xphys, c.d_tmp, sizeof(double) * ne, cudaMemcpyDeviceToHost, s));
+        TCK(cudaStreamSynchronize(s));
+    }
+    c.assembled = false;   // E now holds the final design's moduli
+    return SGLD_OK;
+}

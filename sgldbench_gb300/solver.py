@@ -303,3 +303,41 @@ class VoxelSolver:
         vme = np.zeros(self.numElements)
         self._check(self.lib.sgld_stress(self.ctx, _p(u), _p(s6), _p(vmn), _p(vme)))
         return s6.reshape(self.numNodes, 6), vmn, vme
+
+    # -- SIMP loop (TopOpti_GlobalVolumeConstraint_Tmp.m) ---------------------------
+    def TopOpti_PerformDensityFiltering(self, x, rMin: float) -> np.ndarray:
+        """Cone filter of an element field (TopOpti_PerformDensityFiltering_mex)."""
+        xv = self._vec(x, self.numElements)
+        y = np.zeros(self.numElements)
+        self._check(self.lib.sgld_density_filter(self.ctx, float(rMin), _p(xv), _p(y)))
+        return y
+
+    def TopOpti_SetupDensityFilter(self, rMin: float) -> np.ndarray:
+        """Weight sums Hs of the cone filter (TopOpti_SetupDensityFilter_mex)."""
+        y = np.zeros(self.numElements)
+        self._check(self.lib.sgld_density_filter(self.ctx, float(rMin), None, _p(y)))
+        return y
+
+    def TopOpti_GlobalVolumeConstraint(self, F, volfrac: float = 0.3, rMin: float = 1.5, nLoop: int = 60,
+                                       move: float = 0.1, minChange: float = 1e-4, maxSharpness: float = 0.05,
+                                       penalty: float = 3.0, E0: float = 1.0, Emin: float = 1e-9,
+                                       tol: float = 1e-6, maxIT: int = 500, precision: str = "fp64",
+                                       inner_its: int = 0, x0=None):
+        """The whole SIMP loop on the device.  Returns (xPhys, history list)."""
+        Fv = self._vec(F, self.numDOFs)
+        so = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=1,
+                         precision=L.SGLD_PREC_MIXED if precision == "mixed" else L.SGLD_PREC_FP64,
+                         inner_its=inner_its, history=None, profile=0)
+        o = L.TopOptOpts(volfrac=volfrac, rmin=rMin, move=move, n_loop=nLoop, min_change=minChange,
+                         max_sharpness=maxSharpness, penalty=penalty, E0=E0, Emin=Emin, solve=so)
+        xp = np.zeros(self.numElements)
+        hist = (L.TopOptIter * nLoop)()
+        nit = C.c_int()
+        x0v = self._vec(x0, self.numElements) if x0 is not None else None
+        self._check(self.lib.sgld_topopt(self.ctx, C.byref(o), _p(Fv), _p(x0v) if x0v is not None else None,
+                                         _p(xp), hist, C.byref(nit)))
+        recs = []
+        for i in range(nit.value):
+            h = hist[i]
+            recs.append({k: getattr(h, k) for k, _ in L.TopOptIter._fields_})
+        return xp, recs

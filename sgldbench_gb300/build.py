@@ -62,5 +62,37 @@ def build(force: bool = False) -> str:
     return LIB
 
 
+def build_harness() -> str:
+    """The standalone C++ driver (harness/sgld_harness.cpp) linked to the library."""
+    lib = build()
+    out = os.path.join(HERE, "harness", "sgld_harness")
+    src = os.path.join(HERE, "harness", "sgld_harness.cpp")
+    if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(src), os.path.getmtime(lib)):
+        cmd = ["g++", "-O2", "-std=c++17", "-I", INCLUDE, src, "-o", out, "-L", HERE, "-lsgld_gb300",
+               f"-Wl,-rpath,{HERE}"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"harness build failed:\n{r.stderr}")
+    return out
+
+
+def build_mex_gateway(mex_include: str, out: str) -> str:
+    """Compiles the MEX gateway (mex/sgld_gpu_mex.cpp) against the mex.h found
+    in `mex_include`, with its entry point renamed to sgld_gpu_mex, into the
+    shared object `out` linked to the library.  MATLAB users build it with
+    `mex` instead."""
+    lib = build()
+    src = os.path.join(HERE, "mex", "sgld_gpu_mex.cpp")
+    extra = [os.path.join(mex_include, f) for f in os.listdir(mex_include) if f.endswith(".cpp")]
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-DmexFunction=sgld_gpu_mex", "-I", mex_include,
+           "-I", INCLUDE, src, *extra, "-o", out, "-L", HERE, "-lsgld_gb300", f"-Wl,-rpath,{HERE}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"MEX gateway build failed:\n{r.stderr}")
+    return out
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv))
+    if "--harness" in sys.argv:
+        print(build_harness())

@@ -1,0 +1,179 @@
+/*
+ * sgld_gpu_mex.cpp -- MATLAB MEX gateway of the GB300 solver.
+ *
+ * One mexFunction, first argument a command string; the solver context
+ * persists between calls (one per MATLAB session).  Each command replaces one
+ * function of SGLDBench's solve path and keeps its argument meaning:
+ *
+ *   sgld_gpu_mex('create', voxelizedVolume, numLevels, nonDyadic, poissonRatio, cellSize, omega)
+ *        FEA_VoxelBasedDiscretization.m + Solving_BuildingMeshHierarchy.m (padded grid)
+ *   sgld_gpu_mex('fixed', fixedDOFs)            FEA_SetupVoxelBased.m:13-26 (logical numDOFs)
+ *   sgld_gpu_mex('modulus', eleModulus)         meshHierarchy_(1).eleModulus
+ *   sgld_gpu_mex('assemble')                    Solving_AssembleFEAstencil.m
+ *   y = sgld_gpu_mex('kbyu', u)                 Solving_KbyU_MatrixFree.m
+ *   z = sgld_gpu_mex('vcycle', r)               Solving_Vcycle.m
+ *   [U, its] = sgld_gpu_mex('pcg', F, tol, maxIT[, U0[, 'mixed']])
+ *                                               Solving_PreconditionedConjugateGradientSolver.m
+ *   ce = sgld_gpu_mex('compliance', U)          TopOpti_ComputeUnitCompliance.m
+ *   [s, vm, vmE] = sgld_gpu_mex('stress', U)    FEA_StressAnalysis.m, FEA_ComputePerElementVonMisesStress.m
+ *   y = sgld_gpu_mex('filter', x, rMin)         TopOpti_PerformDensityFiltering_mex
+ *   sgld_gpu_mex('destroy')
+ *
+ * Errors become mexErrMsgIdAndTxt (the reference's error behaviour); a PCG
+ * that reaches maxIT warns, as Solving_PreconditionedConjugateGradientSolver.m:32-35.
+ * Build with MATLAB:  mex -R2018a sgld_gpu_mex.cpp -I<repo>/include -L<lib dir> -lsgld_gb300
+ */
+#include <stdint.h>
+#include <string.h>
+
+#include <vector>
+
+#include "mex.h"
+#include "sgld_gpu.h"
+
+static sgld_ctx *g_ctx = nullptr;
+
+static void check(int rc) {
+    if (rc != SGLD_OK) mexErrMsgIdAndTxt("sgld:gpu", "%s", g_ctx ? sgld_last_error(g_ctx) : "no context");
+}
+
+static void need_ctx() {
+    if (!g_ctx) mexErrMsgIdAndTxt("sgld:state", "call sgld_gpu_mex('create', ...) first");
+}
+
+static const double *dvec(const mxArray *a, size_t n, const char *what) {
+    if (!mxIsDouble(a) || mxGetNumberOfElements(a) != n)
+        mexErrMsgIdAndTxt("sgld:arg", "%s must be a double vector of %zu entries", what, n);
+    return mxGetPr(a);
+}
+
+static int64_t level_count(int what) {
+    int64_t ne = 0, nn = 0;
+    int res[3], span;
+    check(sgld_level_info(g_ctx, 1, res, &span, &ne, &nn));
+    return what == 0 ? ne : 3 * nn;
+}
+
+void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
+    char cmd[32] = {0};
+    if (nrhs < 1 || mxGetString(prhs[0], cmd, sizeof cmd) != 0)
+        mexErrMsgIdAndTxt("sgld:arg", "first argument must be a command string");
+    if (!strcmp(cmd, "create")) {
+        if (nrhs < 2) mexErrMsgIdAndTxt("sgld:arg", "create needs the voxel grid");
+        const mxArray *v = prhs[1];
+        if (mxGetNumberOfDimensions(v) != 3) mexErrMsgIdAndTxt("sgld:arg", "voxel grid must be 3-D");
+        const mwSize *d = mxGetDimensions(v);
+        const size_t n = d[0] * d[1] * d[2];
+        std::vector<uint8_t> solid(n);
+        if (mxIsLogical(v) || mxGetClassID(v) == mxUINT8_CLASS) {
+            const uint8_t *p = (const uint8_t *)mxGetData(v);
+            for (size_t i = 0; i < n; ++i) solid[i] = p[i] ? 1 : 0;
+        } else if (mxIsDouble(v)) {
+            const double *p = mxGetPr(v);
+            for (size_t i = 0; i < n; ++i) solid[i] = p[i] != 0.0;
+        } else {
+            mexErrMsgIdAndTxt("sgld:arg", "voxel grid must be logical, uint8 or double");
+        }
+        sgld_options o;
+        sgld_default_options(&o);
+        if (nrhs > 2) o.num_levels = (int)mxGetScalar(prhs[2]);
+        if (nrhs > 3) o.non_dyadic = (int)mxGetScalar(prhs[3]);
+        if (nrhs > 4) o.poisson_ratio = mxGetScalar(prhs[4]);
+        if (nrhs > 5) o.cell_size = mxGetScalar(prhs[5]);
+        if (nrhs > 6) o.omega = mxGetScalar(prhs[6]);
+        if (g_ctx) sgld_destroy(g_ctx);
+        g_ctx = nullptr;
+        const int rc = sgld_create((int)d[0], (int)d[1], (int)d[2], solid.data(), &o, &g_ctx);
+        if (rc != SGLD_OK) {
+            const char *m = g_ctx ? sgld_last_error(g_ctx) : "create failed";
+            char buf[512];
+            strncpy(buf, m, sizeof buf - 1);
+            buf[sizeof buf - 1] = 0;
+            if (g_ctx) sgld_destroy(g_ctx);
+            g_ctx = nullptr;
+            mexErrMsgIdAndTxt("sgld:gpu", "%s", buf);
+        }
+        if (nlhs > 0) plhs[0] = mxCreateDoubleScalar(sgld_num_levels(g_ctx));
+        return;
+    }
+    if (!strcmp(cmd, "destroy")) {
+        if (g_ctx) sgld_destroy(g_ctx);
+        g_ctx = nullptr;
+        return;
+    }
+    need_ctx();
+    const size_t ndof = (size_t)level_count(1), nel = (size_t)level_count(0);
+    if (!strcmp(cmd, "fixed")) {
+        if (nrhs < 2 || mxGetNumberOfElements(prhs[1]) != ndof)
+            mexErrMsgIdAndTxt("sgld:arg", "fixedDOFs must have numDOFs entries");
+        std::vector<uint8_t> f(ndof);
+        if (mxIsLogical(prhs[1])) {
+            const uint8_t *p = (const uint8_t *)mxGetData(prhs[1]);
+            for (size_t i = 0; i < ndof; ++i) f[i] = p[i] ? 1 : 0;
+        } else {
+            const double *p = dvec(prhs[1], ndof, "fixedDOFs");
+            for (size_t i = 0; i < ndof; ++i) f[i] = p[i] != 0.0;
+        }
+        check(sgld_set_fixed_dofs(g_ctx, f.data()));
+    } else if (!strcmp(cmd, "modulus")) {
+        check(sgld_set_modulus(g_ctx, dvec(prhs[1], nel, "eleModulus")));
+    } else if (!strcmp(cmd, "assemble")) {
+        check(sgld_assemble(g_ctx));
+    } else if (!strcmp(cmd, "kbyu") || !strcmp(cmd, "vcycle")) {
+        const double *u = dvec(prhs[1], ndof, "vector");
+        plhs[0] = mxCreateDoubleMatrix(ndof, 1, mxREAL);
+        check(cmd[0] == 'k' ? sgld_kbyu(g_ctx, u, mxGetPr(plhs[0])) : sgld_vcycle(g_ctx, u, mxGetPr(plhs[0])));
+    } else if (!strcmp(cmd, "pcg")) {
+        if (nrhs < 4) mexErrMsgIdAndTxt("sgld:arg", "pcg needs F, tol, maxIT");
+        const double *F = dvec(prhs[1], ndof, "F");
+        sgld_solve_opts o;
+        memset(&o, 0, sizeof o);
+        o.tol = mxGetScalar(prhs[2]);
+        o.maxit = (int)mxGetScalar(prhs[3]);
+        o.precision = SGLD_PREC_FP64;
+        plhs[0] = mxCreateDoubleMatrix(ndof, 1, mxREAL);
+        if (nrhs > 4 && mxGetNumberOfElements(prhs[4]) == ndof) {
+            memcpy(mxGetPr(plhs[0]), dvec(prhs[4], ndof, "U0"), ndof * sizeof(double));
+            o.use_x0 = 1;
+        }
+        if (nrhs > 5) {
+            char mode[16] = {0};
+            mxGetString(prhs[5], mode, sizeof mode);
+            if (!strcmp(mode, "mixed")) o.precision = SGLD_PREC_MIXED;
+        }
+        sgld_solve_info info;
+        check(sgld_pcg(g_ctx, F, mxGetPr(plhs[0]), &o, &info));
+        if (nlhs > 1) plhs[1] = mxCreateDoubleScalar(info.iterations);
+        if (!info.converged) {
+            mexWarnMsgIdAndTxt("sgld:maxit", "Exceed the maximum iterate numbers");
+            mexPrintf("The iterative process stops at residual = %10.4f\n", info.relres);
+        }
+    } else if (!strcmp(cmd, "compliance")) {
+        plhs[0] = mxCreateDoubleMatrix(nel, 1, mxREAL);
+        double c = 0.0;
+        check(sgld_compliance(g_ctx, dvec(prhs[1], ndof, "U"), mxGetPr(plhs[0]), &c));
+        if (nlhs > 1) plhs[1] = mxCreateDoubleScalar(c);
+    } else if (!strcmp(cmd, "stress")) {
+        const size_t nn = ndof / 3;
+        plhs[0] = mxCreateDoubleMatrix(nn, 6, mxREAL);
+        std::vector<double> rowmajor(6 * nn), vm(nn);
+        mxArray *vme = mxCreateDoubleMatrix(nel, 1, mxREAL);
+        check(sgld_stress(g_ctx, dvec(prhs[1], ndof, "U"), rowmajor.data(), vm.data(), mxGetPr(vme)));
+        double *s = mxGetPr(plhs[0]);   // MATLAB numNodes x 6, column-major
+        for (size_t i = 0; i < nn; ++i)
+            for (int k = 0; k < 6; ++k) s[i + nn * k] = rowmajor[6 * i + k];
+        if (nlhs > 1) {
+            plhs[1] = mxCreateDoubleMatrix(nn, 1, mxREAL);
+            memcpy(mxGetPr(plhs[1]), vm.data(), nn * sizeof(double));
+        }
+        if (nlhs > 2)
+            plhs[2] = vme;
+        else
+            mxDestroyArray(vme);
+    } else if (!strcmp(cmd, "filter")) {
+        plhs[0] = mxCreateDoubleMatrix(nel, 1, mxREAL);
+        check(sgld_density_filter(g_ctx, mxGetScalar(prhs[2]), dvec(prhs[1], nel, "x"), mxGetPr(plhs[0])));
+    } else {
+        mexErrMsgIdAndTxt("sgld:arg", "unknown command '%s'", cmd);
+    }
+}

@@ -196,19 +196,13 @@ def _known_iterations(args):
 def run_ours(args):
     import torch
 
-    from sgldbench_gb300 import VoxelSolver
+    from sgldbench_gb300 import VoxelSolver, replicas
     from sgldbench_gb300 import domains as D
     from sgldbench_gb300.solver import kernel_launches
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        import torch.distributed as dist
-
-        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        dist.init_process_group("nccl", rank=rank, world_size=world)
+    rank, world, local = replicas.dist_env()
     torch.cuda.set_device(local)
+    replicas.init("nccl")
     nx, ny, nz = args.size
     vox, E = workload(nx, ny, nz)
     s = VoxelSolver(vox, num_levels=args.levels, non_dyadic=0, omega=OMEGA, device=local, pad=False)
@@ -231,8 +225,7 @@ def run_ours(args):
         info = step()
     sampler = ClockSampler(local)
     sampler.start()
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     l0 = kernel_launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -245,10 +238,10 @@ def run_ours(args):
     launches = (kernel_launches() - l0) / max(args.steps, 1)
     clocks = sampler.stop()
     t_step = e0.elapsed_time(e1) / 1e3 / args.steps
-    if world > 1:
-        t = torch.tensor([t_step], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(t.item())
+    replicas.barrier()
+    torch.cuda.synchronize()
+    # the slowest replica's time per solve; every rank solved `steps` replicas
+    t_step, solves = replicas.aggregate(t_step, args.steps, device=dev)
     its = infos[-1]["its"]
     # split: one profiled solve (K*u launches timed with events on the library stream)
     pinfo = step(profile=True)
@@ -287,7 +280,8 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
             "data": "synthetic (seeded graded-density cuboid)", "config": workload_config(args),
-            "iterations": its, "dof": ndof, "dof_it_per_s": ndof * its / t_step,
+            "iterations": its, "dof": ndof, "dof_it_per_s": world * ndof * its / t_step,
+            "replica_solves_per_s": solves / (t_step * args.steps),
             "split": {"pcg_s": infos[-1]["seconds"], "assemble_s": t_step - infos[-1]["seconds"],
                       "kbyu_s": pinfo["kbyu_seconds"], "precond_s": pinfo["precond_seconds"]},
             "true_relres": infos[-1]["true_relres"], "converged": infos[-1]["converged"],
@@ -303,8 +297,7 @@ def run_ours(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     s.close()
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    replicas.shutdown()
 
 
 def _peaks():

@@ -15,7 +15,7 @@ device time per step with E and F already in HBM; `e2e` is the same solve
 through the public C ABI with host buffers (E and F copied in, U copied out).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--precision fp64|mixed] [--size NX NY NZ]
+                  [--precision fp64|mixed|mixed_df] [--size NX NY NZ]
 
 Under torchrun (N > 1) every rank solves its own replica on its own GPU (the
 solve path has no data-parallel split; replicas only) and rank 0 reports.
@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed", "mixed_df"], default="fp64")
     ap.add_argument("--size", type=int, nargs=3, default=[256, 128, 128], metavar=("NX", "NY", "NZ"))
     ap.add_argument("--levels", type=int, default=5)
     ap.add_argument("--maxit", type=int, default=2000)

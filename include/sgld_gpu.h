@@ -41,7 +41,11 @@ extern "C" {
 #define SGLD_ERR_NOMEM 5     /* device allocation failed                     */
 
 #define SGLD_PREC_FP64 0     /* reference form: FP64 PCG, FP64 additive V-cycle            */
-#define SGLD_PREC_MIXED 1    /* FP64 flexible PCG outer, FP32 preconditioner (see DESIGN) */
+#define SGLD_PREC_MIXED 1    /* FP64 flexible PCG outer, preconditioner = FP32 inner PCG with
+                                the FP32 V-cycle; same tolerance on the FP64 true residual  */
+#define SGLD_PREC_MIXED_DF 2 /* as SGLD_PREC_MIXED, with the outer K*p in double-float
+                                arithmetic (FP32 pairs, ~2^-48 relative); FP64 vectors,
+                                dot products and exit residual                             */
 
 typedef struct sgld_ctx sgld_ctx;
 
@@ -60,7 +64,7 @@ typedef struct sgld_solve_opts {
     int maxit;             /* iteration cap (maxIT_) */
     int use_x0;            /* 1: x holds the initial guess (Solving_CG_GMGS.m:7 warm start) */
     int precision;         /* SGLD_PREC_* */
-    int inner_its;         /* SGLD_PREC_MIXED: FP32 inner PCG iterations per outer step (0 = default) */
+    int inner_its;         /* SGLD_PREC_MIXED(_DF): FP32 inner PCG iterations per outer step (0 = 12) */
     double *history;       /* optional host buffer [maxit]: relative residual per iteration */
     int profile;           /* 1: time the K*u and preconditioner launches with CUDA events
                               (the SpMV / PtV split of QuickAccess/zTmp_Benchmarking_SpMV.m:63-111) */
@@ -71,7 +75,7 @@ typedef struct sgld_solve_info {
     int converged;         /* 1 if relres < tol */
     double relres;         /* recursive residual norm / ||b|| at exit */
     double true_relres;    /* ||b - K x|| / ||b|| recomputed in FP64 at exit */
-    int inner_iterations;  /* SGLD_PREC_MIXED: total FP32 inner iterations */
+    int inner_iterations;  /* SGLD_PREC_MIXED(_DF): total FP32 inner iterations */
     double seconds;        /* device time of the solve (CUDA events) */
     double kbyu_seconds;   /* profile: summed device time of the outer K*u launches */
     int kbyu_launches;     /* profile: number of those launches */
@@ -90,7 +94,8 @@ int64_t sgld_kernel_launches(void);
  * the mean milliseconds per application.  No counterpart in the reference:
  * it is the kernel-level measurement hook used for rooflines and profiling.
  *   op 0: FP64 K*u   op 1: FP32 K*u   op 2: FP64 V-cycle   op 3: FP32 V-cycle
- *   op 4: assembly (Galerkin levels + coarsest factorization) */
+ *   op 4: assembly (Galerkin levels + coarsest factorization)
+ *   op 5: double-float K*u (the outer operator of SGLD_PREC_MIXED_DF) */
 int sgld_time_op(sgld_ctx *ctx, int op, int reps, double *ms_per_op);
 
 /* Allocation-free K*u with its dot product (no counterpart in the reference).
@@ -169,6 +174,10 @@ int sgld_get_ks(const sgld_ctx *ctx, int level, double *Ks);
  * y(fixedDOFs) = 0. */
 int sgld_kbyu(sgld_ctx *ctx, const double *u, double *y);
 int sgld_kbyu_device(sgld_ctx *ctx, const double *d_u, double *d_y);
+/* The same product in double-float arithmetic (the outer K*p of
+ * SGLD_PREC_MIXED_DF); no counterpart in the reference, exposed so that its
+ * accuracy against the FP64 operator can be checked. */
+int sgld_kbyu_df(sgld_ctx *ctx, const double *u, double *y);
 
 /* Solving_RestrictResidual.m:1-23 / Solving_InterpolationDeviation.m:1-23 for
  * MATLAB level index ii (2..L): coarse = R fine, fine = P coarse (compact DOFs). */

@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(_HERE, "libsgld_gb300.so")
 SGLD_OK = 0
 SGLD_PREC_FP64 = 0
 SGLD_PREC_MIXED = 1
+SGLD_PREC_MIXED_DF = 2
 
 # exported symbols and their signatures (mirrors include/sgld_gpu.h)
 vp, i32, i64, dbl = C.c_void_p, C.c_int, C.c_int64, C.c_double
@@ -67,6 +68,7 @@ SIGNATURES = {
     "sgld_get_diag": (i32, [vp, i32, vp]),
     "sgld_get_ks": (i32, [vp, i32, vp]),
     "sgld_kbyu": (i32, [vp, vp, vp]),
+    "sgld_kbyu_df": (i32, [vp, vp, vp]),
     "sgld_kbyu_device": (i32, [vp, vp, vp]),
     "sgld_restrict": (i32, [vp, i32, vp, vp]),
     "sgld_interpolate": (i32, [vp, i32, vp, vp]),

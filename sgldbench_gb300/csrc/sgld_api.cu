@@ -255,6 +255,7 @@ int setup_templates(sgld_ctx *ctx) {
     CK(cudaMemcpy(c.d_H, H2.data(), H2.size() * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c.d_H + H2.size(), H4.data(), H4.size() * sizeof(double), cudaMemcpyHostToDevice));
     upload_kh(c.Kh, c.stream);
+    upload_kh_df(c.Kh, c.stream);
     return SGLD_OK;
 }
 
@@ -392,7 +393,7 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
 
 int solve_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
     if (o->maxit < 1 || !(o->tol >= 0.0)) return fail(ctx, SGLD_ERR_ARG, "maxit must be >= 1 and tol >= 0");
-    if (o->precision == SGLD_PREC_MIXED) return pcg_mixed_dev(ctx, o, info);
+    if (o->precision == SGLD_PREC_MIXED || o->precision == SGLD_PREC_MIXED_DF) return pcg_mixed_dev(ctx, o, info);
     if (o->precision != SGLD_PREC_FP64) return fail(ctx, SGLD_ERR_ARG, "unknown precision mode");
     return pcg_dev(ctx, o, info);
 }
@@ -550,6 +551,7 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
     for (float **p : {&c.d_e32, &c.d_s32, &c.d_d32, &c.d_t32}) CK(dalloc(p, nv));
     CK(dalloc(&c.d_isc, 16));
     init_kernel_attributes();
+    init_kbyu_df_attributes();
     // partial-sum slots: the largest grid of any kernel that writes per-CTA partials
     // (prolongation: ceil(NY*NX/256) CTAs per node plane)
     c.npart = (int)std::max<int64_t>({(int64_t)152 * 8, (l0.nel + 255) / 256 + 1,
@@ -852,6 +854,17 @@ int sgld_kbyu(sgld_ctx *ctx, const double *u, double *y) {
     return download_nodes(ctx, c.d_q, y);
 }
 
+int sgld_kbyu_df(sgld_ctx *ctx, const double *u, double *y) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!u || !y) return fail(ctx, SGLD_ERR_ARG, "null vector");
+    Ctx &c = ctx->c;
+    if ((rc = upload_nodes(ctx, u, c.d_p))) return rc;
+    launch_kbyu_df(c.lv[0], c.E, c.d_p, c.d_q, nullptr, nullptr, c.stream);
+    CKL();
+    return download_nodes(ctx, c.d_q, y);
+}
+
 static int level_vec_to_dev(sgld_ctx *ctx, int l, const double *h, double *d_full) {
     Ctx &c = ctx->c;
     const Level &lv = c.lv[l];
@@ -1127,8 +1140,11 @@ int pcg_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
 
 // Mixed precision: FP64 flexible PCG whose preconditioner is k FP32 CG
 // iterations with the FP32 additive V-cycle (graph-captured).  The FP64
-// residual recurrence, dot products, stopping test and K*p stay in FP64, so
-// the outer solve reaches the same tolerance on the true residual.
+// residual recurrence, dot products and stopping test stay in FP64, so the
+// outer solve reaches the same tolerance on the true residual.  The outer K*p
+// is the native FP64 operator (SGLD_PREC_MIXED) or the double-float one
+// (SGLD_PREC_MIXED_DF, ~2^-48 relative, FP32 issue rate); the true residual
+// at exit always uses the FP64 operator.
 int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
     Ctx &c = ctx->c;
     const Level &l0 = c.lv[0];
@@ -1137,6 +1153,7 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
     const double tol = o->tol;
     const int maxit = o->maxit;
     const int k = o->inner_its > 0 ? o->inner_its : 12;
+    const bool dfk = o->precision == SGLD_PREC_MIXED_DF;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
@@ -1166,7 +1183,10 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
     bool pc_pending = false;
     for (int it = 1; it <= maxit; ++it) {
         if (prof) CK(cudaEventRecord(pe[0], c.stream));
-        launch_kbyu_f64(l0, c.E, c.d_p, c.d_q, c.d_part, &nb, c.stream);
+        if (dfk)
+            launch_kbyu_df(l0, c.E, c.d_p, c.d_q, c.d_part, &nb, c.stream);
+        else
+            launch_kbyu_f64(l0, c.E, c.d_p, c.d_q, c.d_part, &nb, c.stream);
         if (prof) CK(cudaEventRecord(pe[1], c.stream));
         launch_pcg_scalar(2, c.d_scal, c.d_iflag, c.d_part, nb, tol, maxit, c.stream);
         launch_pcg_update(c.d_x, c.d_r, c.d_p, c.d_q, nv, c.d_scal, c.d_iflag, c.d_part, nbv, c.stream);
@@ -1251,7 +1271,7 @@ int sgld::solve_on_device(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_in
 extern "C" int sgld_time_op(sgld_ctx *ctx, int op, int reps, double *ms_per_op) {
     int rc = check_ready(ctx);
     if (rc) return rc;
-    if (!ms_per_op || reps < 1 || op < 0 || op > 4) return fail(ctx, SGLD_ERR_ARG, "bad op / reps");
+    if (!ms_per_op || reps < 1 || op < 0 || op > 5) return fail(ctx, SGLD_ERR_ARG, "bad op / reps");
     if ((op == 2 || op == 3) && !ctx->c.assembled) return fail(ctx, SGLD_ERR_STATE, "stencil not assembled");
     Ctx &c = ctx->c;
     const Level &l0 = c.lv[0];
@@ -1267,6 +1287,7 @@ extern "C" int sgld_time_op(sgld_ctx *ctx, int op, int reps, double *ms_per_op) 
             case 2: return vcycle_dev(ctx, c.d_p, c.d_z, nullptr, nullptr);
             case 3: return vcycle_dev32(ctx, c.d_r32, c.d_z32, nullptr, nullptr);
             case 4: return sgld_assemble(ctx);
+            case 5: launch_kbyu_df(l0, c.E, c.d_p, c.d_q, nullptr, nullptr, c.stream); break;
         }
         return SGLD_OK;
     };

@@ -121,6 +121,11 @@ void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *
 void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
                      int *nblocks_out, cudaStream_t s);
 void init_kernel_attributes();
+// double-float K*u (kernels_df.cu)
+void upload_kh_df(const double *Kh, cudaStream_t s);
+void init_kbyu_df_attributes();
+void launch_kbyu_df(const Level &l0, const double *E, const double *u, double *y, double *partial_dot,
+                    int *nblocks_out, cudaStream_t s);
 // mixed-precision solve (kernels_mixed.cu)
 void launch_icg_scalar(int op, double *sc, const double *part, int nb, cudaStream_t s);
 void launch_icg_update(float *e, float *s, const float *d, const float *t, int64_t n, const double *sc,

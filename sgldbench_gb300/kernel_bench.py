@@ -2,7 +2,7 @@
 and as the small driver of kernel-level profiler captures.
 
   python -m sgldbench_gb300.kernel_bench [--size NX NY NZ] [--levels L]
-                                         [--ops kbyu64 kbyu32 vcycle64 vcycle32 assemble]
+                                         [--ops kbyu64 kbyu32 kbyu_df vcycle64 vcycle32 assemble]
                                          [--reps N]
 
 Builds the SIMP-graded cantilever of the given size, assembles it and prints
@@ -21,7 +21,7 @@ from .solver import VoxelSolver
 def bytes_and_flops(op: str, nx: int, ny: int, nz: int) -> tuple[int, float]:
     nn = (nx + 1) * (ny + 1) * (nz + 1)
     ne = nx * ny * nz
-    if op == "kbyu64":   # read u, write y (3 doubles per node), node flags, E per element
+    if op in ("kbyu64", "kbyu_df"):   # read u, write y (3 doubles per node), node flags, E per element
         return nn * (48 + 1) + ne * 8, 1176.0 * ne
     if op == "kbyu32":
         return nn * (24 + 1) + ne * 4, 1176.0 * ne
@@ -32,7 +32,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--size", type=int, nargs=3, default=[256, 128, 128])
     ap.add_argument("--levels", type=int, default=5)
-    ap.add_argument("--ops", nargs="+", default=["kbyu64", "kbyu32", "vcycle64", "vcycle32", "assemble"])
+    ap.add_argument("--ops", nargs="+", default=["kbyu64", "kbyu32", "kbyu_df", "vcycle64", "vcycle32", "assemble"])
     ap.add_argument("--reps", type=int, default=10)
     args = ap.parse_args()
     nx, ny, nz = args.size

@@ -57,6 +57,16 @@ def pad_voxels(voxels: np.ndarray, num_levels: int) -> np.ndarray:
     return out
 
 
+_PRECISIONS = {"fp64": L.SGLD_PREC_FP64, "mixed": L.SGLD_PREC_MIXED, "mixed_df": L.SGLD_PREC_MIXED_DF}
+
+
+def _precision(name: str) -> int:
+    """'fp64' (the reference's form), 'mixed' or 'mixed_df' -> SGLD_PREC_*."""
+    if name not in _PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}, not {name!r}")
+    return _PRECISIONS[name]
+
+
 def _info_dict(info) -> dict:
     return {"its": info.iterations, "converged": bool(info.converged), "relres": info.relres,
             "true_relres": info.true_relres, "inner_its": info.inner_iterations, "seconds": info.seconds,
@@ -203,6 +213,13 @@ class VoxelSolver:
         self._check(self.lib.sgld_kbyu(self.ctx, _p(u), _p(y)))
         return y
 
+    def kbyu_double_float(self, uVec) -> np.ndarray:
+        """K u in double-float arithmetic: the outer operator of precision "mixed_df"."""
+        u = self._vec(uVec, self.numDOFs)
+        y = np.zeros_like(u)
+        self._check(self.lib.sgld_kbyu_df(self.ctx, _p(u), _p(y)))
+        return y
+
     def Solving_RestrictResidual(self, rFiner, ii: int) -> np.ndarray:
         r = self._vec(rFiner, self.levels[ii - 2]["numDOFs"])
         out = np.zeros(self.levels[ii - 1]["numDOFs"])
@@ -228,7 +245,7 @@ class VoxelSolver:
         x = np.zeros_like(bv) if x0 is None else self._vec(x0, self.numDOFs).copy()
         hist = np.zeros(maxIT) if history else None
         o = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=int(x0 is not None),
-                        precision=L.SGLD_PREC_MIXED if precision == "mixed" else L.SGLD_PREC_FP64,
+                        precision=_precision(precision),
                         inner_its=inner_its, history=hist.ctypes.data if history else None)
         info = L.SolveInfo()
         self._check(self.lib.sgld_pcg(self.ctx, _p(bv), _p(x), C.byref(o), C.byref(info)))
@@ -240,14 +257,14 @@ class VoxelSolver:
     def pcg_device(self, b_ptr: int, x_ptr: int, tol: float, maxIT: int, use_x0: bool = False,
                    precision: str = "fp64", inner_its: int = 0, profile: bool = False) -> dict:
         o = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=int(use_x0),
-                        precision=L.SGLD_PREC_MIXED if precision == "mixed" else L.SGLD_PREC_FP64,
+                        precision=_precision(precision),
                         inner_its=inner_its, history=None, profile=int(profile))
         info = L.SolveInfo()
         self._check(self.lib.sgld_pcg_device(self.ctx, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(o),
                                              C.byref(info)))
         return _info_dict(info)
 
-    OPS = {"kbyu64": 0, "kbyu32": 1, "vcycle64": 2, "vcycle32": 3, "assemble": 4}
+    OPS = {"kbyu64": 0, "kbyu32": 1, "vcycle64": 2, "vcycle32": 3, "assemble": 4, "kbyu_df": 5}
 
     def time_op(self, op: str, reps: int = 10) -> float:
         """Mean device milliseconds of one internal operator (CUDA events)."""
@@ -326,7 +343,7 @@ class VoxelSolver:
         """The whole SIMP loop on the device.  Returns (xPhys, history list)."""
         Fv = self._vec(F, self.numDOFs)
         so = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=1,
-                         precision=L.SGLD_PREC_MIXED if precision == "mixed" else L.SGLD_PREC_FP64,
+                         precision=_precision(precision),
                          inner_its=inner_its, history=None, profile=0)
         o = L.TopOptOpts(volfrac=volfrac, rmin=rMin, move=move, n_loop=nLoop, min_change=minChange,
                          max_sharpness=maxSharpness, penalty=penalty, E0=E0, Emin=Emin, solve=so)

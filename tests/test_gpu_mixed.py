@@ -58,3 +58,35 @@ def test_mixed_inner_its_change(graded):
     for k in (4, 16):
         U, info = s.pcg(m.F, tol=1e-6, maxIT=500, precision="mixed", inner_its=k)
         assert info["converged"] and info["inner_its"] == k * info["its"]
+
+
+def test_double_float_kbyu_accuracy(graded):
+    """The double-float K*u (outer operator of "mixed_df") agrees with the FP64
+    oracle to 1e-12 of max|K u| on a random field, and to 1e-12 of the
+    unsigned sum |K||u| on a smooth field where the stencil cancels."""
+    m, s, _ = graded
+    rng = np.random.default_rng(11)
+    l1 = m.levels[0]
+    u = rng.standard_normal(l1.numDOFs)
+    y_ref = G.kbyu(m, u)
+    y = s.kbyu_double_float(u)
+    assert np.abs(y - y_ref).max() <= 1e-12 * np.abs(y_ref).max()
+    ramp = np.repeat(np.linspace(0.0, 1.0, l1.numNodes), 3) ** 2
+    y_ref = G.kbyu(m, ramp)
+    # bound of sum_j |K_ij| |u_j|: 8 elements per node, largest Ke row sum, E <= 1
+    scale = 8.0 * np.abs(m.Ke).sum(axis=1).max() * np.abs(ramp).max()
+    assert np.abs(s.kbyu_double_float(ramp) - y_ref).max() <= 1e-12 * scale
+
+
+def test_mixed_df_converges_like_mixed(graded):
+    m, s, U_ref = graded
+    U, info = s.pcg(m.F, tol=1e-6, maxIT=500, precision="mixed_df")
+    _, imx = s.pcg(m.F, tol=1e-6, maxIT=500, precision="mixed")
+    assert info["converged"] and info["true_relres"] < 1.05e-6
+    assert abs(info["its"] - imx["its"]) <= 1
+    _, c = s.TopOpti_ComputeUnitCompliance(U)
+    c_ref = G.compliance(m, U_ref)
+    assert abs(c - c_ref) / abs(c_ref) <= 1e-6
+    U9, info9 = s.pcg(m.F, tol=1e-9, maxIT=500, precision="mixed_df")
+    assert info9["converged"] and info9["true_relres"] < 2e-9
+    assert np.linalg.norm(U9 - U_ref) / np.linalg.norm(U_ref) <= 1e-5

@@ -43,9 +43,9 @@ extern "C" {
 #define SGLD_PREC_FP64 0     /* reference form: FP64 PCG, FP64 additive V-cycle            */
 #define SGLD_PREC_MIXED 1    /* FP64 flexible PCG outer, preconditioner = FP32 inner PCG with
                                 the FP32 V-cycle; same tolerance on the FP64 true residual  */
-#define SGLD_PREC_MIXED_DF 2 /* as SGLD_PREC_MIXED, with the outer K*p in double-float
-                                arithmetic (FP32 pairs, ~2^-48 relative); FP64 vectors,
-                                dot products and exit residual                             */
+#define SGLD_PREC_MIXED_DF 2 /* as SGLD_PREC_MIXED, with every outer K*u (K*p, warm-start
+                                and exit residuals) in double-float arithmetic (FP32
+                                pairs, ~2^-48 relative); FP64 vectors and dot products    */
 
 typedef struct sgld_ctx sgld_ctx;
 
@@ -74,7 +74,8 @@ typedef struct sgld_solve_info {
     int iterations;        /* outer iterations, as the reference's `its` */
     int converged;         /* 1 if relres < tol */
     double relres;         /* recursive residual norm / ||b|| at exit */
-    double true_relres;    /* ||b - K x|| / ||b|| recomputed in FP64 at exit */
+    double true_relres;    /* ||b - K x|| / ||b|| recomputed at exit (FP64 vectors; K x by the
+                              precision mode's outer operator) */
     int inner_iterations;  /* SGLD_PREC_MIXED(_DF): total FP32 inner iterations */
     double seconds;        /* device time of the solve (CUDA events) */
     double kbyu_seconds;   /* profile: summed device time of the outer K*u launches */

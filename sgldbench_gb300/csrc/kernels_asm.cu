@@ -501,26 +501,47 @@ int coarse_factor_invert(Ctx &c) {
 }
 
 // ---- coarse apply: x_L[free] = A^-1 r_L[free] = M' (M r) -------------------------
-// y = M r (M lower triangular): rows in threads, columns split into CSPLIT chunks
+// y = M r (M lower triangular, column-major).  A CTA covers 32 rows and one of
+// CSPLIT column chunks; each warp takes 32-column blocks of the chunk, lane l
+// holding row i0 + l: its 32 loads of a block (one coalesced row segment per
+// column) are independent and in flight together.  The 8 warps' sums meet in
+// shared memory and the chunk's partial goes to part[chunk * n + i].
+constexpr int CL_WARPS = 8;
+
 template <typename T>
-__global__ void k_coarse_lower(const T *__restrict__ M, const int *__restrict__ rows, const T *__restrict__ r, int n,
-                               double *__restrict__ part) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int chunk = (n + CSPLIT - 1) / CSPLIT;
-    const int j0 = blockIdx.y * chunk, j1 = min(min(n, j0 + chunk), i + 1);
-    if (i >= n) return;
-    // four independent accumulators: the chain of one would be latency-bound
-    T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
-    const T *col = M + i;
-    int j = j0;
-    for (; j + 3 < j1; j += 4) {
-        a0 += col[(int64_t)n * j] * r[rows[j]];
-        a1 += col[(int64_t)n * (j + 1)] * r[rows[j + 1]];
-        a2 += col[(int64_t)n * (j + 2)] * r[rows[j + 2]];
-        a3 += col[(int64_t)n * (j + 3)] * r[rows[j + 3]];
+__global__ void __launch_bounds__(32 * CL_WARPS) k_coarse_lower(const T *__restrict__ M, const int *__restrict__ rows,
+                                                               const T *__restrict__ r, int n,
+                                                               double *__restrict__ part) {
+    __shared__ T red[CL_WARPS][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i0 = blockIdx.x * 32, i = i0 + lane;
+    const int chunk = ((n + CSPLIT - 1) / CSPLIT + 31) & ~31;
+    const int j0 = blockIdx.y * chunk, j1 = min(min(n, j0 + chunk), i0 + 32);
+    T acc = T(0);
+    for (int jb = j0 + 32 * w; jb < j1; jb += 32 * CL_WARPS) {
+        const int jl = jb + lane;
+        const T rl = (jl < n) ? r[rows[jl]] : T(0);
+        const int ii = min(i, n - 1);
+        T a0 = T(0), a1 = T(0);
+#pragma unroll
+        for (int q = 0; q < 32; q += 2) {
+            const int ja = jb + q, jc = jb + q + 1;
+            const T ma = (ja < n) ? M[(int64_t)ja * n + ii] : T(0);
+            const T mc = (jc < n) ? M[(int64_t)jc * n + ii] : T(0);
+            const T ra = __shfl_sync(0xffffffffu, rl, q), rc = __shfl_sync(0xffffffffu, rl, q + 1);
+            a0 += (ja <= i) ? ma * ra : T(0);
+            a1 += (jc <= i) ? mc * rc : T(0);
+        }
+        acc += a0 + a1;
     }
-    for (; j < j1; ++j) a0 += col[(int64_t)n * j] * r[rows[j]];
-    part[(int64_t)blockIdx.y * n + i] = (double)((a0 + a1) + (a2 + a3));
+    red[w][lane] = acc;
+    __syncthreads();
+    if (w == 0 && i < n) {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < CL_WARPS; ++k) s += (double)red[k][lane];
+        part[(int64_t)blockIdx.y * n + i] = s;
+    }
 }
 
 template <typename T>
@@ -532,7 +553,8 @@ __global__ void k_coarse_sum(const double *__restrict__ part, int n, T *__restri
     y[i] = (T)s;
 }
 
-// x_j = sum_{i >= j} M[i,j] y_i: one warp per column (coalesced column reads)
+// x_j = sum_{i >= j} M[i,j] y_i: one warp per column (coalesced column reads),
+// four independent accumulators so that four loads per lane are in flight
 template <typename T>
 __global__ void k_coarse_upper(const T *__restrict__ M, const int *__restrict__ rows, const T *__restrict__ y, int n,
                                T *__restrict__ x) {
@@ -540,8 +562,16 @@ __global__ void k_coarse_upper(const T *__restrict__ M, const int *__restrict__ 
     const int lane = threadIdx.x & 31;
     if (j >= n) return;
     const T *col = M + (int64_t)n * j;
-    T acc = T(0);
-    for (int i = j + lane; i < n; i += 32) acc += col[i] * y[i];
+    T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+    int i = j + lane;
+    for (; i + 96 < n; i += 128) {
+        a0 += col[i] * y[i];
+        a1 += col[i + 32] * y[i + 32];
+        a2 += col[i + 64] * y[i + 64];
+        a3 += col[i + 96] * y[i + 96];
+    }
+    for (; i < n; i += 32) a0 += col[i] * y[i];
+    T acc = (a0 + a1) + (a2 + a3);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) x[rows[j]] = acc;
@@ -552,9 +582,9 @@ static void coarse_apply(const Ctx &c, const T *M, const T *rc, T *xc, T *ybuf, 
     const Level &lc = c.lv[c.L - 1];
     cudaMemsetAsync(xc, 0, sizeof(T) * 3 * lc.nnode, s);
     if (c.ncf == 0) return;
-    dim3 g((c.ncf + 127) / 128, CSPLIT);
+    dim3 g((c.ncf + 31) / 32, CSPLIT);
     ++g_launches;
-    k_coarse_lower<T><<<g, 128, 0, s>>>(M, c.d_cfree, rc, c.ncf, c.d_cpart);
+    k_coarse_lower<T><<<g, 32 * CL_WARPS, 0, s>>>(M, c.d_cfree, rc, c.ncf, c.d_cpart);
     ++g_launches;
     k_coarse_sum<T><<<(c.ncf + 127) / 128, 128, 0, s>>>(c.d_cpart, c.ncf, ybuf);
     ++g_launches;

@@ -54,11 +54,26 @@ void launch_icg_scalar(int op, double *sc, const double *part, int nb, cudaStrea
     k_icg_scalar<<<1, MB, 0, s>>>(op, sc, part, nb);
 }
 
+// The FP32 vectors are separate allocations (256-byte aligned), so the
+// streaming kernels below move them as float4 and finish the n % 4 tail
+// element-wise.
+__device__ __forceinline__ float4 fma4(float a, float4 x, float4 y) {
+    return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
+}
+
 // e += alpha d; s -= alpha t
 __global__ void k_icg_update(float *__restrict__ e, float *__restrict__ s, const float *__restrict__ d,
                              const float *__restrict__ t, int64_t n, const double *__restrict__ sc) {
     const float a = (float)sc[IS_ALPHA];
-    for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n; i += (int64_t)gridDim.x * MB) {
+    const int64_t n4 = n >> 2, stride = (int64_t)gridDim.x * MB;
+    float4 *e4 = reinterpret_cast<float4 *>(e), *s4 = reinterpret_cast<float4 *>(s);
+    const float4 *d4 = reinterpret_cast<const float4 *>(d), *t4 = reinterpret_cast<const float4 *>(t);
+    for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n4; i += stride) {
+        e4[i] = fma4(a, d4[i], e4[i]);
+        s4[i] = fma4(-a, t4[i], s4[i]);
+    }
+    const int64_t i = 4 * n4 + blockIdx.x * (int64_t)MB + threadIdx.x;
+    if (i < n) {
         e[i] = fmaf(a, d[i], e[i]);
         s[i] = fmaf(-a, t[i], s[i]);
     }
@@ -74,8 +89,12 @@ void launch_icg_update(float *e, float *s, const float *d, const float *t, int64
 __global__ void k_icg_dupdate(float *__restrict__ d, const float *__restrict__ w, int64_t n,
                               const double *__restrict__ sc) {
     const float b = (float)sc[IS_BETA];
-    for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n; i += (int64_t)gridDim.x * MB)
-        d[i] = fmaf(b, d[i], w[i]);
+    const int64_t n4 = n >> 2, stride = (int64_t)gridDim.x * MB;
+    float4 *d4 = reinterpret_cast<float4 *>(d);
+    const float4 *w4 = reinterpret_cast<const float4 *>(w);
+    for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n4; i += stride) d4[i] = fma4(b, d4[i], w4[i]);
+    const int64_t i = 4 * n4 + blockIdx.x * (int64_t)MB + threadIdx.x;
+    if (i < n) d[i] = fmaf(b, d[i], w[i]);
 }
 
 void launch_icg_dupdate(float *d, const float *w, int64_t n, const double *sc, cudaStream_t st) {

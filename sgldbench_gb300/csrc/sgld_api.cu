@@ -1143,8 +1143,8 @@ int pcg_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
 // residual recurrence, dot products and stopping test stay in FP64, so the
 // outer solve reaches the same tolerance on the true residual.  The outer K*p
 // is the native FP64 operator (SGLD_PREC_MIXED) or the double-float one
-// (SGLD_PREC_MIXED_DF, ~2^-48 relative, FP32 issue rate); the true residual
-// at exit always uses the FP64 operator.
+// (SGLD_PREC_MIXED_DF, ~2^-48 relative, FP32 issue rate), and so are the
+// warm-start residual and the true residual at exit.
 int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
     Ctx &c = ctx->c;
     const Level &l0 = c.lv[0];
@@ -1163,7 +1163,10 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
     launch_dot(c.d_b, c.d_b, nv, c.d_part, nbv, c.stream);
     launch_pcg_scalar(0, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
     if (o->use_x0) {
-        launch_kbyu_f64(l0, c.E, c.d_x, c.d_q, nullptr, nullptr, c.stream);
+        if (dfk)
+            launch_kbyu_df(l0, c.E, c.d_x, c.d_q, nullptr, nullptr, c.stream);
+        else
+            launch_kbyu_f64(l0, c.E, c.d_x, c.d_q, nullptr, nullptr, c.stream);
         launch_residual(c.d_r, c.d_b, c.d_q, nv, c.stream);
     } else {
         CK(cudaMemcpyAsync(c.d_r, c.d_b, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c.stream));
@@ -1236,7 +1239,10 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    launch_kbyu_f64(l0, c.E, c.d_x, c.d_q, nullptr, nullptr, c.stream);
+    if (dfk)
+        launch_kbyu_df(l0, c.E, c.d_x, c.d_q, nullptr, nullptr, c.stream);
+    else
+        launch_kbyu_f64(l0, c.E, c.d_x, c.d_q, nullptr, nullptr, c.stream);
     launch_residual(c.d_tmp, c.d_b, c.d_q, nv, c.stream);
     launch_dot(c.d_tmp, c.d_tmp, nv, c.d_part, nbv, c.stream);
     launch_finalize_sum(c.d_part, nbv, c.d_scal + 17, c.stream);

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "sgld_internal.cuh"
+#include "df_arith.cuh"
 
 namespace sgld {
 
@@ -275,155 +276,199 @@ void launch_coarse_dense(const Level &lc, int ncf, const int *rows_and_pos, doub
 // ---- blocked band Cholesky, NB x NB tiles, column-major n x n ------------------
 constexpr int NB = 32;
 
-// One block column of the band Cholesky.  CTA ib (one warp) handles the
-// 32-row tile kb + ib: every CTA first factors the diagonal tile in shared
-// memory (32 x 32, lane = row), CTA 0 writes it back, and CTA ib > 0 then
-// solves its tile rows against it (X = A_ib L_kk^-T, lane = row).  The FP64
-// work of a panel is spread over the tiles instead of one SM.
-__global__ void __launch_bounds__(32) k_chol_panel(double *A, int n, int k0, int *info) {
+// One block column of the band Cholesky (4 warps per CTA).  FP64 issue is
+// scarce on GB300 (a warp-wide DFMA occupies its SM sub-partition's FP64 pipe
+// for many cycles), so the work of a panel is spread over sub-partitions and
+// SMs:
+//   * every CTA factors the 32 x 32 diagonal tile in shared memory (row = lane,
+//     the rank-1 update of step j split over the 4 warps by column mod 4; the
+//     pivot 1/sqrt(d) is formed by every thread, so it needs no broadcast);
+//   * CTA 0 writes the factored tile back;
+//   * CTA b > 0 solves CP_RS rows of the band below against it (X = A L^-T):
+//     16 lanes per row, two columns per lane in registers, x_q broadcast by a
+//     16-wide shuffle.
+constexpr int CP_THREADS = 128;
+constexpr int CP_RS = 8;
+
+__global__ void __launch_bounds__(CP_THREADS) k_chol_panel(double *A, int n, int k0, int rend, int *info) {
     __shared__ double T[NB][NB + 1];
-    __shared__ double rd[NB];
-    const int lane = threadIdx.x;
+    __shared__ double rd[NB], ld[NB];
+    const int t = threadIdx.x, r = t & 31, w = t >> 5;
     const int m = min(NB, n - k0);
-    for (int j = 0; j < NB; ++j)
-        T[lane][j] = (lane < m && j < m) ? A[(int64_t)(k0 + lane) + (int64_t)n * (k0 + j)] : (lane == j ? 1.0 : 0.0);
-    __syncwarp();
-    for (int j = 0; j < m; ++j) {
-        if (lane == j) {
-            double d = T[j][j];
-            if (!(d > 0.0)) {
-                if (info && blockIdx.x == 0) atomicExch(info, k0 + j + 1);
-                d = 1.0;
-            }
-            d = sqrt(d);
-            T[j][j] = d;
-            rd[j] = 1.0 / d;
+    for (int idx = t; idx < NB * NB; idx += CP_THREADS) {
+        const int rr = idx & 31, cc = idx >> 5;
+        T[rr][cc] = (rr < m && cc < m) ? A[(int64_t)(k0 + rr) + (int64_t)n * (k0 + cc)] : (rr == cc ? 1.0 : 0.0);
+    }
+    __syncthreads();
+    for (int j = 0; j < NB; ++j) {
+        // T[j][j] is read here and never written in the loop (the factor's
+        // diagonal goes to ld[]), so no thread can overwrite it early
+        double d = T[j][j];
+        const bool bad = !(d > 0.0);
+        if (bad) d = 1.0;
+        const double y = rsqrt(d);
+        if (w == 0 && r > j) T[r][j] *= y;
+        if (t == 0) {
+            rd[j] = y;
+            ld[j] = d * y;
+            if (bad && blockIdx.x == 0 && info) atomicExch(info, k0 + j + 1);
         }
-        __syncwarp();
-        if (lane > j) T[lane][j] *= rd[j];
-        __syncwarp();
-        if (lane > j)
-            for (int q = j + 1; q <= lane; ++q) T[lane][q] -= T[lane][j] * T[q][j];
-        __syncwarp();
+        __syncthreads();
+        if (r > j) {
+            const double lrj = T[r][j];
+            for (int q = j + 1 + ((w - j - 1) & 3); q <= r; q += 4) T[r][q] -= lrj * T[q][j];
+        }
+        __syncthreads();
     }
     if (blockIdx.x == 0) {
-        if (lane < m)
-            for (int j = 0; j < m; ++j) A[(int64_t)(k0 + lane) + (int64_t)n * (k0 + j)] = (j <= lane) ? T[lane][j] : 0.0;
+        for (int idx = t; idx < NB * NB; idx += CP_THREADS) {
+            const int rr = idx & 31, cc = idx >> 5;
+            if (rr < m && cc < m)
+                A[(int64_t)(k0 + rr) + (int64_t)n * (k0 + cc)] = rr > cc ? T[rr][cc] : (rr == cc ? ld[rr] : 0.0);
+        }
         return;
     }
-    const int row = k0 + NB * blockIdx.x + lane;
-    if (row >= n) return;
-    double x[NB];
-#pragma unroll
-    for (int j = 0; j < NB; ++j) x[j] = (j < m) ? A[(int64_t)row + (int64_t)n * (k0 + j)] : 0.0;
-#pragma unroll
-    for (int j = 0; j < NB; ++j) {
-        double v = x[j];
-#pragma unroll
-        for (int q = 0; q < j; ++q) v -= x[q] * T[j][q];
-        x[j] = v * rd[j];
+    const int rr = t >> 4, g = t & 15;
+    const int row = k0 + NB + (blockIdx.x - 1) * CP_RS + rr;
+    const bool live = row < rend;
+    double a0 = 0.0, a1 = 0.0;
+    if (live) {
+        if (g < m) a0 = A[(int64_t)row + (int64_t)n * (k0 + g)];
+        if (g + 16 < m) a1 = A[(int64_t)row + (int64_t)n * (k0 + g + 16)];
     }
-#pragma unroll
-    for (int j = 0; j < NB; ++j)
-        if (j < m) A[(int64_t)row + (int64_t)n * (k0 + j)] = x[j];
+#pragma unroll 4
+    for (int q = 0; q < NB; ++q) {
+        const double xl = (q < 16 ? a0 : a1) * rd[q];
+        const double xq = __shfl_sync(0xffffffffu, xl, q & 15, 16);
+        if (g == (q & 15)) {
+            if (q < 16)
+                a0 = xq;
+            else
+                a1 = xq;
+        }
+        if (g > q) a0 -= xq * T[g][q];
+        if (g + 16 > q) a1 -= xq * T[g + 16][q];
+    }
+    if (live) {
+        if (g < m) A[(int64_t)row + (int64_t)n * (k0 + g)] = a0;
+        if (g + 16 < m) A[(int64_t)row + (int64_t)n * (k0 + g + 16)] = a1;
+    }
 }
 
-// trailing update A[i,j] -= A[i,k] A[j,k]' for k < j <= i <= kend (tile pairs)
-__global__ void k_syrk_update(double *A, int n, int k0, int jb0, int nbt) {
-    // map blockIdx.x -> (ii, jj) with 0 <= jj <= ii < nbt
+// trailing update A[i,j] -= sum_k A[i,k] A[j,k] over the panel's columns k for
+// the band tiles below it: blockIdx.x = tile pair (ii >= jj), blockIdx.y =
+// SY_RS-row slice of tile ii (slices spread one pair's FP64 work over SMs)
+constexpr int SY_RS = 8;
+
+__global__ void __launch_bounds__(256) k_syrk_update(double *A, int n, int k0, int jb0, int nbt) {
     int p = blockIdx.x, ii = 0;
     while (p > ii) {
         p -= ii + 1;
         ++ii;
     }
     const int jj = p;
-    const int i0 = (jb0 + ii) * NB, j0 = (jb0 + jj) * NB;
-    __shared__ double Ai[NB][NB + 1], Aj[NB][NB + 1];
-    const int t = threadIdx.x;   // 256 threads
+    const int i0 = (jb0 + ii) * NB + blockIdx.y * SY_RS, j0 = (jb0 + jj) * NB;
+    __shared__ double Ai[SY_RS][NB + 1], Aj[NB][NB + 1];
+    const int t = threadIdx.x;
     const int m = min(NB, n - k0);
     for (int idx = t; idx < NB * NB; idx += 256) {
-        const int r = idx % NB, c = idx / NB;
-        Ai[r][c] = (i0 + r < n && c < m) ? A[(int64_t)(i0 + r) + (int64_t)n * (k0 + c)] : 0.0;
+        const int r = idx & 31, c = idx >> 5;
         Aj[r][c] = (j0 + r < n && c < m) ? A[(int64_t)(j0 + r) + (int64_t)n * (k0 + c)] : 0.0;
     }
-    __syncthreads();
-    for (int idx = t; idx < NB * NB; idx += 256) {
-        const int r = idx % NB, c = idx / NB;
-        if (i0 + r >= n || j0 + c >= n) continue;
-        if (ii == jj && c > r) continue;
-        double v = 0.0;
-#pragma unroll 8
-        for (int q = 0; q < NB; ++q) v += Ai[r][q] * Aj[c][q];
-        A[(int64_t)(i0 + r) + (int64_t)n * (j0 + c)] -= v;
+    {
+        const int r = t & (SY_RS - 1), c = t / SY_RS;
+        Ai[r][c] = (i0 + r < n && c < m) ? A[(int64_t)(i0 + r) + (int64_t)n * (k0 + c)] : 0.0;
     }
+    __syncthreads();
+    const int r = t & (SY_RS - 1), c = t / SY_RS;
+    const int gi = i0 + r, gj = j0 + c;
+    if (gi >= n || gj >= n || gj > gi) return;
+    double v0 = 0.0, v1 = 0.0;
+#pragma unroll
+    for (int q = 0; q < NB; q += 2) {
+        v0 += Ai[r][q] * Aj[c][q];
+        v1 += Ai[r][q + 1] * Aj[c][q + 1];
+    }
+    A[(int64_t)gi + (int64_t)n * gj] -= v0 + v1;
 }
 
-__global__ void k_to_f32(const double *a, float *b, int64_t n) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (float)a[i];
-}
-
-// Band of L stored by diagonals: LB[d*n + i] = L[i, i-b+d], d = 0..b (0 outside
-// the matrix), so that lanes holding consecutive rows read consecutive words.
-__global__ void k_band_rows(const double *__restrict__ L, int n, int b, double *__restrict__ LB) {
+// Band of L stored by diagonals in double-float form: LBh/LBl[d*n + i] =
+// L[i, i-b+d], d = 0..b (0 outside the matrix), so that lanes holding
+// consecutive rows read consecutive words; rdh/rdl[i] = 1 / L[i,i].
+__global__ void k_band_rows(const double *__restrict__ L, int n, int b, float *__restrict__ LBh,
+                            float *__restrict__ LBl, float *__restrict__ rdh, float *__restrict__ rdl) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < n) {
+        const df r = df_from(1.0 / L[t + (int64_t)n * t]);
+        rdh[t] = r.hi;
+        rdl[t] = r.lo;
+    }
     if (t >= (int64_t)n * (b + 1)) return;
     const int d = (int)(t / n), i = (int)(t % n);
     const int k = i - b + d;
-    LB[t] = (k >= 0) ? L[(int64_t)i + (int64_t)n * k] : 0.0;
+    const df v = df_from(k >= 0 ? L[(int64_t)i + (int64_t)n * k] : 0.0);
+    LBh[t] = v.hi;
+    LBl[t] = v.lo;
 }
 
-// M = L^-1: warp w of the CTA owns column c and walks down it 32 rows at a
-// time, lane l holding row i = i0 + l of the block:
+// M = L^-1 in double-float arithmetic (GB300's FP64 issue rate would bound
+// the n^2 b / 2 multiply-adds).  Warp w of the CTA owns column c and walks
+// down it 32 rows at a time, lane l holding row i = i0 + l of the block:
 //   1. s_l = sum_{k=max(c,i-b)}^{i0-1} L[i,k] M[k,c]   (rows above the block,
 //      kept in a shared ring of R >= b+1 values), all lanes in parallel;
 //   2. within the block, rows finish in order: lane t forms
 //      M[i0+t,c] = (delta - s_t) / L[i0+t,i0+t], broadcasts it, and the
 //      lanes below subtract its contribution.
-// LB holds the band of L by diagonals (see k_band_rows), rdiag = 1/diag(L).
-__global__ void k_trinv_cols(const double *__restrict__ LB, const double *__restrict__ rdiag, int n, int b, int R,
-                             double *__restrict__ M) {
-    extern __shared__ double ringmem[];
+// Writes M in FP64 (hi + lo) and in FP32 (the FP32 V-cycle's copy).
+__global__ void k_trinv_cols(const float *__restrict__ LBh, const float *__restrict__ LBl,
+                             const float *__restrict__ rdh, const float *__restrict__ rdl, int n, int b, int R,
+                             double *__restrict__ M, float *__restrict__ M32) {
+    extern __shared__ float2 ringmem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int c = blockIdx.x * (blockDim.x >> 5) + w;
     if (c >= n) return;
-    double *ring = ringmem + (int64_t)w * R;
+    float2 *ring = ringmem + (int64_t)w * R;
     for (int i0 = c; i0 < n; i0 += 32) {
         const int i = i0 + lane;
         const bool valid = i < n;
-        const double *col = LB + (valid ? i : i0);   // col[d*n] = L[i, i-b+d]
-        double s0 = 0.0, s1 = 0.0;
+        const int64_t base = valid ? i : i0;   // LB*[d*n + base] = L[i, i-b+d]
+        df s0 = {0.f, 0.f}, s1 = {0.f, 0.f};
         if (valid) {
             // k = i - b + t runs over [max(c, i-b), i0)
             const int t0 = max(0, c - (i - b));
             const int t1 = b - lane;   // k < i0
             int t = t0;
             for (; t + 1 < t1; t += 2) {
-                s0 += col[(int64_t)t * n] * ring[(i - b + t) & (R - 1)];
-                s1 += col[(int64_t)(t + 1) * n] * ring[(i - b + t + 1) & (R - 1)];
+                const float2 m0 = ring[(i - b + t) & (R - 1)], m1 = ring[(i - b + t + 1) & (R - 1)];
+                s0 = df_add(s0, df_mul({LBh[(int64_t)t * n + base], LBl[(int64_t)t * n + base]}, {m0.x, m0.y}));
+                s1 = df_add(s1, df_mul({LBh[(int64_t)(t + 1) * n + base], LBl[(int64_t)(t + 1) * n + base]},
+                                       {m1.x, m1.y}));
             }
-            if (t < t1) s0 += col[(int64_t)t * n] * ring[(i - b + t) & (R - 1)];
+            if (t < t1) {
+                const float2 m0 = ring[(i - b + t) & (R - 1)];
+                s0 = df_add(s0, df_mul({LBh[(int64_t)t * n + base], LBl[(int64_t)t * n + base]}, {m0.x, m0.y}));
+            }
         }
-        double s = s0 + s1;
-        double v = 0.0;
+        df s = df_add(s0, s1);
+        const df rdi = valid ? df{rdh[i], rdl[i]} : df{0.f, 0.f};
+        df v = {0.f, 0.f};
 #pragma unroll 4
         for (int t = 0; t < 32; ++t) {
             if (i0 + t >= n) break;
-            if (lane == t) v = ((i == c ? 1.0 : 0.0) - s) * rdiag[i];
-            const double vt = __shfl_sync(0xffffffffu, v, t);
-            if (lane > t && valid && lane - t <= b) s += col[(int64_t)(b - lane + t) * n] * vt;   // L[i, i0+t]
+            if (lane == t) v = df_mul(df_sub({i == c ? 1.f : 0.f, 0.f}, s), rdi);
+            const df vt = df_shfl(v, t);
+            if (lane > t && valid && lane - t <= b) {
+                const int64_t o = (int64_t)(b - lane + t) * n + base;   // L[i, i0+t]
+                s = df_add(s, df_mul({LBh[o], LBl[o]}, vt));
+            }
         }
         if (valid) {
-            ring[i & (R - 1)] = v;
-            M[(int64_t)i + (int64_t)n * c] = v;
+            ring[i & (R - 1)] = make_float2(v.hi, v.lo);
+            M[(int64_t)i + (int64_t)n * c] = df_to(v);
+            M32[(int64_t)i + (int64_t)n * c] = v.hi;
         }
         __syncwarp();
     }
-}
-
-__global__ void k_recip_diag(const double *__restrict__ L, int n, double *__restrict__ rd) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) rd[i] = 1.0 / L[(int64_t)i + (int64_t)n * i];
 }
 
 // Enqueues the whole factorization (band Cholesky, L^-1, FP32 copy); no host
@@ -438,27 +483,29 @@ static void factor_enqueue(Ctx &c, int *d_info) {
         const int k0 = kb * NB;
         const int kend = min(nblk - 1, kb + bw);
         const int nbelow = kend - kb;
+        const int rend = min(n, (kend + 1) * NB);
+        const int ntrsm = rend > k0 + NB ? (rend - k0 - NB + CP_RS - 1) / CP_RS : 0;
         ++g_launches;
-        k_chol_panel<<<1 + nbelow, NB, 0, c.stream>>>(A, n, k0, d_info);
+        k_chol_panel<<<1 + ntrsm, CP_THREADS, 0, c.stream>>>(A, n, k0, rend, d_info);
         if (nbelow > 0) {
             const int npairs = nbelow * (nbelow + 1) / 2;
             ++g_launches;
-            k_syrk_update<<<npairs, 256, 0, c.stream>>>(A, n, k0, kb + 1, nbelow);
+            k_syrk_update<<<dim3(npairs, NB / SY_RS), 256, 0, c.stream>>>(A, n, k0, kb + 1, nbelow);
         }
     }
     const int b = c.cband;
-    double *rdiag = c.d_LB + (int64_t)n * (b + 1);
+    // d_LB (n (b+1) + n doubles) holds the double-float band and 1/diag:
+    // 2 n (b+1) + 2 n floats
+    float *LBh = reinterpret_cast<float *>(c.d_LB), *LBl = LBh + (int64_t)n * (b + 1);
+    float *rdh = LBl + (int64_t)n * (b + 1), *rdl = rdh + n;
     ++g_launches;
-    k_band_rows<<<(unsigned)(((int64_t)n * (b + 1) + 255) / 256), 256, 0, c.stream>>>(A, n, b, c.d_LB);
-    ++g_launches;
-    k_recip_diag<<<(n + 255) / 256, 256, 0, c.stream>>>(A, n, rdiag);
+    k_band_rows<<<(unsigned)(((int64_t)n * (b + 1) + 255) / 256), 256, 0, c.stream>>>(A, n, b, LBh, LBl, rdh,
+                                                                                      rdl);
     cudaMemsetAsync(c.d_Ainv, 0, sizeof(double) * (size_t)n * n, c.stream);
+    cudaMemsetAsync(c.d_Ainv32, 0, sizeof(float) * (size_t)n * n, c.stream);
     ++g_launches;
     k_trinv_cols<<<(n + c.trinv_warps - 1) / c.trinv_warps, 32 * c.trinv_warps, c.trinv_smem, c.stream>>>(
-        c.d_LB, rdiag, n, b, c.trinv_ring, c.d_Ainv);
-    const int64_t nn = (int64_t)n * n;
-    ++g_launches;
-    k_to_f32<<<(unsigned)((nn + 255) / 256), 256, 0, c.stream>>>(c.d_Ainv, c.d_Ainv32, nn);
+        LBh, LBl, rdh, rdl, n, b, c.trinv_ring, c.d_Ainv, c.d_Ainv32);
 }
 
 // Cholesky of the dense coarsest matrix in d_Ac (lower, in place) and
@@ -472,8 +519,8 @@ int coarse_factor_invert(Ctx &c) {
         int R = 32;
         while (R < c.cband + 1) R <<= 1;
         int warps = 8;
-        while (warps > 1 && (size_t)warps * R * sizeof(double) > 200 * 1024) warps >>= 1;
-        const size_t smem = (size_t)warps * R * sizeof(double);
+        while (warps > 1 && (size_t)warps * R * sizeof(float2) > 200 * 1024) warps >>= 1;
+        const size_t smem = (size_t)warps * R * sizeof(float2);
         if (smem > 220 * 1024) return -2;
         cudaFuncSetAttribute(k_trinv_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         c.trinv_ring = R;

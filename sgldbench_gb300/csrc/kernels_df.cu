@@ -3,50 +3,17 @@
 //
 // GB300 issues FP64 at about 1/64 of its FP32 rate, and the FP64 K*u
 // (kernels_stencil.cu) is bound by that issue rate.  A double-float value
-// hi + lo carries 48 significant bits; sums use Knuth's TwoSum and products
-// the FMA-based TwoProd (Dekker 1971, with the FMA formulation of the
-// error-free product), ~11 FP32 operations per add and ~7 per multiply.  The
+// hi + lo carries 48 significant bits (df_arith.cuh: Knuth's TwoSum, the FMA
+// form of Dekker's product; ~11 FP32 operations per add, ~7 per multiply).  The
 // result is within a few units of 2^-48 of the FP64 operator (tests compare
 // to 1e-12), enough for the FP64 residual recurrence of the outer flexible
-// PCG, whose final true residual is still formed with the native FP64 K*u.
+// PCG and for its true residual at exit (relative tolerances >= 1e-12).
 // The data stay FP64 in HBM; values are split into (hi, lo) when a node
 // layer is staged and joined when a node's sum is stored.
 #include "sgld_internal.cuh"
+#include "df_arith.cuh"
 
 namespace sgld {
-
-struct df {
-    float hi, lo;
-};
-
-__device__ __forceinline__ df df_from(double v) {
-    const float h = __double2float_rn(v);
-    return {h, __double2float_rn(v - (double)h)};
-}
-__device__ __forceinline__ double df_to(df a) { return (double)a.hi + (double)a.lo; }
-
-// The error-free transforms must not be contracted or reassociated, so every
-// operation is an explicitly rounded intrinsic (nvcc never fuses those).
-__device__ __forceinline__ df quick_two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b);
-    return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ df df_add(df a, df b) {
-    const float s = __fadd_rn(a.hi, b.hi);
-    const float bb = __fsub_rn(s, a.hi);
-    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
-    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
-    return quick_two_sum(s, e);
-}
-__device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
-__device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
-__device__ __forceinline__ df df_mul(df a, df b) {
-    const float p = __fmul_rn(a.hi, b.hi);
-    float e = __fmaf_rn(a.hi, b.hi, -p);
-    e = __fmaf_rn(a.hi, b.lo, e);
-    e = __fmaf_rn(a.lo, b.hi, e);
-    return quick_two_sum(p, e);
-}
 
 __constant__ float c_khh[KH_NNZ], c_khl[KH_NNZ];
 

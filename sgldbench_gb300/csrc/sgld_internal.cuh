@@ -63,7 +63,8 @@ struct Ctx {
     double *d_Ac = nullptr;         // [ncf*ncf] dense matrix / Cholesky factor
     double *d_Ainv = nullptr;       // [ncf*ncf] inverse (symmetric)
     float *d_Ainv32 = nullptr;
-    double *d_LB = nullptr;         // [ncf*(cband+1) + ncf] band rows of the Cholesky factor, 1/diag
+    double *d_LB = nullptr;         // [ncf*(cband+1) + ncf] doubles holding the Cholesky band and
+                                    // 1/diag as float pairs (hi, lo arrays)
     double *d_cy = nullptr;         // [2*ncf] intermediate of the coarse apply
     // SIMP loop fields on the finest element grid (allocated on first use)
     double *t_x = nullptr, *t_xp = nullptr, *t_hs = nullptr, *t_ce = nullptr, *t_dcs = nullptr, *t_dvs = nullptr,

@@ -392,84 +392,160 @@ __global__ void __launch_bounds__(256) k_syrk_update(double *A, int n, int k0, i
     A[(int64_t)gi + (int64_t)n * gj] -= v0 + v1;
 }
 
-// Band of L stored by diagonals in double-float form: LBh/LBl[d*n + i] =
-// L[i, i-b+d], d = 0..b (0 outside the matrix), so that lanes holding
-// consecutive rows read consecutive words; rdh/rdl[i] = 1 / L[i,i].
-__global__ void k_band_rows(const double *__restrict__ L, int n, int b, float *__restrict__ LBh,
-                            float *__restrict__ LBl, float *__restrict__ rdh, float *__restrict__ rdl) {
+// Band of L by columns in double-float form: LB[k*(b+1) + j] = L[k+j, k]
+// (j = 0..b, zero past n), so that the rows of one column are contiguous;
+// rd[i] = 1 / L[i,i].
+__global__ void k_band_cols(const double *__restrict__ L, int n, int b, float2 *__restrict__ LB,
+                            float2 *__restrict__ rd) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t < n) {
         const df r = df_from(1.0 / L[t + (int64_t)n * t]);
-        rdh[t] = r.hi;
-        rdl[t] = r.lo;
+        rd[t] = make_float2(r.hi, r.lo);
     }
     if (t >= (int64_t)n * (b + 1)) return;
-    const int d = (int)(t / n), i = (int)(t % n);
-    const int k = i - b + d;
-    const df v = df_from(k >= 0 ? L[(int64_t)i + (int64_t)n * k] : 0.0);
-    LBh[t] = v.hi;
-    LBl[t] = v.lo;
+    const int k = (int)(t / (b + 1)), j = (int)(t % (b + 1));
+    const df v = df_from(k + j < n ? L[(int64_t)(k + j) + (int64_t)n * k] : 0.0);
+    LB[t] = make_float2(v.hi, v.lo);
 }
 
-// M = L^-1 in double-float arithmetic (GB300's FP64 issue rate would bound
-// the n^2 b / 2 multiply-adds).  Warp w of the CTA owns column c and walks
-// down it 32 rows at a time, lane l holding row i = i0 + l of the block:
-//   1. s_l = sum_{k=max(c,i-b)}^{i0-1} L[i,k] M[k,c]   (rows above the block,
-//      kept in a shared ring of R >= b+1 values), all lanes in parallel;
-//   2. within the block, rows finish in order: lane t forms
-//      M[i0+t,c] = (delta - s_t) / L[i0+t,i0+t], broadcasts it, and the
-//      lanes below subtract its contribution.
+__device__ __forceinline__ float2 band_at(const float2 *__restrict__ LB, int b, int i, int k) {
+    return LB[(int64_t)k * (b + 1) + (i - k)];   // requires 0 <= i - k <= b
+}
+
+// Inverses of the aligned 32 x 32 diagonal blocks of L (double-float),
+// column-major per block: D[kb*1024 + t*32 + r] = (L_kb^-1)[r, t].  One warp
+// per block, lane t forms column t by forward substitution (rows past n are
+// treated as identity rows).
+__global__ void __launch_bounds__(32) k_block_inverse(const float2 *__restrict__ LB, const float2 *__restrict__ rd,
+                                                      int n, int b, float2 *__restrict__ D) {
+    __shared__ float2 Ls[32][33];   // L_kb[r][k], k < r
+    __shared__ float2 X[32][33];    // X[r][t] = column t of the inverse
+    const int t = threadIdx.x, i0 = blockIdx.x * 32;
+    for (int r = 0; r < 32; ++r) {
+        const int i = i0 + r, k = i0 + t;
+        Ls[r][t] = (t < r && i < n && i - k <= b) ? band_at(LB, b, i, k) : make_float2(0.f, 0.f);
+    }
+    __syncwarp();
+    auto rdiag = [&](int r) -> df {
+        const int i = i0 + r;
+        return i < n ? df{rd[i].x, rd[i].y} : df{1.f, 0.f};
+    };
+    for (int r = 0; r < 32; ++r) {
+        df x = {0.f, 0.f};
+        if (r == t) {
+            x = rdiag(r);
+        } else if (r > t) {
+            df s = {0.f, 0.f};
+            for (int k = t; k < r; ++k) s = df_add(s, df_mul({Ls[r][k].x, Ls[r][k].y}, {X[k][t].x, X[k][t].y}));
+            x = df_mul(df_neg(s), rdiag(r));
+        }
+        X[r][t] = make_float2(x.hi, x.lo);
+    }
+    __syncwarp();
+    for (int tt = 0; tt < 32; ++tt) D[(int64_t)blockIdx.x * 1024 + tt * 32 + t] = X[t][tt];
+}
+
+// Compensated double-float dot-product accumulator (the Dot2 scheme of Ogita,
+// Rump and Oishi, 2005, with the low parts of the operands folded into the
+// error term): s + e carries the running sum.
+struct dacc {
+    float s = 0.f, e = 0.f;
+    __device__ __forceinline__ void add(float2 a, float2 b) {
+        const float p = __fmul_rn(a.x, b.x);
+        float pe = __fmaf_rn(a.x, b.x, -p);
+        pe = __fmaf_rn(a.x, b.y, pe);
+        pe = __fmaf_rn(a.y, b.x, pe);
+        const float t = __fadd_rn(s, p);
+        const float bb = __fsub_rn(t, s);
+        const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+        s = t;
+        e = __fadd_rn(e, __fadd_rn(err, pe));
+    }
+    __device__ __forceinline__ df value() const { return quick_two_sum(s, e); }
+};
+
+// M = L^-1 in double-float arithmetic, a CTA per group of TI_G columns
+// c0..c0+TI_G-1 walking down aligned 32-row blocks i0 (GB300's FP64 issue
+// rate would bound the n^2 b / 2 multiply-adds):
+//   1. S = L[i0:i0+32, i0-b:i0] * M[i0-b:i0, group]: the band tile is staged
+//      in shared memory by TI_KC-column chunks, the group's earlier rows of M
+//      sit in a shared ring of R >= b + 32 rows; thread (row r = lane, column
+//      pair of its warp) accumulates two entries with no masking (the band
+//      tile and the ring hold zeros where L or M vanish);
+//   2. M[i0:i0+32, group] = D_blk (E - S) with the block's precomputed
+//      inverse, E the identity columns of the group.
 // Writes M in FP64 (hi + lo) and in FP32 (the FP32 V-cycle's copy).
-__global__ void k_trinv_cols(const float *__restrict__ LBh, const float *__restrict__ LBl,
-                             const float *__restrict__ rdh, const float *__restrict__ rdl, int n, int b, int R,
-                             double *__restrict__ M, float *__restrict__ M32) {
-    extern __shared__ float2 ringmem[];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int c = blockIdx.x * (blockDim.x >> 5) + w;
-    if (c >= n) return;
-    float2 *ring = ringmem + (int64_t)w * R;
-    for (int i0 = c; i0 < n; i0 += 32) {
-        const int i = i0 + lane;
-        const bool valid = i < n;
-        const int64_t base = valid ? i : i0;   // LB*[d*n + base] = L[i, i-b+d]
-        df s0 = {0.f, 0.f}, s1 = {0.f, 0.f};
-        if (valid) {
-            // k = i - b + t runs over [max(c, i-b), i0)
-            const int t0 = max(0, c - (i - b));
-            const int t1 = b - lane;   // k < i0
-            int t = t0;
-            for (; t + 1 < t1; t += 2) {
-                const float2 m0 = ring[(i - b + t) & (R - 1)], m1 = ring[(i - b + t + 1) & (R - 1)];
-                s0 = df_add(s0, df_mul({LBh[(int64_t)t * n + base], LBl[(int64_t)t * n + base]}, {m0.x, m0.y}));
-                s1 = df_add(s1, df_mul({LBh[(int64_t)(t + 1) * n + base], LBl[(int64_t)(t + 1) * n + base]},
-                                       {m1.x, m1.y}));
+constexpr int TI_G = 16, TI_KC = 64, TI_THREADS = 256;
+
+__global__ void __launch_bounds__(TI_THREADS) k_trinv_tiles(const float2 *__restrict__ LB,
+                                                            const float2 *__restrict__ D, int n, int b, int R,
+                                                            double *__restrict__ M, float *__restrict__ M32) {
+    extern __shared__ float2 tsm[];
+    float2 *ring = tsm;                       // [R][TI_G]
+    float2 *Lt = ring + (int64_t)R * TI_G;    // [32][TI_KC + 1]
+    float2 *rhs = Lt + 32 * (TI_KC + 1);      // [32][TI_G]
+    const int t = threadIdx.x, r = t & 31, gp = (t >> 5) * 2;
+    const int c0 = blockIdx.x * TI_G;
+    for (int idx = t; idx < R * TI_G; idx += TI_THREADS) ring[idx] = make_float2(0.f, 0.f);
+    __syncthreads();
+    for (int i0 = c0 & ~31; i0 < n; i0 += 32) {
+        dacc a0, a1;
+        const int kbeg = max(0, i0 - b);
+        for (int kc = kbeg; kc < i0; kc += TI_KC) {
+            const int kn = min(TI_KC, i0 - kc);
+            for (int idx = t; idx < 32 * TI_KC; idx += TI_THREADS) {
+                const int rr = idx & 31, kk = idx >> 5, i = i0 + rr, k = kc + kk;
+                Lt[rr * (TI_KC + 1) + kk] =
+                    (kk < kn && i < n && i - k <= b) ? band_at(LB, b, i, k) : make_float2(0.f, 0.f);
             }
-            if (t < t1) {
-                const float2 m0 = ring[(i - b + t) & (R - 1)];
-                s0 = df_add(s0, df_mul({LBh[(int64_t)t * n + base], LBl[(int64_t)t * n + base]}, {m0.x, m0.y}));
-            }
-        }
-        df s = df_add(s0, s1);
-        const df rdi = valid ? df{rdh[i], rdl[i]} : df{0.f, 0.f};
-        df v = {0.f, 0.f};
+            __syncthreads();
 #pragma unroll 4
-        for (int t = 0; t < 32; ++t) {
-            if (i0 + t >= n) break;
-            if (lane == t) v = df_mul(df_sub({i == c ? 1.f : 0.f, 0.f}, s), rdi);
-            const df vt = df_shfl(v, t);
-            if (lane > t && valid && lane - t <= b) {
-                const int64_t o = (int64_t)(b - lane + t) * n + base;   // L[i, i0+t]
-                s = df_add(s, df_mul({LBh[o], LBl[o]}, vt));
+            for (int kk = 0; kk < kn; ++kk) {
+                const float2 l = Lt[r * (TI_KC + 1) + kk];
+                const float2 *m = ring + (int64_t)((kc + kk) & (R - 1)) * TI_G + gp;
+                a0.add(l, m[0]);
+                a1.add(l, m[1]);
+            }
+            __syncthreads();
+        }
+        const int i = i0 + r;
+        {
+            df e0 = df_neg(a0.value()), e1 = df_neg(a1.value());
+            if (i == c0 + gp) e0 = df_add(e0, {1.f, 0.f});
+            if (i == c0 + gp + 1) e1 = df_add(e1, {1.f, 0.f});
+            rhs[r * TI_G + gp] = make_float2(e0.hi, e0.lo);
+            rhs[r * TI_G + gp + 1] = make_float2(e1.hi, e1.lo);
+        }
+        __syncthreads();
+        dacc v0, v1;
+        const float2 *dblk = D + (int64_t)(i0 >> 5) * 1024 + r;
+#pragma unroll 8
+        for (int q = 0; q < 32; ++q) {
+            const float2 d = q <= r ? dblk[q * 32] : make_float2(0.f, 0.f);
+            v0.add(d, rhs[q * TI_G + gp]);
+            v1.add(d, rhs[q * TI_G + gp + 1]);
+        }
+        const df x0 = v0.value(), x1 = v1.value();
+        float2 *slot = ring + (int64_t)(i & (R - 1)) * TI_G + gp;
+        // rows above a column's start come out as exact zeros
+        slot[0] = make_float2(x0.hi, x0.lo);
+        slot[1] = make_float2(x1.hi, x1.lo);
+        if (i < n) {
+            const int ca = c0 + gp, cb = ca + 1;
+            if (ca < n && i >= ca) {
+                M[(int64_t)i + (int64_t)n * ca] = df_to(x0);
+                M32[(int64_t)i + (int64_t)n * ca] = x0.hi;
+            }
+            if (cb < n && i >= cb) {
+                M[(int64_t)i + (int64_t)n * cb] = df_to(x1);
+                M32[(int64_t)i + (int64_t)n * cb] = x1.hi;
             }
         }
-        if (valid) {
-            ring[i & (R - 1)] = make_float2(v.hi, v.lo);
-            M[(int64_t)i + (int64_t)n * c] = df_to(v);
-            M32[(int64_t)i + (int64_t)n * c] = v.hi;
-        }
-        __syncwarp();
+        __syncthreads();
     }
 }
+
+size_t trinv_smem_bytes(int R) { return sizeof(float2) * ((size_t)R * TI_G + 32 * (TI_KC + 1) + 32 * TI_G); }
 
 // Enqueues the whole factorization (band Cholesky, L^-1, FP32 copy); no host
 // synchronisation, so the sequence is captured once into a CUDA graph.
@@ -494,18 +570,18 @@ static void factor_enqueue(Ctx &c, int *d_info) {
         }
     }
     const int b = c.cband;
-    // d_LB (n (b+1) + n doubles) holds the double-float band and 1/diag:
-    // 2 n (b+1) + 2 n floats
-    float *LBh = reinterpret_cast<float *>(c.d_LB), *LBl = LBh + (int64_t)n * (b + 1);
-    float *rdh = LBl + (int64_t)n * (b + 1), *rdl = rdh + n;
+    // d_LB (n (b+1) + n + nblk 1024 doubles) holds, as float pairs, the band
+    // by columns, 1/diag and the diagonal-block inverses
+    float2 *LB = reinterpret_cast<float2 *>(c.d_LB), *rd = LB + (int64_t)n * (b + 1), *D = rd + n;
     ++g_launches;
-    k_band_rows<<<(unsigned)(((int64_t)n * (b + 1) + 255) / 256), 256, 0, c.stream>>>(A, n, b, LBh, LBl, rdh,
-                                                                                      rdl);
+    k_band_cols<<<(unsigned)(((int64_t)n * (b + 1) + 255) / 256), 256, 0, c.stream>>>(A, n, b, LB, rd);
+    ++g_launches;
+    k_block_inverse<<<nblk, 32, 0, c.stream>>>(LB, rd, n, b, D);
     cudaMemsetAsync(c.d_Ainv, 0, sizeof(double) * (size_t)n * n, c.stream);
     cudaMemsetAsync(c.d_Ainv32, 0, sizeof(float) * (size_t)n * n, c.stream);
     ++g_launches;
-    k_trinv_cols<<<(n + c.trinv_warps - 1) / c.trinv_warps, 32 * c.trinv_warps, c.trinv_smem, c.stream>>>(
-        LBh, LBl, rdh, rdl, n, b, c.trinv_ring, c.d_Ainv, c.d_Ainv32);
+    k_trinv_tiles<<<(n + TI_G - 1) / TI_G, TI_THREADS, c.trinv_smem, c.stream>>>(LB, D, n, b, c.trinv_ring,
+                                                                                 c.d_Ainv, c.d_Ainv32);
 }
 
 // Cholesky of the dense coarsest matrix in d_Ac (lower, in place) and
@@ -517,14 +593,11 @@ int coarse_factor_invert(Ctx &c) {
     int *d_info = c.d_iflag + 8;
     if (!c.factor_graph) {
         int R = 32;
-        while (R < c.cband + 1) R <<= 1;
-        int warps = 8;
-        while (warps > 1 && (size_t)warps * R * sizeof(float2) > 200 * 1024) warps >>= 1;
-        const size_t smem = (size_t)warps * R * sizeof(float2);
+        while (R < c.cband + 32) R <<= 1;
+        const size_t smem = trinv_smem_bytes(R);
         if (smem > 220 * 1024) return -2;
-        cudaFuncSetAttribute(k_trinv_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_trinv_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         c.trinv_ring = R;
-        c.trinv_warps = warps;
         c.trinv_smem = smem;
         const int64_t before = g_launches;
         cudaGraph_t g = nullptr;

@@ -713,7 +713,8 @@ int sgld_set_fixed_dofs(sgld_ctx *ctx, const uint8_t *fixed) {
         CK(dalloc(&c.d_Ainv, (size_t)ncf * ncf));
         CK(dalloc(&c.d_Ainv32, (size_t)ncf * ncf));
         CK(dalloc(&c.d_cpart, (size_t)CSPLIT * ncf));
-        CK(dalloc(&c.d_LB, (size_t)ncf * (band + 1) + ncf));
+        // band + 1/diag + inverses of the 32 x 32 diagonal blocks, as float pairs
+        CK(dalloc(&c.d_LB, (size_t)ncf * (band + 1) + ncf + (size_t)((ncf + 31) / 32) * 1024));
         CK(dalloc(&c.d_cy, 2 * (size_t)ncf));
         CK(dalloc(&c.d_cfree, (size_t)ncf + 3 * lc.nnode));
         if (c.inner_graph) {   // the captured graphs hold the old coarse buffers

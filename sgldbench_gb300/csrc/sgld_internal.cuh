@@ -63,8 +63,9 @@ struct Ctx {
     double *d_Ac = nullptr;         // [ncf*ncf] dense matrix / Cholesky factor
     double *d_Ainv = nullptr;       // [ncf*ncf] inverse (symmetric)
     float *d_Ainv32 = nullptr;
-    double *d_LB = nullptr;         // [ncf*(cband+1) + ncf] doubles holding the Cholesky band and
-                                    // 1/diag as float pairs (hi, lo arrays)
+    double *d_LB = nullptr;         // [ncf*(cband+1) + ncf + ceil(ncf/32)*1024] doubles holding the
+                                    // Cholesky band, 1/diag and the diagonal-block inverses as
+                                    // float pairs (hi, lo arrays)
     double *d_cy = nullptr;         // [2*ncf] intermediate of the coarse apply
     // SIMP loop fields on the finest element grid (allocated on first use)
     double *t_x = nullptr, *t_xp = nullptr, *t_hs = nullptr, *t_ce = nullptr, *t_dcs = nullptr, *t_dvs = nullptr,
@@ -72,7 +73,7 @@ struct Ctx {
     double t_rmin = -1.0;
     cudaGraphExec_t factor_graph = nullptr;   // captured factorization of the coarsest matrix
     int64_t factor_graph_launches = 0;
-    int trinv_ring = 0, trinv_warps = 0;
+    int trinv_ring = 0;
     size_t trinv_smem = 0;
     double *d_cpart = nullptr;      // [CSPLIT*ncf] GEMV partials
     // templates for the level-2 Galerkin assembly

@@ -276,10 +276,21 @@ void launch_coarse_dense(const Level &lc, int ncf, const int *rows_and_pos, doub
 // ---- blocked band Cholesky, NB x NB tiles, column-major n x n ------------------
 constexpr int NB = 32;
 
-// One block column of the band Cholesky (4 warps per CTA).  FP64 issue is
-// scarce on GB300 (a warp-wide DFMA occupies its SM sub-partition's FP64 pipe
-// for many cycles), so the work of a panel is spread over sub-partitions and
-// SMs:
+// 1/sqrt(d) in double-float: FP32 seed, two Newton steps y += y (1 - d y^2) / 2
+__device__ __forceinline__ df df_rsqrt(df d) {
+    df y = {rsqrtf(d.hi), 0.f};
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const df h = df_sub({1.f, 0.f}, df_mul(df_mul(d, y), y));
+        y = df_add(y, df_mul(df_mul(y, {0.5f, 0.f}), h));
+    }
+    return y;
+}
+
+// One block column of the band Cholesky (4 warps per CTA), in double-float
+// arithmetic: GB300's FP64 pipe would serialise the pivot chain (a warp-wide
+// FP64 instruction occupies its sub-partition for many cycles).  The matrix
+// stays FP64 in memory; tiles are split into (hi, lo) on load.
 //   * every CTA factors the 32 x 32 diagonal tile in shared memory (row = lane,
 //     the rank-1 update of step j split over the 4 warps by column mod 4; the
 //     pivot 1/sqrt(d) is formed by every thread, so it needs no broadcast);
@@ -291,32 +302,33 @@ constexpr int CP_THREADS = 128;
 constexpr int CP_RS = 8;
 
 __global__ void __launch_bounds__(CP_THREADS) k_chol_panel(double *A, int n, int k0, int rend, int *info) {
-    __shared__ double T[NB][NB + 1];
-    __shared__ double rd[NB], ld[NB];
+    __shared__ df T[NB][NB + 1];
+    __shared__ df rd[NB], ld[NB];
     const int t = threadIdx.x, r = t & 31, w = t >> 5;
     const int m = min(NB, n - k0);
     for (int idx = t; idx < NB * NB; idx += CP_THREADS) {
         const int rr = idx & 31, cc = idx >> 5;
-        T[rr][cc] = (rr < m && cc < m) ? A[(int64_t)(k0 + rr) + (int64_t)n * (k0 + cc)] : (rr == cc ? 1.0 : 0.0);
+        T[rr][cc] = (rr < m && cc < m && cc <= rr) ? df_from(A[(int64_t)(k0 + rr) + (int64_t)n * (k0 + cc)])
+                                                   : df{rr == cc ? 1.f : 0.f, 0.f};
     }
     __syncthreads();
     for (int j = 0; j < NB; ++j) {
         // T[j][j] is read here and never written in the loop (the factor's
         // diagonal goes to ld[]), so no thread can overwrite it early
-        double d = T[j][j];
-        const bool bad = !(d > 0.0);
-        if (bad) d = 1.0;
-        const double y = rsqrt(d);
-        if (w == 0 && r > j) T[r][j] *= y;
+        df d = T[j][j];
+        const bool bad = !(d.hi > 0.f);
+        if (bad) d = {1.f, 0.f};
+        const df y = df_rsqrt(d);
+        if (w == 0 && r > j) T[r][j] = df_mul(T[r][j], y);
         if (t == 0) {
             rd[j] = y;
-            ld[j] = d * y;
+            ld[j] = df_mul(d, y);
             if (bad && blockIdx.x == 0 && info) atomicExch(info, k0 + j + 1);
         }
         __syncthreads();
         if (r > j) {
-            const double lrj = T[r][j];
-            for (int q = j + 1 + ((w - j - 1) & 3); q <= r; q += 4) T[r][q] -= lrj * T[q][j];
+            const df lrj = T[r][j];
+            for (int q = j + 1 + ((w - j - 1) & 3); q <= r; q += 4) T[r][q] = df_sub(T[r][q], df_mul(lrj, T[q][j]));
         }
         __syncthreads();
     }
@@ -324,40 +336,60 @@ __global__ void __launch_bounds__(CP_THREADS) k_chol_panel(double *A, int n, int
         for (int idx = t; idx < NB * NB; idx += CP_THREADS) {
             const int rr = idx & 31, cc = idx >> 5;
             if (rr < m && cc < m)
-                A[(int64_t)(k0 + rr) + (int64_t)n * (k0 + cc)] = rr > cc ? T[rr][cc] : (rr == cc ? ld[rr] : 0.0);
+                A[(int64_t)(k0 + rr) + (int64_t)n * (k0 + cc)] =
+                    rr > cc ? df_to(T[rr][cc]) : (rr == cc ? df_to(ld[rr]) : 0.0);
         }
         return;
     }
     const int rr = t >> 4, g = t & 15;
     const int row = k0 + NB + (blockIdx.x - 1) * CP_RS + rr;
     const bool live = row < rend;
-    double a0 = 0.0, a1 = 0.0;
+    df a0 = {0.f, 0.f}, a1 = {0.f, 0.f};
     if (live) {
-        if (g < m) a0 = A[(int64_t)row + (int64_t)n * (k0 + g)];
-        if (g + 16 < m) a1 = A[(int64_t)row + (int64_t)n * (k0 + g + 16)];
+        if (g < m) a0 = df_from(A[(int64_t)row + (int64_t)n * (k0 + g)]);
+        if (g + 16 < m) a1 = df_from(A[(int64_t)row + (int64_t)n * (k0 + g + 16)]);
     }
 #pragma unroll 4
     for (int q = 0; q < NB; ++q) {
-        const double xl = (q < 16 ? a0 : a1) * rd[q];
-        const double xq = __shfl_sync(0xffffffffu, xl, q & 15, 16);
+        const df xq = df_shfl(df_mul(q < 16 ? a0 : a1, rd[q]), q & 15, 16);
         if (g == (q & 15)) {
             if (q < 16)
                 a0 = xq;
             else
                 a1 = xq;
         }
-        if (g > q) a0 -= xq * T[g][q];
-        if (g + 16 > q) a1 -= xq * T[g + 16][q];
+        if (g > q) a0 = df_sub(a0, df_mul(xq, T[g][q]));
+        if (g + 16 > q) a1 = df_sub(a1, df_mul(xq, T[g + 16][q]));
     }
     if (live) {
-        if (g < m) A[(int64_t)row + (int64_t)n * (k0 + g)] = a0;
-        if (g + 16 < m) A[(int64_t)row + (int64_t)n * (k0 + g + 16)] = a1;
+        if (g < m) A[(int64_t)row + (int64_t)n * (k0 + g)] = df_to(a0);
+        if (g + 16 < m) A[(int64_t)row + (int64_t)n * (k0 + g + 16)] = df_to(a1);
     }
 }
 
+// Compensated double-float dot-product accumulator (the Dot2 scheme of Ogita,
+// Rump and Oishi, 2005, with the low parts of the operands folded into the
+// error term): s + e carries the running sum.
+struct dacc {
+    float s = 0.f, e = 0.f;
+    __device__ __forceinline__ void add(float2 a, float2 b) {
+        const float p = __fmul_rn(a.x, b.x);
+        float pe = __fmaf_rn(a.x, b.x, -p);
+        pe = __fmaf_rn(a.x, b.y, pe);
+        pe = __fmaf_rn(a.y, b.x, pe);
+        const float t = __fadd_rn(s, p);
+        const float bb = __fsub_rn(t, s);
+        const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+        s = t;
+        e = __fadd_rn(e, __fadd_rn(err, pe));
+    }
+    __device__ __forceinline__ df value() const { return quick_two_sum(s, e); }
+};
+
 // trailing update A[i,j] -= sum_k A[i,k] A[j,k] over the panel's columns k for
 // the band tiles below it: blockIdx.x = tile pair (ii >= jj), blockIdx.y =
-// SY_RS-row slice of tile ii (slices spread one pair's FP64 work over SMs)
+// SY_RS-row slice of tile ii (slices spread one pair's work over SMs).  The
+// products are summed in double-float; A stays FP64.
 constexpr int SY_RS = 8;
 
 __global__ void __launch_bounds__(256) k_syrk_update(double *A, int n, int k0, int jb0, int nbt) {
@@ -368,28 +400,27 @@ __global__ void __launch_bounds__(256) k_syrk_update(double *A, int n, int k0, i
     }
     const int jj = p;
     const int i0 = (jb0 + ii) * NB + blockIdx.y * SY_RS, j0 = (jb0 + jj) * NB;
-    __shared__ double Ai[SY_RS][NB + 1], Aj[NB][NB + 1];
+    __shared__ float2 Ai[SY_RS][NB + 1], Aj[NB][NB + 1];
     const int t = threadIdx.x;
     const int m = min(NB, n - k0);
     for (int idx = t; idx < NB * NB; idx += 256) {
         const int r = idx & 31, c = idx >> 5;
-        Aj[r][c] = (j0 + r < n && c < m) ? A[(int64_t)(j0 + r) + (int64_t)n * (k0 + c)] : 0.0;
+        const df v = df_from((j0 + r < n && c < m) ? A[(int64_t)(j0 + r) + (int64_t)n * (k0 + c)] : 0.0);
+        Aj[r][c] = make_float2(v.hi, v.lo);
     }
     {
         const int r = t & (SY_RS - 1), c = t / SY_RS;
-        Ai[r][c] = (i0 + r < n && c < m) ? A[(int64_t)(i0 + r) + (int64_t)n * (k0 + c)] : 0.0;
+        const df v = df_from((i0 + r < n && c < m) ? A[(int64_t)(i0 + r) + (int64_t)n * (k0 + c)] : 0.0);
+        Ai[r][c] = make_float2(v.hi, v.lo);
     }
     __syncthreads();
     const int r = t & (SY_RS - 1), c = t / SY_RS;
     const int gi = i0 + r, gj = j0 + c;
     if (gi >= n || gj >= n || gj > gi) return;
-    double v0 = 0.0, v1 = 0.0;
+    dacc v;
 #pragma unroll
-    for (int q = 0; q < NB; q += 2) {
-        v0 += Ai[r][q] * Aj[c][q];
-        v1 += Ai[r][q + 1] * Aj[c][q + 1];
-    }
-    A[(int64_t)gi + (int64_t)n * gj] -= v0 + v1;
+    for (int q = 0; q < NB; ++q) v.add(Ai[r][q], Aj[c][q]);
+    A[(int64_t)gi + (int64_t)n * gj] -= df_to(v.value());
 }
 
 // Band of L by columns in double-float form: LB[k*(b+1) + j] = L[k+j, k]
@@ -444,25 +475,6 @@ __global__ void __launch_bounds__(32) k_block_inverse(const float2 *__restrict__
     __syncwarp();
     for (int tt = 0; tt < 32; ++tt) D[(int64_t)blockIdx.x * 1024 + tt * 32 + t] = X[t][tt];
 }
-
-// Compensated double-float dot-product accumulator (the Dot2 scheme of Ogita,
-// Rump and Oishi, 2005, with the low parts of the operands folded into the
-// error term): s + e carries the running sum.
-struct dacc {
-    float s = 0.f, e = 0.f;
-    __device__ __forceinline__ void add(float2 a, float2 b) {
-        const float p = __fmul_rn(a.x, b.x);
-        float pe = __fmaf_rn(a.x, b.x, -p);
-        pe = __fmaf_rn(a.x, b.y, pe);
-        pe = __fmaf_rn(a.y, b.x, pe);
-        const float t = __fadd_rn(s, p);
-        const float bb = __fsub_rn(t, s);
-        const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
-        s = t;
-        e = __fadd_rn(e, __fadd_rn(err, pe));
-    }
-    __device__ __forceinline__ df value() const { return quick_two_sum(s, e); }
-};
 
 // M = L^-1 in double-float arithmetic, a CTA per group of TI_G columns
 // c0..c0+TI_G-1 walking down aligned 32-row blocks i0 (GB300's FP64 issue

@@ -57,13 +57,60 @@ __global__ void k_restrict(const T *__restrict__ rf, T *__restrict__ rc, int nyc
     rc[3 * n + 2] = a2;
 }
 
+// The same restriction with the span S a compile-time constant: the
+// (2S-1)^3 taps unroll, the weights are constants and the indices stay 32-bit
+// (grids below 2^31 / 3 nodes).  Lanes hold consecutive coarse y, so for one
+// (dx, dz) a warp's taps cover a contiguous run of fine nodes.
+template <typename T, int S>
+__global__ void __launch_bounds__(128) k_restrict_s(const T *__restrict__ rf, T *__restrict__ rc, int nyc, int nxc,
+                                                    int nzc) {
+    const int NYc = nyc + 1, NXc = nxc + 1;
+    const int NYf = S * nyc + 1, NXf = S * nxc + 1, NZf = S * nzc + 1;
+    const int pl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pl >= NYc * NXc) return;
+    const int I = pl % NYc, J = pl / NYc, Kz = blockIdx.y;
+    const T inv = T(1) / T(S);
+    T a0 = T(0), a1 = T(0), a2 = T(0);
+#pragma unroll
+    for (int dz = -S + 1; dz < S; ++dz) {
+        const int fz = S * Kz + dz;
+        if (fz < 0 || fz >= NZf) continue;
+        const T wz = T(S - (dz < 0 ? -dz : dz)) * inv;
+#pragma unroll
+        for (int dx = -S + 1; dx < S; ++dx) {
+            const int fx = S * J + dx;
+            if (fx < 0 || fx >= NXf) continue;
+            const T wxz = T(S - (dx < 0 ? -dx : dx)) * inv * wz;
+            const int base = NYf * (fx + NXf * fz);
+#pragma unroll
+            for (int dy = -S + 1; dy < S; ++dy) {
+                const int fy = S * I + dy;
+                if (fy < 0 || fy >= NYf) continue;
+                const T w = T(S - (dy < 0 ? -dy : dy)) * inv * wxz;
+                const int f = 3 * (fy + base);
+                a0 += w * rf[f];
+                a1 += w * rf[f + 1];
+                a2 += w * rf[f + 2];
+            }
+        }
+    }
+    const int n = 3 * (pl + NYc * NXc * Kz);
+    rc[n] = a0;
+    rc[n + 1] = a1;
+    rc[n + 2] = a2;
+}
+
 template <typename T>
 void launch_restrict(const Level &fine, const Level &coarse, const T *rf, T *rc, cudaStream_t st) {
-    const int64_t nn = coarse.nnode;
     ++g_launches;
-    (void)nn;
     const dim3 g((unsigned)(((coarse.ny + 1) * (coarse.nx + 1) + 127) / 128), (unsigned)(coarse.nz + 1));
-    k_restrict<T><<<g, 128, 0, st>>>(rf, rc, coarse.ny, coarse.nx, coarse.nz, coarse.span);
+    const bool small = 3 * (int64_t)fine.nnode < (int64_t)INT32_MAX;
+    if (small && coarse.span == 2)
+        k_restrict_s<T, 2><<<g, 128, 0, st>>>(rf, rc, coarse.ny, coarse.nx, coarse.nz);
+    else if (small && coarse.span == 4)
+        k_restrict_s<T, 4><<<g, 128, 0, st>>>(rf, rc, coarse.ny, coarse.nx, coarse.nz);
+    else
+        k_restrict<T><<<g, 128, 0, st>>>(rf, rc, coarse.ny, coarse.nx, coarse.nz, coarse.span);
 }
 template void launch_restrict<double>(const Level &, const Level &, const double *, double *, cudaStream_t);
 template void launch_restrict<float>(const Level &, const Level &, const float *, float *, cudaStream_t);
@@ -148,11 +195,120 @@ __global__ void k_prolong_smooth(const T *__restrict__ xc, const T *__restrict__
     }
 }
 
+// The same operator with a thread per coarse node (I, J, K) writing the
+// fine nodes (S I + ry, S J + rx, S K + rz), 0 <= ry, rx, rz < S (only 0
+// past the last coarse cell of an axis): the 8 coarse corners are loaded once
+// per S^3 fine nodes instead of once per fine node, and the interpolation is
+// done axis by axis (z, then x, then y).  Span S is a compile-time constant,
+// indices are 32-bit.  Same result as k_prolong_smooth up to the order of the
+// interpolation sums.
+template <typename T, int S, bool FINAL>
+__global__ void __launch_bounds__(128) k_prolong_cells(const T *__restrict__ xc, const T *__restrict__ rf,
+                                                       const T *__restrict__ D, const uint8_t *__restrict__ nflag,
+                                                       T omega, T *__restrict__ xf, int nyc, int nxc, int nzc,
+                                                       double *__restrict__ partial) {
+    const int NYc = nyc + 1, NXc = nxc + 1;
+    const int NYf = S * nyc + 1, NXf = S * nxc + 1;
+    const int pl = blockIdx.x * blockDim.x + threadIdx.x;
+    const int K = blockIdx.y;
+    T dot = T(0);
+    if (pl < NYc * NXc) {
+        const int I = pl % NYc, J = pl / NYc;
+        const int ly = I < nyc ? S : 1, lx = J < nxc ? S : 1, lz = K < nzc ? S : 1;
+        T cv[2][2][2][3];   // [c (z)][b (x)][a (y)][component]
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+                for (int a = 0; a < 2; ++a) {
+                    const bool in = !((a && I == nyc) || (b && J == nxc) || (c && K == nzc));
+                    const int m = 3 * ((I + a) + NYc * ((J + b) + NXc * (K + c)));
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) cv[c][b][a][q] = in ? xc[m + q] : T(0);
+                }
+        const T inv = T(1) / T(S);
+#pragma unroll
+        for (int rz = 0; rz < S; ++rz) {
+            if (rz >= lz) break;
+            const T wz1 = T(rz) * inv, wz0 = T(S - rz) * inv;
+            T qz[2][2][3];
+#pragma unroll
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) qz[b][a][q] = wz0 * cv[0][b][a][q] + wz1 * cv[1][b][a][q];
+#pragma unroll
+            for (int rx = 0; rx < S; ++rx) {
+                if (rx >= lx) break;
+                const T wx1 = T(rx) * inv, wx0 = T(S - rx) * inv;
+                T qx[2][3];
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) qx[a][q] = wx0 * qz[0][a][q] + wx1 * qz[1][a][q];
+                const int rowbase = NYf * ((S * J + rx) + NXf * (S * K + rz)) + S * I;
+#pragma unroll
+                for (int ry = 0; ry < S; ++ry) {
+                    if (ry >= ly) break;
+                    const T wy1 = T(ry) * inv, wy0 = T(S - ry) * inv;
+                    const int f = rowbase + ry;
+                    const uint8_t fl = nflag[f];
+                    T o[3] = {T(0), T(0), T(0)};
+                    if (fl & NF_ACTIVE) {
+                        T r[3];
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            r[q] = rf[3 * f + q];
+                            const T t = (omega * r[q]) * D[3 * f + q];
+                            o[q] = (t + (wy0 * qx[0][q] + wy1 * qx[1][q])) + t;
+                        }
+                        if (FINAL) {
+#pragma unroll
+                            for (int q = 0; q < 3; ++q)
+                                if (fl & (NF_FIXX << q)) o[q] = T(0);
+                            dot += o[0] * r[0] + o[1] * r[1] + o[2] * r[2];
+                        }
+                    }
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) xf[3 * f + q] = o[q];
+                }
+            }
+        }
+    }
+    if (FINAL && partial) {
+        __shared__ double red[4];
+        const double sum = warp_block_sum<T>(dot, red);
+        if (threadIdx.x == 0) partial[blockIdx.x + gridDim.x * blockIdx.y] = sum;
+    }
+}
+
 template <typename T>
 void launch_prolong_smooth(const Level &fine, const Level &coarse, const T *xc, const T *rf, const T *diag, T omega,
                            T *xf, bool final_level, double *partial_dot, int *nblocks_out, cudaStream_t st) {
-    const int64_t nn = fine.nnode;
-    (void)nn;
+    const bool small = 3 * (int64_t)fine.nnode < (int64_t)INT32_MAX;
+    if (small && (coarse.span == 2 || coarse.span == 4)) {
+        const dim3 g((unsigned)(((coarse.ny + 1) * (coarse.nx + 1) + 127) / 128), (unsigned)(coarse.nz + 1));
+        if (nblocks_out) *nblocks_out = (int)(g.x * g.y);
+        ++g_launches;
+#define PCELLS(S, F)                                                                                              \
+    k_prolong_cells<T, S, F><<<g, 128, 0, st>>>(xc, rf, diag, fine.nflag, omega, xf, coarse.ny, coarse.nx, coarse.nz, \
+                                                F ? partial_dot : nullptr)
+        if (coarse.span == 2) {
+            if (final_level)
+                PCELLS(2, true);
+            else
+                PCELLS(2, false);
+        } else {
+            if (final_level)
+                PCELLS(4, true);
+            else
+                PCELLS(4, false);
+        }
+#undef PCELLS
+        return;
+    }
     const dim3 nb((unsigned)(((fine.ny + 1) * (fine.nx + 1) + 255) / 256), (unsigned)(fine.nz + 1));
     if (nblocks_out) *nblocks_out = (int)(nb.x * nb.y);
     ++g_launches;

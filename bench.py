@@ -50,6 +50,11 @@ def parse():
     ap.add_argument("--size", type=int, nargs=3, default=[256, 128, 128], metavar=("NX", "NY", "NZ"))
     ap.add_argument("--levels", type=int, default=5)
     ap.add_argument("--maxit", type=int, default=2000)
+    ap.add_argument("--inner-its", type=int, default=0,
+                    help="cap on the FP32 inner CG iterations per outer step of the mixed solves (0 = library "
+                         "default); exact count when --inner-tol is 0 and this is > 0")
+    ap.add_argument("--inner-tol", type=float, default=0.0,
+                    help="inner CG stops at ||s|| <= inner_tol ||r|| (0 = library default 1e-3)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-iters", type=int, default=5, help="PCG iterations in the CPU sample")
     return ap.parse_args()
@@ -68,6 +73,7 @@ def workload_config(args):
     nx, ny, nz = args.size
     return {"workload": f"SIMP-graded cantilever {nx}x{ny}x{nz} voxels (config 1)", "grid": [nx, ny, nz],
             "levels": args.levels, "dyadic": True, "omega": OMEGA, "tol": TOL, "precision": args.precision,
+            "inner_its": args.inner_its, "inner_tol": args.inner_tol,
             "l2": "inputs larger than L2 (each DOF vector > 100 MB at the default size)"}
 
 
@@ -219,7 +225,7 @@ def run_ours(args):
         s.set_modulus_device(E_d.data_ptr())
         s.Solving_AssembleFEAstencil()
         return s.pcg_device(F_d.data_ptr(), U_d.data_ptr(), TOL, args.maxit, precision=args.precision,
-                            profile=profile)
+                            inner_its=args.inner_its, inner_tol=args.inner_tol, profile=profile)
 
     for _ in range(max(args.warmup, 0)):
         info = step()
@@ -255,7 +261,8 @@ def run_ours(args):
         t0.record(stream)
         s.set_modulus(E)
         s.Solving_AssembleFEAstencil()
-        U_h, inf = s.pcg(F, tol=TOL, maxIT=args.maxit, precision=args.precision)
+        U_h, inf = s.pcg(F, tol=TOL, maxIT=args.maxit, precision=args.precision, inner_its=args.inner_its,
+                         inner_tol=args.inner_tol)
         t1.record(stream)
         torch.cuda.synchronize()
         e2e.append(t0.elapsed_time(t1) / 1e3)

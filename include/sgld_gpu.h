@@ -64,10 +64,17 @@ typedef struct sgld_solve_opts {
     int maxit;             /* iteration cap (maxIT_) */
     int use_x0;            /* 1: x holds the initial guess (Solving_CG_GMGS.m:7 warm start) */
     int precision;         /* SGLD_PREC_* */
-    int inner_its;         /* SGLD_PREC_MIXED(_DF): FP32 inner PCG iterations per outer step (0 = 12) */
+    int inner_its;         /* SGLD_PREC_MIXED(_DF): cap on the FP32 inner CG iterations per outer
+                              step (0 = 64); with inner_tol == 0 and inner_its > 0, exactly
+                              inner_its iterations */
     double *history;       /* optional host buffer [maxit]: relative residual per iteration */
     int profile;           /* 1: time the K*u and preconditioner launches with CUDA events
                               (the SpMV / PtV split of QuickAccess/zTmp_Benchmarking_SpMV.m:63-111) */
+    double inner_tol;      /* SGLD_PREC_MIXED(_DF): the inner CG of an outer step stops once its
+                              FP32 residual is below max(inner_tol, tol / (2 relres)) times
+                              the outer residual, relres = the outer relative residual so
+                              far (inner_tol 0 = 3e-4 when inner_its == 0); decided on the
+                              device */
 } sgld_solve_opts;
 
 typedef struct sgld_solve_info {
@@ -76,7 +83,7 @@ typedef struct sgld_solve_info {
     double relres;         /* recursive residual norm / ||b|| at exit */
     double true_relres;    /* ||b - K x|| / ||b|| recomputed at exit (FP64 vectors; K x by the
                               precision mode's outer operator) */
-    int inner_iterations;  /* SGLD_PREC_MIXED(_DF): total FP32 inner iterations */
+    int inner_iterations;  /* SGLD_PREC_MIXED(_DF): total FP32 inner CG iterations run */
     double seconds;        /* device time of the solve (CUDA events) */
     double kbyu_seconds;   /* profile: summed device time of the outer K*u launches */
     int kbyu_launches;     /* profile: number of those launches */

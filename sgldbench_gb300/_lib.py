@@ -28,7 +28,7 @@ class Options(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("tol", dbl), ("maxit", i32), ("use_x0", i32), ("precision", i32), ("inner_its", i32),
-                ("history", vp), ("profile", i32)]
+                ("history", vp), ("profile", i32), ("inner_tol", dbl)]
 
 
 class SolveInfo(C.Structure):

@@ -32,21 +32,85 @@ __device__ double msum_partials(const double *__restrict__ part, int nb) {
     return mblock_reduce(s);
 }
 
-// inner scalars (FP64 storage): [0] rho, [1] alpha, [2] beta, [3] rho_new
-enum { IS_RHO = 0, IS_ALPHA = 1, IS_BETA = 2 };
+// inner scalars (FP64 storage): rho = z.s of the last iteration, alpha, beta,
+// r0 = s.s at entry, the iteration count of this inner solve and the total
+// over the outer solve (reset by the host at the start of each solve)
+enum { IS_RHO = 0, IS_ALPHA = 1, IS_BETA = 2, IS_R0 = 3, IS_IT = 4 };
 
-// op 0: rho = sum; op 1: alpha = rho / sum; op 2: beta = sum / rho, rho = sum
+// op 0: r0 = sum, rho = 0, it = 0; op 1: alpha = rho / sum;
+// op 2: beta = sum / rho (0 on the first iteration, rho = 0), rho = sum
 __global__ void k_icg_scalar(int op, double *__restrict__ sc, const double *__restrict__ part, int nb) {
     const double s = msum_partials(part, nb);
     if (threadIdx.x != 0) return;
     if (op == 0) {
-        sc[IS_RHO] = s;
+        sc[IS_R0] = s;
+        sc[IS_RHO] = 0.0;
+        sc[IS_IT] = 0.0;
     } else if (op == 1) {
         sc[IS_ALPHA] = (s != 0.0) ? sc[IS_RHO] / s : 0.0;
     } else {
         sc[IS_BETA] = (sc[IS_RHO] != 0.0) ? s / sc[IS_RHO] : 0.0;
         sc[IS_RHO] = s;
     }
+}
+
+// end of an inner iteration: count it and keep iterating while it < kmax and
+// ||s|| > eta ||s_0||, eta = max(eta_min, tol / (2 relres)) with the outer
+// solve's tolerance and current relative residual (outer[15], outer[3]): the
+// inner solve of the last outer step only goes as far as the outer tolerance
+// needs.  eta_min <= 0: exactly kmax iterations.  Sets the condition of the
+// graph's while node.
+__global__ void k_icg_cond(cudaGraphConditionalHandle h, double *__restrict__ sc, const double *__restrict__ part,
+                           int nb, int kmax, double eta_min, const double *__restrict__ outer,
+                           double *__restrict__ total) {
+    const double ss = msum_partials(part, nb);
+    if (threadIdx.x != 0) return;
+    const double it = sc[IS_IT] + 1.0;
+    sc[IS_IT] = it;
+    *total += 1.0;
+    bool more = it < (double)kmax;
+    if (more && eta_min > 0.0) {
+        const double relres = outer[3], tol = outer[15];
+        const double eta = (relres > 0.0) ? fmax(eta_min, 0.5 * tol / relres) : eta_min;
+        more = ss > eta * eta * sc[IS_R0];
+    }
+    cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+void launch_icg_cond(cudaGraphConditionalHandle h, double *sc, const double *part, int nb, int kmax,
+                     double eta_min, const double *outer, double *total, cudaStream_t s) {
+    ++g_launches;
+    k_icg_cond<<<1, MB, 0, s>>>(h, sc, part, nb, kmax, eta_min, outer, total);
+}
+
+// s = r, e = 0, d = 0 and partial sums of s.s (entry of an inner solve)
+__global__ void k_icg_init(const float *__restrict__ r, float *__restrict__ s, float *__restrict__ e,
+                           float *__restrict__ d, int64_t n, double *__restrict__ part) {
+    float acc = 0.f;
+    for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n; i += (int64_t)gridDim.x * MB) {
+        const float v = r[i];
+        s[i] = v;
+        e[i] = 0.f;
+        d[i] = 0.f;
+        acc = fmaf(v, v, acc);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    __shared__ double wred[MB / 32];
+    if ((threadIdx.x & 31) == 0) wred[threadIdx.x >> 5] = (double)acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < MB / 32; ++i) t += wred[i];
+        part[blockIdx.x] = t;
+    }
+}
+
+int launch_icg_init(const float *r, float *s, float *e, float *d, int64_t n, double *part, cudaStream_t st) {
+    ++g_launches;
+    const int nb = reduce_blocks(n);
+    k_icg_init<<<nb, MB, 0, st>>>(r, s, e, d, n, part);
+    return nb;
 }
 
 void launch_icg_scalar(int op, double *sc, const double *part, int nb, cudaStream_t s) {
@@ -61,28 +125,48 @@ __device__ __forceinline__ float4 fma4(float a, float4 x, float4 y) {
     return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
 }
 
-// e += alpha d; s -= alpha t
+// e += alpha d; s -= alpha t; partial sums of s.s (new s) when part != null
 __global__ void k_icg_update(float *__restrict__ e, float *__restrict__ s, const float *__restrict__ d,
-                             const float *__restrict__ t, int64_t n, const double *__restrict__ sc) {
+                             const float *__restrict__ t, int64_t n, const double *__restrict__ sc,
+                             double *__restrict__ part) {
     const float a = (float)sc[IS_ALPHA];
     const int64_t n4 = n >> 2, stride = (int64_t)gridDim.x * MB;
     float4 *e4 = reinterpret_cast<float4 *>(e), *s4 = reinterpret_cast<float4 *>(s);
     const float4 *d4 = reinterpret_cast<const float4 *>(d), *t4 = reinterpret_cast<const float4 *>(t);
+    float acc = 0.f;
     for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n4; i += stride) {
         e4[i] = fma4(a, d4[i], e4[i]);
-        s4[i] = fma4(-a, t4[i], s4[i]);
+        const float4 v = fma4(-a, t4[i], s4[i]);
+        s4[i] = v;
+        acc = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, acc))));
     }
     const int64_t i = 4 * n4 + blockIdx.x * (int64_t)MB + threadIdx.x;
     if (i < n) {
         e[i] = fmaf(a, d[i], e[i]);
-        s[i] = fmaf(-a, t[i], s[i]);
+        const float v = fmaf(-a, t[i], s[i]);
+        s[i] = v;
+        acc = fmaf(v, v, acc);
+    }
+    if (part) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        __shared__ double wred[MB / 32];
+        if ((threadIdx.x & 31) == 0) wred[threadIdx.x >> 5] = (double)acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tt = 0.0;
+            for (int k = 0; k < MB / 32; ++k) tt += wred[k];
+            part[blockIdx.x] = tt;
+        }
     }
 }
 
-void launch_icg_update(float *e, float *s, const float *d, const float *t, int64_t n, const double *sc,
-                       cudaStream_t st) {
+int launch_icg_update(float *e, float *s, const float *d, const float *t, int64_t n, const double *sc,
+                      double *part, cudaStream_t st) {
     ++g_launches;
-    k_icg_update<<<reduce_blocks(n), MB, 0, st>>>(e, s, d, t, n, sc);
+    const int nb = reduce_blocks(n);
+    k_icg_update<<<nb, MB, 0, st>>>(e, s, d, t, n, sc, part);
+    return nb;
 }
 
 // d = w + beta d

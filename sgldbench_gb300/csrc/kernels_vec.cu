@@ -58,7 +58,7 @@ void launch_finalize_sum(const double *partial, int nb, double *out, cudaStream_
 }
 
 // scalar slots
-enum { S_NORMB = 0, S_X1 = 1, S_LAM = 2, S_RES = 3, S_BETA = 4, S_PQ = 5, S_RR = 6 };
+enum { S_NORMB = 0, S_X1 = 1, S_LAM = 2, S_RES = 3, S_BETA = 4, S_PQ = 5, S_RR = 6, S_TOL = 15 };
 enum { I_ITS = 0, I_DONE = 1, I_STOP = 2 };
 
 // op: 0 normB = sqrt(sum); 1 x1 = sum; 2 lambda = x1 / sum;
@@ -69,7 +69,10 @@ __global__ void k_pcg_scalar(int op, double *__restrict__ scal, int *__restrict_
     if (op != 5) s = sum_partials(part, nb);
     if (threadIdx.x != 0) return;
     switch (op) {
-        case 0: scal[S_NORMB] = sqrt(s); break;
+        case 0:
+            scal[S_NORMB] = sqrt(s);
+            scal[S_TOL] = tol;
+            break;
         case 1: scal[S_X1] = s; break;
         case 2:
             if (iflag[I_STOP]) return;
@@ -100,6 +103,7 @@ __global__ void k_pcg_scalar(int op, double *__restrict__ scal, int *__restrict_
             iflag[I_ITS] = 0;
             iflag[I_DONE] = 0;
             iflag[I_STOP] = 0;
+            scal[S_RES] = 1.0;
             break;
     }
 }

@@ -305,51 +305,80 @@ int vcycle_dev32(sgld_ctx *ctx, const float *r, float *z, double *partial, int *
     return SGLD_OK;
 }
 
-// k FP32 CG iterations on K e = r32 from e = 0, preconditioned by the FP32
-// V-cycle; result in d_e32.  Enqueue only (no host synchronisation), so the
-// sequence can be captured into a graph.
-void inner_enqueue(sgld_ctx *ctx, int k) {
+// Inner solve of the mixed-precision preconditioner: FP32 CG on K e = r32 from
+// e = 0, preconditioned by the FP32 V-cycle, result in d_e32.  It is one CUDA
+// graph built once per (context, kmax, eta): entry nodes (s = r, e = d = 0,
+// r0 = s.s) followed by a while node whose body is one CG iteration
+//   z = V s;  beta = z.s / rho;  d = z + beta d;  t = K d;
+//   alpha = z.s / d.t;  e += alpha d;  s -= alpha t;  continue?
+// The last kernel of the body decides on the device whether to iterate again
+// (kmax iterations, or ||s|| <= max(eta, tol / (2 relres)) ||r|| first when
+// eta > 0, relres being the outer solve's current relative residual), so the
+// solve needs no host round trip.  d_isc[IS_TOTAL] counts the iterations run.
+constexpr int IS_TOTAL = 8;
+
+static int build_inner_graph(sgld_ctx *ctx, int kmax, double eta) {
     Ctx &c = ctx->c;
     const Level &l0 = c.lv[0];
     const int64_t nv = 3 * l0.nnode;
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    int64_t before = g_launches;
+    CK(cudaStreamBeginCaptureToGraph(c.stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const int nbi = launch_icg_init(c.d_r32, c.d_s32, c.d_e32, c.d_d32, nv, c.d_part2, c.stream);
+    launch_icg_scalar(0, c.d_isc, c.d_part2, nbi, c.stream);
+    cudaStreamCaptureStatus st;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    CK(cudaStreamGetCaptureInfo(c.stream, &st, nullptr, nullptr, &deps, nullptr, &ndeps));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    CK(cudaGraphAddNode(&wnode, g, deps, nullptr, ndeps, &cp));
+    CK(cudaStreamUpdateCaptureDependencies(c.stream, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    CK(cudaStreamEndCapture(c.stream, &g));
+    c.inner_entry_launches = g_launches - before;
+    before = g_launches;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(c.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     int nb = 0;
-    cudaMemcpyAsync(c.d_s32, c.d_r32, sizeof(float) * nv, cudaMemcpyDeviceToDevice, c.stream);
-    cudaMemsetAsync(c.d_e32, 0, sizeof(float) * nv, c.stream);
     vcycle_dev32(ctx, c.d_s32, c.d_z32, c.d_part2, &nb);
-    launch_icg_scalar(0, c.d_isc, c.d_part2, nb, c.stream);
-    cudaMemcpyAsync(c.d_d32, c.d_z32, sizeof(float) * nv, cudaMemcpyDeviceToDevice, c.stream);
-    for (int j = 1; j <= k; ++j) {
-        launch_kbyu_f32(l0, c.d_E32, c.d_d32, c.d_t32, c.d_part2, &nb, c.stream);
-        launch_icg_scalar(1, c.d_isc, c.d_part2, nb, c.stream);
-        launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.stream);
-        if (j == k) break;
-        vcycle_dev32(ctx, c.d_s32, c.d_z32, c.d_part2, &nb);
-        launch_icg_scalar(2, c.d_isc, c.d_part2, nb, c.stream);
-        launch_icg_dupdate(c.d_d32, c.d_z32, nv, c.d_isc, c.stream);
-    }
+    launch_icg_scalar(2, c.d_isc, c.d_part2, nb, c.stream);
+    launch_icg_dupdate(c.d_d32, c.d_z32, nv, c.d_isc, c.stream);
+    launch_kbyu_f32(l0, c.d_E32, c.d_d32, c.d_t32, c.d_part2, &nb, c.stream);
+    launch_icg_scalar(1, c.d_isc, c.d_part2, nb, c.stream);
+    nb = launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.d_part2, c.stream);
+    launch_icg_cond(h, c.d_isc, c.d_part2, nb, kmax, eta, c.d_scal, c.d_isc + IS_TOTAL, c.stream);
+    CK(cudaStreamEndCapture(c.stream, &body));
+    c.inner_body_launches = g_launches - before;
+    g_launches = before - c.inner_entry_launches;
+    const cudaError_t e = cudaGraphInstantiate(&c.inner_graph, g, 0);
+    cudaGraphDestroy(g);
+    CK(e);
+    c.inner_graph_k = kmax;
+    c.inner_graph_eta = eta;
+    return SGLD_OK;
 }
 
-// runs the inner solve through a CUDA graph captured once per (context, k)
-int inner_run(sgld_ctx *ctx, int k) {
+// one inner solve (graph launch); launch accounting of the iterations is done
+// by the caller from d_isc[IS_TOTAL]
+int inner_run(sgld_ctx *ctx, int kmax, double eta) {
     Ctx &c = ctx->c;
-    if (!c.inner_graph || c.inner_graph_k != k) {
+    if (!c.inner_graph || c.inner_graph_k != kmax || c.inner_graph_eta != eta) {
         if (c.inner_graph) {
             cudaGraphExecDestroy(c.inner_graph);
             c.inner_graph = nullptr;
         }
-        const int64_t before = g_launches;
-        cudaGraph_t g = nullptr;
-        CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
-        inner_enqueue(ctx, k);
-        CK(cudaStreamEndCapture(c.stream, &g));
-        c.inner_graph_launches = g_launches - before;
-        g_launches = before;
-        CK(cudaGraphInstantiate(&c.inner_graph, g, 0));
-        cudaGraphDestroy(g);
-        c.inner_graph_k = k;
+        int rc = build_inner_graph(ctx, kmax, eta);
+        if (rc) return rc;
     }
     CK(cudaGraphLaunch(c.inner_graph, c.stream));
-    g_launches += c.inner_graph_launches;
+    g_launches += c.inner_entry_launches;
     return SGLD_OK;
 }
 
@@ -1153,8 +1182,14 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
     const int nbv = reduce_blocks(nv);
     const double tol = o->tol;
     const int maxit = o->maxit;
-    const int k = o->inner_its > 0 ? o->inner_its : 12;
+    // inner solve: a fixed inner_its iterations when inner_tol == 0 and
+    // inner_its > 0; otherwise stop at ||s|| <= max(inner_tol, tol / (2 relres))
+    // ||r|| (inner_tol default 3e-4) or after inner_its (default 64) iterations
+    const bool fixed_k = o->inner_its > 0 && !(o->inner_tol > 0.0);
+    const int k = o->inner_its > 0 ? o->inner_its : 64;
+    const double eta = fixed_k ? 0.0 : (o->inner_tol > 0.0 ? o->inner_tol : 3e-4);
     const bool dfk = o->precision == SGLD_PREC_MIXED_DF;
+    CK(cudaMemsetAsync(c.d_isc + IS_TOTAL, 0, sizeof(double), c.stream));
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
@@ -1173,7 +1208,7 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
         CK(cudaMemcpyAsync(c.d_r, c.d_b, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c.stream));
     }
     launch_narrow(c.d_r, c.d_r32, nv, c.stream);
-    if ((rc = inner_run(ctx, k))) return rc;
+    if ((rc = inner_run(ctx, k, eta))) return rc;
     launch_widen_dots(c.d_e32, c.d_z, c.d_r, c.d_r, nv, c.d_part, c.d_part2, nbv, c.stream);
     launch_flex_beta(c.d_scal, c.d_iflag, c.d_part, c.d_part2, nbv, 1, c.stream);
     CK(cudaMemcpyAsync(c.d_p, c.d_z, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c.stream));
@@ -1183,7 +1218,7 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
     if (prof)
         for (auto &e : pe) CK(cudaEventCreate(&e));
     double kb_ms = 0.0, pc_ms = 0.0;
-    int kb_n = 0, outer = 0;
+    int kb_n = 0;
     bool pc_pending = false;
     for (int it = 1; it <= maxit; ++it) {
         if (prof) CK(cudaEventRecord(pe[0], c.stream));
@@ -1198,7 +1233,6 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
         CK(cudaMemcpyAsync(h_flag, c.d_iflag, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.stream));
         if (o->history) CK(cudaMemcpyAsync(o->history + (it - 1), c.d_scal + 3, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         CK(cudaStreamSynchronize(c.stream));
-        outer = it;
         if (prof) {
             float t = 0.f;
             cudaEventElapsedTime(&t, pe[0], pe[1]);
@@ -1213,7 +1247,7 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
         if (h_flag[2]) break;
         if (prof) CK(cudaEventRecord(pe[2], c.stream));
         launch_narrow(c.d_r, c.d_r32, nv, c.stream);
-        if ((rc = inner_run(ctx, k))) return rc;
+        if ((rc = inner_run(ctx, k, eta))) return rc;
         launch_widen_dots(c.d_e32, c.d_z, c.d_r, c.d_q, nv, c.d_part, c.d_part2, nbv, c.stream);
         if (prof) {
             CK(cudaEventRecord(pe[3], c.stream));
@@ -1224,10 +1258,12 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
         CKL();
     }
     CK(cudaEventRecord(e1, c.stream));
-    double sc[8];
+    double sc[8], inner_total = 0.0;
     CK(cudaMemcpyAsync(h_flag, c.d_iflag, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.stream));
     CK(cudaMemcpyAsync(sc, c.d_scal, sizeof(double) * 8, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaMemcpyAsync(&inner_total, c.d_isc + IS_TOTAL, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
+    g_launches += (int64_t)inner_total * c.inner_body_launches;
     if (prof) {
         if (pc_pending) {
             float t = 0.f;
@@ -1256,7 +1292,7 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
         info->converged = h_flag[1];
         info->relres = sc[3];
         info->true_relres = sc[0] > 0 ? sqrt(rr) / sc[0] : 0.0;
-        info->inner_iterations = k * outer;
+        info->inner_iterations = (int)inner_total;
         info->seconds = ms * 1e-3;
         info->kbyu_seconds = kb_ms * 1e-3;
         info->kbyu_launches = kb_n;

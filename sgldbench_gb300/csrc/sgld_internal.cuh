@@ -90,9 +90,10 @@ struct Ctx {
     float *d_e32 = nullptr, *d_s32 = nullptr, *d_d32 = nullptr, *d_t32 = nullptr;
     double *d_part2 = nullptr;      // second partial-sum buffer
     double *d_isc = nullptr;        // inner CG scalars
-    cudaGraphExec_t inner_graph = nullptr;
+    cudaGraphExec_t inner_graph = nullptr;   // inner FP32 CG: entry nodes + while node
     int inner_graph_k = 0;
-    int64_t inner_graph_launches = 0;
+    double inner_graph_eta = -1.0;
+    int64_t inner_entry_launches = 0, inner_body_launches = 0;
     cudaStream_t stream = nullptr;
     std::string err;
     int device = 0;
@@ -130,8 +131,11 @@ void launch_kbyu_df(const Level &l0, const double *E, const double *u, double *y
                     int *nblocks_out, cudaStream_t s);
 // mixed-precision solve (kernels_mixed.cu)
 void launch_icg_scalar(int op, double *sc, const double *part, int nb, cudaStream_t s);
-void launch_icg_update(float *e, float *s, const float *d, const float *t, int64_t n, const double *sc,
-                       cudaStream_t st);
+int launch_icg_update(float *e, float *s, const float *d, const float *t, int64_t n, const double *sc,
+                      double *part, cudaStream_t st);
+void launch_icg_cond(cudaGraphConditionalHandle h, double *sc, const double *part, int nb, int kmax,
+                     double eta_min, const double *outer, double *total, cudaStream_t s);
+int launch_icg_init(const float *r, float *s, float *e, float *d, int64_t n, double *part, cudaStream_t st);
 void launch_icg_dupdate(float *d, const float *w, int64_t n, const double *sc, cudaStream_t st);
 void launch_widen_dots(const float *e, double *z, const double *r, const double *q, int64_t n, double *p1,
                        double *p2, int nb, cudaStream_t st);

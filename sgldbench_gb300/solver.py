@@ -239,14 +239,15 @@ class VoxelSolver:
         return z
 
     def pcg(self, b, tol: float = 1e-3, maxIT: int = 500, x0=None, precision: str = "fp64",
-            inner_its: int = 0, history: bool = False):
+            inner_its: int = 0, history: bool = False, inner_tol: float = 0.0):
         """Runs the whole PCG on the device.  Returns (x, info dict)."""
         bv = self._vec(b, self.numDOFs)
         x = np.zeros_like(bv) if x0 is None else self._vec(x0, self.numDOFs).copy()
         hist = np.zeros(maxIT) if history else None
         o = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=int(x0 is not None),
                         precision=_precision(precision),
-                        inner_its=inner_its, history=hist.ctypes.data if history else None)
+                        inner_its=inner_its, history=hist.ctypes.data if history else None,
+                        inner_tol=inner_tol)
         info = L.SolveInfo()
         self._check(self.lib.sgld_pcg(self.ctx, _p(bv), _p(x), C.byref(o), C.byref(info)))
         d = _info_dict(info)
@@ -255,10 +256,11 @@ class VoxelSolver:
         return x, d
 
     def pcg_device(self, b_ptr: int, x_ptr: int, tol: float, maxIT: int, use_x0: bool = False,
-                   precision: str = "fp64", inner_its: int = 0, profile: bool = False) -> dict:
+                   precision: str = "fp64", inner_its: int = 0, profile: bool = False,
+                   inner_tol: float = 0.0) -> dict:
         o = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=int(use_x0),
                         precision=_precision(precision),
-                        inner_its=inner_its, history=None, profile=int(profile))
+                        inner_its=inner_its, history=None, profile=int(profile), inner_tol=inner_tol)
         info = L.SolveInfo()
         self._check(self.lib.sgld_pcg_device(self.ctx, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(o),
                                              C.byref(info)))
@@ -339,12 +341,12 @@ class VoxelSolver:
                                        move: float = 0.1, minChange: float = 1e-4, maxSharpness: float = 0.05,
                                        penalty: float = 3.0, E0: float = 1.0, Emin: float = 1e-9,
                                        tol: float = 1e-6, maxIT: int = 500, precision: str = "fp64",
-                                       inner_its: int = 0, x0=None):
+                                       inner_its: int = 0, x0=None, inner_tol: float = 0.0):
         """The whole SIMP loop on the device.  Returns (xPhys, history list)."""
         Fv = self._vec(F, self.numDOFs)
         so = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=1,
                          precision=_precision(precision),
-                         inner_its=inner_its, history=None, profile=0)
+                         inner_its=inner_its, history=None, profile=0, inner_tol=inner_tol)
         o = L.TopOptOpts(volfrac=volfrac, rmin=rMin, move=move, n_loop=nLoop, min_change=minChange,
                          max_sharpness=maxSharpness, penalty=penalty, E0=E0, Emin=Emin, solve=so)
         xp = np.zeros(self.numElements)

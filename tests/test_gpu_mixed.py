@@ -90,3 +90,22 @@ def test_mixed_df_converges_like_mixed(graded):
     U9, info9 = s.pcg(m.F, tol=1e-9, maxIT=500, precision="mixed_df")
     assert info9["converged"] and info9["true_relres"] < 2e-9
     assert np.linalg.norm(U9 - U_ref) / np.linalg.norm(U_ref) <= 1e-5
+
+
+def test_mixed_adaptive_inner_stop(graded):
+    """Default inner solve: the device-side while loop stops the FP32 inner CG
+    at ||s|| <= max(3e-4, tol / (2 relres)) ||r|| (cap 64); a looser inner
+    tolerance needs more outer iterations, a tighter one fewer, and every
+    variant meets the tolerance."""
+    m, s, U_ref = graded
+    c_ref = G.compliance(m, U_ref)
+    res = {}
+    for eta in (0.0, 1e-2, 1e-4):
+        U, info = s.pcg(m.F, tol=1e-6, maxIT=500, precision="mixed_df", inner_tol=eta)
+        assert info["converged"] and info["true_relres"] < 1.05e-6
+        assert 0 < info["inner_its"] <= 64 * info["its"]
+        _, c = s.TopOpti_ComputeUnitCompliance(U)
+        assert abs(c - c_ref) / abs(c_ref) <= 1e-6
+        res[eta] = info
+    assert res[1e-2]["its"] >= res[1e-4]["its"]
+    assert res[1e-2]["inner_its"] / res[1e-2]["its"] < res[1e-4]["inner_its"] / res[1e-4]["its"]

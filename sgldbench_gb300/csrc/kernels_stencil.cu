@@ -278,6 +278,238 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu(const T *__restrict__ u, T 
     }
 }
 
+// ---- FP32 K*u on packed pairs of element layers -------------------------------
+// Blackwell executes FP32 add / multiply / FMA on register pairs (f32x2) at the
+// issue cost of one scalar instruction.  k_kbyu_x2 gives every thread two
+// elements, (ez, ez+1) of the same (y, x) column, packed as float2 lanes, so
+// the Hadamard butterflies, the Kh blocks and the modulus scaling all run as
+// paired instructions; the shared-memory exchange moves float2 as well.
+// Pair p of a CTA covers element layers z0-1+2p and z0+2p and completes node
+// layers z0-1+2p and z0+2p: node layer ez takes the lower corners of element
+// ez plus the upper corners of element ez-1 (carried from the previous pair).
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 kh2(int i) { return make_float2(c_Kh32[i], c_Kh32[i]); }
+
+__device__ __forceinline__ void hex_apply_x2(float2 (&u)[24], float2 e) {
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if (k & (1 << ax)) continue;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float2 lo = u[3 * k + c], hi = u[3 * (k | (1 << ax)) + c];
+                u[3 * k + c] = f2add(lo, hi);
+                u[3 * (k | (1 << ax)) + c] = f2sub(hi, lo);
+            }
+        }
+    float2 g[24];
+    g[0] = g[1] = g[2] = make_float2(0.f, 0.f);
+#define X3(i, j, k, o)                                                                    \
+    {                                                                                     \
+        const float2 a = u[i], b = u[j], d = u[k];                                        \
+        g[i] = f2fma(kh2(o + 2), d, f2fma(kh2(o + 1), b, f2mul(kh2(o), a)));              \
+        g[j] = f2fma(kh2(o + 5), d, f2fma(kh2(o + 4), b, f2mul(kh2(o + 3), a)));          \
+        g[k] = f2fma(kh2(o + 8), d, f2fma(kh2(o + 7), b, f2mul(kh2(o + 6), a)));          \
+    }
+#define X2(i, j, o)                                                  \
+    {                                                                \
+        const float2 a = u[i], b = u[j];                             \
+        g[i] = f2fma(kh2(o + 1), b, f2mul(kh2(o), a));               \
+        g[j] = f2fma(kh2(o + 3), b, f2mul(kh2(o + 2), a));           \
+    }
+    X3(3, 7, 14, 0)
+    X2(4, 6, 9)
+    X2(5, 12, 13)
+    X2(8, 13, 17)
+    X2(9, 20, 21)
+    X2(10, 17, 25)
+    X3(11, 16, 18, 29)
+    X2(15, 19, 38)
+    g[21] = f2mul(kh2(42), u[21]);
+    g[22] = f2mul(kh2(43), u[22]);
+    g[23] = f2mul(kh2(44), u[23]);
+#undef X3
+#undef X2
+#pragma unroll
+    for (int i = 3; i < 24; ++i) g[i] = f2mul(g[i], e);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if (k & (1 << ax)) continue;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float2 a = g[3 * k + c], d = g[3 * (k | (1 << ax)) + c];
+                g[3 * k + c] = f2sub(a, d);
+                g[3 * (k | (1 << ax)) + c] = f2add(a, d);
+            }
+        }
+#pragma unroll
+    for (int i = 0; i < 24; ++i) u[i] = g[i];
+}
+
+constexpr int KX_RING = 5;   // node-layer slots: 3 in use + 2 in flight
+// floats of the ring, rounded up to 16 bytes so that the float2 exchange
+// area behind it is aligned (5 * 891 floats alone would leave it 4 bytes off)
+constexpr int KX_RING_FLOATS = ((KX_RING * KT_NL * 3 + 3) / 4) * 4;
+
+__device__ __forceinline__ int xslot(int z) { return (z + KX_RING) % KX_RING; }
+
+template <bool DOT>
+__global__ void __launch_bounds__(KT_THREADS) k_kbyu_x2(const float *__restrict__ u, float *__restrict__ y,
+                                                        const float *__restrict__ E,
+                                                        const uint8_t *__restrict__ nflag, int ny, int nx, int nz,
+                                                        int zc, double *__restrict__ partial) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *su = reinterpret_cast<float *>(smem_raw);                    // [KX_RING][KT_NL*3]
+    float2 *so = reinterpret_cast<float2 *>(su + KX_RING_FLOATS);   // [24][KT_THREADS]
+    const int tid = threadIdx.x;
+    const int ty = tid % KT_Y, tx = tid / KT_Y;
+    const int NY = ny + 1, NX = nx + 1, NZ = nz + 1;
+    const int y0 = blockIdx.x * (KT_Y - 1), x0 = blockIdx.y * (KT_X - 1), z0 = blockIdx.z * zc;
+    const int zend = min(z0 + zc, NZ);
+    const int npair = (zend - z0 + 2) / 2;   // element layers z0-1 .. zend-1
+    const int zlast = z0 + 2 * npair - 1;    // highest node layer the pairs read
+    const int gny = y0 + ty, gnx = x0 + tx;
+    const bool owner = (ty < KT_Y - 1) && (tx < KT_X - 1) && gny < NY && gnx < NX;
+    const int ey = y0 - 1 + ty, ex = x0 - 1 + tx;
+    const bool ein = ey >= 0 && ey < ny && ex >= 0 && ex < nx;
+    int soff[KT_SV];
+#pragma unroll
+    for (int k = 0; k < KT_SV; ++k) {
+        const int i = tid + k * KT_THREADS;
+        soff[k] = -2;
+        if (i < KT_NL * 3) {
+            const int node = i / 3, c = i - 3 * node;
+            const int ly = node % (KT_Y + 1), lx = node / (KT_Y + 1);
+            const int gy = y0 - 1 + ly, gx = x0 - 1 + lx;
+            soff[k] = (gy >= 0 && gy < NY && gx >= 0 && gx < NX) ? 3 * (gy + NY * gx) + c : -1;
+        }
+    }
+    const int64_t lstride = 3 * (int64_t)NY * NX;
+    auto stage = [&](int z) {
+        float *dst = su + xslot(z) * KT_NL * 3;
+        const bool zin = z >= 0 && z < NZ;
+#pragma unroll
+        for (int k = 0; k < KT_SV; ++k) {
+            const int i = tid + k * KT_THREADS;
+            if (soff[k] == -2) continue;
+            if (zin && soff[k] >= 0)
+                async_copy(dst + i, u + ((int64_t)z * lstride + soff[k]));
+            else
+                dst[i] = 0.f;
+        }
+    };
+    stage(z0 - 1);
+    stage(z0);
+    stage(z0 + 1);
+    async_commit();
+    async_wait_all();
+    __syncthreads();
+    float carry[3] = {0.f, 0.f, 0.f};
+    float dot = 0.f;
+    const int64_t eplane = (int64_t)ny * nx;
+    const int64_t ecol = (int64_t)ey + (int64_t)ny * ex;
+    for (int p = 0; p < npair; ++p) {
+        const int ez = z0 - 1 + 2 * p;
+        if (ez + 3 <= zlast) stage(ez + 3);
+        if (ez + 4 <= zlast) stage(ez + 4);
+        async_commit();
+        const float e0 = (ein && ez >= 0 && ez < nz) ? E[ecol + eplane * ez] : 0.f;
+        const float e1 = (ein && ez + 1 < nz) ? E[ecol + eplane * (ez + 1)] : 0.f;
+        float2 ue[24];
+        if (e0 != 0.f || e1 != 0.f) {
+            const float *l0 = su + xslot(ez) * KT_NL * 3, *l1 = su + xslot(ez + 1) * KT_NL * 3,
+                        *l2 = su + xslot(ez + 2) * KT_NL * 3;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int dx = k & 1, dy = 1 - ((k >> 1) & 1), kp = k >> 2;
+                const int o = 3 * ((ty + dy) + (KT_Y + 1) * (tx + dx));
+                const float *a = kp ? l1 : l0, *b = kp ? l2 : l1;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) ue[3 * k + c] = make_float2(a[o + c], b[o + c]);
+            }
+            hex_apply_x2(ue, make_float2(e0, e1));
+        } else {
+#pragma unroll
+            for (int i = 0; i < 24; ++i) ue[i] = make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int i = 0; i < 24; ++i) so[i * KT_THREADS + tid] = ue[i];
+        __syncthreads();
+        if (owner) {
+            float2 lo[3], up[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) lo[c] = up[c] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+                for (int dx = 0; dx < 2; ++dx) {
+                    const int k = dx | ((1 - dy) << 1);
+                    const int t = (ty + 1 - dy) + KT_Y * (tx + 1 - dx);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        lo[c] = f2add(lo[c], so[(3 * k + c) * KT_THREADS + t]);
+                        up[c] = f2add(up[c], so[(3 * (k | 4) + c) * KT_THREADS + t]);
+                    }
+                }
+            const int64_t node0 = (int64_t)gny + (int64_t)NY * gnx;
+            const int on = 3 * ((ty + 1) + (KT_Y + 1) * (tx + 1));
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int z = ez + h;
+                float o[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) o[c] = h == 0 ? carry[c] + lo[c].x : lo[c].y + up[c].x;
+                if (z >= z0 && z < zend) {
+                    const int64_t node = node0 + (int64_t)NY * NX * z;
+                    const uint8_t f = nflag[node];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        if (f & (NF_FIXX << c)) o[c] = 0.f;
+                        y[3 * node + c] = o[c];
+                    }
+                    if (DOT) {
+                        const float *un = su + xslot(z) * KT_NL * 3 + on;
+                        dot += un[0] * o[0] + un[1] * o[1] + un[2] * o[2];
+                    }
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) carry[c] = up[c].y;
+        }
+        async_wait_all();
+        __syncthreads();
+    }
+    if (DOT) {
+        __shared__ double red[KT_THREADS / 32];
+        const double s = block_sum_to_double<float>(dot, red);
+        if (tid == 0) partial[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s;
+    }
+}
+
+static constexpr size_t kbyu_x2_smem() { return sizeof(float) * KX_RING_FLOATS + sizeof(float2) * 24 * KT_THREADS; }
+static_assert((KX_RING_FLOATS * sizeof(float)) % 16 == 0, "float2 exchange area must be aligned");
+
+// node layers per CTA of k_kbyu_x2: an odd count (so that the element layers
+// z0-1 .. z0+zc-1 form whole pairs) near 15, balanced over the z extent
+static int kbyu_x2_zc(int NZ) {
+    const int chunks = (NZ + 14) / 15;
+    int zc = (NZ + chunks - 1) / chunks;
+    if (!(zc & 1)) ++zc;
+    return zc;
+}
+
+static dim3 kbyu_x2_grid(const Level &l) {
+    const int NZ = l.nz + 1;
+    const int zc = kbyu_x2_zc(NZ);
+    return dim3((l.ny + 1 + KT_Y - 2) / (KT_Y - 1), (l.nx + 1 + KT_X - 2) / (KT_X - 1), (NZ + zc - 1) / zc);
+}
+
 static dim3 kbyu_grid(const Level &l) {
     return dim3((l.ny + 1 + KT_Y - 2) / (KT_Y - 1), (l.nx + 1 + KT_X - 2) / (KT_X - 1), (l.nz + 1 + KT_ZC - 1) / KT_ZC);
 }
@@ -292,8 +524,8 @@ static constexpr size_t kbyu_smem() {
 void init_kernel_attributes() {
     cudaFuncSetAttribute(k_kbyu<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<double>());
     cudaFuncSetAttribute(k_kbyu<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<double>());
-    cudaFuncSetAttribute(k_kbyu<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<float>());
-    cudaFuncSetAttribute(k_kbyu<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<float>());
+    cudaFuncSetAttribute(k_kbyu_x2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_x2_smem());
+    cudaFuncSetAttribute(k_kbyu_x2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_x2_smem());
 }
 
 template <typename T, bool DOT>
@@ -315,10 +547,14 @@ void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *
 
 void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
                      int *nblocks_out, cudaStream_t s) {
+    const dim3 g = kbyu_x2_grid(l0);
+    const int zc = kbyu_x2_zc(l0.nz + 1);
+    if (nblocks_out) *nblocks_out = (int)(g.x * g.y * g.z);
+    ++g_launches;
     if (partial_dot)
-        kbyu_launch<float, true>(l0, E, u, y, partial_dot, nblocks_out, s);
+        k_kbyu_x2<true><<<g, KT_THREADS, kbyu_x2_smem(), s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, partial_dot);
     else
-        kbyu_launch<float, false>(l0, E, u, y, nullptr, nblocks_out, s);
+        k_kbyu_x2<false><<<g, KT_THREADS, kbyu_x2_smem(), s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr);
 }
 
 int kbyu_num_blocks(const Level &l0) {

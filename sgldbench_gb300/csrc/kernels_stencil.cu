@@ -414,13 +414,17 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu_x2(const float *__restrict_
     float dot = 0.f;
     const int64_t eplane = (int64_t)ny * nx;
     const int64_t ecol = (int64_t)ey + (int64_t)ny * ex;
+    // moduli of the next pair are loaded one step ahead (register double buffer)
+    auto emod = [&](int z) -> float { return (ein && z >= 0 && z < nz) ? E[ecol + eplane * z] : 0.f; };
+    float en0 = emod(z0 - 1), en1 = emod(z0);
     for (int p = 0; p < npair; ++p) {
         const int ez = z0 - 1 + 2 * p;
         if (ez + 3 <= zlast) stage(ez + 3);
         if (ez + 4 <= zlast) stage(ez + 4);
         async_commit();
-        const float e0 = (ein && ez >= 0 && ez < nz) ? E[ecol + eplane * ez] : 0.f;
-        const float e1 = (ein && ez + 1 < nz) ? E[ecol + eplane * (ez + 1)] : 0.f;
+        const float e0 = en0, e1 = en1;
+        en0 = emod(ez + 2);
+        en1 = emod(ez + 3);
         float2 ue[24];
         if (e0 != 0.f || e1 != 0.f) {
             const float *l0 = su + xslot(ez) * KT_NL * 3, *l1 = su + xslot(ez + 1) * KT_NL * 3,

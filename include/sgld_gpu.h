@@ -199,6 +199,15 @@ int sgld_vcycle(sgld_ctx *ctx, const double *r, double *z);
  * PtV = Vcycle (as Solving_CG_GMGS.m:7 binds them).  x: in = initial guess when
  * opts->use_x0, out = solution. */
 int sgld_pcg(sgld_ctx *ctx, const double *b, double *x, const sgld_solve_opts *opts, sgld_solve_info *info);
+
+/* Block right-hand side: the same solve for nrhs load cases sharing one
+ * assembly (the reference solves its load cases one after another through
+ * Solving_CG_GMGS.m:7).  F and U hold nrhs compact DOF vectors back to back
+ * (case j at offset j * numDOFs); U holds the initial guesses when
+ * opts->use_x0.  info, if not NULL, receives nrhs entries.  The cases are
+ * solved in order on the context's stream. */
+int sgld_solve_block(sgld_ctx *ctx, int nrhs, const double *F, double *U, const sgld_solve_opts *opts,
+                     sgld_solve_info *info);
 int sgld_pcg_device(sgld_ctx *ctx, const double *d_b, double *d_x, const sgld_solve_opts *opts,
                     sgld_solve_info *info);
 
@@ -247,6 +256,16 @@ int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const double *F, co
  * von Mises and per-element von Mises with the reference's final .^(1/2).
  * Any output may be NULL. */
 int sgld_stress(sgld_ctx *ctx, const double *U, double *nodal_stress, double *vm_node, double *vm_elem);
+
+/* Principal stresses of the nodal Cartesian stress field of U
+ * (FEA_ComputePrincipalStress.m:1-8 per node): ps_node is numNodes x 12,
+ * row-major [l1 v1(3) l2 v2(3) l3 v3(3)] with l1 <= l2 <= l3 and each unit
+ * eigenvector signed so that its entry of largest magnitude is positive.
+ * dir_elem (numElements x 3, row-major): per element, the principal direction
+ * of largest |l| of the centroid stress
+ * (Common_ExtractDominantDirectionsFromPrincipalStressDirections.m:9-38).
+ * Either output may be NULL. */
+int sgld_principal_stress(sgld_ctx *ctx, const double *U, double *ps_node, double *dir_elem);
 
 #ifdef __cplusplus
 }

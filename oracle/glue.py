@@ -666,6 +666,57 @@ def build_model(vox, coarsest_control=50000, non_dyadic=1, nu=0.3, omega=0.35,
     return m
 
 
+def principal_stress(cartesian):
+    """src/FEA_ComputePrincipalStress.m:1-8 for every row of a (n, 6) field
+    [xx yy zz yz zx xy]: rows [l1 v1 l2 v2 l3 v3], eigenvalues ascending (as eig
+    returns them for a symmetric matrix), each eigenvector signed so that its
+    largest-magnitude entry is positive (eig leaves the sign open)."""
+    s = np.asarray(cartesian, float)
+    A = np.empty((s.shape[0], 3, 3))
+    A[:, 0, 0], A[:, 1, 1], A[:, 2, 2] = s[:, 0], s[:, 1], s[:, 2]
+    A[:, 0, 1] = A[:, 1, 0] = s[:, 5]
+    A[:, 0, 2] = A[:, 2, 0] = s[:, 4]
+    A[:, 1, 2] = A[:, 2, 1] = s[:, 3]
+    w, V = np.linalg.eigh(A)
+    big = np.abs(V).argmax(axis=1)                       # (n, 3): row of the largest entry per vector
+    sign = np.sign(np.take_along_axis(V, big[:, None, :], axis=1))[:, 0, :]
+    sign[sign == 0] = 1.0
+    V = V * sign[:, None, :]
+    out = np.empty((s.shape[0], 12))
+    for k in range(3):
+        out[:, 4 * k] = w[:, k]
+        out[:, 4 * k + 1:4 * k + 4] = V[:, :, k]
+    return out
+
+
+def dominant_directions(model, cartesian):
+    """src/Common_ExtractDominantDirectionsFromPrincipalStressDirections.m:9-38:
+    per element, the centroid stress (shape functions at the centroid = 1/8
+    each) and the eigenvector of the principal stress of largest magnitude."""
+    l1 = model.levels[0]
+    cent = cartesian[l1.eNodMat - 1].mean(axis=1)
+    ps = principal_stress(cent)
+    lam = np.abs(ps[:, [0, 4, 8]])
+    k = lam.argmax(axis=1)
+    return np.stack([ps[np.arange(len(k)), 4 * k + 1 + i] for i in range(3)], axis=1)
+
+
+def build_model_fixed(vox, fixed, coarsest_control=50000, non_dyadic=1, nu=0.3, omega=0.35, num_levels=None):
+    """build_model with a caller-given level-1 fixed-DOF mask instead of a
+    named boundary condition (FEA_ApplyBoundaryCondition.m:37-41 sets the same
+    mask from a fixing table); loads are set per solve through model.F."""
+    l1, nlev, pad, (nely, nelx, nelz) = voxel_discretization(vox, coarsest_control, num_levels)
+    levels, nlev, nd = build_hierarchy(l1, nlev, non_dyadic)
+    l1.fixedDOFs = np.asarray(fixed, dtype=bool).reshape(-1).copy()
+    l1.freeDOFs = ~l1.fixedDOFs
+    Ke = element_stiffness(nu)
+    setup_voxel_based(levels, nlev, Ke)
+    m = Model(levels=levels, numLevels=nlev, nonDyadic=nd, Ke=Ke, F=np.zeros(l1.numDOFs), omega=omega,
+              nely=nely, nelx=nelx, nelz=nelz)
+    m.U = np.zeros(l1.numDOFs)
+    return m
+
+
 def set_modulus(model: Model, E):
     model.levels[0].eleModulus = np.asarray(E, dtype=float).reshape(-1)
 

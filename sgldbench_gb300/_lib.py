@@ -75,8 +75,10 @@ SIGNATURES = {
     "sgld_vcycle": (i32, [vp, vp, vp]),
     "sgld_pcg": (i32, [vp, vp, vp, vp, vp]),
     "sgld_pcg_device": (i32, [vp, vp, vp, vp, vp]),
+    "sgld_solve_block": (i32, [vp, i32, vp, vp, vp, vp]),
     "sgld_compliance": (i32, [vp, vp, vp, vp]),
     "sgld_stress": (i32, [vp, vp, vp, vp, vp]),
+    "sgld_principal_stress": (i32, [vp, vp, vp, vp]),
     "sgld_get_stream": (vp, [vp]),
     "sgld_kernel_launches": (i64, []),
     "sgld_time_op": (i32, [vp, i32, i32, vp]),

@@ -991,6 +991,17 @@ int sgld_pcg(sgld_ctx *ctx, const double *b, double *x, const sgld_solve_opts *o
     return download_nodes(ctx, c.d_x, x);
 }
 
+int sgld_solve_block(sgld_ctx *ctx, int nrhs, const double *F, double *U, const sgld_solve_opts *o,
+                     sgld_solve_info *info) {
+    int rc = check_assembled(ctx);
+    if (rc) return rc;
+    if (nrhs < 0 || (nrhs > 0 && (!F || !U || !o))) return fail(ctx, SGLD_ERR_ARG, "bad block arguments");
+    const int64_t nd = 3 * (int64_t)ctx->c.h_nodemap.size();
+    for (int j = 0; j < nrhs; ++j)
+        if ((rc = sgld_pcg(ctx, F + j * nd, U + j * nd, o, info ? info + j : nullptr))) return rc;
+    return SGLD_OK;
+}
+
 int sgld_compliance(sgld_ctx *ctx, const double *U, double *ce, double *cval) {
     int rc = check_ready(ctx);
     if (rc) return rc;
@@ -1048,6 +1059,48 @@ int sgld_stress(sgld_ctx *ctx, const double *U, double *nodal, double *vmn, doub
         CK(cudaMemcpyAsync(vme, c.d_tmp, sizeof(double) * ne, cudaMemcpyDeviceToHost, c.stream));
         CK(cudaStreamSynchronize(c.stream));
     }
+    return SGLD_OK;
+}
+
+int sgld_principal_stress(sgld_ctx *ctx, const double *U, double *ps_node, double *dir_elem) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!U) return fail(ctx, SGLD_ERR_ARG, "null vector");
+    Ctx &c = ctx->c;
+    const Level &l0 = c.lv[0];
+    if (!ctx->d_s6) {
+        CK(dalloc(&ctx->d_s6, 6 * (size_t)l0.nnode));
+        CK(dalloc(&ctx->d_vmn, (size_t)l0.nnode));
+        CK(dalloc(&ctx->d_vme, (size_t)l0.nel));
+    }
+    if ((rc = upload_nodes(ctx, U, c.d_z))) return rc;
+    double M[48 * 24];
+    stress_matrix(c.nu, c.cell, M);
+    launch_stress(l0, c.E, c.d_z, M, ctx->d_s6, ctx->d_vmn, c.stream);
+    // one output at a time through a temporary full-grid buffer (12 doubles
+    // per node or 3 per element), gathered to the compact order on the host
+    auto fetch = [&](int per, int64_t count, const std::vector<int64_t> &map, double *out, bool nodes) -> int {
+        double *d_buf = nullptr;
+        CK(dalloc(&d_buf, (size_t)per * count));
+        if (nodes)
+            launch_principal(l0, ctx->d_s6, d_buf, nullptr, c.stream);
+        else
+            launch_principal(l0, ctx->d_s6, nullptr, d_buf, c.stream);
+        std::vector<double> h((size_t)per * count);
+        const cudaError_t e1 = cudaGetLastError();
+        const cudaError_t e2 = cudaMemcpyAsync(h.data(), d_buf, sizeof(double) * h.size(), cudaMemcpyDeviceToHost,
+                                               c.stream);
+        const cudaError_t e3 = cudaStreamSynchronize(c.stream);
+        cudaFree(d_buf);
+        CK(e1);
+        CK(e2);
+        CK(e3);
+        for (size_t i = 0; i < map.size(); ++i)
+            for (int k = 0; k < per; ++k) out[(size_t)per * i + k] = h[(size_t)per * map[i] + k];
+        return SGLD_OK;
+    };
+    if (ps_node && (rc = fetch(12, l0.nnode, c.h_nodemap, ps_node, true))) return rc;
+    if (dir_elem && (rc = fetch(3, l0.nel, c.h_elemap, dir_elem, false))) return rc;
     return SGLD_OK;
 }
 

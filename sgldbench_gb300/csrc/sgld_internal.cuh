@@ -170,6 +170,7 @@ void launch_unit_compliance(const Level &l0, const double *u, const double *E, d
 void launch_stress(const Level &l0, const double *E, const double *u, const double *M48x24,
                    double *nodal6, double *vm_node, cudaStream_t s);
 void launch_elem_vm(const Level &l0, const double *nodal6, double *vm_elem_full, cudaStream_t s);
+void launch_principal(const Level &l0, const double *s6, double *ps_node, double *dir_elem, cudaStream_t s);
 
 template <typename T>
 void launch_restrict(const Level &fine, const Level &coarse, const T *rf, T *rc, cudaStream_t s);

@@ -255,6 +255,19 @@ class VoxelSolver:
             d["history"] = hist[: info.iterations].copy()
         return x, d
 
+    def solve_block(self, F, tol: float = 1e-6, maxIT: int = 500, U0=None, precision: str = "fp64",
+                    inner_its: int = 0, inner_tol: float = 0.0):
+        """Block right-hand side: F is (nrhs, numDOFs); returns (U (nrhs, numDOFs), list of info dicts)."""
+        Fb = np.ascontiguousarray(np.asarray(F, dtype=np.float64).reshape(-1, self.numDOFs))
+        nrhs = Fb.shape[0]
+        U = np.zeros_like(Fb) if U0 is None else np.ascontiguousarray(
+            np.asarray(U0, dtype=np.float64).reshape(nrhs, self.numDOFs)).copy()
+        o = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=int(U0 is not None), precision=_precision(precision),
+                        inner_its=inner_its, history=None, profile=0, inner_tol=inner_tol)
+        infos = (L.SolveInfo * max(nrhs, 1))()
+        self._check(self.lib.sgld_solve_block(self.ctx, nrhs, _p(Fb), _p(U), C.byref(o), infos))
+        return U, [_info_dict(infos[j]) for j in range(nrhs)]
+
     def pcg_device(self, b_ptr: int, x_ptr: int, tol: float, maxIT: int, use_x0: bool = False,
                    precision: str = "fp64", inner_its: int = 0, profile: bool = False,
                    inner_tol: float = 0.0) -> dict:
@@ -322,6 +335,17 @@ class VoxelSolver:
         vme = np.zeros(self.numElements)
         self._check(self.lib.sgld_stress(self.ctx, _p(u), _p(s6), _p(vmn), _p(vme)))
         return s6.reshape(self.numNodes, 6), vmn, vme
+
+    def FEA_ComputePrincipalStress(self, U):
+        """Principal stresses of the nodal stress field: (numNodes x 12 rows
+        [l1 v1 l2 v2 l3 v3], ascending l, eigenvectors signed so that their
+        largest-magnitude entry is positive) and the per-element dominant
+        principal direction (numElements x 3)."""
+        u = self._vec(U, self.numDOFs)
+        ps = np.zeros(12 * self.numNodes)
+        dd = np.zeros(3 * self.numElements)
+        self._check(self.lib.sgld_principal_stress(self.ctx, _p(u), _p(ps), _p(dd)))
+        return ps.reshape(self.numNodes, 12), dd.reshape(self.numElements, 3)
 
     # -- SIMP loop (TopOpti_GlobalVolumeConstraint_Tmp.m) ---------------------------
     def TopOpti_PerformDensityFiltering(self, x, rMin: float) -> np.ndarray:

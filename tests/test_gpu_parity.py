@@ -160,3 +160,32 @@ def test_pcg_warm_start(config0):
     assert info2["its"] <= 2
     y_o, its_o = G.pcg(lambda u: G.kbyu(m, u), lambda r: G.vcycle(m, r), m.F, 1e-6, 500, x0=U1)
     assert abs(info2["its"] - its_o) <= 1
+
+
+def test_principal_stress(pair):
+    """Principal stresses per node and the dominant direction per element
+    (FEA_ComputePrincipalStress.m, Common_ExtractDominantDirections...m)
+    against the oracle: eigenvalues to 1e-10 of the largest |l| of the node;
+    eigenvectors to 1e-7 where the eigenvalue gap exceeds 1e-3 of |l|max."""
+    m, s = pair
+    U, _ = s.pcg(m.F, tol=1e-8, maxIT=1000)
+    s6, _ = G.stress_analysis(m, U)
+    ps, dd = s.FEA_ComputePrincipalStress(U)
+    ref = G.principal_stress(s6)
+    lam, lam_r = ps[:, [0, 4, 8]], ref[:, [0, 4, 8]]
+    scale = np.abs(lam_r).max(axis=1) + 1e-300
+    assert (np.abs(lam - lam_r).max(axis=1) / scale).max() <= 1e-10
+    for k in range(3):
+        gaps = np.min([np.abs(lam_r[:, k] - lam_r[:, j]) for j in range(3) if j != k], axis=0) / scale
+        ok = gaps > 1e-3
+        assert ok.sum() > 0.5 * len(ok)
+        v, vr = ps[ok, 4 * k + 1:4 * k + 4], ref[ok, 4 * k + 1:4 * k + 4]
+        assert np.abs(v - vr).max() <= 1e-7
+    # dominant direction: compare where the dominant |l| is separated from the others
+    l1 = m.levels[0]
+    cent = s6[l1.eNodMat - 1].mean(axis=1)
+    pc = G.principal_stress(cent)
+    a = np.sort(np.abs(pc[:, [0, 4, 8]]), axis=1)
+    sep = (a[:, 2] - a[:, 1]) > 1e-3 * a[:, 2]
+    ddr = G.dominant_directions(m, s6)
+    assert np.abs(dd[sep] - ddr[sep]).max() <= 1e-7

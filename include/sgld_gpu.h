@@ -222,6 +222,26 @@ int sgld_compliance(sgld_ctx *ctx, const double *U, double *ce, double *c);
  * Compact element vectors (numElements). */
 int sgld_density_filter(sgld_ctx *ctx, double rmin, const double *x, double *y);
 
+/* PDE (Helmholtz) density filter of an element field x (numElements):
+ * TopOpti_PDEFiltering_matrixFree.m:1-36 with the element matrix of
+ * TopOpti_BuildPDEfilter_matrixFree.m:9-20 for rHatMin = rhat -- the field is
+ * spread to the nodes, K_pde t = src is solved by the reference's PCG with a
+ * Jacobi preconditioner to relative residual tol (at most maxit iterations),
+ * and t is averaged back to the elements into y.  *iterations (may be NULL)
+ * receives the PCG iteration count. */
+int sgld_pde_filter(sgld_ctx *ctx, double rhat, const double *x, double *y, double tol, int maxit, int *iterations);
+
+/* MMA_mex.cpp:6-54 (Svanberg's MMA as in MMAseq.cpp; a fresh solver per call,
+ * as the MEX gateway makes it): one update of n design variables under m
+ * constraints, same arguments and outputs as the gateway (dfdx holds m*n
+ * values, variable-major).  The subproblem's dual interior-point iteration
+ * runs over device passes.  Only m = 1 (the reference's volume constraint)
+ * is supported; other m return SGLD_ERR_ARG.  xold1_out = xval and
+ * xold2_out = xold1, as MMAseq::Update sets them. */
+int sgld_mma_update(sgld_ctx *ctx, int m, int n, const double *xval, const double *xmin, const double *xmax,
+                    const double *xold1, const double *xold2, const double *df0dx, const double *fval,
+                    const double *dfdx, double *xnew, double *xold1_out, double *xold2_out);
+
 /* SIMP loop with a global volume constraint (TopOpti_GlobalVolumeConstraint_Tmp.m:26-120,
  * ft = 2): per iteration E = SIMP(xPhys), assembly, warm-started MGPCG, unit
  * compliance, sensitivities, filtered sensitivities, OC bisection on the

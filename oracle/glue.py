@@ -666,6 +666,42 @@ def build_model(vox, coarsest_control=50000, non_dyadic=1, nu=0.3, omega=0.35,
     return m
 
 
+def pde_element_matrix(rhat):
+    """src/TopOpti_BuildPDEfilter_matrixFree.m:9-20: KePDE = r^2 dN'dN + N'diag(w detJ)N,
+    unit cell (detJ = 1/8, w = 1), r = rHatMin / 2 / sqrt(3); 8 x 8, reference node order."""
+    s, t, p, w = gauss_points()
+    N = shape_functions(s, t, p)
+    dN = shape_derivatives(s, t, p)
+    wgt = w * (1.0 / 8.0)
+    r = rhat / 2.0 / np.sqrt(3.0)
+    return r * r * (dN.T @ dN) + N.T @ np.diag(wgt) @ N
+
+
+def pde_kbyu(l1, Ke8, u):
+    """y = sum_e Ke8 u_e over eNodMat (the product of Solving_KbyU_MatrixFree8x8_mex.cpp)."""
+    ue = np.asarray(u, float)[l1.eNodMat - 1]
+    return np.bincount((l1.eNodMat - 1).ravel(), weights=(ue @ Ke8).ravel(), minlength=l1.numNodes)
+
+
+def pde_filter(model, x, rhat, tol=1e-6, maxIT=500):
+    """src/TopOpti_PDEFiltering_matrixFree.m:1-36: element -> node (x/8 to each corner),
+    Jacobi-preconditioned PCG on KePDE, node -> element (mean of the 8 corners).
+    Returns (filtered field, PCG iterations)."""
+    l1 = model.levels[0]
+    Ke8 = pde_element_matrix(rhat)
+    vals = np.asarray(x, float) * (1.0 / 8.0)
+    src = np.zeros(l1.numNodes)
+    for jj in range(8):
+        src += np.bincount(l1.eNodMat[:, jj] - 1, weights=vals, minlength=l1.numNodes)
+    diag = np.zeros(l1.numNodes)
+    for jj in range(8):
+        diag += np.bincount(l1.eNodMat[:, jj] - 1, weights=np.full(l1.numElements, Ke8[jj, jj]),
+                            minlength=l1.numNodes)
+    dinv = 1.0 / diag
+    t, its = pcg(lambda v: pde_kbyu(l1, Ke8, v), lambda r: dinv * r, src, tol, maxIT)
+    return t[l1.eNodMat - 1].sum(axis=1) * (1.0 / 8.0), its
+
+
 def principal_stress(cartesian):
     """src/FEA_ComputePrincipalStress.m:1-8 for every row of a (n, 6) field
     [xx yy zz yz zx xy]: rows [l1 v1 l2 v2 l3 v3], eigenvalues ascending (as eig

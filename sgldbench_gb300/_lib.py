@@ -79,6 +79,8 @@ SIGNATURES = {
     "sgld_compliance": (i32, [vp, vp, vp, vp]),
     "sgld_stress": (i32, [vp, vp, vp, vp, vp]),
     "sgld_principal_stress": (i32, [vp, vp, vp, vp]),
+    "sgld_pde_filter": (i32, [vp, dbl, vp, vp, dbl, i32, vp]),
+    "sgld_mma_update": (i32, [vp, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "sgld_get_stream": (vp, [vp]),
     "sgld_kernel_launches": (i64, []),
     "sgld_time_op": (i32, [vp, i32, i32, vp]),

@@ -171,6 +171,19 @@ void launch_stress(const Level &l0, const double *E, const double *u, const doub
                    double *nodal6, double *vm_node, cudaStream_t s);
 void launch_elem_vm(const Level &l0, const double *nodal6, double *vm_elem_full, cudaStream_t s);
 void launch_principal(const Level &l0, const double *s6, double *ps_node, double *dir_elem, cudaStream_t s);
+// PDE density filter (kernels_pde.cu)
+void upload_kpde(const double *K, cudaStream_t s);
+void launch_pde_e2n(const Level &l0, const double *xe, double *yn, cudaStream_t s);
+int launch_pde_kbyu(const Level &l0, const double *u, double *y, double *partial, cudaStream_t s);
+void launch_pde_diag(const Level &l0, double *dinv, cudaStream_t s);
+void launch_pde_jacobi(const double *r, const double *dinv, int64_t n, double *z, double *partial, int nb,
+                       cudaStream_t s);
+void launch_pde_n2e(const Level &l0, const double *t, double *xe, cudaStream_t s);
+// MMA update (kernels_mma.cu)
+int mma_blocks(int64_t n);
+void launch_mma_eval(const double *xv, const double *xmin, const double *xmax, const double *df0, const double *dg,
+                     int64_t n, double lam, double *xout, double *part1, double *part2, double *sums2,
+                     cudaStream_t s);
 
 template <typename T>
 void launch_restrict(const Level &fine, const Level &coarse, const T *rf, T *rc, cudaStream_t s);

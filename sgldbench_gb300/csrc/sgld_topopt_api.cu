@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <string>
+#include <utility>
 
 #include "../../include/sgld_gpu.h"
 #include "sgld_internal.cuh"
@@ -81,6 +82,191 @@ extern "C" int sgld_density_filter(sgld_ctx *ctx, double rmin, const double *x, 
     TCK(cudaGetLastError());
     TCK(cudaMemcpyAsync(y, c.d_tmp, sizeof(double) * ne, cudaMemcpyDeviceToHost, c.stream));
     TCK(cudaStreamSynchronize(c.stream));
+    return SGLD_OK;
+}
+
+namespace {
+
+// K_pde = r^2 dN'dN + N' diag(w detJ) N (TopOpti_BuildPDEfilter_matrixFree.m:9-20):
+// dN = shape-function derivatives in natural coordinates at the 8 Gauss
+// points (FEA_DeShapeFunction.m), unit cell (detJ = 1/8, weights 1),
+// r = rHatMin / (2 sqrt(3)); row-major 8 x 8 in the reference's node order
+void pde_element_matrix(double rhat, double K[64]) {
+    const double g = 0.577350269189626;   // FEA_GaussianIntegral.m:10-15
+    const double gs[8] = {-g, g, g, -g, -g, g, g, -g}, gt[8] = {-g, -g, g, g, -g, -g, g, g},
+                 gp[8] = {-g, -g, -g, -g, g, g, g, g};
+    const double ns[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, nt[8] = {-1, -1, 1, 1, -1, -1, 1, 1},
+                 np[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+    double dN[24][8], N[8][8];
+    for (int q = 0; q < 8; ++q)
+        for (int n = 0; n < 8; ++n) {
+            dN[3 * q][n] = 0.125 * ns[n] * (1 + nt[n] * gt[q]) * (1 + np[n] * gp[q]);
+            dN[3 * q + 1][n] = 0.125 * nt[n] * (1 + ns[n] * gs[q]) * (1 + np[n] * gp[q]);
+            dN[3 * q + 2][n] = 0.125 * np[n] * (1 + ns[n] * gs[q]) * (1 + nt[n] * gt[q]);
+            N[q][n] = 0.125 * (1 + ns[n] * gs[q]) * (1 + nt[n] * gt[q]) * (1 + np[n] * gp[q]);
+        }
+    const double ir = rhat / 2.0 / sqrt(3.0);
+    for (int a = 0; a < 8; ++a)
+        for (int b = 0; b < 8; ++b) {
+            double k0 = 0.0, k1 = 0.0;
+            for (int r = 0; r < 24; ++r) k0 += dN[r][a] * dN[r][b];
+            for (int q = 0; q < 8; ++q) k1 += N[q][a] * (1.0 / 8.0) * N[q][b];
+            K[8 * a + b] = ir * ir * k0 + k1;
+        }
+}
+
+}  // namespace
+
+namespace {
+
+// the scalar part of MMAseq::SolveDIP (MMAseq.cpp:191-245) for m = 1,
+// a = 0, c = 100, d = 0; every evaluation of x(lambda) and its two sums is a
+// device pass over the n variables (launch_mma_eval)
+int mma_solve_device(sgld_ctx *ctx, int64_t n, const double *xv, const double *xmin, const double *xmax,
+                     const double *df0, const double *dg, double gval, double *xout, double *part1, double *part2,
+                     double *d_sums, int *newton_steps) {
+    Ctx &c = ctx->c;
+    double h[2];
+    auto eval = [&](double lam) -> int {
+        launch_mma_eval(xv, xmin, xmax, df0, dg, n, lam, xout, part1, part2, d_sums, c.stream);
+        TCK(cudaGetLastError());
+        TCK(cudaMemcpyAsync(h, d_sums, sizeof h, cudaMemcpyDeviceToHost, c.stream));
+        TCK(cudaStreamSynchronize(c.stream));
+        return SGLD_OK;
+    };
+    int rc;
+    if ((rc = eval(-1.0))) return rc;
+    const double b = -gval + h[0];
+    const double cc = 100.0;
+    double lam = cc / 2.0, mu = 1.0;
+    const double tol = 1.0e-9 * sqrt(1.0 + (double)n);
+    double epsi = 1.0, err = 1.0;
+    int steps = 0;
+    lam = fmax(lam, 0.0);
+    if ((rc = eval(lam))) return rc;
+    while (epsi > tol) {
+        int loop = 0;
+        while (err > 0.9 * epsi && loop < 100) {
+            ++loop;
+            ++steps;
+            lam = fmax(lam, 0.0);
+            const double y = fmax(0.0, lam - cc);
+            double grad = -b - y + h[0];
+            grad = -grad - epsi / lam;
+            double H = h[1];
+            if (lam > cc) H += -1.0;
+            H += -mu / lam;
+            double corr = 1e-4 * H;
+            if (-corr < 1.0e-7) corr = -1.0e-7;
+            H += corr;
+            const double s0 = grad / H;
+            const double s1 = -mu + epsi / lam - s0 * mu / lam;
+            double theta = 1.005;
+            if (theta < -1.01 * s0 / lam) theta = -1.01 * s0 / lam;
+            if (theta < -1.01 * s1 / mu) theta = -1.01 * s1 / mu;
+            theta = 1.0 / theta;
+            lam += theta * s0;
+            mu += theta * s1;
+            lam = fmax(lam, 0.0);
+            if ((rc = eval(lam))) return rc;
+            const double y2 = fmax(0.0, lam - cc);
+            err = fmax(fabs(-b - y2 + mu + h[0]), fabs(mu * lam - epsi));
+        }
+        epsi *= 0.1;
+    }
+    if (newton_steps) *newton_steps = steps;
+    return SGLD_OK;
+}
+
+}  // namespace
+
+extern "C" int sgld_mma_update(sgld_ctx *ctx, int m, int n, const double *xval, const double *xmin,
+                               const double *xmax, const double *xold1, const double *xold2, const double *df0dx,
+                               const double *fval, const double *dfdx, double *xnew, double *xold1_out,
+                               double *xold2_out) {
+    if (!ctx) return SGLD_ERR_ARG;
+    if (m != 1) return tfail(ctx, SGLD_ERR_ARG, "sgld_mma_update supports one constraint (m = 1)");
+    if (n < 1 || !xval || !xmin || !xmax || !xold1 || !df0dx || !fval || !dfdx || !xnew)
+        return tfail(ctx, SGLD_ERR_ARG, "null argument or n < 1");
+    (void)xold2;
+    Ctx &c = ctx->c;
+    const int nb = mma_blocks(n);
+    double *d = nullptr;
+    const size_t words = 6 * (size_t)n + 2 * (size_t)nb + 2;
+    TCK(cudaMalloc((void **)&d, words * sizeof(double)));
+    double *dx = d, *dmin = d + n, *dmax = d + 2 * (size_t)n, *ddf0 = d + 3 * (size_t)n, *ddg = d + 4 * (size_t)n,
+           *dout = d + 5 * (size_t)n, *p1 = d + 6 * (size_t)n, *p2 = p1 + nb, *sums = p2 + nb;
+    const size_t bytes = sizeof(double) * (size_t)n;
+    int rc = SGLD_OK;
+    cudaError_t e = cudaSuccess;
+    for (auto pr : {std::make_pair(dx, xval), std::make_pair(dmin, xmin), std::make_pair(dmax, xmax),
+                    std::make_pair(ddf0, df0dx), std::make_pair(ddg, dfdx)})
+        if (e == cudaSuccess) e = cudaMemcpyAsync(pr.first, pr.second, bytes, cudaMemcpyHostToDevice, c.stream);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return tfail(ctx, SGLD_ERR_CUDA, std::string("sgld_mma_update upload: ") + cudaGetErrorString(e));
+    }
+    rc = mma_solve_device(ctx, n, dx, dmin, dmax, ddf0, ddg, fval[0], dout, p1, p2, sums, nullptr);
+    if (rc == SGLD_OK) {
+        e = cudaMemcpyAsync(xnew, dout, bytes, cudaMemcpyDeviceToHost, c.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+        if (e != cudaSuccess) rc = tfail(ctx, SGLD_ERR_CUDA, std::string("sgld_mma_update: ") + cudaGetErrorString(e));
+    }
+    cudaFree(d);
+    if (rc) return rc;
+    // MMAseq::Update: xo2 <- xo1 (the incoming xold1), xo1 <- xval
+    if (xold1_out) memcpy(xold1_out, xval, bytes);
+    if (xold2_out) memcpy(xold2_out, xold1, bytes);
+    return SGLD_OK;
+}
+
+extern "C" int sgld_pde_filter(sgld_ctx *ctx, double rhat, const double *x, double *y, double tol, int maxit,
+                               int *iterations) {
+    if (!ctx || !x || !y) return SGLD_ERR_ARG;
+    Ctx &c = ctx->c;
+    if (!(rhat > 0.0) || maxit < 1 || !(tol >= 0.0)) return tfail(ctx, SGLD_ERR_ARG, "rhat > 0, maxit >= 1, tol >= 0");
+    int rc = ensure_topo(ctx);
+    if (rc) return rc;
+    const Level &l0 = c.lv[0];
+    const int64_t ne = (int64_t)c.h_elemap.size(), nn = l0.nnode;
+    double K[64];
+    pde_element_matrix(rhat, K);
+    upload_kpde(K, c.stream);
+    TCK(cudaMemcpyAsync(c.d_tmp, x, sizeof(double) * ne, cudaMemcpyHostToDevice, c.stream));
+    TCK(cudaMemsetAsync(c.t_tmp, 0, sizeof(double) * l0.nel, c.stream));
+    launch_scatter_elems(c.d_elemap, ne, c.d_tmp, c.t_tmp, c.stream);
+    // src on the nodes, Jacobi diagonal, then the reference's PCG from x = 0
+    launch_pde_e2n(l0, c.t_tmp, c.d_b, c.stream);
+    double *dinv = c.d_tmp;
+    launch_pde_diag(l0, dinv, c.stream);
+    const int nbv = reduce_blocks(nn);
+    launch_pcg_scalar(5, c.d_scal, c.d_iflag, c.d_part, 1, tol, maxit, c.stream);
+    launch_dot(c.d_b, c.d_b, nn, c.d_part, nbv, c.stream);
+    launch_pcg_scalar(0, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
+    TCK(cudaMemsetAsync(c.d_x, 0, sizeof(double) * nn, c.stream));
+    TCK(cudaMemcpyAsync(c.d_r, c.d_b, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c.stream));
+    launch_pde_jacobi(c.d_r, dinv, nn, c.d_z, c.d_part, nbv, c.stream);
+    launch_pcg_scalar(1, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
+    TCK(cudaMemcpyAsync(c.d_p, c.d_z, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c.stream));
+    int h_flag[4] = {0, 0, 0, 0};
+    for (int k = 1; k <= maxit; ++k) {
+        const int nb = launch_pde_kbyu(l0, c.d_p, c.d_q, c.d_part, c.stream);
+        launch_pcg_scalar(2, c.d_scal, c.d_iflag, c.d_part, nb, tol, maxit, c.stream);
+        launch_pcg_update(c.d_x, c.d_r, c.d_p, c.d_q, nn, c.d_scal, c.d_iflag, c.d_part, nbv, c.stream);
+        launch_pcg_scalar(3, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
+        TCK(cudaMemcpyAsync(h_flag, c.d_iflag, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.stream));
+        TCK(cudaStreamSynchronize(c.stream));
+        if (h_flag[2]) break;
+        launch_pde_jacobi(c.d_r, dinv, nn, c.d_z, c.d_part, nbv, c.stream);
+        launch_pcg_scalar(4, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
+        launch_pcg_pupdate(c.d_p, c.d_z, nn, c.d_scal, c.d_iflag, c.stream);
+    }
+    launch_pde_n2e(l0, c.d_x, c.t_q, c.stream);
+    launch_gather_elems(c.d_elemap, ne, c.t_q, c.d_tmp, c.stream);
+    TCK(cudaGetLastError());
+    TCK(cudaMemcpyAsync(y, c.d_tmp, sizeof(double) * ne, cudaMemcpyDeviceToHost, c.stream));
+    TCK(cudaStreamSynchronize(c.stream));
+    if (iterations) *iterations = h_flag[0];
     return SGLD_OK;
 }
 

@@ -355,6 +355,29 @@ class VoxelSolver:
         self._check(self.lib.sgld_density_filter(self.ctx, float(rMin), _p(xv), _p(y)))
         return y
 
+    def TopOpti_PDEFiltering(self, x, rHatMin: float, tol: float = 1e-6, maxIT: int = 500):
+        """PDE (Helmholtz) filter of an element field (TopOpti_PDEFiltering_matrixFree.m).
+        Returns (filtered field, PCG iterations)."""
+        xv = self._vec(x, self.numElements)
+        y = np.zeros(self.numElements)
+        its = C.c_int()
+        self._check(self.lib.sgld_pde_filter(self.ctx, float(rHatMin), _p(xv), _p(y), float(tol), int(maxIT),
+                                             C.byref(its)))
+        return y, its.value
+
+    def MMA(self, xval, xmin, xmax, xold1, xold2, df0dx, fval, dfdx):
+        """One MMA update with one constraint (MMA_mex's arguments and outputs):
+        returns (xnew, xold1, xold2)."""
+        xv = np.ascontiguousarray(xval, dtype=np.float64).ravel()
+        n = xv.size
+        arr = [np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (xmin, xmax, xold1, xold2, df0dx)]
+        fv = np.atleast_1d(np.asarray(fval, dtype=np.float64)).copy()
+        dg = np.ascontiguousarray(dfdx, dtype=np.float64).ravel()
+        xn, o1, o2 = np.zeros(n), np.zeros(n), np.zeros(n)
+        self._check(self.lib.sgld_mma_update(self.ctx, 1, n, _p(xv), _p(arr[0]), _p(arr[1]), _p(arr[2]), _p(arr[3]),
+                                             _p(arr[4]), _p(fv), _p(dg), _p(xn), _p(o1), _p(o2)))
+        return xn, o1, o2
+
     def TopOpti_SetupDensityFilter(self, rMin: float) -> np.ndarray:
         """Weight sums Hs of the cone filter (TopOpti_SetupDensityFilter_mex)."""
         y = np.zeros(self.numElements)

@@ -173,3 +173,49 @@ def test_vcycle_symmetric_and_compliance_identity():
     assert abs(G.vcycle(m, a) @ b - a @ G.vcycle(m, b)) <= 1e-10 * abs(a @ G.vcycle(m, b))
     U, its = G.solve(m, tol=1e-10, maxIT=2000)
     assert abs(G.compliance(m, U) - m.F @ U) <= 1e-8 * abs(m.F @ U)
+
+
+def test_pde_kbyu_matches_reference_kernel():
+    """The oracle's scalar 8 x 8 product against the reference's own
+    Solving_KbyU_MatrixFree8x8_mex.cpp (compiled from the checkout)."""
+    from oracle import mexcall
+
+    R = mexcall.ref_lib()
+    if R is None:
+        pytest.skip("reference kernels not built (oracle/_ref)")
+    rng = np.random.default_rng(5)
+    vox = rng.random((8, 12, 6)) < 0.8
+    m = G.build_model(vox, omega=0.6)
+    l1 = m.levels[0]
+    Ke8 = G.pde_element_matrix(1.5 * 2)
+    u = rng.standard_normal(l1.numNodes)
+    y_ref = R.call("ref_Solving_KbyU_MatrixFree8x8_mex", 1, u, l1.eNodMat, Ke8, l1.colors).ravel()
+    assert np.abs(G.pde_kbyu(l1, Ke8, u) - y_ref).max() <= 1e-13 * np.abs(y_ref).max()
+    # element matrix: symmetric, rows of the Laplacian part sum to zero, mass part sums to the volume
+    s, t, p, w = G.gauss_points()
+    dN = G.shape_derivatives(s, t, p)
+    assert np.allclose(Ke8, Ke8.T) and abs((dN.T @ dN).sum()) < 1e-12
+    assert abs(G.pde_element_matrix(0.0).sum() - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("m", [1, 2])
+def test_mma_restatement_matches_reference(m):
+    """oracle/mma.py against the reference's own MMA_mex.cpp + MMAseq.cpp
+    (compiled from the checkout): one update of a SIMP-like problem."""
+    from oracle import mma, mexcall
+
+    R = mexcall.ref_lib()
+    if R is None:
+        pytest.skip("reference kernels not built (oracle/_ref)")
+    rng = np.random.default_rng(7 + m)
+    n = 3000
+    x = rng.uniform(0.05, 0.95, n)
+    xmin, xmax = np.maximum(0, x - 0.1), np.minimum(1, x + 0.1)
+    df0 = -rng.uniform(0.001, 2.0, n)
+    dfdx = np.stack([np.ones(n) / (n * 0.3), rng.uniform(-1, 1, n) / n][:m], axis=1).reshape(-1)
+    fval = np.array([x.sum() / (n * 0.3) - 1, 0.05][:m])
+    xo1, xo2 = x * 0.98, x * 0.97
+    ref = R.call("ref_MMA_mex", 3, float(m), float(n), x, xmin, xmax, xo1, xo2, df0, fval, dfdx)
+    out = mma.mma_update(m, n, x, xmin, xmax, xo1, xo2, df0, fval, dfdx)
+    for a, b in zip(out, ref):
+        assert np.abs(a - np.asarray(b).ravel()).max() <= 1e-12

@@ -11,8 +11,12 @@ in for the reference's voxelized models.
 
 One step = one full solve for a given modulus field: set E, assemble the
 Galerkin hierarchy and the coarsest factor, run PCG to 1e-6.  `value` is the
-device time per step with E and F already in HBM; `e2e` is the same solve
-through the public C ABI with host buffers (E and F copied in, U copied out).
+device time per step with E and F already in HBM, for the mixed-precision
+solve (FP64 flexible PCG, FP32 inner CG with the FP32 V-cycle, double-float
+outer K*u) unless --precision says otherwise; `plain_fp64` is the reference
+form (FP64 PCG, FP64 V-cycle) timed the same way right after; `e2e` is the
+headline solve through the public C ABI with host buffers (E and F copied in,
+U copied out).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--precision fp64|mixed|mixed_df] [--size NX NY NZ]
@@ -46,7 +50,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", choices=["fp64", "mixed", "mixed_df"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed", "mixed_df"], default="mixed_df")
+    ap.add_argument("--fp64-steps", type=int, default=2, help="plain FP64 solves timed beside the headline")
     ap.add_argument("--size", type=int, nargs=3, default=[256, 128, 128], metavar=("NX", "NY", "NZ"))
     ap.add_argument("--levels", type=int, default=5)
     ap.add_argument("--maxit", type=int, default=2000)
@@ -249,43 +254,72 @@ def run_ours(args):
     # the slowest replica's time per solve; every rank solved `steps` replicas
     t_step, solves = replicas.aggregate(t_step, args.steps, device=dev)
     its = infos[-1]["its"]
-    # split: one profiled solve (K*u launches timed with events on the library stream)
+    # split: one profiled solve (outer K*u launches timed with events on the library stream)
     pinfo = step(profile=True)
-    # end to end through the public API with host buffers
+    # the reference form, same workload, timed the same way (device events)
+    fp64 = None
+    if args.precision != "fp64" and args.fp64_steps > 0:
+        def step64():
+            s.set_modulus_device(E_d.data_ptr())
+            s.Solving_AssembleFEAstencil()
+            return s.pcg_device(F_d.data_ptr(), U_d.data_ptr(), TOL, args.maxit, precision="fp64")
+        step64()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        f0.record(stream)
+        for _ in range(args.fp64_steps):
+            i64 = step64()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        t64 = f0.elapsed_time(f1) / 1e3 / args.fp64_steps
+        fp64 = {"value": t64, "unit": "s", "iterations": i64["its"], "true_relres": i64["true_relres"],
+                "steps": args.fp64_steps, "speedup_of_headline": t64 / t_step}
+    # end to end through the public API with host buffers (page-locked, as a
+    # caller streaming load cases would hold them)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
-    U_h = np.zeros_like(F)
+    E_h = torch.from_numpy(E).pin_memory().numpy()
+    F_h = torch.from_numpy(F).pin_memory().numpy()
+    U_h = torch.zeros(F.size, dtype=torch.float64).pin_memory().numpy()
     e2e = []
     for _ in range(args.steps):
         torch.cuda.synchronize()
         t0.record(stream)
-        s.set_modulus(E)
+        s.set_modulus(E_h)
         s.Solving_AssembleFEAstencil()
-        U_h, inf = s.pcg(F, tol=TOL, maxIT=args.maxit, precision=args.precision, inner_its=args.inner_its,
-                         inner_tol=args.inner_tol)
+        U_h, inf = s.pcg(F_h, tol=TOL, maxIT=args.maxit, precision=args.precision, inner_its=args.inner_its,
+                         inner_tol=args.inner_tol, out=U_h)
         t1.record(stream)
         torch.cuda.synchronize()
         e2e.append(t0.elapsed_time(t1) / 1e3)
     h2d = E.nbytes + F.nbytes
     d2h = U_h.nbytes
     ndof = s.numDOFs
-    # roofline of the dominant kernel (outer FP64 K*u)
-    l0info = s.levels[0]
+    # roofline of the dominant kernel: the K*u of the solve's inner loop
     NN = (nx + 1) * (ny + 1) * (nz + 1)
-    kbyu_bytes = NN * (3 * 8 * 2 + 1) + nx * ny * nz * 8    # read u, write y, node flags, E
-    kbyu_flops = 1176.0 * nx * ny * nz
-    kb_avg = pinfo["kbyu_seconds"] / max(pinfo["kbyu_launches"], 1)
+    NE = nx * ny * nz
     peaks = _peaks()
-    achieved = kbyu_bytes / kb_avg / 1e9
+    if args.precision == "fp64":
+        kname, kbytes = "k_kbyu<double> (FP64 K*u)", NN * (3 * 8 * 2 + 1) + NE * 8
+        kb_avg = pinfo["kbyu_seconds"] / max(pinfo["kbyu_launches"], 1)
+        how = "CUDA events around every K*u launch of one solve on the library stream"
+        note = "FP64 K*u is FP64-issue-bound on GB300 (ncu: FP64 pipe ~84 % busy)"
+    else:
+        kname, kbytes = "k_kbyu_x2 (FP32 K*u of the inner CG, f32x2 packed)", NN * (3 * 4 * 2 + 1) + NE * 4
+        kb_avg = s.time_op("kbyu32", 20) * 1e-3
+        how = ("CUDA events around 20 back-to-back launches on the library stream (sgld_time_op) right after "
+               "the timed region; inside the timed region the kernel runs in the inner CG's graph")
+        note = ("FP32 K*u is issue/latency-bound (ncu: issue 52 %, FMA pipe 42 %), not HBM-bound; the "
+                "HBM fraction is reported against the measured copy bandwidth")
+    achieved = kbytes / kb_avg / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": _ncu_traffic(),
-                "kernel": "k_kbyu<double> (outer FP64 K*u)", "avg_launch_ms": kb_avg * 1e3,
-                "algorithmic_bytes_per_launch": kbyu_bytes, "peak_source": peaks["source"],
-                "fp64_tflops_equiv": kbyu_flops / kb_avg / 1e12,
-                "note": "FP64 K*u is FP64-issue-bound on GB300; HBM fraction reported against measured copy BW"}
+                "frac": achieved / peaks["hbm_gbs"], "traffic": _ncu_traffic(args.precision),
+                "kernel": kname, "avg_launch_ms": kb_avg * 1e3, "launch_timing": how,
+                "algorithmic_bytes_per_launch": kbytes, "peak_source": peaks["source"],
+                "dense_equiv_tflops": 1152.0 * NE / kb_avg / 1e12, "note": note}
     line = {"metric": METRIC, "value": t_step, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
+            "vs_baseline": None, "dtype": {"fp64": "f64", "mixed": "f64+f32", "mixed_df": "f64+f32+df32"}[args.precision],
             "data": "synthetic (seeded graded-density cuboid)", "config": workload_config(args),
             "iterations": its, "dof": ndof, "dof_it_per_s": world * ndof * its / t_step,
             "replica_solves_per_s": solves / (t_step * args.steps),
@@ -295,12 +329,16 @@ def run_ours(args):
             "e2e": {"value": float(np.mean(e2e)), "unit": "s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(round(launches)), "roofline": roofline, "clocks": clocks}
+    if fp64:
+        line["plain_fp64"] = fp64
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
-        r = cpu_time_to_solve(vox, E, args.levels, its, args.cpu_iters, steps=1, warmup=0)
+        its_ref = fp64["iterations"] if fp64 else (its if args.precision == "fp64" else _known_iterations(args))
+        r = cpu_time_to_solve(vox, E, args.levels, its_ref, args.cpu_iters, steps=1, warmup=0)
         line["cpu_baseline"] = {"value": r["seconds"], "unit": "s", "cores": r["cores"], "kind": "port",
-                                "sample": f"oracle assembly + {args.cpu_iters} PCG iterations, extrapolated "
-                                          f"to {its} iterations", "detail": r}
+                                "sample": f"oracle assembly + {args.cpu_iters} PCG iterations of the reference "
+                                          f"(FP64) algorithm, extrapolated to its {its_ref} iterations",
+                                "detail": r}
     if rank == 0:
         print(json.dumps(line), flush=True)
     s.close()
@@ -317,14 +355,18 @@ def _peaks():
         return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def _ncu_traffic():
-    """DRAM bytes per K*u launch from the committed ncu capture, if recorded."""
+def _ncu_traffic(precision):
+    """DRAM bytes per launch of the roofline kernel from the committed ncu
+    capture (profiles/kbyu_traffic.json), if recorded."""
     p = os.path.join(ROOT, "profiles", "kbyu_traffic.json")
     try:
         with open(p) as f:
-            return json.load(f).get("dram_bytes_per_launch_full")
+            d = json.load(f)
     except (OSError, ValueError):
         return None
+    if precision == "fp64":
+        return d.get("dram_bytes_per_launch_full")
+    return d.get("k_kbyu_x2", {}).get("dram_bytes_per_launch")
 
 
 def main():

@@ -77,6 +77,31 @@ __global__ void k_icg_cond(cudaGraphConditionalHandle h, double *__restrict__ sc
     cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
+// the same decision written to *flag for a host-driven loop (profiling: the
+// kernels of a conditional graph body do not appear in a profiler's launch list)
+__global__ void k_icg_cond_flag(int *flag, double *__restrict__ sc, const double *__restrict__ part, int nb,
+                                int kmax, double eta_min, const double *__restrict__ outer,
+                                double *__restrict__ total) {
+    const double ss = msum_partials(part, nb);
+    if (threadIdx.x != 0) return;
+    const double it = sc[IS_IT] + 1.0;
+    sc[IS_IT] = it;
+    *total += 1.0;
+    bool more = it < (double)kmax;
+    if (more && eta_min > 0.0) {
+        const double relres = outer[3], tol = outer[15];
+        const double eta = (relres > 0.0) ? fmax(eta_min, 0.5 * tol / relres) : eta_min;
+        more = ss > eta * eta * sc[IS_R0];
+    }
+    *flag = more ? 1 : 0;
+}
+
+void launch_icg_cond_flag(int *flag, double *sc, const double *part, int nb, int kmax, double eta_min,
+                          const double *outer, double *total, cudaStream_t s) {
+    ++g_launches;
+    k_icg_cond_flag<<<1, MB, 0, s>>>(flag, sc, part, nb, kmax, eta_min, outer, total);
+}
+
 void launch_icg_cond(cudaGraphConditionalHandle h, double *sc, const double *part, int nb, int kmax,
                      double eta_min, const double *outer, double *total, cudaStream_t s) {
     ++g_launches;

@@ -2,6 +2,7 @@
 // matrices, assembly and the PCG driver.  Every entry point mirrors one
 // function of the reference's solve path (cited in the header).
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -365,10 +366,45 @@ static int build_inner_graph(sgld_ctx *ctx, int kmax, double eta) {
     return SGLD_OK;
 }
 
+// The same inner solve with the loop on the host (one kernel sequence per
+// iteration, a flag read back after each): selected by the environment
+// variable SGLD_INNER_LOOP=host so that profilers, which do not list the
+// kernels of a conditional graph body, see every launch.  Same kernels, same
+// arithmetic, same stopping rule.
+static int inner_run_host(sgld_ctx *ctx, int kmax, double eta) {
+    Ctx &c = ctx->c;
+    const Level &l0 = c.lv[0];
+    const int64_t nv = 3 * l0.nnode;
+    int *d_flag = c.d_iflag + 12;
+    const int nbi = launch_icg_init(c.d_r32, c.d_s32, c.d_e32, c.d_d32, nv, c.d_part2, c.stream);
+    launch_icg_scalar(0, c.d_isc, c.d_part2, nbi, c.stream);
+    for (int it = 0; it < kmax; ++it) {
+        int nb = 0;
+        vcycle_dev32(ctx, c.d_s32, c.d_z32, c.d_part2, &nb);
+        launch_icg_scalar(2, c.d_isc, c.d_part2, nb, c.stream);
+        launch_icg_dupdate(c.d_d32, c.d_z32, nv, c.d_isc, c.stream);
+        launch_kbyu_f32(l0, c.d_E32, c.d_d32, c.d_t32, c.d_part2, &nb, c.stream);
+        launch_icg_scalar(1, c.d_isc, c.d_part2, nb, c.stream);
+        nb = launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.d_part2, c.stream);
+        launch_icg_cond_flag(d_flag, c.d_isc, c.d_part2, nb, kmax, eta, c.d_scal, c.d_isc + IS_TOTAL, c.stream);
+        int more = 0;
+        CK(cudaMemcpyAsync(&more, d_flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaStreamSynchronize(c.stream));
+        if (!more) break;
+    }
+    return SGLD_OK;
+}
+
+static bool inner_loop_on_host() {
+    const char *v = getenv("SGLD_INNER_LOOP");
+    return v && strcmp(v, "host") == 0;
+}
+
 // one inner solve (graph launch); launch accounting of the iterations is done
 // by the caller from d_isc[IS_TOTAL]
 int inner_run(sgld_ctx *ctx, int kmax, double eta) {
     Ctx &c = ctx->c;
+    if (inner_loop_on_host()) return inner_run_host(ctx, kmax, eta);   // launches counted as made
     if (!c.inner_graph || c.inner_graph_k != kmax || c.inner_graph_eta != eta) {
         if (c.inner_graph) {
             cudaGraphExecDestroy(c.inner_graph);
@@ -1316,7 +1352,7 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
     CK(cudaMemcpyAsync(sc, c.d_scal, sizeof(double) * 8, cudaMemcpyDeviceToHost, c.stream));
     CK(cudaMemcpyAsync(&inner_total, c.d_isc + IS_TOTAL, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
-    g_launches += (int64_t)inner_total * c.inner_body_launches;
+    if (!inner_loop_on_host()) g_launches += (int64_t)inner_total * c.inner_body_launches;
     if (prof) {
         if (pc_pending) {
             float t = 0.f;

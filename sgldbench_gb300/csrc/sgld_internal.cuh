@@ -136,6 +136,8 @@ int launch_icg_update(float *e, float *s, const float *d, const float *t, int64_
 void launch_icg_cond(cudaGraphConditionalHandle h, double *sc, const double *part, int nb, int kmax,
                      double eta_min, const double *outer, double *total, cudaStream_t s);
 int launch_icg_init(const float *r, float *s, float *e, float *d, int64_t n, double *part, cudaStream_t st);
+void launch_icg_cond_flag(int *flag, double *sc, const double *part, int nb, int kmax, double eta_min,
+                          const double *outer, double *total, cudaStream_t s);
 void launch_icg_dupdate(float *d, const float *w, int64_t n, const double *sc, cudaStream_t st);
 void launch_widen_dots(const float *e, double *z, const double *r, const double *q, int64_t n, double *p1,
                        double *p2, int nb, cudaStream_t st);

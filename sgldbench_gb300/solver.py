@@ -239,10 +239,21 @@ class VoxelSolver:
         return z
 
     def pcg(self, b, tol: float = 1e-3, maxIT: int = 500, x0=None, precision: str = "fp64",
-            inner_its: int = 0, history: bool = False, inner_tol: float = 0.0):
-        """Runs the whole PCG on the device.  Returns (x, info dict)."""
+            inner_its: int = 0, history: bool = False, inner_tol: float = 0.0, out=None):
+        """Runs the whole PCG on the device.  Returns (x, info dict).  ``out``:
+        optional float64 array of numDOFs entries to receive x (for example
+        page-locked host memory)."""
         bv = self._vec(b, self.numDOFs)
-        x = np.zeros_like(bv) if x0 is None else self._vec(x0, self.numDOFs).copy()
+        if out is not None:
+            if out.dtype != np.float64 or out.size != self.numDOFs or not out.flags.c_contiguous:
+                raise ValueError("out must be a contiguous float64 array of numDOFs entries")
+            x = out
+            if x0 is None:
+                x[...] = 0.0
+            else:
+                x[...] = self._vec(x0, self.numDOFs)
+        else:
+            x = np.zeros_like(bv) if x0 is None else self._vec(x0, self.numDOFs).copy()
         hist = np.zeros(maxIT) if history else None
         o = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=int(x0 is not None),
                         precision=_precision(precision),

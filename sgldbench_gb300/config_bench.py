@@ -62,6 +62,7 @@ def _errors(s, U, U_ref):
 def _solve_pair(s, F, tol=1e-6, maxit=5000, reps=2):
     """FP64 and mixed_df solves of one load case, each with its assembly."""
     out = {}
+    s.Solving_AssembleFEAstencil()
     U_ref, _ = s.pcg(F, tol=1e-10, maxIT=20000)
     for prec in ("fp64", "mixed_df"):
         def run():

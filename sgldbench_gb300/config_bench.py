@@ -2,7 +2,7 @@
 
   0  solid 64 x 32 x 32 cuboid, E = 1, cantilever, 3 levels (first step 4:1), omega 0.6
   1  SIMP-graded 256 x 128 x 128 cantilever, 5 dyadic levels
-  2  512 x 256 x 256 union of spheres and boxes (~40 % solid), lowest 4 layers fixed,
+  2  512 x 256 x 256 union of spheres and boxes grown to ~40 % solid, lowest 4 layers fixed,
      8 load cases over surface patches, block right-hand side, 6 dyadic levels
   3  SIMP loop on config 1's cantilever: volume fraction 0.3, p = 3, rmin 1.5, OC, 60 iterations
   4  1024 x 512 x 512 thresholded Gaussian blobs (~30 % solid), lowest 4 layers fixed,
@@ -134,7 +134,7 @@ def config_block(nx, ny, nz, vox, levels, nrhs, cfg):
 
 
 def config2():
-    vox = D.blobby_union(512, 256, 256, seed=0)
+    vox = D.blobby_union(512, 256, 256, seed=0, fill=0.4)
     return config_block(512, 256, 256, vox, 6, 8, 2)
 
 

@@ -100,24 +100,45 @@ def _largest_component(mask: np.ndarray) -> np.ndarray:
 
 
 def blobby_union(nx: int, ny: int, nz: int, seed: int = 0, n_spheres: int = 12, n_boxes: int = 8,
-                 r_range=(20, 60), edge_range=(30, 120)) -> np.ndarray:
+                 r_range=(20, 60), edge_range=(30, 120), fill: float | None = None) -> np.ndarray:
     """Config-2 style domain: union of seeded spheres and axis-aligned boxes,
     largest 26-connected component.  Radii / edges scale with the grid when it
-    is smaller than 512 x 256 x 256."""
+    is smaller than 512 x 256 x 256.  With ``fill``, every radius and edge is
+    multiplied by one common factor (>= 1, found by bisection) so that the
+    largest component covers about that fraction of the box: at the literal
+    sizes twelve spheres and eight boxes cover only 10-20 % of a 512 x 256 x
+    256 box and split into several components."""
     rng = np.random.default_rng(seed)
     scale = min(nx / 512, ny / 256, nz / 256)
+    spheres = [(rng.uniform(*r_range) * scale, rng.uniform([0, 0, 0], [ny, nx, nz])) for _ in range(n_spheres)]
+    boxes = [(rng.uniform(*edge_range, size=3) * scale, rng.uniform([0, 0, 0], [ny, nx, nz])) for _ in range(n_boxes)]
     y, x, z = np.ogrid[:ny, :nx, :nz]
-    m = np.zeros((ny, nx, nz), bool)
-    for _ in range(n_spheres):
-        r = rng.uniform(*r_range) * scale
-        c = rng.uniform([0, 0, 0], [ny, nx, nz])
-        m |= (y - c[0]) ** 2 + (x - c[1]) ** 2 + (z - c[2]) ** 2 <= r * r
-    for _ in range(n_boxes):
-        e = rng.uniform(*edge_range, size=3) * scale
-        lo = rng.uniform([0, 0, 0], [ny, nx, nz])
-        hi = lo + e
-        m[int(lo[0]):int(hi[0]), int(lo[1]):int(hi[1]), int(lo[2]):int(hi[2])] = True
-    return _largest_component(m)
+
+    def build(k):
+        m = np.zeros((ny, nx, nz), bool)
+        for r, c in spheres:
+            m |= (y - c[0]) ** 2 + (x - c[1]) ** 2 + (z - c[2]) ** 2 <= (k * r) ** 2
+        for e, lo in boxes:
+            hi = lo + k * e
+            m[int(lo[0]):int(hi[0]), int(lo[1]):int(hi[1]), int(lo[2]):int(hi[2])] = True
+        return _largest_component(m)
+
+    if fill is None:
+        return build(1.0)
+    lo_k, hi_k = 1.0, 4.0
+    best = build(lo_k)
+    if best.mean() >= fill:
+        return best
+    for _ in range(12):
+        mid = 0.5 * (lo_k + hi_k)
+        m = build(mid)
+        if m.mean() >= fill:
+            hi_k, best = mid, m
+        else:
+            lo_k = mid
+        if abs(m.mean() - fill) < 0.01:
+            return m
+    return best
 
 
 def gaussian_blobs(nx: int, ny: int, nz: int, seed: int = 0, n_blobs: int = 64, fill: float = 0.3) -> np.ndarray:

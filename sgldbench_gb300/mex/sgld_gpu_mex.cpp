@@ -12,7 +12,8 @@
  *   sgld_gpu_mex('assemble')                    Solving_AssembleFEAstencil.m
  *   y = sgld_gpu_mex('kbyu', u)                 Solving_KbyU_MatrixFree.m
  *   z = sgld_gpu_mex('vcycle', r)               Solving_Vcycle.m
- *   [U, its] = sgld_gpu_mex('pcg', F, tol, maxIT[, U0[, 'mixed']])
+ *   [U, its] = sgld_gpu_mex('pcg', F, tol, maxIT[, U0[, 'fp64' | 'mixed' | 'mixed64']])
+ *       'mixed' = SGLD_PREC_MIXED_DF, 'mixed64' = SGLD_PREC_MIXED
  *                                               Solving_PreconditionedConjugateGradientSolver.m
  *   ce = sgld_gpu_mex('compliance', U)          TopOpti_ComputeUnitCompliance.m
  *   [s, vm, vmE] = sgld_gpu_mex('stress', U)    FEA_StressAnalysis.m, FEA_ComputePerElementVonMisesStress.m
@@ -139,7 +140,9 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
         if (nrhs > 5) {
             char mode[16] = {0};
             mxGetString(prhs[5], mode, sizeof mode);
-            if (!strcmp(mode, "mixed")) o.precision = SGLD_PREC_MIXED;
+            if (!strcmp(mode, "mixed")) o.precision = SGLD_PREC_MIXED_DF;
+            else if (!strcmp(mode, "mixed64")) o.precision = SGLD_PREC_MIXED;
+            else if (strcmp(mode, "fp64")) mexErrMsgIdAndTxt("sgld:arg", "precision must be 'fp64', 'mixed' or 'mixed64'");
         }
         sgld_solve_info info;
         check(sgld_pcg(g_ctx, F, mxGetPr(plhs[0]), &o, &info));

@@ -45,4 +45,23 @@ __device__ __forceinline__ df df_shfl(df v, int src, int width = 32) {
     return {__shfl_sync(0xffffffffu, v.hi, src, width), __shfl_sync(0xffffffffu, v.lo, src, width)};
 }
 
+// Compensated double-float dot-product accumulator (the Dot2 scheme of Ogita,
+// Rump and Oishi, 2005, with the low parts of the operands folded into the
+// error term): s + e carries the running sum.
+struct dacc {
+    float s = 0.f, e = 0.f;
+    __device__ __forceinline__ void add(float2 a, float2 b) {
+        const float p = __fmul_rn(a.x, b.x);
+        float pe = __fmaf_rn(a.x, b.x, -p);
+        pe = __fmaf_rn(a.x, b.y, pe);
+        pe = __fmaf_rn(a.y, b.x, pe);
+        const float t = __fadd_rn(s, p);
+        const float bb = __fsub_rn(t, s);
+        const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+        s = t;
+        e = __fadd_rn(e, __fadd_rn(err, pe));
+    }
+    __device__ __forceinline__ df value() const { return quick_two_sum(s, e); }
+};
+
 }  // namespace sgld

@@ -52,12 +52,17 @@ static void upload_pairs(cudaStream_t s) {
 // thread t owns one upper-triangle entry and keeps EB accumulators.
 constexpr int EB = 16;
 
+// The sums run in compensated double-float arithmetic (Dot2 accumulators, at
+// the FP32 issue rate): in FP64 the kernel was bound by GB300's FP64 pipe
+// (ncu: 99 % busy).  H2 holds the templates as (hi, lo) float pairs; E is
+// split on load.
 template <int NQ>
-__global__ void __launch_bounds__(320) k_asm_templates(const double *__restrict__ E, const uint8_t *__restrict__ eact_c,
-                                                       const double *__restrict__ H, int nyc, int nxc, int nzc,
-                                                       double *__restrict__ Ks) {
+__global__ void __launch_bounds__(320) k_asm_templates_df(const double *__restrict__ E,
+                                                          const uint8_t *__restrict__ eact_c,
+                                                          const float2 *__restrict__ H2, int nyc, int nxc, int nzc,
+                                                          double *__restrict__ Ks) {
     constexpr int S = (NQ == 8) ? 2 : 4;
-    __shared__ double ev[EB][NQ];
+    __shared__ float2 ev[EB][NQ];
     const int64_t nel = (int64_t)nyc * nxc * nzc;
     const int64_t e0 = (int64_t)blockIdx.x * EB;
     const int nyf = S * nyc, nxf = S * nxc;
@@ -70,27 +75,27 @@ __global__ void __launch_bounds__(320) k_asm_templates(const double *__restrict_
             const int oy = q % S, ox = (q / S) % S, oz = q / (S * S);
             v = E[(int64_t)(S * cy + oy) + (int64_t)nyf * ((S * cx + ox) + (int64_t)nxf * (S * cz + oz))];
         }
-        ev[k][q] = v;
+        const df d = df_from(v);
+        ev[k][q] = make_float2(d.hi, d.lo);
     }
     __syncthreads();
     const int t = threadIdx.x;
     if (t >= 300) return;
     const int r = c_pr[t], c = c_pc[t];
     const int off = r + 24 * c, offt = c + 24 * r;
-    double acc[EB];
-#pragma unroll
-    for (int k = 0; k < EB; ++k) acc[k] = 0.0;
+    dacc acc[EB];
     for (int q = 0; q < NQ; ++q) {
-        const double h = H[576 * q + off];
+        const float2 h = H2[576 * q + off];
 #pragma unroll
-        for (int k = 0; k < EB; ++k) acc[k] += ev[k][q] * h;
+        for (int k = 0; k < EB; ++k) acc[k].add(ev[k][q], h);
     }
 #pragma unroll
     for (int k = 0; k < EB; ++k) {
         const int64_t e = e0 + k;
         if (e < nel && eact_c[e]) {
-            Ks[576 * e + off] = acc[k];
-            Ks[576 * e + offt] = acc[k];
+            const double v = df_to(acc[k].value());
+            Ks[576 * e + off] = v;
+            Ks[576 * e + offt] = v;
         }
     }
 }
@@ -99,10 +104,13 @@ void launch_asm_templates(const Level &coarse, int S, const double *E, const dou
     upload_pairs(s);
     const unsigned nb = (unsigned)((coarse.nel + EB - 1) / EB);
     ++g_launches;
+    // the float-pair copy of every template sits (8 + 64) * 576 entries after
+    // its FP64 form (setup_templates lays out FP64 span 2, span 4, then the pairs)
+    const float2 *H2 = reinterpret_cast<const float2 *>(H + 72 * 576);
     if (S == 2)
-        k_asm_templates<8><<<nb, 320, 0, s>>>(E, coarse.eact, H, coarse.ny, coarse.nx, coarse.nz, Ks);
+        k_asm_templates_df<8><<<nb, 320, 0, s>>>(E, coarse.eact, H2, coarse.ny, coarse.nx, coarse.nz, Ks);
     else
-        k_asm_templates<64><<<nb, 320, 0, s>>>(E, coarse.eact, H, coarse.ny, coarse.nx, coarse.nz, Ks);
+        k_asm_templates_df<64><<<nb, 320, 0, s>>>(E, coarse.eact, H2, coarse.ny, coarse.nx, coarse.nz, Ks);
 }
 
 // Jacobi diagonal of a span-2 coarse level without its element matrices:
@@ -367,24 +375,6 @@ __global__ void __launch_bounds__(CP_THREADS) k_chol_panel(double *A, int n, int
     }
 }
 
-// Compensated double-float dot-product accumulator (the Dot2 scheme of Ogita,
-// Rump and Oishi, 2005, with the low parts of the operands folded into the
-// error term): s + e carries the running sum.
-struct dacc {
-    float s = 0.f, e = 0.f;
-    __device__ __forceinline__ void add(float2 a, float2 b) {
-        const float p = __fmul_rn(a.x, b.x);
-        float pe = __fmaf_rn(a.x, b.x, -p);
-        pe = __fmaf_rn(a.x, b.y, pe);
-        pe = __fmaf_rn(a.y, b.x, pe);
-        const float t = __fadd_rn(s, p);
-        const float bb = __fsub_rn(t, s);
-        const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
-        s = t;
-        e = __fadd_rn(e, __fadd_rn(err, pe));
-    }
-    __device__ __forceinline__ df value() const { return quick_two_sum(s, e); }
-};
 
 // trailing update A[i,j] -= sum_k A[i,k] A[j,k] over the panel's columns k for
 // the band tiles below it: blockIdx.x = tile pair (ii >= jj), blockIdx.y =
@@ -553,6 +543,21 @@ __global__ void __launch_bounds__(TI_THREADS) k_trinv_tiles(const float2 *__rest
                 M32[(int64_t)i + (int64_t)n * cb] = x1.hi;
             }
         }
+        // the transpose into the upper triangle (M^T, column-major), staged
+        // through shared memory so that the stores run along the group's columns
+        __syncthreads();
+        rhs[r * TI_G + gp] = make_float2(x0.hi, x0.lo);
+        rhs[r * TI_G + gp + 1] = make_float2(x1.hi, x1.lo);
+        __syncthreads();
+        for (int idx = t; idx < 32 * TI_G; idx += TI_THREADS) {
+            const int g = idx % TI_G, rr = idx / TI_G;
+            const int cc = c0 + g, ii = i0 + rr;
+            if (ii < n && cc < n && ii > cc) {
+                const float2 v = rhs[rr * TI_G + g];
+                M[(int64_t)cc + (int64_t)n * ii] = (double)v.x + (double)v.y;
+                M32[(int64_t)cc + (int64_t)n * ii] = v.x;
+            }
+        }
         __syncthreads();
     }
 }
@@ -633,80 +638,66 @@ int coarse_factor_invert(Ctx &c) {
 }
 
 // ---- coarse apply: x_L[free] = A^-1 r_L[free] = M' (M r) -------------------------
-// y = M r (M lower triangular, column-major).  A CTA covers 32 rows and one of
-// CSPLIT column chunks; each warp takes 32-column blocks of the chunk, lane l
-// holding row i0 + l: its 32 loads of a block (one coalesced row segment per
-// column) are independent and in flight together.  The 8 warps' sums meet in
-// shared memory and the chunk's partial goes to part[chunk * n + i].
+// The inverse factor is stored square: M (lower triangle, column-major) and
+// its transpose in the upper triangle, so that both products are column-major
+// GEMVs with coalesced loads.  A CTA covers 32 output rows and one of CSPLIT
+// column chunks; each warp takes 32-column blocks of the chunk, lane l holding
+// row i0 + l: its 32 loads of a block (one coalesced row segment per column)
+// are independent and in flight together.  The 8 warps' sums meet in shared
+// memory and the chunk's partial goes to part[chunk * n + row].
+//   lower (UPPER = false): y_i = sum_{j <= i} M[i + n j] v[rows[j]]
+//   upper (UPPER = true):  x_j = sum_{i >= j} M[j + n i] v[i]   (= (M' v)_j)
 constexpr int CL_WARPS = 8;
 
-template <typename T>
-__global__ void __launch_bounds__(32 * CL_WARPS) k_coarse_lower(const T *__restrict__ M, const int *__restrict__ rows,
-                                                               const T *__restrict__ r, int n,
-                                                               double *__restrict__ part) {
+template <typename T, bool UPPER>
+__global__ void __launch_bounds__(32 * CL_WARPS) k_coarse_gemv(const T *__restrict__ M, const int *__restrict__ rows,
+                                                              const T *__restrict__ v, int n,
+                                                              double *__restrict__ part) {
     __shared__ T red[CL_WARPS][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i0 = blockIdx.x * 32, i = i0 + lane;
     const int chunk = ((n + CSPLIT - 1) / CSPLIT + 31) & ~31;
-    const int j0 = blockIdx.y * chunk, j1 = min(min(n, j0 + chunk), i0 + 32);
+    int j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+    if (UPPER)
+        j0 = max(j0, i0);
+    else
+        j1 = min(j1, i0 + 32);
+    const int ii = min(i, n - 1);
     T acc = T(0);
     for (int jb = j0 + 32 * w; jb < j1; jb += 32 * CL_WARPS) {
         const int jl = jb + lane;
-        const T rl = (jl < n) ? r[rows[jl]] : T(0);
-        const int ii = min(i, n - 1);
+        const T vl = (jl < n) ? (UPPER ? v[jl] : v[rows[jl]]) : T(0);
         T a0 = T(0), a1 = T(0);
 #pragma unroll
         for (int q = 0; q < 32; q += 2) {
             const int ja = jb + q, jc = jb + q + 1;
             const T ma = (ja < n) ? M[(int64_t)ja * n + ii] : T(0);
             const T mc = (jc < n) ? M[(int64_t)jc * n + ii] : T(0);
-            const T ra = __shfl_sync(0xffffffffu, rl, q), rc = __shfl_sync(0xffffffffu, rl, q + 1);
-            a0 += (ja <= i) ? ma * ra : T(0);
-            a1 += (jc <= i) ? mc * rc : T(0);
+            const T va = __shfl_sync(0xffffffffu, vl, q), vc = __shfl_sync(0xffffffffu, vl, q + 1);
+            a0 += (UPPER ? ja >= i : ja <= i) ? ma * va : T(0);
+            a1 += (UPPER ? jc >= i : jc <= i) ? mc * vc : T(0);
         }
         acc += a0 + a1;
     }
     red[w][lane] = acc;
     __syncthreads();
     if (w == 0 && i < n) {
-        double s = 0.0;
+        double sum = 0.0;
 #pragma unroll
-        for (int k = 0; k < CL_WARPS; ++k) s += (double)red[k][lane];
-        part[(int64_t)blockIdx.y * n + i] = s;
+        for (int k = 0; k < CL_WARPS; ++k) sum += (double)red[k][lane];
+        part[(int64_t)blockIdx.y * n + i] = sum;
     }
 }
 
-template <typename T>
-__global__ void k_coarse_sum(const double *__restrict__ part, int n, T *__restrict__ y) {
+// y_i = sum of the chunk partials (compact), or x[rows[i]] = that sum (scatter)
+template <typename T, bool SCATTER>
+__global__ void k_coarse_sum(const double *__restrict__ part, int n, const int *__restrict__ rows,
+                             T *__restrict__ y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double s = 0.0;
     for (int k = 0; k < CSPLIT; ++k) s += part[(int64_t)k * n + i];
-    y[i] = (T)s;
-}
-
-// x_j = sum_{i >= j} M[i,j] y_i: one warp per column (coalesced column reads),
-// four independent accumulators so that four loads per lane are in flight
-template <typename T>
-__global__ void k_coarse_upper(const T *__restrict__ M, const int *__restrict__ rows, const T *__restrict__ y, int n,
-                               T *__restrict__ x) {
-    const int j = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (j >= n) return;
-    const T *col = M + (int64_t)n * j;
-    T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
-    int i = j + lane;
-    for (; i + 96 < n; i += 128) {
-        a0 += col[i] * y[i];
-        a1 += col[i + 32] * y[i + 32];
-        a2 += col[i + 64] * y[i + 64];
-        a3 += col[i + 96] * y[i + 96];
-    }
-    for (; i < n; i += 32) a0 += col[i] * y[i];
-    T acc = (a0 + a1) + (a2 + a3);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) x[rows[j]] = acc;
+    y[SCATTER ? rows[i] : i] = (T)s;
 }
 
 template <typename T>
@@ -714,13 +705,13 @@ static void coarse_apply(const Ctx &c, const T *M, const T *rc, T *xc, T *ybuf, 
     const Level &lc = c.lv[c.L - 1];
     cudaMemsetAsync(xc, 0, sizeof(T) * 3 * lc.nnode, s);
     if (c.ncf == 0) return;
-    dim3 g((c.ncf + 31) / 32, CSPLIT);
-    ++g_launches;
-    k_coarse_lower<T><<<g, 32 * CL_WARPS, 0, s>>>(M, c.d_cfree, rc, c.ncf, c.d_cpart);
-    ++g_launches;
-    k_coarse_sum<T><<<(c.ncf + 127) / 128, 128, 0, s>>>(c.d_cpart, c.ncf, ybuf);
-    ++g_launches;
-    k_coarse_upper<T><<<(unsigned)(((int64_t)c.ncf * 32 + 255) / 256), 256, 0, s>>>(M, c.d_cfree, ybuf, c.ncf, xc);
+    const dim3 g((c.ncf + 31) / 32, CSPLIT);
+    const unsigned gs = (unsigned)((c.ncf + 127) / 128);
+    g_launches += 4;
+    k_coarse_gemv<T, false><<<g, 32 * CL_WARPS, 0, s>>>(M, c.d_cfree, rc, c.ncf, c.d_cpart);
+    k_coarse_sum<T, false><<<gs, 128, 0, s>>>(c.d_cpart, c.ncf, c.d_cfree, ybuf);
+    k_coarse_gemv<T, true><<<g, 32 * CL_WARPS, 0, s>>>(M, c.d_cfree, ybuf, c.ncf, c.d_cpart);
+    k_coarse_sum<T, true><<<gs, 128, 0, s>>>(c.d_cpart, c.ncf, c.d_cfree, xc);
 }
 
 void launch_coarse_apply_f64(const Ctx &c, const double *rc, double *xc, cudaStream_t s) {

@@ -46,6 +46,7 @@ __global__ void k_icg_scalar(int op, double *__restrict__ sc, const double *__re
         sc[IS_R0] = s;
         sc[IS_RHO] = 0.0;
         sc[IS_IT] = 0.0;
+        sc[IS_ALPHA] = 0.0;   // the first d update adds alpha * d = 0 to e
     } else if (op == 1) {
         sc[IS_ALPHA] = (s != 0.0) ? sc[IS_RHO] / s : 0.0;
     } else {
@@ -150,24 +151,27 @@ __device__ __forceinline__ float4 fma4(float a, float4 x, float4 y) {
     return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
 }
 
-// e += alpha d; s -= alpha t; partial sums of s.s (new s) when part != null
+// s -= alpha t; partial sums of s.s (new s) when part != null.  The matching
+// e += alpha d is deferred to the next d update (k_icg_dupdate), or, after the
+// last iteration, to k_widen_dots: d is read there anyway, which saves one
+// pass over e and d per iteration.
 __global__ void k_icg_update(float *__restrict__ e, float *__restrict__ s, const float *__restrict__ d,
                              const float *__restrict__ t, int64_t n, const double *__restrict__ sc,
                              double *__restrict__ part) {
+    (void)e;
+    (void)d;
     const float a = (float)sc[IS_ALPHA];
     const int64_t n4 = n >> 2, stride = (int64_t)gridDim.x * MB;
-    float4 *e4 = reinterpret_cast<float4 *>(e), *s4 = reinterpret_cast<float4 *>(s);
-    const float4 *d4 = reinterpret_cast<const float4 *>(d), *t4 = reinterpret_cast<const float4 *>(t);
+    float4 *s4 = reinterpret_cast<float4 *>(s);
+    const float4 *t4 = reinterpret_cast<const float4 *>(t);
     float acc = 0.f;
     for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n4; i += stride) {
-        e4[i] = fma4(a, d4[i], e4[i]);
         const float4 v = fma4(-a, t4[i], s4[i]);
         s4[i] = v;
         acc = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, acc))));
     }
     const int64_t i = 4 * n4 + blockIdx.x * (int64_t)MB + threadIdx.x;
     if (i < n) {
-        e[i] = fmaf(a, d[i], e[i]);
         const float v = fmaf(-a, t[i], s[i]);
         s[i] = v;
         acc = fmaf(v, v, acc);
@@ -194,30 +198,42 @@ int launch_icg_update(float *e, float *s, const float *d, const float *t, int64_
     return nb;
 }
 
+// e += alpha d (the previous iteration's step, alpha still in place); then
 // d = w + beta d
-__global__ void k_icg_dupdate(float *__restrict__ d, const float *__restrict__ w, int64_t n,
+__global__ void k_icg_dupdate(float *__restrict__ e, float *__restrict__ d, const float *__restrict__ w, int64_t n,
                               const double *__restrict__ sc) {
-    const float b = (float)sc[IS_BETA];
+    const float a = (float)sc[IS_ALPHA], b = (float)sc[IS_BETA];
     const int64_t n4 = n >> 2, stride = (int64_t)gridDim.x * MB;
-    float4 *d4 = reinterpret_cast<float4 *>(d);
+    float4 *e4 = reinterpret_cast<float4 *>(e), *d4 = reinterpret_cast<float4 *>(d);
     const float4 *w4 = reinterpret_cast<const float4 *>(w);
-    for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n4; i += stride) d4[i] = fma4(b, d4[i], w4[i]);
+    for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n4; i += stride) {
+        const float4 dv = d4[i];
+        e4[i] = fma4(a, dv, e4[i]);
+        d4[i] = fma4(b, dv, w4[i]);
+    }
     const int64_t i = 4 * n4 + blockIdx.x * (int64_t)MB + threadIdx.x;
-    if (i < n) d[i] = fmaf(b, d[i], w[i]);
+    if (i < n) {
+        const float dv = d[i];
+        e[i] = fmaf(a, dv, e[i]);
+        d[i] = fmaf(b, dv, w[i]);
+    }
 }
 
-void launch_icg_dupdate(float *d, const float *w, int64_t n, const double *sc, cudaStream_t st) {
+void launch_icg_dupdate(float *e, float *d, const float *w, int64_t n, const double *sc, cudaStream_t st) {
     ++g_launches;
-    k_icg_dupdate<<<reduce_blocks(n), MB, 0, st>>>(d, w, n, sc);
+    k_icg_dupdate<<<reduce_blocks(n), MB, 0, st>>>(e, d, w, n, sc);
 }
 
-// z64 = e32 (masked at fixed DOFs by construction), partials of z.r and z.q
-__global__ void k_widen_dots(const float *__restrict__ e, double *__restrict__ z, const double *__restrict__ r,
+// z64 = e32 + alpha d32 (the last iteration's deferred step; masked at fixed
+// DOFs by construction), partials of z.r and z.q
+__global__ void k_widen_dots(const float *__restrict__ e, const float *__restrict__ d,
+                             const double *__restrict__ sc, double *__restrict__ z, const double *__restrict__ r,
                              const double *__restrict__ q, int64_t n, double *__restrict__ p1,
                              double *__restrict__ p2) {
+    const float al = (float)sc[IS_ALPHA];
     double a = 0.0, b = 0.0;
     for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n; i += (int64_t)gridDim.x * MB) {
-        const double zi = (double)e[i];
+        const double zi = (double)fmaf(al, d[i], e[i]);
         z[i] = zi;
         a += zi * r[i];
         b += zi * q[i];
@@ -230,10 +246,10 @@ __global__ void k_widen_dots(const float *__restrict__ e, double *__restrict__ z
     }
 }
 
-void launch_widen_dots(const float *e, double *z, const double *r, const double *q, int64_t n, double *p1,
-                       double *p2, int nb, cudaStream_t st) {
+void launch_widen_dots(const float *e, const float *d, const double *sc, double *z, const double *r,
+                       const double *q, int64_t n, double *p1, double *p2, int nb, cudaStream_t st) {
     ++g_launches;
-    k_widen_dots<<<nb, MB, 0, st>>>(e, z, r, q, n, p1, p2);
+    k_widen_dots<<<nb, MB, 0, st>>>(e, d, sc, z, r, q, n, p1, p2);
 }
 
 // outer flexible-PCG scalars after the preconditioner: beta = -lambda zq / x1, x1 = zr

@@ -252,9 +252,20 @@ int setup_templates(sgld_ctx *ctx) {
     make_templates(c.Ke, 2, H2);
     make_templates(c.Ke, 4, H4);
     if (c.d_H) cudaFree(c.d_H);
-    CK(dalloc(&c.d_H, H2.size() + H4.size()));
-    CK(cudaMemcpy(c.d_H, H2.data(), H2.size() * sizeof(double), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(c.d_H + H2.size(), H4.data(), H4.size() * sizeof(double), cudaMemcpyHostToDevice));
+    // FP64 span-2 and span-4 templates, then the same values as (hi, lo) float
+    // pairs for the double-float assembly kernel
+    const size_t nh = H2.size() + H4.size();
+    std::vector<double> all(2 * nh);
+    std::copy(H2.begin(), H2.end(), all.begin());
+    std::copy(H4.begin(), H4.end(), all.begin() + H2.size());
+    float *pairs = reinterpret_cast<float *>(all.data() + nh);
+    for (size_t i = 0; i < nh; ++i) {
+        const float hi = (float)all[i];
+        pairs[2 * i] = hi;
+        pairs[2 * i + 1] = (float)(all[i] - (double)hi);
+    }
+    CK(dalloc(&c.d_H, 2 * nh));
+    CK(cudaMemcpy(c.d_H, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
     upload_kh(c.Kh, c.stream);
     upload_kh_df(c.Kh, c.stream);
     return SGLD_OK;
@@ -350,7 +361,7 @@ static int build_inner_graph(sgld_ctx *ctx, int kmax, double eta) {
     int nb = 0;
     vcycle_dev32(ctx, c.d_s32, c.d_z32, c.d_part2, &nb);
     launch_icg_scalar(2, c.d_isc, c.d_part2, nb, c.stream);
-    launch_icg_dupdate(c.d_d32, c.d_z32, nv, c.d_isc, c.stream);
+    launch_icg_dupdate(c.d_e32, c.d_d32, c.d_z32, nv, c.d_isc, c.stream);
     launch_kbyu_f32(l0, c.d_E32, c.d_d32, c.d_t32, c.d_part2, &nb, c.stream);
     launch_icg_scalar(1, c.d_isc, c.d_part2, nb, c.stream);
     nb = launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.d_part2, c.stream);
@@ -382,7 +393,7 @@ static int inner_run_host(sgld_ctx *ctx, int kmax, double eta) {
         int nb = 0;
         vcycle_dev32(ctx, c.d_s32, c.d_z32, c.d_part2, &nb);
         launch_icg_scalar(2, c.d_isc, c.d_part2, nb, c.stream);
-        launch_icg_dupdate(c.d_d32, c.d_z32, nv, c.d_isc, c.stream);
+        launch_icg_dupdate(c.d_e32, c.d_d32, c.d_z32, nv, c.d_isc, c.stream);
         launch_kbyu_f32(l0, c.d_E32, c.d_d32, c.d_t32, c.d_part2, &nb, c.stream);
         launch_icg_scalar(1, c.d_isc, c.d_part2, nb, c.stream);
         nb = launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.d_part2, c.stream);
@@ -1298,7 +1309,7 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
     }
     launch_narrow(c.d_r, c.d_r32, nv, c.stream);
     if ((rc = inner_run(ctx, k, eta))) return rc;
-    launch_widen_dots(c.d_e32, c.d_z, c.d_r, c.d_r, nv, c.d_part, c.d_part2, nbv, c.stream);
+    launch_widen_dots(c.d_e32, c.d_d32, c.d_isc, c.d_z, c.d_r, c.d_r, nv, c.d_part, c.d_part2, nbv, c.stream);
     launch_flex_beta(c.d_scal, c.d_iflag, c.d_part, c.d_part2, nbv, 1, c.stream);
     CK(cudaMemcpyAsync(c.d_p, c.d_z, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c.stream));
     int h_flag[4] = {0, 0, 0, 0};
@@ -1337,7 +1348,7 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
         if (prof) CK(cudaEventRecord(pe[2], c.stream));
         launch_narrow(c.d_r, c.d_r32, nv, c.stream);
         if ((rc = inner_run(ctx, k, eta))) return rc;
-        launch_widen_dots(c.d_e32, c.d_z, c.d_r, c.d_q, nv, c.d_part, c.d_part2, nbv, c.stream);
+        launch_widen_dots(c.d_e32, c.d_d32, c.d_isc, c.d_z, c.d_r, c.d_q, nv, c.d_part, c.d_part2, nbv, c.stream);
         if (prof) {
             CK(cudaEventRecord(pe[3], c.stream));
             pc_pending = true;

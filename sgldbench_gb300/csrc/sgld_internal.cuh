@@ -77,7 +77,8 @@ struct Ctx {
     size_t trinv_smem = 0;
     double *d_cpart = nullptr;      // [CSPLIT*ncf] GEMV partials
     // templates for the level-2 Galerkin assembly
-    double *d_H = nullptr;          // [(8 + 64) * 576] templates for span 2, then span 4
+    double *d_H = nullptr;          // [2 (8 + 64) * 576] templates for span 2, span 4, then both as
+                                    // (hi, lo) float pairs
     // PCG vectors (full grid, FP64)
     double *d_b = nullptr, *d_x = nullptr, *d_r = nullptr, *d_z = nullptr, *d_p = nullptr, *d_q = nullptr;
     double *d_tmp = nullptr;
@@ -138,8 +139,9 @@ void launch_icg_cond(cudaGraphConditionalHandle h, double *sc, const double *par
 int launch_icg_init(const float *r, float *s, float *e, float *d, int64_t n, double *part, cudaStream_t st);
 void launch_icg_cond_flag(int *flag, double *sc, const double *part, int nb, int kmax, double eta_min,
                           const double *outer, double *total, cudaStream_t s);
-void launch_icg_dupdate(float *d, const float *w, int64_t n, const double *sc, cudaStream_t st);
-void launch_widen_dots(const float *e, double *z, const double *r, const double *q, int64_t n, double *p1,
+void launch_icg_dupdate(float *e, float *d, const float *w, int64_t n, const double *sc, cudaStream_t st);
+void launch_widen_dots(const float *e, const float *d, const double *sc, double *z, const double *r,
+                       const double *q, int64_t n, double *p1,
                        double *p2, int nb, cudaStream_t st);
 void launch_flex_beta(double *scal, const int *iflag, const double *p1, const double *p2, int nb, int first,
                       cudaStream_t st);

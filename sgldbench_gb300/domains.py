@@ -88,10 +88,14 @@ def simp_modulus(rho, E0: float = 1.0, Emin: float = 1e-9, p: float = 3.0):
     return Emin + np.asarray(rho, dtype=np.float64) ** p * (E0 - Emin)
 
 
-def _largest_component(mask: np.ndarray) -> np.ndarray:
-    from scipy.ndimage import label
+def _largest_component(mask: np.ndarray, connectivity: int = 6) -> np.ndarray:
+    """Largest connected component: face-connected (6) by default, so that no
+    part hangs on a shared node or edge (a mechanical hinge that makes the
+    stiffness matrix near-singular); 26 gives the corner-connected component."""
+    from scipy.ndimage import generate_binary_structure, label
 
-    lab, n = label(mask, structure=np.ones((3, 3, 3), bool))
+    rank = {6: 1, 18: 2, 26: 3}[connectivity]
+    lab, n = label(mask, structure=generate_binary_structure(3, rank))
     if n <= 1:
         return mask
     sizes = np.bincount(lab.reshape(-1))
@@ -102,7 +106,8 @@ def _largest_component(mask: np.ndarray) -> np.ndarray:
 def blobby_union(nx: int, ny: int, nz: int, seed: int = 0, n_spheres: int = 12, n_boxes: int = 8,
                  r_range=(20, 60), edge_range=(30, 120), fill: float | None = None) -> np.ndarray:
     """Config-2 style domain: union of seeded spheres and axis-aligned boxes,
-    largest 26-connected component.  Radii / edges scale with the grid when it
+    largest face-connected component (26-connected parts joined only through
+    a node or an edge would hinge).  Radii / edges scale with the grid when it
     is smaller than 512 x 256 x 256.  With ``fill``, every radius and edge is
     multiplied by one common factor (>= 1, found by bisection) so that the
     largest component covers about that fraction of the box: at the literal

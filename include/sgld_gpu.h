@@ -204,8 +204,12 @@ int sgld_pcg(sgld_ctx *ctx, const double *b, double *x, const sgld_solve_opts *o
  * assembly (the reference solves its load cases one after another through
  * Solving_CG_GMGS.m:7).  F and U hold nrhs compact DOF vectors back to back
  * (case j at offset j * numDOFs); U holds the initial guesses when
- * opts->use_x0.  info, if not NULL, receives nrhs entries.  The cases are
- * solved in order on the context's stream. */
+ * opts->use_x0.  info, if not NULL, receives nrhs entries.  In the mixed
+ * precision modes the whole block is one CUDA-graph launch (per case: the
+ * outer flexible PCG and the inner FP32 CG as device-side while loops, so no
+ * host round trip between iterations or cases); info[j].seconds is the
+ * block's device time / nrhs.  In FP64 the cases are solved one after
+ * another. */
 int sgld_solve_block(sgld_ctx *ctx, int nrhs, const double *F, double *U, const sgld_solve_opts *opts,
                      sgld_solve_info *info);
 int sgld_pcg_device(sgld_ctx *ctx, const double *d_b, double *d_x, const sgld_solve_opts *opts,

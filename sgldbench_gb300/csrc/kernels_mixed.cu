@@ -78,6 +78,22 @@ __global__ void k_icg_cond(cudaGraphConditionalHandle h, double *__restrict__ sc
     cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
+// after the outer residual test: keep the outer while loop going and apply
+// the preconditioner (the if node) unless the solve stopped (iflag[2])
+__global__ void k_outer_cond(cudaGraphConditionalHandle hw, cudaGraphConditionalHandle hi,
+                             const int *__restrict__ iflag) {
+    if (threadIdx.x != 0) return;
+    const unsigned go = iflag[2] ? 0u : 1u;
+    cudaGraphSetConditional(hw, go);
+    cudaGraphSetConditional(hi, go);
+}
+
+void launch_outer_cond(cudaGraphConditionalHandle hw, cudaGraphConditionalHandle hi, const int *iflag,
+                       cudaStream_t s) {
+    ++g_launches;
+    k_outer_cond<<<1, 32, 0, s>>>(hw, hi, iflag);
+}
+
 // the same decision written to *flag for a host-driven loop (profiling: the
 // kernels of a conditional graph body do not appear in a profiler's launch list)
 __global__ void k_icg_cond_flag(int *flag, double *__restrict__ sc, const double *__restrict__ part, int nb,

@@ -500,7 +500,8 @@ static constexpr size_t kbyu_x2_smem() { return sizeof(float) * KX_RING_FLOATS +
 static_assert((KX_RING_FLOATS * sizeof(float)) % 16 == 0, "float2 exchange area must be aligned");
 
 // node layers per CTA of k_kbyu_x2: an odd count (so that the element layers
-// z0-1 .. z0+zc-1 form whole pairs) near 15, balanced over the z extent
+// z0-1 .. z0+zc-1 form whole pairs).  Default: near 15, balanced over the z
+// extent; sgld_assemble's tuner (tune_kbyu_f32) may set another per level.
 static int kbyu_x2_zc(int NZ) {
     const int chunks = (NZ + 14) / 15;
     int zc = (NZ + chunks - 1) / chunks;
@@ -508,9 +509,11 @@ static int kbyu_x2_zc(int NZ) {
     return zc;
 }
 
+int kbyu_f32_zc(const Level &l) { return l.kx_zc > 0 ? l.kx_zc : kbyu_x2_zc(l.nz + 1); }
+
 static dim3 kbyu_x2_grid(const Level &l) {
     const int NZ = l.nz + 1;
-    const int zc = kbyu_x2_zc(NZ);
+    const int zc = kbyu_f32_zc(l);
     return dim3((l.ny + 1 + KT_Y - 2) / (KT_Y - 1), (l.nx + 1 + KT_X - 2) / (KT_X - 1), (NZ + zc - 1) / zc);
 }
 
@@ -552,7 +555,7 @@ void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *
 void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
                      int *nblocks_out, cudaStream_t s) {
     const dim3 g = kbyu_x2_grid(l0);
-    const int zc = kbyu_x2_zc(l0.nz + 1);
+    const int zc = kbyu_f32_zc(l0);
     if (nblocks_out) *nblocks_out = (int)(g.x * g.y * g.z);
     ++g_launches;
     if (partial_dot)

@@ -299,20 +299,21 @@ int vcycle_dev(sgld_ctx *ctx, const double *r, double *z, double *partial, int *
 }
 
 // the same additive V-cycle in FP32 (mixed-precision preconditioner)
-int vcycle_dev32(sgld_ctx *ctx, const float *r, float *z, double *partial, int *nb) {
+int vcycle_dev32(sgld_ctx *ctx, const float *r, float *z, double *partial, int *nb, cudaStream_t st = nullptr) {
     Ctx &c = ctx->c;
+    if (!st) st = c.stream;
     const int L = c.L;
     const float *rf = r;
     for (int l = 1; l < L; ++l) {
-        launch_restrict<float>(c.lv[l - 1], c.lv[l], rf, c.lv[l].r32, c.stream);
+        launch_restrict<float>(c.lv[l - 1], c.lv[l], rf, c.lv[l].r32, st);
         rf = c.lv[l].r32;
     }
-    launch_coarse_apply_f32(c, c.lv[L - 1].r32, c.lv[L - 1].x32, c.stream);
+    launch_coarse_apply_f32(c, c.lv[L - 1].r32, c.lv[L - 1].x32, st);
     for (int l = L - 2; l >= 0; --l) {
         const float *rl = (l == 0) ? r : c.lv[l].r32;
         float *xl = (l == 0) ? z : c.lv[l].x32;
         launch_prolong_smooth<float>(c.lv[l], c.lv[l + 1], c.lv[l + 1].x32, rl, c.lv[l].idiag32, (float)c.omega, xl,
-                                     l == 0, l == 0 ? partial : nullptr, l == 0 ? nb : nullptr, c.stream);
+                                     l == 0, l == 0 ? partial : nullptr, l == 0 ? nb : nullptr, st);
     }
     return SGLD_OK;
 }
@@ -329,46 +330,82 @@ int vcycle_dev32(sgld_ctx *ctx, const float *r, float *z, double *partial, int *
 // solve needs no host round trip.  d_isc[IS_TOTAL] counts the iterations run.
 constexpr int IS_TOTAL = 8;
 
-static int build_inner_graph(sgld_ctx *ctx, int kmax, double eta) {
-    Ctx &c = ctx->c;
-    const Level &l0 = c.lv[0];
-    const int64_t nv = 3 * l0.nnode;
-    cudaGraph_t g = nullptr;
-    CK(cudaGraphCreate(&g, 0));
-    cudaGraphConditionalHandle h;
-    CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
-    int64_t before = g_launches;
-    CK(cudaStreamBeginCaptureToGraph(c.stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    const int nbi = launch_icg_init(c.d_r32, c.d_s32, c.d_e32, c.d_d32, nv, c.d_part2, c.stream);
-    launch_icg_scalar(0, c.d_isc, c.d_part2, nbi, c.stream);
+// Adds a conditional node after the current capture position of stream s
+// (which must be capturing) with handle h (created by the caller on the graph
+// s captures into) and returns its body graph; capture continues after it.
+static int add_conditional(sgld_ctx *ctx, cudaStream_t s, cudaGraphConditionalHandle h,
+                           cudaGraphConditionalNodeType type, cudaGraph_t *body) {
     cudaStreamCaptureStatus st;
     const cudaGraphNode_t *deps = nullptr;
     size_t ndeps = 0;
-    CK(cudaStreamGetCaptureInfo(c.stream, &st, nullptr, nullptr, &deps, nullptr, &ndeps));
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &ndeps));
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = h;
-    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.type = type;
     cp.conditional.size = 1;
-    cudaGraphNode_t wnode;
-    CK(cudaGraphAddNode(&wnode, g, deps, nullptr, ndeps, &cp));
-    CK(cudaStreamUpdateCaptureDependencies(c.stream, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies));
-    CK(cudaStreamEndCapture(c.stream, &g));
-    c.inner_entry_launches = g_launches - before;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp));
+    CK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    *body = cp.conditional.phGraph_out[0];
+    return SGLD_OK;
+}
+
+static cudaGraph_t capturing_graph(cudaStream_t s) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamGetCaptureInfo(s, &st, nullptr, &g, nullptr, nullptr, nullptr) != cudaSuccess) return nullptr;
+    return g;
+}
+
+// Captures one inner solve: entry kernels on s (capturing), then a while node
+// whose body (one CG iteration) is captured on stream sb.  *entry / *body
+// receive the kernel launches of each part.
+static int capture_inner(sgld_ctx *ctx, cudaStream_t s, cudaStream_t sb, int kmax, double eta, int64_t *entry,
+                         int64_t *body_n) {
+    Ctx &c = ctx->c;
+    const Level &l0 = c.lv[0];
+    const int64_t nv = 3 * l0.nnode;
+    int64_t before = g_launches;
+    const int nbi = launch_icg_init(c.d_r32, c.d_s32, c.d_e32, c.d_d32, nv, c.d_part2, s);
+    launch_icg_scalar(0, c.d_isc, c.d_part2, nbi, s);
+    *entry = g_launches - before;
+    cudaGraphConditionalHandle h;
+    CK(cudaGraphConditionalHandleCreate(&h, capturing_graph(s), 1, cudaGraphCondAssignDefault));
+    cudaGraph_t body = nullptr;
+    int rc = add_conditional(ctx, s, h, cudaGraphCondTypeWhile, &body);
+    if (rc) return rc;
     before = g_launches;
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    CK(cudaStreamBeginCaptureToGraph(c.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    CK(cudaStreamBeginCaptureToGraph(sb, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     int nb = 0;
-    vcycle_dev32(ctx, c.d_s32, c.d_z32, c.d_part2, &nb);
-    launch_icg_scalar(2, c.d_isc, c.d_part2, nb, c.stream);
-    launch_icg_dupdate(c.d_e32, c.d_d32, c.d_z32, nv, c.d_isc, c.stream);
-    launch_kbyu_f32(l0, c.d_E32, c.d_d32, c.d_t32, c.d_part2, &nb, c.stream);
-    launch_icg_scalar(1, c.d_isc, c.d_part2, nb, c.stream);
-    nb = launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.d_part2, c.stream);
-    launch_icg_cond(h, c.d_isc, c.d_part2, nb, kmax, eta, c.d_scal, c.d_isc + IS_TOTAL, c.stream);
-    CK(cudaStreamEndCapture(c.stream, &body));
-    c.inner_body_launches = g_launches - before;
-    g_launches = before - c.inner_entry_launches;
+    vcycle_dev32(ctx, c.d_s32, c.d_z32, c.d_part2, &nb, sb);
+    launch_icg_scalar(2, c.d_isc, c.d_part2, nb, sb);
+    launch_icg_dupdate(c.d_e32, c.d_d32, c.d_z32, nv, c.d_isc, sb);
+    launch_kbyu_f32(l0, c.d_E32, c.d_d32, c.d_t32, c.d_part2, &nb, sb);
+    launch_icg_scalar(1, c.d_isc, c.d_part2, nb, sb);
+    nb = launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.d_part2, sb);
+    launch_icg_cond(h, c.d_isc, c.d_part2, nb, kmax, eta, c.d_scal, c.d_isc + IS_TOTAL, sb);
+    CK(cudaStreamEndCapture(sb, &body));
+    *body_n = g_launches - before;
+    return SGLD_OK;
+}
+
+static int build_inner_graph(sgld_ctx *ctx, int kmax, double eta) {
+    Ctx &c = ctx->c;
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    const int64_t before = g_launches;
+    CK(cudaStreamBeginCaptureToGraph(c.stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    int rc = capture_inner(ctx, c.stream, c.aux[0], kmax, eta, &c.inner_entry_launches, &c.inner_body_launches);
+    cudaGraph_t g2 = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(c.stream, &g2);
+    g_launches = before;
+    if (rc) {
+        cudaGraphDestroy(g);
+        return rc;
+    }
+    CK(ec);
     const cudaError_t e = cudaGraphInstantiate(&c.inner_graph, g, 0);
     cudaGraphDestroy(g);
     CK(e);
@@ -466,6 +503,8 @@ int download_nodes(sgld_ctx *ctx, const double *d_full, double *h) {
 
 int pcg_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info);
 int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info);
+static int run_solve_graph(sgld_ctx *ctx, int nrhs, bool staged, const sgld_solve_opts *o, sgld_solve_info *infos);
+static int ensure_block_buffers(sgld_ctx *ctx, int nrhs);
 
 int solve_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
     if (o->maxit < 1 || !(o->tol >= 0.0)) return fail(ctx, SGLD_ERR_ARG, "maxit must be >= 1 and tol >= 0");
@@ -559,6 +598,7 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
     *out = ctx;
     if (cudaSetDevice(c.device) != cudaSuccess) return fail(ctx, SGLD_ERR_CUDA, "cudaSetDevice failed");
     CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    for (auto &a : c.aux) CK(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
     // element / node activity per level (host)
     ctx->nodemaps.resize(L);
     ctx->elemaps.resize(L);
@@ -663,6 +703,11 @@ void sgld_destroy(sgld_ctx *ctx) {
     if (c.inner_graph) cudaGraphExecDestroy(c.inner_graph);
     if (c.factor_graph) cudaGraphExecDestroy(c.factor_graph);
     if (c.stream) cudaStreamDestroy(c.stream);
+    for (auto &a : c.aux)
+        if (a) cudaStreamDestroy(a);
+    if (c.solve_graph) cudaGraphExecDestroy(c.solve_graph);
+    for (void *p : {(void *)c.d_blk, (void *)c.d_binfo})
+        if (p) cudaFree(p);
     delete ctx;
 }
 
@@ -793,6 +838,10 @@ int sgld_set_fixed_dofs(sgld_ctx *ctx, const uint8_t *fixed) {
         CK(dalloc(&c.d_LB, (size_t)ncf * (band + 1) + ncf + (size_t)((ncf + 31) / 32) * 1024));
         CK(dalloc(&c.d_cy, 2 * (size_t)ncf));
         CK(dalloc(&c.d_cfree, (size_t)ncf + 3 * lc.nnode));
+        if (c.solve_graph) {
+            cudaGraphExecDestroy(c.solve_graph);
+            c.solve_graph = nullptr;
+        }
         if (c.inner_graph) {   // the captured graphs hold the old coarse buffers
             cudaGraphExecDestroy(c.inner_graph);
             c.inner_graph = nullptr;
@@ -837,6 +886,51 @@ int sgld_set_modulus(sgld_ctx *ctx, const double *E) {
     return sgld_set_modulus_device(ctx, c.d_tmp);
 }
 
+// Autotuner of the FP32 K*u's z-chunk (node layers per CTA): times each odd
+// candidate with CUDA events on the context's stream (3 launches after a
+// warm-up) and keeps the fastest in lv[0].kx_zc.  Runs once per context, at
+// the first assembly (never during a graph capture); SGLD_AUTOTUNE=0 keeps
+// the default rule.  The chunk trades halo work (one extra element layer per
+// CTA) against the number of CTAs in flight.
+static int tune_kbyu_f32(sgld_ctx *ctx) {
+    Ctx &c = ctx->c;
+    Level &l0 = c.lv[0];
+    if (c.kbyu_tuned) return SGLD_OK;
+    c.kbyu_tuned = true;
+    const char *v = getenv("SGLD_AUTOTUNE");
+    if (v && strcmp(v, "0") == 0) return SGLD_OK;
+    const int NZ = l0.nz + 1;
+    std::vector<int> cand;
+    for (int zc : {7, 9, 11, 15, 21, 31, 47})
+        if (zc <= NZ) cand.push_back(zc);
+    cand.push_back(0);   // the default rule
+    CK(cudaMemsetAsync(c.d_r32, 0, sizeof(float) * 3 * (size_t)l0.nnode, c.stream));
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    float best = 1e30f;
+    int best_zc = 0;
+    for (int zc : cand) {
+        l0.kx_zc = zc;
+        launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, c.stream);
+        CK(cudaEventRecord(a, c.stream));
+        for (int r = 0; r < 3; ++r) launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, c.stream);
+        CK(cudaEventRecord(b, c.stream));
+        CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best) {
+            best = ms;
+            best_zc = zc;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    l0.kx_zc = best_zc;
+    CKL();
+    return SGLD_OK;
+}
+
 int sgld_assemble(sgld_ctx *ctx) {
     int rc = check_ready(ctx);
     if (rc) return rc;
@@ -873,6 +967,10 @@ int sgld_assemble(sgld_ctx *ctx) {
     CKL();
     CK(cudaStreamSynchronize(c.stream));
     c.assembled = true;
+    if (!c.kbyu_tuned) {
+        const int rct = tune_kbyu_f32(ctx);
+        if (rct) return rct;
+    }
     return SGLD_OK;
 }
 
@@ -1044,6 +1142,20 @@ int sgld_solve_block(sgld_ctx *ctx, int nrhs, const double *F, double *U, const 
     if (rc) return rc;
     if (nrhs < 0 || (nrhs > 0 && (!F || !U || !o))) return fail(ctx, SGLD_ERR_ARG, "bad block arguments");
     const int64_t nd = 3 * (int64_t)ctx->c.h_nodemap.size();
+    const bool mixed = o && (o->precision == SGLD_PREC_MIXED || o->precision == SGLD_PREC_MIXED_DF);
+    if (nrhs > 0 && mixed && !o->history && !o->profile && !inner_loop_on_host()) {
+        // all cases in one graph launch: F (and U0) staged in d_blk, U back from it
+        if (o->maxit < 1 || !(o->tol >= 0.0)) return fail(ctx, SGLD_ERR_ARG, "maxit must be >= 1 and tol >= 0");
+        Ctx &c = ctx->c;
+        if ((rc = ensure_block_buffers(ctx, nrhs))) return rc;
+        const size_t bytes = sizeof(double) * (size_t)nrhs * nd;
+        CK(cudaMemcpyAsync(c.d_blk, F, bytes, cudaMemcpyHostToDevice, c.stream));
+        if (o->use_x0) CK(cudaMemcpyAsync(c.d_blk + (size_t)nrhs * nd, U, bytes, cudaMemcpyHostToDevice, c.stream));
+        if ((rc = run_solve_graph(ctx, nrhs, true, o, info))) return rc;
+        CK(cudaMemcpyAsync(U, c.d_blk + (size_t)nrhs * nd, bytes, cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaStreamSynchronize(c.stream));
+        return SGLD_OK;
+    }
     for (int j = 0; j < nrhs; ++j)
         if ((rc = sgld_pcg(ctx, F + j * nd, U + j * nd, o, info ? info + j : nullptr))) return rc;
     return SGLD_OK;
@@ -1276,6 +1388,9 @@ int pcg_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
 // (SGLD_PREC_MIXED_DF, ~2^-48 relative, FP32 issue rate), and so are the
 // warm-start residual and the true residual at exit.
 int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
+    // the whole solve as one graph launch unless a per-iteration host record
+    // (history, profile) or the host-driven inner loop is asked for
+    if (!o->history && !o->profile && !inner_loop_on_host()) return run_solve_graph(ctx, 1, false, o, info);
     Ctx &c = ctx->c;
     const Level &l0 = c.lv[0];
     const int64_t nv = 3 * l0.nnode;
@@ -1397,6 +1512,202 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
         info->kbyu_seconds = kb_ms * 1e-3;
         info->kbyu_launches = kb_n;
         info->precond_seconds = pc_ms * 1e-3;
+    }
+    return SGLD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The mixed-precision solve of one or several load cases as ONE CUDA graph:
+// per case a prologue, the outer flexible-PCG loop as a conditional while
+// node, and an epilogue.  The outer body is
+//   q = K p; lambda; x, r update; residual test; set the loop conditions;
+//   if not stopped (conditional if node): r32 = r; inner FP32 CG (its own
+//     while node, nested); z = e + alpha d; flexible beta; p = z + beta p,
+// so a whole block of cases runs from one launch with no host round trip.
+// Staged cases take F (and U0) from d_blk (compact DOFs, case after case) and
+// return U there; an unstaged single case uses d_b / d_x as they are.
+// Per-case results land in d_binfo (8 doubles each): the outer flags (4 ints),
+// relative residual, ||b||, true residual^2, inner iterations.
+static int build_solve_graph(sgld_ctx *ctx, int nrhs, bool staged, bool use_x0, int kmax, double eta, double tol,
+                             int maxit, bool dfk) {
+    Ctx &c = ctx->c;
+    const Level &l0 = c.lv[0];
+    const int64_t nv = 3 * l0.nnode, ncomp = (int64_t)c.h_nodemap.size(), nd = 3 * ncomp;
+    const int nbv = reduce_blocks(nv);
+    auto kbyu_outer = [&](const double *u, double *y, double *part, int *nb, cudaStream_t st) {
+        if (dfk)
+            launch_kbyu_df(l0, c.E, u, y, part, nb, st);
+        else
+            launch_kbyu_f64(l0, c.E, u, y, part, nb, st);
+    };
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    const int64_t start = g_launches;
+    cudaStream_t s = c.stream;
+    CK(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    int rc = SGLD_OK;
+    int64_t fixed = 0, outer = 0, ifb = 0, inner = 0, e_in = 0;
+    for (int j = 0; j < nrhs && rc == SGLD_OK; ++j) {
+        int64_t t0 = g_launches;
+        cudaMemsetAsync(c.d_isc + IS_TOTAL, 0, sizeof(double), s);
+        if (staged) {
+            cudaMemsetAsync(c.d_b, 0, sizeof(double) * nv, s);
+            launch_scatter_nodes(c.d_nodemap, ncomp, c.d_blk + j * nd, c.d_b, s);
+            cudaMemsetAsync(c.d_x, 0, sizeof(double) * nv, s);
+            if (use_x0) launch_scatter_nodes(c.d_nodemap, ncomp, c.d_blk + (nrhs + j) * nd, c.d_x, s);
+        }
+        launch_pcg_scalar(5, c.d_scal, c.d_iflag, c.d_part, 1, tol, maxit, s);
+        launch_dot(c.d_b, c.d_b, nv, c.d_part, nbv, s);
+        launch_pcg_scalar(0, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, s);
+        if (use_x0) {
+            kbyu_outer(c.d_x, c.d_q, nullptr, nullptr, s);
+            launch_residual(c.d_r, c.d_b, c.d_q, nv, s);
+        } else {
+            cudaMemcpyAsync(c.d_r, c.d_b, sizeof(double) * nv, cudaMemcpyDeviceToDevice, s);
+        }
+        launch_narrow(c.d_r, c.d_r32, nv, s);
+        const int64_t t1 = g_launches;
+        if ((rc = capture_inner(ctx, s, c.aux[0], kmax, eta, &e_in, &inner))) break;
+        const int64_t t2 = g_launches;
+        launch_widen_dots(c.d_e32, c.d_d32, c.d_isc, c.d_z, c.d_r, c.d_r, nv, c.d_part, c.d_part2, nbv, s);
+        launch_flex_beta(c.d_scal, c.d_iflag, c.d_part, c.d_part2, nbv, 1, s);
+        cudaMemcpyAsync(c.d_p, c.d_z, sizeof(double) * nv, cudaMemcpyDeviceToDevice, s);
+        const int64_t t3 = g_launches;
+        // outer loop
+        cudaGraphConditionalHandle hw;
+        if (cudaGraphConditionalHandleCreate(&hw, capturing_graph(s), 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+            rc = fail(ctx, SGLD_ERR_CUDA, "conditional handle");
+            break;
+        }
+        cudaGraph_t wbody = nullptr;
+        if ((rc = add_conditional(ctx, s, hw, cudaGraphCondTypeWhile, &wbody))) break;
+        cudaStream_t sw = c.aux[0], si = c.aux[1];
+        CK(cudaStreamBeginCaptureToGraph(sw, wbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        const int64_t t4 = g_launches;
+        int nb = 0;
+        kbyu_outer(c.d_p, c.d_q, c.d_part, &nb, sw);
+        launch_pcg_scalar(2, c.d_scal, c.d_iflag, c.d_part, nb, tol, maxit, sw);
+        launch_pcg_update(c.d_x, c.d_r, c.d_p, c.d_q, nv, c.d_scal, c.d_iflag, c.d_part, nbv, sw);
+        launch_pcg_scalar(3, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, sw);
+        cudaGraphConditionalHandle hi;
+        CK(cudaGraphConditionalHandleCreate(&hi, capturing_graph(sw), 0, cudaGraphCondAssignDefault));
+        launch_outer_cond(hw, hi, c.d_iflag, sw);
+        const int64_t t5 = g_launches;
+        cudaGraph_t ibody = nullptr;
+        if ((rc = add_conditional(ctx, sw, hi, cudaGraphCondTypeIf, &ibody))) break;
+        CK(cudaStreamBeginCaptureToGraph(si, ibody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        launch_narrow(c.d_r, c.d_r32, nv, si);
+        const int64_t t6 = g_launches;
+        int64_t e2 = 0, b2 = 0;
+        if ((rc = capture_inner(ctx, si, c.aux[2], kmax, eta, &e2, &b2))) break;
+        const int64_t t7 = g_launches;
+        launch_widen_dots(c.d_e32, c.d_d32, c.d_isc, c.d_z, c.d_r, c.d_q, nv, c.d_part, c.d_part2, nbv, si);
+        launch_flex_beta(c.d_scal, c.d_iflag, c.d_part, c.d_part2, nbv, 0, si);
+        launch_pcg_pupdate(c.d_p, c.d_z, nv, c.d_scal, c.d_iflag, si);
+        const int64_t t8 = g_launches;
+        CK(cudaStreamEndCapture(si, &ibody));
+        CK(cudaStreamEndCapture(sw, &wbody));
+        // epilogue: true residual, results, U
+        const int64_t t9 = g_launches;
+        kbyu_outer(c.d_x, c.d_q, nullptr, nullptr, s);
+        launch_residual(c.d_tmp, c.d_b, c.d_q, nv, s);
+        launch_dot(c.d_tmp, c.d_tmp, nv, c.d_part, nbv, s);
+        double *info = c.d_binfo + 8 * j;
+        launch_finalize_sum(c.d_part, nbv, info + 4, s);
+        cudaMemcpyAsync(info, c.d_iflag, 4 * sizeof(int), cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(info + 2, c.d_scal + 3, sizeof(double), cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(info + 3, c.d_scal + 0, sizeof(double), cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(info + 5, c.d_isc + IS_TOTAL, sizeof(double), cudaMemcpyDeviceToDevice, s);
+        if (staged) launch_gather_nodes(c.d_nodemap, ncomp, c.d_x, c.d_blk + (nrhs + j) * nd, s);
+        const int64_t t10 = g_launches;
+        fixed = (t1 - t0) + e_in + (t3 - t2) + (t10 - t9);
+        outer = t5 - t4;
+        ifb = (t6 - t5) + e2 + (t8 - t7);
+    }
+    cudaGraph_t gend = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(s, &gend);
+    g_launches = start;
+    if (rc == SGLD_OK && ec != cudaSuccess) rc = fail(ctx, SGLD_ERR_CUDA, std::string("solve graph capture: ") + cudaGetErrorString(ec));
+    if (rc == SGLD_OK) {
+        const cudaError_t ei = cudaGraphInstantiate(&c.solve_graph, g, 0);
+        if (ei != cudaSuccess) rc = fail(ctx, SGLD_ERR_CUDA, std::string("solve graph instantiate: ") + cudaGetErrorString(ei));
+    }
+    cudaGraphDestroy(g);
+    c.sg_fixed = fixed;
+    c.sg_outer = outer;
+    c.sg_if = ifb;
+    c.sg_inner = inner;
+    return rc;
+}
+
+static int ensure_block_buffers(sgld_ctx *ctx, int nrhs) {
+    Ctx &c = ctx->c;
+    if (nrhs <= c.blk_cap) return SGLD_OK;
+    if (c.d_blk) cudaFree(c.d_blk);
+    if (c.d_binfo) cudaFree(c.d_binfo);
+    c.d_blk = nullptr;
+    c.d_binfo = nullptr;
+    c.blk_cap = 0;
+    if (c.solve_graph) {   // the graph refers to the old buffers
+        cudaGraphExecDestroy(c.solve_graph);
+        c.solve_graph = nullptr;
+    }
+    const size_t nd = 3 * c.h_nodemap.size();
+    CK(dalloc(&c.d_blk, 2 * (size_t)nrhs * nd));
+    CK(dalloc(&c.d_binfo, 8 * (size_t)nrhs));
+    c.blk_cap = nrhs;
+    return SGLD_OK;
+}
+
+// runs the solve graph for nrhs cases (building it when the key changed)
+static int run_solve_graph(sgld_ctx *ctx, int nrhs, bool staged, const sgld_solve_opts *o, sgld_solve_info *infos) {
+    Ctx &c = ctx->c;
+    const bool fixed_k = o->inner_its > 0 && !(o->inner_tol > 0.0);
+    const int kmax = o->inner_its > 0 ? o->inner_its : 64;
+    const double eta = fixed_k ? 0.0 : (o->inner_tol > 0.0 ? o->inner_tol : 3e-4);
+    const bool dfk = o->precision == SGLD_PREC_MIXED_DF;
+    int rc = ensure_block_buffers(ctx, std::max(nrhs, 1));
+    if (rc) return rc;
+    const std::vector<double> key = {(double)nrhs, staged ? 1.0 : 0.0, o->use_x0 ? 1.0 : 0.0, (double)kmax, eta,
+                                     o->tol, (double)o->maxit, dfk ? 1.0 : 0.0};
+    if (!c.solve_graph || key != c.solve_key) {
+        if (c.solve_graph) {
+            cudaGraphExecDestroy(c.solve_graph);
+            c.solve_graph = nullptr;
+        }
+        if ((rc = build_solve_graph(ctx, nrhs, staged, o->use_x0 != 0, kmax, eta, o->tol, o->maxit, dfk))) return rc;
+        c.solve_key = key;
+    }
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, c.stream));
+    CK(cudaGraphLaunch(c.solve_graph, c.stream));
+    CK(cudaEventRecord(e1, c.stream));
+    std::vector<double> res(8 * (size_t)nrhs);
+    CK(cudaMemcpyAsync(res.data(), c.d_binfo, sizeof(double) * res.size(), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (int j = 0; j < nrhs; ++j) {
+        const double *r = res.data() + 8 * j;
+        int fl[4];
+        memcpy(fl, r, sizeof fl);
+        const int its = fl[0];
+        g_launches += c.sg_fixed + (int64_t)its * c.sg_outer + (int64_t)std::max(its - 1, 0) * c.sg_if +
+                      (int64_t)r[5] * c.sg_inner;
+        if (infos) {
+            sgld_solve_info &in = infos[j];
+            memset(&in, 0, sizeof in);
+            in.iterations = its;
+            in.converged = fl[1];
+            in.relres = r[2];
+            in.true_relres = r[3] > 0 ? sqrt(r[4]) / r[3] : 0.0;
+            in.inner_iterations = (int)r[5];
+            in.seconds = ms * 1e-3 / nrhs;
+        }
     }
     return SGLD_OK;
 }

@@ -30,6 +30,7 @@ constexpr int KH_NNZ = 45;
 struct Level {
     int nx = 0, ny = 0, nz = 0;   // elements
     int span = 1;                 // coarsening factor from the next finer level
+    int kx_zc = 0;                // node layers per CTA of the FP32 K*u (0 = default rule; set by the tuner)
     int64_t nel = 0, nnode = 0;   // full-grid counts
     int64_t nel_active = 0, nnode_active = 0;
     uint8_t *eact = nullptr;      // [nel] element non-empty
@@ -91,6 +92,16 @@ struct Ctx {
     float *d_e32 = nullptr, *d_s32 = nullptr, *d_d32 = nullptr, *d_t32 = nullptr;
     double *d_part2 = nullptr;      // second partial-sum buffer
     double *d_isc = nullptr;        // inner CG scalars
+    cudaStream_t aux[3] = {nullptr, nullptr, nullptr};   // capture streams of conditional bodies
+    // whole mixed-precision solves of a block of load cases as one graph
+    // (outer and inner loops as device-side while nodes), cached by its key
+    cudaGraphExec_t solve_graph = nullptr;
+    std::vector<double> solve_key;
+    int64_t sg_fixed = 0, sg_outer = 0, sg_if = 0, sg_inner = 0;   // launches per part
+    double *d_blk = nullptr;   // [2 nrhs numDOFs] compact F and U of the block
+    double *d_binfo = nullptr; // [8 nrhs] per-case results
+    int blk_cap = 0;
+    bool kbyu_tuned = false;   // the FP32 K*u z-chunk was tuned (tune_kbyu_f32)
     cudaGraphExec_t inner_graph = nullptr;   // inner FP32 CG: entry nodes + while node
     int inner_graph_k = 0;
     double inner_graph_eta = -1.0;
@@ -125,6 +136,7 @@ void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *
 void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
                      int *nblocks_out, cudaStream_t s);
 void init_kernel_attributes();
+int kbyu_f32_zc(const Level &l0);   // node layers per CTA the FP32 K*u uses on this level
 // double-float K*u (kernels_df.cu)
 void upload_kh_df(const double *Kh, cudaStream_t s);
 void init_kbyu_df_attributes();
@@ -137,6 +149,8 @@ int launch_icg_update(float *e, float *s, const float *d, const float *t, int64_
 void launch_icg_cond(cudaGraphConditionalHandle h, double *sc, const double *part, int nb, int kmax,
                      double eta_min, const double *outer, double *total, cudaStream_t s);
 int launch_icg_init(const float *r, float *s, float *e, float *d, int64_t n, double *part, cudaStream_t st);
+void launch_outer_cond(cudaGraphConditionalHandle hw, cudaGraphConditionalHandle hi, const int *iflag,
+                       cudaStream_t s);
 void launch_icg_cond_flag(int *flag, double *sc, const double *part, int nb, int kmax, double eta_min,
                           const double *outer, double *total, cudaStream_t s);
 void launch_icg_dupdate(float *e, float *d, const float *w, int64_t n, const double *sc, cudaStream_t st);

@@ -78,6 +78,19 @@ __global__ void k_icg_cond(cudaGraphConditionalHandle h, double *__restrict__ sc
     cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
+// sets a conditional handle: a handle's default value is applied when the
+// top-level graph is launched, not when a conditional body containing its
+// node runs again, so a loop nested in another loop's body is re-armed with
+// this kernel before each entry
+__global__ void k_set_cond(cudaGraphConditionalHandle h, unsigned v) {
+    if (threadIdx.x == 0) cudaGraphSetConditional(h, v);
+}
+
+void launch_set_cond(cudaGraphConditionalHandle h, unsigned v, cudaStream_t s) {
+    ++g_launches;
+    k_set_cond<<<1, 32, 0, s>>>(h, v);
+}
+
 // after the outer residual test: keep the outer while loop going and apply
 // the preconditioner (the if node) unless the solve stopped (iflag[2])
 __global__ void k_outer_cond(cudaGraphConditionalHandle hw, cudaGraphConditionalHandle hi,

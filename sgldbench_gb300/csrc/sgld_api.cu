@@ -367,12 +367,13 @@ static int capture_inner(sgld_ctx *ctx, cudaStream_t s, cudaStream_t sb, int kma
     Ctx &c = ctx->c;
     const Level &l0 = c.lv[0];
     const int64_t nv = 3 * l0.nnode;
+    cudaGraphConditionalHandle h;
+    CK(cudaGraphConditionalHandleCreate(&h, capturing_graph(s), 1, cudaGraphCondAssignDefault));
     int64_t before = g_launches;
     const int nbi = launch_icg_init(c.d_r32, c.d_s32, c.d_e32, c.d_d32, nv, c.d_part2, s);
     launch_icg_scalar(0, c.d_isc, c.d_part2, nbi, s);
+    launch_set_cond(h, 1u, s);   // re-arm: the loop may sit in another loop's body
     *entry = g_launches - before;
-    cudaGraphConditionalHandle h;
-    CK(cudaGraphConditionalHandleCreate(&h, capturing_graph(s), 1, cudaGraphCondAssignDefault));
     cudaGraph_t body = nullptr;
     int rc = add_conditional(ctx, s, h, cudaGraphCondTypeWhile, &body);
     if (rc) return rc;

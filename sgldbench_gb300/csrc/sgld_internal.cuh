@@ -151,6 +151,7 @@ void launch_icg_cond(cudaGraphConditionalHandle h, double *sc, const double *par
 int launch_icg_init(const float *r, float *s, float *e, float *d, int64_t n, double *part, cudaStream_t st);
 void launch_outer_cond(cudaGraphConditionalHandle hw, cudaGraphConditionalHandle hi, const int *iflag,
                        cudaStream_t s);
+void launch_set_cond(cudaGraphConditionalHandle h, unsigned v, cudaStream_t s);
 void launch_icg_cond_flag(int *flag, double *sc, const double *part, int nb, int kmax, double eta_min,
                           const double *outer, double *total, cudaStream_t s);
 void launch_icg_dupdate(float *e, float *d, const float *w, int64_t n, const double *sc, cudaStream_t st);

@@ -261,7 +261,18 @@ typedef struct sgld_topopt_opts {
     double penalty;        /* SIMPpenalty_ (0 = 3) */
     double E0, Emin;       /* modulus_, modulusMin_ (0 = 1, 1e-6) */
     sgld_solve_opts solve; /* tol_, maxIT_, precision of every MGPCG solve (warm-started) */
+    int optimizer;         /* SGLD_OPT_OC (0, the loop's bisection) or SGLD_OPT_MMA (1: the
+                              MMA update of TopOpti_GlobalVolumeConstraint.m:139-156, one
+                              volume constraint, passive elements excluded from the variables) */
 } sgld_topopt_opts;
+
+#define SGLD_OPT_OC 0
+#define SGLD_OPT_MMA 1
+
+/* Passive elements (passiveElements_, IO_ImportTopVoxels.m:76-80): n compact
+ * 0-based element indices kept solid by the SIMP loop (x = xPhys = 1,
+ * TopOpti_GlobalVolumeConstraint.m:162,179).  n = 0 clears the set. */
+int sgld_set_passive(sgld_ctx *ctx, int64_t n, const int64_t *elements);
 
 typedef struct sgld_topopt_iter {
     int loop, cg_iterations;

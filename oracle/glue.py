@@ -777,6 +777,8 @@ class TopOptOptions:
     E0: float = 1.0               # modulus_
     Emin: float = 1.0e-9          # modulusMin_
     tol: float = 1.0e-6           # tol_
+    optimizer: str = "OC"         # optimizer_: "OC" (the _Tmp loop's bisection) or "MMA"
+    passive: np.ndarray = None    # passiveElements_ (compact 0-based), kept solid
     maxit: int = 500              # maxIT_
 
 
@@ -808,19 +810,35 @@ def topopt_global_volume(model: Model, opt: TopOptOptions, history=None):
         dc = K.density_filter(dc / Hs, opt.rmin, emf, rx, ry, rz)            # :76
         dv = K.density_filter(dv / Hs, opt.rmin, emf, rx, ry, rz)            # :77
         g = float(xPhys.mean() - opt.volfrac)                                # :83
-        lo, hi = 0.0, 1e9                                                    # :84
-        while (hi - lo) / (lo + hi) > 1e-6:                                  # :85-90
-            lmid = 0.5 * (hi + lo)
-            xnew = np.maximum(0.0, np.maximum(x - opt.move, np.minimum(1.0, np.minimum(x + opt.move,
-                                                                                      x * np.sqrt(-dc / dv / lmid)))))
-            gt = g + float(np.sum(dv * (xnew - x)))
-            if gt > 0:
-                lo = lmid
-            else:
-                hi = lmid
-        change = float(np.abs(xnew - x).max())                              # :91
+        pas = np.zeros(n, bool) if opt.passive is None else np.isin(np.arange(n), opt.passive)
+        if opt.optimizer == "MMA":
+            # TopOpti_GlobalVolumeConstraint.m:139-156 (one volume constraint)
+            from oracle import mma
+            var = np.nonzero(~pas)[0]
+            xval = x[var]
+            xmin, xmax = np.maximum(0.0, xval - opt.move), np.minimum(1.0, xval + opt.move)
+            fval = xPhys.sum() / (n * opt.volfrac) - 1.0
+            xmma, _, _ = mma.mma_update(1, var.size, xval, xmin, xmax, xval, xval, dc[var], fval,
+                                        dv[var] / (n * opt.volfrac))
+            change = float(np.abs(xmma - xval).max())
+            xnew = np.ones(n)
+            xnew[var] = xmma
+        else:
+            lo, hi = 0.0, 1e9                                                # :84
+            while (hi - lo) / (lo + hi) > 1e-6:                              # :85-90
+                lmid = 0.5 * (hi + lo)
+                xnew = np.maximum(0.0, np.maximum(x - opt.move, np.minimum(1.0, np.minimum(
+                    x + opt.move, x * np.sqrt(-dc / dv / lmid)))))
+                xnew[pas] = 1.0                                              # GlobalVolumeConstraint.m:162
+                gt = g + float(np.sum(dv * (xnew - x)))
+                if gt > 0:
+                    lo = lmid
+                else:
+                    hi = lmid
+            change = float(np.abs(xnew - x).max())                          # :91
         x = xnew
         xPhys = K.density_filter(xnew, opt.rmin, emf, rx, ry, rz) / Hs       # :99
+        xPhys[pas] = 1.0                                                     # GlobalVolumeConstraint.m:179
         sharp = float(4.0 * np.sum(xPhys * (1.0 - xPhys)) / n)               # :102
         hist.append({"loop": loop, "c": c, "vol": vol, "sharp": sharp, "change": change, "g": g, "its": its})
     return xPhys, hist

@@ -39,7 +39,8 @@ class SolveInfo(C.Structure):
 
 class TopOptOpts(C.Structure):
     _fields_ = [("volfrac", dbl), ("rmin", dbl), ("move", dbl), ("n_loop", i32), ("min_change", dbl),
-                ("max_sharpness", dbl), ("penalty", dbl), ("E0", dbl), ("Emin", dbl), ("solve", SolveOpts)]
+                ("max_sharpness", dbl), ("penalty", dbl), ("E0", dbl), ("Emin", dbl), ("solve", SolveOpts),
+                ("optimizer", i32)]
 
 
 class TopOptIter(C.Structure):
@@ -81,6 +82,7 @@ SIGNATURES = {
     "sgld_principal_stress": (i32, [vp, vp, vp, vp]),
     "sgld_pde_filter": (i32, [vp, dbl, vp, vp, dbl, i32, vp]),
     "sgld_mma_update": (i32, [vp, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    "sgld_set_passive": (i32, [vp, i64, vp]),
     "sgld_get_stream": (vp, [vp]),
     "sgld_kernel_launches": (i64, []),
     "sgld_time_op": (i32, [vp, i32, i32, vp]),

@@ -10,6 +10,8 @@
 // order (z outer, x, y inner).
 #include <math.h>
 
+#include <algorithm>
+
 #include "sgld_internal.cuh"
 
 namespace sgld {
@@ -146,6 +148,10 @@ __device__ __forceinline__ double oc_new(double xe, double qe, double rs, double
     return fmax(0.0, fmax(xe - move, fmin(1.0, fmin(xe + move, qe * rs))));
 }
 
+// element flags of level 1: bit 0 active, bit 1 passive (kept solid by the
+// SIMP loop; TopOpti_GlobalVolumeConstraint.m:162,179)
+constexpr uint8_t EF_PASSIVE = 2;
+
 __global__ void k_oc_step(const double *__restrict__ x, const double *__restrict__ q, const double *__restrict__ dv,
                           const uint8_t *__restrict__ eact, int64_t n, double move, const double *__restrict__ st,
                           double *__restrict__ part) {
@@ -155,7 +161,8 @@ __global__ void k_oc_step(const double *__restrict__ x, const double *__restrict
     double s = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB) {
         if (!eact[e]) continue;
-        s += dv[e] * (oc_new(x[e], q[e], rs, move) - x[e]);
+        const double xn = (eact[e] & EF_PASSIVE) ? 1.0 : oc_new(x[e], q[e], rs, move);
+        s += dv[e] * (xn - x[e]);
     }
     s = tblock_sum(s);
     if (threadIdx.x == 0) part[blockIdx.x] = s;
@@ -200,7 +207,7 @@ __global__ void k_oc_apply(double *__restrict__ x, const double *__restrict__ q,
     double m = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB) {
         if (!eact[e]) continue;
-        const double xn = oc_new(x[e], q[e], rs, move);
+        const double xn = (eact[e] & EF_PASSIVE) ? 1.0 : oc_new(x[e], q[e], rs, move);
         m = fmax(m, fabs(xn - x[e]));
         x[e] = xn;
     }
@@ -215,10 +222,57 @@ __global__ void k_max_partials(const double *__restrict__ part, int nb, double *
     if (threadIdx.x == 0) out[0] = m;
 }
 
+// y = a / b on active elements (passive ones: 1), 0 elsewhere
 __global__ void k_div(const double *__restrict__ a, const double *__restrict__ b, const uint8_t *__restrict__ eact,
                       int64_t n, double *__restrict__ y) {
     for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB)
-        y[e] = eact[e] ? a[e] / b[e] : 0.0;
+        y[e] = eact[e] ? ((eact[e] & EF_PASSIVE) ? 1.0 : a[e] / b[e]) : 0.0;
+}
+
+// MMA inputs of the design variables (active, not passive elements; full-grid
+// indices var[i]): xval, xmin = max(0, x - move), xmax = min(1, x + move),
+// df0dx = dc, dfdx = dv * scale (TopOpti_GlobalVolumeConstraint.m:142-151)
+__global__ void k_mma_gather(const int64_t *__restrict__ var, int64_t nvar, const double *__restrict__ x,
+                             const double *__restrict__ dc, const double *__restrict__ dv, double move, double scale,
+                             double *__restrict__ xv, double *__restrict__ xmin, double *__restrict__ xmax,
+                             double *__restrict__ df0, double *__restrict__ dg) {
+    for (int64_t i = blockIdx.x * (int64_t)TB + threadIdx.x; i < nvar; i += (int64_t)gridDim.x * TB) {
+        const int64_t e = var[i];
+        const double xe = x[e];
+        xv[i] = xe;
+        xmin[i] = fmax(0.0, xe - move);
+        xmax[i] = fmin(1.0, xe + move);
+        df0[i] = dc[e];
+        dg[i] = dv[e] * scale;
+    }
+}
+
+// x(var) = MMA result; passive elements to 1 (x = onesArrSingle before the
+// variables are written, :154-155); partial max |xnew - xval| (:153)
+__global__ void k_mma_scatter(const int64_t *__restrict__ var, int64_t nvar, const double *__restrict__ xn,
+                              const double *__restrict__ xv, double *__restrict__ x, double *__restrict__ part) {
+    double m = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)TB + threadIdx.x; i < nvar; i += (int64_t)gridDim.x * TB) {
+        x[var[i]] = xn[i];
+        m = fmax(m, fabs(xn[i] - xv[i]));
+    }
+    m = tblock_max(m);
+    if (threadIdx.x == 0) part[blockIdx.x] = m;
+}
+
+__global__ void k_set_passive_x(double *__restrict__ x, const uint8_t *__restrict__ eact, int64_t n) {
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB)
+        if (eact[e] & EF_PASSIVE) x[e] = 1.0;
+}
+
+// eact bit 1: cleared everywhere, then set for the listed full-grid elements
+__global__ void k_clear_passive(uint8_t *__restrict__ eact, int64_t n) {
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB)
+        eact[e] = (uint8_t)(eact[e] & ~EF_PASSIVE);
+}
+__global__ void k_mark_passive(uint8_t *__restrict__ eact, const int64_t *__restrict__ full, int64_t np) {
+    for (int64_t i = blockIdx.x * (int64_t)TB + threadIdx.x; i < np; i += (int64_t)gridDim.x * TB)
+        eact[full[i]] = (uint8_t)(eact[full[i]] | EF_PASSIVE);
 }
 
 __global__ void k_fill_active(double *__restrict__ y, const uint8_t *__restrict__ eact, int64_t n, double v) {
@@ -263,6 +317,32 @@ void launch_max_partials(const double *part, int nb, double *out, cudaStream_t s
 void launch_div(const Level &l0, const double *a, const double *b, double *y, int nb, cudaStream_t s) {
     ++g_launches;
     k_div<<<nb, TB, 0, s>>>(a, b, l0.eact, l0.nel, y);
+}
+int launch_mma_gather(const int64_t *var, int64_t nvar, const double *x, const double *dc, const double *dv,
+                      double move, double scale, double *xv, double *xmin, double *xmax, double *df0, double *dg,
+                      cudaStream_t s) {
+    ++g_launches;
+    const int nb = (int)std::min<int64_t>((nvar + TB - 1) / TB, 152 * 8);
+    k_mma_gather<<<std::max(nb, 1), TB, 0, s>>>(var, nvar, x, dc, dv, move, scale, xv, xmin, xmax, df0, dg);
+    return std::max(nb, 1);
+}
+void launch_mma_scatter(const int64_t *var, int64_t nvar, const double *xn, const double *xv, double *x,
+                        double *part, int nb, cudaStream_t s) {
+    ++g_launches;
+    k_mma_scatter<<<nb, TB, 0, s>>>(var, nvar, xn, xv, x, part);
+}
+void launch_set_passive_x(const Level &l0, double *x, int nb, cudaStream_t s) {
+    ++g_launches;
+    k_set_passive_x<<<nb, TB, 0, s>>>(x, l0.eact, l0.nel);
+}
+void launch_mark_passive(const Level &l0, const int64_t *full, int64_t np, int nb, cudaStream_t s) {
+    ++g_launches;
+    k_clear_passive<<<nb, TB, 0, s>>>(l0.eact, l0.nel);
+    if (np > 0) {
+        ++g_launches;
+        const int nb2 = (int)std::max<int64_t>(1, std::min<int64_t>((np + TB - 1) / TB, 152 * 8));
+        k_mark_passive<<<nb2, TB, 0, s>>>(l0.eact, full, np);
+    }
 }
 void launch_fill_active(const Level &l0, double *y, double v, int nb, cudaStream_t s) {
     ++g_launches;

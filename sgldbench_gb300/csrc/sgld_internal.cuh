@@ -102,6 +102,7 @@ struct Ctx {
     double *d_binfo = nullptr; // [8 nrhs] per-case results
     int blk_cap = 0;
     bool kbyu_tuned = false;   // the FP32 K*u z-chunk was tuned (tune_kbyu_f32)
+    std::vector<int64_t> h_passive;   // passive elements (full-grid indices, sorted) of the SIMP loop
     cudaGraphExec_t inner_graph = nullptr;   // inner FP32 CG: entry nodes + while node
     int inner_graph_k = 0;
     double inner_graph_eta = -1.0;
@@ -184,6 +185,13 @@ void launch_oc_apply(const Level &l0, double *x, const double *q, double move, c
 void launch_max_partials(const double *part, int nb, double *out, cudaStream_t s);
 void launch_div(const Level &l0, const double *a, const double *b, double *y, int nb, cudaStream_t s);
 void launch_fill_active(const Level &l0, double *y, double v, int nb, cudaStream_t s);
+int launch_mma_gather(const int64_t *var, int64_t nvar, const double *x, const double *dc, const double *dv,
+                      double move, double scale, double *xv, double *xmin, double *xmax, double *df0, double *dg,
+                      cudaStream_t s);
+void launch_mma_scatter(const int64_t *var, int64_t nvar, const double *xn, const double *xv, double *x,
+                        double *part, int nb, cudaStream_t s);
+void launch_set_passive_x(const Level &l0, double *x, int nb, cudaStream_t s);
+void launch_mark_passive(const Level &l0, const int64_t *full, int64_t np, int nb, cudaStream_t s);
 void launch_unit_compliance(const Level &l0, const double *u, const double *E, double *ce_full,
                             double *partial, int *nblocks_out, cudaStream_t s);
 void launch_stress(const Level &l0, const double *E, const double *u, const double *M48x24,

@@ -4,6 +4,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <utility>
 
@@ -270,6 +271,30 @@ extern "C" int sgld_pde_filter(sgld_ctx *ctx, double rhat, const double *x, doub
     return SGLD_OK;
 }
 
+extern "C" int sgld_set_passive(sgld_ctx *ctx, int64_t n, const int64_t *elements) {
+    if (!ctx || n < 0 || (n > 0 && !elements)) return SGLD_ERR_ARG;
+    Ctx &c = ctx->c;
+    const int64_t ne = (int64_t)c.h_elemap.size();
+    std::vector<int64_t> full((size_t)n);
+    for (int64_t i = 0; i < n; ++i) {
+        if (elements[i] < 0 || elements[i] >= ne) return tfail(ctx, SGLD_ERR_ARG, "passive element index out of range");
+        full[i] = c.h_elemap[elements[i]];
+    }
+    std::sort(full.begin(), full.end());
+    full.erase(std::unique(full.begin(), full.end()), full.end());
+    int64_t *d_full = nullptr;
+    if (!full.empty()) {
+        TCK(cudaMalloc((void **)&d_full, sizeof(int64_t) * full.size()));
+        TCK(cudaMemcpyAsync(d_full, full.data(), sizeof(int64_t) * full.size(), cudaMemcpyHostToDevice, c.stream));
+    }
+    launch_mark_passive(c.lv[0], d_full, (int64_t)full.size(), reduce_blocks(c.lv[0].nel), c.stream);
+    const cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (d_full) cudaFree(d_full);
+    TCK(e);
+    c.h_passive = std::move(full);
+    return SGLD_OK;
+}
+
 extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const double *F, const double *x0,
                            double *xphys, sgld_topopt_iter *hist, int *n_iter) {
     if (!ctx || !opts || !F) return SGLD_ERR_ARG;
@@ -314,6 +339,43 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
     TCK(cudaGetLastError());
     cudaEvent_t ev[5];
     for (auto &e : ev) TCK(cudaEventCreate(&e));
+    // MMA: design variables = active elements that are not passive
+    int64_t nvar = 0;
+    int64_t *d_var = nullptr;
+    double *mma_buf = nullptr, *mma_xv = nullptr, *mma_xmin = nullptr, *mma_xmax = nullptr, *mma_df0 = nullptr,
+           *mma_dg = nullptr, *mma_xo = nullptr, *mma_p1 = nullptr, *mma_p2 = nullptr, *mma_sums = nullptr;
+    struct Free {
+        void *a, *b;
+        ~Free() {
+            if (a) cudaFree(a);
+            if (b) cudaFree(b);
+        }
+    } mma_free{nullptr, nullptr};
+    if (o.optimizer == SGLD_OPT_MMA) {
+        std::vector<int64_t> var;
+        var.reserve(c.h_elemap.size());
+        for (int64_t e : c.h_elemap)
+            if (!std::binary_search(c.h_passive.begin(), c.h_passive.end(), e)) var.push_back(e);
+        nvar = (int64_t)var.size();
+        if (nvar == 0) return tfail(ctx, SGLD_ERR_ARG, "MMA: no design variables (every element passive)");
+        const int nbm = mma_blocks(nvar);
+        TCK(cudaMalloc((void **)&d_var, sizeof(int64_t) * nvar));
+        mma_free.a = d_var;
+        TCK(cudaMemcpyAsync(d_var, var.data(), sizeof(int64_t) * nvar, cudaMemcpyHostToDevice, s));
+        TCK(cudaMalloc((void **)&mma_buf, sizeof(double) * (6 * (size_t)nvar + 2 * (size_t)nbm + 2)));
+        mma_free.b = mma_buf;
+        mma_xv = mma_buf;
+        mma_xmin = mma_xv + nvar;
+        mma_xmax = mma_xmin + nvar;
+        mma_df0 = mma_xmax + nvar;
+        mma_dg = mma_df0 + nvar;
+        mma_xo = mma_dg + nvar;
+        mma_p1 = mma_xo + nvar;
+        mma_p2 = mma_p1 + nbm;
+        mma_sums = mma_p2 + nbm;
+    } else if (o.optimizer != SGLD_OPT_OC) {
+        return tfail(ctx, SGLD_ERR_ARG, "optimizer must be SGLD_OPT_OC or SGLD_OPT_MMA");
+    }
     sgld_solve_opts so = o.solve;
     so.use_x0 = 1;
     so.history = nullptr;
@@ -340,18 +402,32 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
         cudaEvent_t evf;
         TCK(cudaEventCreate(&evf));
         TCK(cudaEventRecord(evf, s));
-        launch_topo_q(l0, c.t_x, c.t_dc, c.t_dv, c.t_q, nb, s);
-        double done = 0.0;
-        for (int round = 0; round < 8 && done == 0.0; ++round) {                   // :85-90
-            for (int k = 0; k < 32; ++k) {
-                launch_oc_step(l0, c.t_x, c.t_q, c.t_dv, o.move, c.t_st, c.d_part, nb, s);
-                launch_oc_scalar(1, c.t_st, c.d_part, nb, nact, o.volfrac, s);
+        if (o.optimizer == SGLD_OPT_MMA) {
+            // TopOpti_GlobalVolumeConstraint.m:139-156: one MMA update of the
+            // design variables under fval = sum(xPhys)/(n V) - 1 <= 0
+            const int nbm = launch_mma_gather(d_var, nvar, c.t_x, c.t_dc, c.t_dv, o.move, 1.0 / (nact * o.volfrac),
+                                              mma_xv, mma_xmin, mma_xmax, mma_df0, mma_dg, s);
+            const double fval = vol / (nact * o.volfrac) - 1.0;
+            if ((rc = mma_solve_device(ctx, nvar, mma_xv, mma_xmin, mma_xmax, mma_df0, mma_dg, fval, mma_xo,
+                                       mma_p1, mma_p2, mma_sums, nullptr)))
+                return rc;
+            if (!c.h_passive.empty()) launch_set_passive_x(l0, c.t_x, nb, s);
+            launch_mma_scatter(d_var, nvar, mma_xo, mma_xv, c.t_x, c.d_part, nbm, s);
+            launch_max_partials(c.d_part, nbm, c.t_st + T_CHANGE, s);
+        } else {
+            launch_topo_q(l0, c.t_x, c.t_dc, c.t_dv, c.t_q, nb, s);
+            double done = 0.0;
+            for (int round = 0; round < 8 && done == 0.0; ++round) {               // :85-90
+                for (int k = 0; k < 32; ++k) {
+                    launch_oc_step(l0, c.t_x, c.t_q, c.t_dv, o.move, c.t_st, c.d_part, nb, s);
+                    launch_oc_scalar(1, c.t_st, c.d_part, nb, nact, o.volfrac, s);
+                }
+                TCK(cudaMemcpyAsync(&done, c.t_st + OC_DONE, sizeof(double), cudaMemcpyDeviceToHost, s));
+                TCK(cudaStreamSynchronize(s));
             }
-            TCK(cudaMemcpyAsync(&done, c.t_st + OC_DONE, sizeof(double), cudaMemcpyDeviceToHost, s));
-            TCK(cudaStreamSynchronize(s));
+            launch_oc_apply(l0, c.t_x, c.t_q, o.move, c.t_st, c.d_part, nb, s);   // :91-92
+            launch_max_partials(c.d_part, nb, c.t_st + T_CHANGE, s);
         }
-        launch_oc_apply(l0, c.t_x, c.t_q, o.move, c.t_st, c.d_part, nb, s);       // :91-92
-        launch_max_partials(c.d_part, nb, c.t_st + T_CHANGE, s);
         cudaEvent_t evo;
         TCK(cudaEventCreate(&evo));
         TCK(cudaEventRecord(evo, s));

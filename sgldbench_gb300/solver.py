@@ -366,6 +366,11 @@ class VoxelSolver:
         self._check(self.lib.sgld_density_filter(self.ctx, float(rMin), _p(xv), _p(y)))
         return y
 
+    def set_passive(self, elements):
+        """Passive elements (compact 0-based indices) kept solid by the SIMP loop."""
+        idx = np.ascontiguousarray(np.asarray(elements, dtype=np.int64).ravel())
+        self._check(self.lib.sgld_set_passive(self.ctx, idx.size, _p(idx) if idx.size else None))
+
     def TopOpti_PDEFiltering(self, x, rHatMin: float, tol: float = 1e-6, maxIT: int = 500):
         """PDE (Helmholtz) filter of an element field (TopOpti_PDEFiltering_matrixFree.m).
         Returns (filtered field, PCG iterations)."""
@@ -399,14 +404,18 @@ class VoxelSolver:
                                        move: float = 0.1, minChange: float = 1e-4, maxSharpness: float = 0.05,
                                        penalty: float = 3.0, E0: float = 1.0, Emin: float = 1e-9,
                                        tol: float = 1e-6, maxIT: int = 500, precision: str = "fp64",
-                                       inner_its: int = 0, x0=None, inner_tol: float = 0.0):
+                                       inner_its: int = 0, x0=None, inner_tol: float = 0.0,
+                                       optimizer: str = "OC"):
         """The whole SIMP loop on the device.  Returns (xPhys, history list)."""
         Fv = self._vec(F, self.numDOFs)
         so = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=1,
                          precision=_precision(precision),
                          inner_its=inner_its, history=None, profile=0, inner_tol=inner_tol)
+        if optimizer not in ("OC", "MMA"):
+            raise ValueError("optimizer must be 'OC' or 'MMA'")
         o = L.TopOptOpts(volfrac=volfrac, rmin=rMin, move=move, n_loop=nLoop, min_change=minChange,
-                         max_sharpness=maxSharpness, penalty=penalty, E0=E0, Emin=Emin, solve=so)
+                         max_sharpness=maxSharpness, penalty=penalty, E0=E0, Emin=Emin, solve=so,
+                         optimizer=1 if optimizer == "MMA" else 0)
         xp = np.zeros(self.numElements)
         hist = (L.TopOptIter * nLoop)()
         nit = C.c_int()

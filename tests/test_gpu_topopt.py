@@ -122,3 +122,31 @@ def test_mma_update_matches_oracle(built_lib):
         assert np.abs(xn - rn).max() <= 1e-9
         assert np.array_equal(o1, r1) and np.array_equal(o2, r2)
         assert np.all(xn >= xmin - 1e-15) and np.all(xn <= xmax + 1e-15)
+
+
+@pytest.mark.parametrize("optimizer", ["OC", "MMA"])
+def test_simp_loop_optimizer_and_passive(built_lib, optimizer):
+    """The SIMP loop with the MMA update (TopOpti_GlobalVolumeConstraint.m:
+    139-156) or OC, with passive elements kept solid (:162, :179), against the
+    oracle: compliance per iteration within 1e-6, final xPhys within 1e-5,
+    passive xPhys exactly 1."""
+    from sgldbench_gb300 import VoxelSolver
+
+    vox = np.ones((8, 16, 8), bool)
+    m = G.build_model(vox, omega=0.6)
+    s = VoxelSolver(vox, omega=0.6)
+    s.set_fixed_dofs(m.levels[0].fixedDOFs)
+    n = m.levels[0].numElements
+    passive = np.arange(0, n, 17)
+    s.set_passive(passive)
+    opt = G.TopOptOptions(n_loop=5, tol=1e-10, maxit=2000, Emin=1e-9, optimizer=optimizer, passive=passive)
+    xp_o, hist_o = G.topopt_global_volume(m, opt)
+    xp, hist = s.TopOpti_GlobalVolumeConstraint(m.F, volfrac=0.3, rMin=1.5, nLoop=5, tol=1e-10, maxIT=2000,
+                                                Emin=1e-9, optimizer=optimizer)
+    s.set_passive([])
+    assert len(hist) == len(hist_o)
+    for a, b in zip(hist, hist_o):
+        assert abs(a["compliance"] - b["c"]) <= 1e-6 * abs(b["c"])
+        assert abs(a["change"] - b["change"]) <= 1e-5
+    assert _rel(xp, xp_o) <= 1e-5
+    assert np.all(xp[passive] == 1.0)

@@ -287,6 +287,10 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu(const T *__restrict__ u, T 
 // Pair p of a CTA covers element layers z0-1+2p and z0+2p and completes node
 // layers z0-1+2p and z0+2p: node layer ez takes the lower corners of element
 // ez plus the upper corners of element ez-1 (carried from the previous pair).
+// The corner sums are gathered in two steps: along y inside the warp (lanes
+// are consecutive y, so the neighbour's corner arrives by a shuffle), then
+// along x through shared memory (the next warp is the next x column), which
+// leaves 6 float2 per thread in shared memory instead of 24.
 __device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 __device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
@@ -366,7 +370,7 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu_x2(const float *__restrict_
                                                         int zc, double *__restrict__ partial) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *su = reinterpret_cast<float *>(smem_raw);                    // [KX_RING][KT_NL*3]
-    float2 *so = reinterpret_cast<float2 *>(su + KX_RING_FLOATS);   // [24][KT_THREADS]
+    float2 *so = reinterpret_cast<float2 *>(su + KX_RING_FLOATS);   // [6][KT_THREADS]
     const int tid = threadIdx.x;
     const int ty = tid % KT_Y, tx = tid / KT_Y;
     const int NY = ny + 1, NX = nx + 1, NZ = nz + 1;
@@ -442,25 +446,30 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu_x2(const float *__restrict_
 #pragma unroll
             for (int i = 0; i < 24; ++i) ue[i] = make_float2(0.f, 0.f);
         }
+        // y step: Y_dx = corner (dx, dy=1) of this element + corner (dx, dy=0)
+        // of the element one lane up (corner k = dx | (1-dy) << 1 | kp << 2)
+        float2 y1[2][3];   // dx = 1: stays in this thread (the owner's own column)
 #pragma unroll
-        for (int i = 0; i < 24; ++i) so[i * KT_THREADS + tid] = ue[i];
+        for (int kp = 0; kp < 2; ++kp)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float2 a1 = ue[3 * (1 | (kp << 2)) + c], b1 = ue[3 * (1 | 2 | (kp << 2)) + c];
+                const float2 a0 = ue[3 * (kp << 2) + c], b0 = ue[3 * (2 | (kp << 2)) + c];
+                y1[kp][c] = f2add(a1, make_float2(__shfl_down_sync(0xffffffffu, b1.x, 1),
+                                                  __shfl_down_sync(0xffffffffu, b1.y, 1)));
+                so[(3 * kp + c) * KT_THREADS + tid] =
+                    f2add(a0, make_float2(__shfl_down_sync(0xffffffffu, b0.x, 1),
+                                          __shfl_down_sync(0xffffffffu, b0.y, 1)));
+            }
         __syncthreads();
         if (owner) {
+            // x step: dx = 0 comes from the next column (the next warp)
             float2 lo[3], up[3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) lo[c] = up[c] = make_float2(0.f, 0.f);
-#pragma unroll
-            for (int dy = 0; dy < 2; ++dy)
-#pragma unroll
-                for (int dx = 0; dx < 2; ++dx) {
-                    const int k = dx | ((1 - dy) << 1);
-                    const int t = (ty + 1 - dy) + KT_Y * (tx + 1 - dx);
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        lo[c] = f2add(lo[c], so[(3 * k + c) * KT_THREADS + t]);
-                        up[c] = f2add(up[c], so[(3 * (k | 4) + c) * KT_THREADS + t]);
-                    }
-                }
+            for (int c = 0; c < 3; ++c) {
+                lo[c] = f2add(y1[0][c], so[c * KT_THREADS + tid + KT_Y]);
+                up[c] = f2add(y1[1][c], so[(3 + c) * KT_THREADS + tid + KT_Y]);
+            }
             const int64_t node0 = (int64_t)gny + (int64_t)NY * gnx;
             const int on = 3 * ((ty + 1) + (KT_Y + 1) * (tx + 1));
 #pragma unroll
@@ -496,7 +505,7 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu_x2(const float *__restrict_
     }
 }
 
-static constexpr size_t kbyu_x2_smem() { return sizeof(float) * KX_RING_FLOATS + sizeof(float2) * 24 * KT_THREADS; }
+static constexpr size_t kbyu_x2_smem() { return sizeof(float) * KX_RING_FLOATS + sizeof(float2) * 6 * KT_THREADS; }
 static_assert((KX_RING_FLOATS * sizeof(float)) % 16 == 0, "float2 exchange area must be aligned");
 
 // node layers per CTA of k_kbyu_x2: an odd count (so that the element layers

@@ -309,8 +309,8 @@ def run_ours(args):
         kb_avg = s.time_op("kbyu32", 20) * 1e-3
         how = ("CUDA events around 20 back-to-back launches on the library stream (sgld_time_op) right after "
                "the timed region; inside the timed region the kernel runs in the inner CG's graph")
-        note = ("FP32 K*u is issue/latency-bound (ncu: issue 52 %, FMA pipe 42 %), not HBM-bound; the "
-                "HBM fraction is reported against the measured copy bandwidth")
+        note = ("FP32 K*u is issue/latency-bound, not HBM-bound; the HBM fraction is reported against the "
+                "measured copy bandwidth. Autotuned tile: %s" % json.dumps(s.kbyu_tile()))
     achieved = kbytes / kb_avg / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": _ncu_traffic(args.precision),

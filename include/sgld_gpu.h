@@ -106,6 +106,12 @@ int64_t sgld_kernel_launches(void);
  *   op 5: double-float K*u (the outer operator of SGLD_PREC_MIXED_DF) */
 int sgld_time_op(sgld_ctx *ctx, int op, int reps, double *ms_per_op);
 
+/* The tile of the FP32 K*u on the finest level: x width in elements (8 or 16)
+ * and node layers per CTA, as chosen by the autotuner at the first
+ * sgld_assemble (or the defaults before it / with SGLD_AUTOTUNE=0).  No
+ * counterpart in the reference; reported beside measurements. */
+int sgld_kbyu_tile(const sgld_ctx *ctx, int *tile_x, int *z_chunk);
+
 /* Allocation-free K*u with its dot product (no counterpart in the reference).
  *
  * For callers that must not allocate device memory when they apply the

@@ -86,6 +86,7 @@ SIGNATURES = {
     "sgld_get_stream": (vp, [vp]),
     "sgld_kernel_launches": (i64, []),
     "sgld_time_op": (i32, [vp, i32, i32, vp]),
+    "sgld_kbyu_tile": (i32, [vp, vp, vp]),
     "sgld_kbyu_dot_noalloc": (i32, [vp, vp, vp, vp, vp]),
     "sgld_density_filter": (i32, [vp, dbl, vp, vp]),
     "sgld_topopt": (i32, [vp, vp, vp, vp, vp, vp, vp]),

@@ -291,6 +291,9 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu(const T *__restrict__ u, T 
 // are consecutive y, so the neighbour's corner arrives by a shuffle), then
 // along x through shared memory (the next warp is the next x column), which
 // leaves 6 float2 per thread in shared memory instead of 24.
+// The tile is 32 (y) x TX (x) elements; a CTA owns 31 x (TX-1) node columns,
+// so a wider tile recomputes fewer halo elements (15 % at TX = 8, 9 % at 16)
+// and stages fewer halo nodes, at the same 1024 threads per SM.
 __device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 __device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
@@ -357,20 +360,31 @@ __device__ __forceinline__ void hex_apply_x2(float2 (&u)[24], float2 e) {
 }
 
 constexpr int KX_RING = 5;   // node-layer slots: 3 in use + 2 in flight
-// floats of the ring, rounded up to 16 bytes so that the float2 exchange
-// area behind it is aligned (5 * 891 floats alone would leave it 4 bytes off)
-constexpr int KX_RING_FLOATS = ((KX_RING * KT_NL * 3 + 3) / 4) * 4;
+
+// geometry of the 32 x TX tile
+template <int TX>
+struct KxTile {
+    static constexpr int THREADS = KT_Y * TX;
+    static constexpr int NL = (KT_Y + 1) * (TX + 1);             // staged nodes per layer
+    static constexpr int SV = (NL * 3 + THREADS - 1) / THREADS;  // staged words per thread and layer
+    // floats of the ring, rounded up to 16 bytes so that the float2 exchange
+    // area behind it is aligned (5 * 891 floats alone would leave it 4 bytes off)
+    static constexpr int RING_FLOATS = ((KX_RING * NL * 3 + 3) / 4) * 4;
+    static constexpr size_t SMEM = sizeof(float) * RING_FLOATS + sizeof(float2) * 6 * THREADS;
+    static_assert((RING_FLOATS * sizeof(float)) % 16 == 0, "float2 exchange area must be aligned");
+};
 
 __device__ __forceinline__ int xslot(int z) { return (z + KX_RING) % KX_RING; }
 
-template <bool DOT>
-__global__ void __launch_bounds__(KT_THREADS) k_kbyu_x2(const float *__restrict__ u, float *__restrict__ y,
-                                                        const float *__restrict__ E,
-                                                        const uint8_t *__restrict__ nflag, int ny, int nx, int nz,
-                                                        int zc, double *__restrict__ partial) {
+template <int TX, bool DOT>
+__global__ void __launch_bounds__(KT_Y * TX, 1024 / (KT_Y * TX))
+    k_kbyu_x2(const float *__restrict__ u, float *__restrict__ y, const float *__restrict__ E,
+              const uint8_t *__restrict__ nflag, int ny, int nx, int nz, int zc, double *__restrict__ partial) {
+    using G = KxTile<TX>;
+    constexpr int KT_X = TX, KT_THREADS = G::THREADS, KT_NL = G::NL, KT_SV = G::SV;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *su = reinterpret_cast<float *>(smem_raw);                    // [KX_RING][KT_NL*3]
-    float2 *so = reinterpret_cast<float2 *>(su + KX_RING_FLOATS);   // [6][KT_THREADS]
+    float *su = reinterpret_cast<float *>(smem_raw);                  // [KX_RING][KT_NL*3]
+    float2 *so = reinterpret_cast<float2 *>(su + G::RING_FLOATS);   // [6][KT_THREADS]
     const int tid = threadIdx.x;
     const int ty = tid % KT_Y, tx = tid / KT_Y;
     const int NY = ny + 1, NX = nx + 1, NZ = nz + 1;
@@ -505,9 +519,6 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu_x2(const float *__restrict_
     }
 }
 
-static constexpr size_t kbyu_x2_smem() { return sizeof(float) * KX_RING_FLOATS + sizeof(float2) * 6 * KT_THREADS; }
-static_assert((KX_RING_FLOATS * sizeof(float)) % 16 == 0, "float2 exchange area must be aligned");
-
 // node layers per CTA of k_kbyu_x2: an odd count (so that the element layers
 // z0-1 .. z0+zc-1 form whole pairs).  Default: near 15, balanced over the z
 // extent; sgld_assemble's tuner (tune_kbyu_f32) may set another per level.
@@ -519,11 +530,13 @@ static int kbyu_x2_zc(int NZ) {
 }
 
 int kbyu_f32_zc(const Level &l) { return l.kx_zc > 0 ? l.kx_zc : kbyu_x2_zc(l.nz + 1); }
+// tile width in x: 16 unless the tuner chose 8
+int kbyu_f32_tx(const Level &l) { return l.kx_tx == 8 ? 8 : 16; }
 
 static dim3 kbyu_x2_grid(const Level &l) {
     const int NZ = l.nz + 1;
-    const int zc = kbyu_f32_zc(l);
-    return dim3((l.ny + 1 + KT_Y - 2) / (KT_Y - 1), (l.nx + 1 + KT_X - 2) / (KT_X - 1), (NZ + zc - 1) / zc);
+    const int zc = kbyu_f32_zc(l), tx = kbyu_f32_tx(l);
+    return dim3((l.ny + 1 + KT_Y - 2) / (KT_Y - 1), (l.nx + 1 + tx - 2) / (tx - 1), (NZ + zc - 1) / zc);
 }
 
 static dim3 kbyu_grid(const Level &l) {
@@ -540,8 +553,10 @@ static constexpr size_t kbyu_smem() {
 void init_kernel_attributes() {
     cudaFuncSetAttribute(k_kbyu<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<double>());
     cudaFuncSetAttribute(k_kbyu<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<double>());
-    cudaFuncSetAttribute(k_kbyu_x2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_x2_smem());
-    cudaFuncSetAttribute(k_kbyu_x2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_x2_smem());
+    cudaFuncSetAttribute(k_kbyu_x2<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KxTile<8>::SMEM);
+    cudaFuncSetAttribute(k_kbyu_x2<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KxTile<8>::SMEM);
+    cudaFuncSetAttribute(k_kbyu_x2<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KxTile<16>::SMEM);
+    cudaFuncSetAttribute(k_kbyu_x2<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KxTile<16>::SMEM);
 }
 
 template <typename T, bool DOT>
@@ -567,10 +582,19 @@ void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, 
     const int zc = kbyu_f32_zc(l0);
     if (nblocks_out) *nblocks_out = (int)(g.x * g.y * g.z);
     ++g_launches;
-    if (partial_dot)
-        k_kbyu_x2<true><<<g, KT_THREADS, kbyu_x2_smem(), s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, partial_dot);
-    else
-        k_kbyu_x2<false><<<g, KT_THREADS, kbyu_x2_smem(), s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr);
+    if (kbyu_f32_tx(l0) == 8) {
+        using G = KxTile<8>;
+        if (partial_dot)
+            k_kbyu_x2<8, true><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, partial_dot);
+        else
+            k_kbyu_x2<8, false><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr);
+    } else {
+        using G = KxTile<16>;
+        if (partial_dot)
+            k_kbyu_x2<16, true><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, partial_dot);
+        else
+            k_kbyu_x2<16, false><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr);
+    }
 }
 
 int kbyu_num_blocks(const Level &l0) {

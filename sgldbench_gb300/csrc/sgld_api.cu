@@ -714,6 +714,14 @@ void sgld_destroy(sgld_ctx *ctx) {
 
 int sgld_num_levels(const sgld_ctx *ctx) { return ctx ? ctx->c.L : -1; }
 
+int sgld_kbyu_tile(const sgld_ctx *ctx, int *tile_x, int *z_chunk) {
+    if (!ctx || ctx->c.L < 1) return SGLD_ERR_ARG;
+    const Level &l0 = ctx->c.lv[0];
+    if (tile_x) *tile_x = kbyu_f32_tx(l0);
+    if (z_chunk) *z_chunk = kbyu_f32_zc(l0);
+    return SGLD_OK;
+}
+
 int sgld_level_info(const sgld_ctx *ctx, int level, int res[3], int *span, int64_t *ne, int64_t *nn) {
     if (!ctx || level < 1 || level > ctx->c.L) return SGLD_ERR_ARG;
     const Level &l = ctx->c.lv[level - 1];
@@ -887,12 +895,13 @@ int sgld_set_modulus(sgld_ctx *ctx, const double *E) {
     return sgld_set_modulus_device(ctx, c.d_tmp);
 }
 
-// Autotuner of the FP32 K*u's z-chunk (node layers per CTA): times each odd
-// candidate with CUDA events on the context's stream (3 launches after a
-// warm-up) and keeps the fastest in lv[0].kx_zc.  Runs once per context, at
-// the first assembly (never during a graph capture); SGLD_AUTOTUNE=0 keeps
-// the default rule.  The chunk trades halo work (one extra element layer per
-// CTA) against the number of CTAs in flight.
+// Autotuner of the FP32 K*u's tile: x width (8 or 16 elements) times z-chunk
+// (node layers per CTA).  Times each candidate with CUDA events on the
+// context's stream (3 launches after a warm-up) and keeps the fastest in
+// lv[0].kx_tx / kx_zc.  Runs once per context, at the first assembly (never
+// during a graph capture); SGLD_AUTOTUNE=0 keeps the default tile.  Width
+// and chunk trade halo work (one extra element column / layer per CTA)
+// against the number of CTAs in flight.
 static int tune_kbyu_f32(sgld_ctx *ctx) {
     Ctx &c = ctx->c;
     Level &l0 = c.lv[0];
@@ -910,23 +919,27 @@ static int tune_kbyu_f32(sgld_ctx *ctx) {
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
     float best = 1e30f;
-    int best_zc = 0;
-    for (int zc : cand) {
-        l0.kx_zc = zc;
-        launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, c.stream);
-        CK(cudaEventRecord(a, c.stream));
-        for (int r = 0; r < 3; ++r) launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, c.stream);
-        CK(cudaEventRecord(b, c.stream));
-        CK(cudaEventSynchronize(b));
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, a, b);
-        if (ms < best) {
-            best = ms;
-            best_zc = zc;
+    int best_zc = 0, best_tx = 0;
+    for (int tx : {16, 8})
+        for (int zc : cand) {
+            l0.kx_tx = tx;
+            l0.kx_zc = zc;
+            launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, c.stream);
+            CK(cudaEventRecord(a, c.stream));
+            for (int r = 0; r < 3; ++r) launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, c.stream);
+            CK(cudaEventRecord(b, c.stream));
+            CK(cudaEventSynchronize(b));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            if (ms < best) {
+                best = ms;
+                best_zc = zc;
+                best_tx = tx;
+            }
         }
-    }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    l0.kx_tx = best_tx;
     l0.kx_zc = best_zc;
     CKL();
     return SGLD_OK;

@@ -31,6 +31,7 @@ struct Level {
     int nx = 0, ny = 0, nz = 0;   // elements
     int span = 1;                 // coarsening factor from the next finer level
     int kx_zc = 0;                // node layers per CTA of the FP32 K*u (0 = default rule; set by the tuner)
+    int kx_tx = 0;                // x width of the FP32 K*u tile, 8 or 16 (0 = 16; set by the tuner)
     int64_t nel = 0, nnode = 0;   // full-grid counts
     int64_t nel_active = 0, nnode_active = 0;
     uint8_t *eact = nullptr;      // [nel] element non-empty
@@ -138,6 +139,7 @@ void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, 
                      int *nblocks_out, cudaStream_t s);
 void init_kernel_attributes();
 int kbyu_f32_zc(const Level &l0);   // node layers per CTA the FP32 K*u uses on this level
+int kbyu_f32_tx(const Level &l0);   // x width (elements) of the FP32 K*u tile on this level
 // double-float K*u (kernels_df.cu)
 void upload_kh_df(const double *Kh, cudaStream_t s);
 void init_kbyu_df_attributes();

@@ -49,6 +49,8 @@ def main():
         rec = {"op": op, "size": args.size, "ms": ms}
         if b:
             rec.update({"bytes": b, "GBps": b / ms / 1e6, "dense_equiv_TFLOPs": f / ms / 1e9})
+        if op == "kbyu32":
+            rec["tile"] = s.kbyu_tile()
         print(json.dumps(rec), flush=True)
     s.close()
 

@@ -298,6 +298,12 @@ class VoxelSolver:
         self._check(self.lib.sgld_time_op(self.ctx, self.OPS[op], int(reps), C.byref(ms)))
         return ms.value
 
+    def kbyu_tile(self) -> dict:
+        """Tile of the FP32 K*u on the finest level (x width, node layers per CTA)."""
+        tx, zc = C.c_int(), C.c_int()
+        self._check(self.lib.sgld_kbyu_tile(self.ctx, C.byref(tx), C.byref(zc)))
+        return {"tile_x": tx.value, "z_chunk": zc.value}
+
     @property
     def stream(self) -> int:
         """cudaStream_t of this context (every call runs on it)."""

@@ -270,6 +270,23 @@ typedef struct sgld_topopt_opts {
     int optimizer;         /* SGLD_OPT_OC (0, the loop's bisection) or SGLD_OPT_MMA (1: the
                               MMA update of TopOpti_GlobalVolumeConstraint.m:139-156, one
                               volume constraint, passive elements excluded from the variables) */
+    /* Learned warm start (no counterpart in the reference, which warm-starts
+     * every solve from the previous displacement U, Solving_CG_GMGS.m:7).
+     * With learned = 1 a U-Net (sgld_net_*) on the node grid of level
+     * net_level is trained online on this loop's own solves: input the
+     * restricted initial residual, the previous displacement change d, a
+     * log-modulus field and the active-node mask; target the direction of the
+     * displacement change the solve is about to find.  Its output v,
+     * prolongated to the finest grid, and d span the correction: the start is
+     * U + a d + b v with (a, b) minimising the energy error (a 2x2 Galerkin
+     * system), kept only if it lowers the residual in the norm of the FP64
+     * V-cycle M (r'Mr, which tracks the error's energy).  learned = 2 uses d
+     * alone (the same method without the network, for comparison).  The
+     * converged answer is the plain solve's: only iteration counts change. */
+    int learned;           /* 0 off, 1 network + previous change, 2 previous change only */
+    int net_level;         /* MATLAB level index of the network's grid (0 = 3, clamped to [1, levels]) */
+    int net_train_steps;   /* Adam steps after each solve (0 = 4) */
+    float net_lr;          /* Adam learning rate (0 = 1e-3) */
 } sgld_topopt_opts;
 
 #define SGLD_OPT_OC 0
@@ -284,6 +301,14 @@ typedef struct sgld_topopt_iter {
     int loop, cg_iterations;
     double compliance, volume, sharpness, change, constraint;   /* cHist_, volHist_, sharpHist_, change, consHist_ */
     double t_assemble, t_solve, t_opt, t_filter;                 /* tHist_ columns (device seconds) */
+    /* learned warm start (zero when it is off or has no model yet) */
+    int net_used;          /* the network proposed a guess this iteration */
+    int net_accepted;      /* ... and it lowered the initial residual, so the solve started from it */
+    double net_r0_ratio;   /* sqrt(r1'M r1 / r0'M r0), r1 = F - K u_start, r0 = F - K U (the step taken) */
+    double ext_r0_ratio;   /* the same for the previous change d alone (without the network) */
+    double net_loss;       /* training loss of the last Adam step after the solve */
+    double t_net;          /* device seconds of the network's guess and training */
+    int inner_iterations;  /* inner FP32 CG iterations of the solve (mixed precision; 0 for FP64) */
 } sgld_topopt_iter;
 
 /* x0: initial design (NULL = volfrac everywhere, TopOpti_CallTopOpti.m:34);
@@ -307,6 +332,40 @@ int sgld_stress(sgld_ctx *ctx, const double *U, double *nodal_stress, double *vm
  * (Common_ExtractDominantDirectionsFromPrincipalStressDirections.m:9-38).
  * Either output may be NULL. */
 int sgld_principal_stress(sgld_ctx *ctx, const double *U, double *ps_node, double *dir_elem);
+
+/* ---- the learned warm start's network on its own ------------------------------
+ * No counterpart in the reference.  A 3D convolutional U-Net on a node grid
+ * (ny, nx, nz), tensors channels-last [v][c] with v = y + ny (x + nx z):
+ *   encoder level l: relu(conv3) twice, then 2x average pooling (ceil);
+ *   decoder level l: relu(conv3) on level l+1 to w_l channels, nearest 2x
+ *   upsampling plus the encoder's level-l output, relu(conv3);
+ *   head: linear 1x1x1 convolution to out_channels (FP32 output).
+ * Activations and weights are BF16 on the device, every product accumulates
+ * in FP32, the master weights and Adam moments are FP32.  Parameters, per
+ * convolution W[taps][cin][cout] then b[cout], convolutions in the order
+ * a_0, b_0, .., a_{L-1}, b_{L-1}, u_{L-2}, m_{L-2}, .., u_0, m_0, head.
+ * levels in [1, 4]; widths NULL = {16, 32, 48, 64}; channel counts are
+ * multiples of 4 up to 64 (in_channels too).  The network uses its own CUDA
+ * stream on the current device. */
+typedef struct sgld_net sgld_net;
+
+int sgld_net_create(int ny, int nx, int nz, int in_channels, int out_channels, int levels, const int *widths,
+                    unsigned long long seed, sgld_net **out);
+void sgld_net_destroy(sgld_net *net);
+const char *sgld_net_last_error(const sgld_net *net);
+int64_t sgld_net_num_params(const sgld_net *net);
+int sgld_net_get_params(sgld_net *net, float *params);
+/* also resets the Adam moments and step count */
+int sgld_net_set_params(sgld_net *net, const float *params);
+/* x [V][in_channels] (rounded to BF16 on upload) -> y [V][out_channels] */
+int sgld_net_forward(sgld_net *net, const float *x, float *y);
+/* loss = sum_v mask_v |y_v - target_v|^2 / (out_channels sum_v mask_v) (mask NULL = 1)
+ * and its gradient with respect to every parameter (grad may be NULL) */
+int sgld_net_grad(sgld_net *net, const float *x, const float *target, const float *mask, double *loss,
+                  float *grad);
+/* sgld_net_grad followed by one Adam step (beta 0.9, 0.999, eps 1e-8); loss before the step */
+int sgld_net_train_step(sgld_net *net, const float *x, const float *target, const float *mask, float lr,
+                        double *loss);
 
 #ifdef __cplusplus
 }

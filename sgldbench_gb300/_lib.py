@@ -40,13 +40,16 @@ class SolveInfo(C.Structure):
 class TopOptOpts(C.Structure):
     _fields_ = [("volfrac", dbl), ("rmin", dbl), ("move", dbl), ("n_loop", i32), ("min_change", dbl),
                 ("max_sharpness", dbl), ("penalty", dbl), ("E0", dbl), ("Emin", dbl), ("solve", SolveOpts),
-                ("optimizer", i32)]
+                ("optimizer", i32), ("learned", i32), ("net_level", i32), ("net_train_steps", i32),
+                ("net_lr", C.c_float)]
 
 
 class TopOptIter(C.Structure):
     _fields_ = [("loop", i32), ("cg_iterations", i32), ("compliance", dbl), ("volume", dbl), ("sharpness", dbl),
                 ("change", dbl), ("constraint", dbl), ("t_assemble", dbl), ("t_solve", dbl), ("t_opt", dbl),
-                ("t_filter", dbl)]
+                ("t_filter", dbl), ("net_used", i32), ("net_accepted", i32), ("net_r0_ratio", dbl),
+                ("ext_r0_ratio", dbl),
+                ("net_loss", dbl), ("t_net", dbl), ("inner_iterations", i32)]
 
 
 SIGNATURES = {
@@ -87,6 +90,15 @@ SIGNATURES = {
     "sgld_kernel_launches": (i64, []),
     "sgld_time_op": (i32, [vp, i32, i32, vp]),
     "sgld_kbyu_tile": (i32, [vp, vp, vp]),
+    "sgld_net_create": (i32, [i32, i32, i32, i32, i32, i32, vp, C.c_ulonglong, vp]),
+    "sgld_net_destroy": (None, [vp]),
+    "sgld_net_last_error": (C.c_char_p, [vp]),
+    "sgld_net_num_params": (i64, [vp]),
+    "sgld_net_get_params": (i32, [vp, vp]),
+    "sgld_net_set_params": (i32, [vp, vp]),
+    "sgld_net_forward": (i32, [vp, vp, vp]),
+    "sgld_net_grad": (i32, [vp, vp, vp, vp, vp, vp]),
+    "sgld_net_train_step": (i32, [vp, vp, vp, vp, C.c_float, vp]),
     "sgld_kbyu_dot_noalloc": (i32, [vp, vp, vp, vp, vp]),
     "sgld_density_filter": (i32, [vp, dbl, vp, vp]),
     "sgld_topopt": (i32, [vp, vp, vp, vp, vp, vp, vp]),

@@ -707,6 +707,7 @@ void sgld_destroy(sgld_ctx *ctx) {
     for (auto &a : c.aux)
         if (a) cudaStreamDestroy(a);
     if (c.solve_graph) cudaGraphExecDestroy(c.solve_graph);
+    learned_free(c.lws);
     for (void *p : {(void *)c.d_blk, (void *)c.d_binfo})
         if (p) cudaFree(p);
     delete ctx;
@@ -1730,6 +1731,10 @@ static int run_solve_graph(sgld_ctx *ctx, int nrhs, bool staged, const sgld_solv
 
 // PCG on the context's own full-grid vectors (b in d_b, x in d_x), used by the
 // SIMP driver (sgld_topopt_api.cu)
+int sgld::vcycle_f64(sgld_ctx *ctx, const double *r, double *z, double *partial, int *nb) {
+    return vcycle_dev(ctx, r, z, partial, nb);
+}
+
 int sgld::solve_on_device(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
     int rc = check_assembled(ctx);
     if (rc) return rc;

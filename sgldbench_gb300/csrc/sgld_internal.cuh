@@ -108,6 +108,7 @@ struct Ctx {
     int inner_graph_k = 0;
     double inner_graph_eta = -1.0;
     int64_t inner_entry_launches = 0, inner_body_launches = 0;
+    struct LearnedWS *lws = nullptr;   // learned warm start of the SIMP loop (sgld_learned.cu)
     cudaStream_t stream = nullptr;
     std::string err;
     int device = 0;
@@ -127,6 +128,13 @@ struct sgld_ctx {
 namespace sgld {
 
 constexpr int CSPLIT = 16;   // column chunks of the coarse GEMV
+
+// learned warm start of the SIMP loop (sgld_learned.cu)
+void learned_free(LearnedWS *w);
+int learned_setup(sgld_ctx *ctx, LearnedWS **pw, int net_level, bool need_net);
+int learned_before_solve(sgld_ctx *ctx, LearnedWS *w, int mode, double E0, int *used, int *accepted,
+                         double *ratio, double *ext_ratio);
+int learned_after_solve(sgld_ctx *ctx, LearnedWS *w, int mode, int steps, float lr, double *loss);
 
 // number of kernels this library has launched (host-side counter, one per launch)
 extern int64_t g_launches;
@@ -170,6 +178,9 @@ struct sgld_solve_info;
 namespace sgld {
 // PCG on the context's own full-grid vectors d_b / d_x (sgld_api.cu)
 int solve_on_device(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info);
+// FP64 additive V-cycle z = M r on full-grid vectors; with partial, the CTA
+// partials of z.r (nb of them) for launch_finalize_sum
+int vcycle_f64(sgld_ctx *ctx, const double *r, double *z, double *partial, int *nb);
 // SIMP loop (kernels_topopt.cu)
 void upload_filter_weights(double rmin, int *radius, cudaStream_t s);
 void launch_density_filter(const Level &l0, const double *x, int r, double *y, cudaStream_t s);

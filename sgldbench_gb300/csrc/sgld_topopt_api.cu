@@ -376,6 +376,16 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
     } else if (o.optimizer != SGLD_OPT_OC) {
         return tfail(ctx, SGLD_ERR_ARG, "optimizer must be SGLD_OPT_OC or SGLD_OPT_MMA");
     }
+    if (o.learned < 0 || o.learned > 2) return tfail(ctx, SGLD_ERR_ARG, "learned must be 0, 1 or 2");
+    if (o.learned) {   // a fresh network per loop
+        learned_free(c.lws);
+        c.lws = nullptr;
+        if ((rc = learned_setup(ctx, &c.lws, o.net_level, o.learned == 1))) return rc;
+    }
+    const int net_steps = o.net_train_steps > 0 ? o.net_train_steps : 4;
+    const float net_lr = o.net_lr > 0.f ? o.net_lr : 1e-3f;
+    cudaEvent_t evn[4];
+    for (auto &e : evn) TCK(cudaEventCreate(&e));
     sgld_solve_opts so = o.solve;
     so.use_x0 = 1;
     so.history = nullptr;
@@ -388,10 +398,19 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
         launch_oc_scalar(0, c.t_st, c.t_st + T_VOL, 1, nact, o.volfrac, s);        // g (:83), bisection bounds
         TCK(cudaEventRecord(ev[0], s));
         if ((rc = sgld_assemble(ctx))) return rc;                                  // :54
+        int net_used = 0, net_acc = 0;
+        double net_ratio = 0.0, net_ext = 0.0, net_loss = 0.0;
+        TCK(cudaEventRecord(evn[0], s));
+        if (o.learned &&
+            (rc = learned_before_solve(ctx, c.lws, o.learned, o.E0, &net_used, &net_acc, &net_ratio, &net_ext)))
+            return rc;
+        TCK(cudaEventRecord(evn[1], s));
         TCK(cudaEventRecord(ev[1], s));
         sgld_solve_info si;
         if ((rc = solve_on_device(ctx, &so, &si))) return rc;                      // :57
         TCK(cudaEventRecord(ev[2], s));
+        if (o.learned && (rc = learned_after_solve(ctx, c.lws, o.learned, net_steps, net_lr, &net_loss))) return rc;
+        TCK(cudaEventRecord(evn[2], s));
         int nbc = 0;
         launch_unit_compliance(l0, c.d_x, c.E, c.t_ce, c.d_part, &nbc, s);        // :59, :63
         launch_finalize_sum(c.d_part, nbc, c.t_st + T_C, s);
@@ -456,11 +475,19 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
             h.t_solve = elapsed(ev[1], ev[2]) * 1e-3;
             h.t_opt = (elapsed(ev[2], ev[3]) + elapsed(evf, evo)) * 1e-3;
             h.t_filter = (elapsed(ev[3], evf) + elapsed(evo, ev[4])) * 1e-3;
+            h.inner_iterations = si.inner_iterations;
+            h.net_used = net_used;
+            h.net_accepted = net_acc;
+            h.net_r0_ratio = net_ratio;
+            h.ext_r0_ratio = net_ext;
+            h.net_loss = net_loss;
+            h.t_net = (elapsed(evn[0], evn[1]) + elapsed(ev[2], evn[2])) * 1e-3;
         }
         cudaEventDestroy(evf);
         cudaEventDestroy(evo);
     }
     for (auto &e : ev) cudaEventDestroy(e);
+    for (auto &e : evn) cudaEventDestroy(e);
     if (n_iter) *n_iter = loop;
     if (xphys) {
         launch_gather_elems(c.d_elemap, ne, c.t_xp, c.d_tmp, s);

@@ -411,8 +411,15 @@ class VoxelSolver:
                                        penalty: float = 3.0, E0: float = 1.0, Emin: float = 1e-9,
                                        tol: float = 1e-6, maxIT: int = 500, precision: str = "fp64",
                                        inner_its: int = 0, x0=None, inner_tol: float = 0.0,
-                                       optimizer: str = "OC"):
-        """The whole SIMP loop on the device.  Returns (xPhys, history list)."""
+                                       optimizer: str = "OC", learned: int = 0, net_level: int = 0,
+                                       net_train_steps: int = 0, net_lr: float = 0.0):
+        """The whole SIMP loop on the device.  Returns (xPhys, history list).
+
+        learned=1 turns on the learned warm start (a U-Net on the grid of
+        level ``net_level`` trained online on the loop's solves, combined with
+        the previous displacement change); learned=2 uses the previous change
+        alone.  The solves still run to ``tol``, so only iteration counts
+        change."""
         Fv = self._vec(F, self.numDOFs)
         so = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=1,
                          precision=_precision(precision),
@@ -421,7 +428,8 @@ class VoxelSolver:
             raise ValueError("optimizer must be 'OC' or 'MMA'")
         o = L.TopOptOpts(volfrac=volfrac, rmin=rMin, move=move, n_loop=nLoop, min_change=minChange,
                          max_sharpness=maxSharpness, penalty=penalty, E0=E0, Emin=Emin, solve=so,
-                         optimizer=1 if optimizer == "MMA" else 0)
+                         optimizer=1 if optimizer == "MMA" else 0, learned=int(learned),
+                         net_level=net_level, net_train_steps=net_train_steps, net_lr=net_lr)
         xp = np.zeros(self.numElements)
         hist = (L.TopOptIter * nLoop)()
         nit = C.c_int()

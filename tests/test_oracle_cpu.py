@@ -219,3 +219,35 @@ def test_mma_restatement_matches_reference(m):
     out = mma.mma_update(m, n, x, xmin, xmax, xo1, xo2, df0, fval, dfdx)
     for a, b in zip(out, ref):
         assert np.abs(a - np.asarray(b).ravel()).max() <= 1e-12
+
+
+@pytest.mark.parametrize("levels,widths", [(1, [4]), (2, [4, 8]), (3, [4, 8, 8])])
+def test_net_oracle_gradient(levels, widths):
+    """The U-Net restatement's backward pass equals central finite differences
+    of its loss (float64, no rounding): pins the oracle the GPU is checked against."""
+    from oracle.net import UNet
+
+    rng = np.random.default_rng(levels)
+    dims = (7, 5, 4)
+    n = UNet(dims, 4, 3, levels, widths, emulate=False)
+    V = int(np.prod(dims))
+    p = rng.standard_normal(n.nparam) * 0.3
+    x = rng.standard_normal((V, 4))
+    t = rng.standard_normal((V, 3))
+    m = (rng.random(V) > 0.2).astype(float)
+    _, g, _ = n.value_and_grad(p, x, t, m)
+    h = 1e-6
+    for _ in range(3):
+        d = rng.standard_normal(n.nparam)
+        lp, _, _ = n.value_and_grad(p + h * d, x, t, m)
+        lm, _, _ = n.value_and_grad(p - h * d, x, t, m)
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - g @ d) <= 1e-7 * abs(g @ d)
+
+
+def test_net_oracle_bf16_rounding():
+    """Round to nearest even at the BF16 boundary (8 mantissa bits)."""
+    from oracle.net import bf16
+
+    v = bf16(np.array([1.0, 1.0 + 2.0 ** -8, 1.0 + 3 * 2.0 ** -9, -3.14159, 0.0]))
+    assert v.tolist() == [1.0, 1.0, 1.0078125, -3.140625, 0.0]

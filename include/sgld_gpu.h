@@ -317,6 +317,40 @@ typedef struct sgld_topopt_iter {
 int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const double *F, const double *x0, double *xphys,
                 sgld_topopt_iter *hist, int *n_iter);
 
+/* Local-volume-constrained loop (porous infill), TopOpti_LocalVolumeConstraint.m:33-269:
+ * compliance normalised by the solid domain's, the p-norm of the PDE-filtered
+ * (radius rhat) local volume fraction held below alpha
+ * (Initialize4GradedPorosity with alphaMax_ = alphaMin_), density filter
+ * (rmin) and Heaviside projection (beta, eta) of the design, one MMA update
+ * per iteration (passive elements excluded and kept solid), beta doubling
+ * every beta_interval iterations up to beta_max, and the sensitivity penalty
+ * raised by penalty_increment every penalty_interval iterations (capped at 3).
+ * Starts from x = alpha (TopOpti_CallTopOpti.m:41-45).  hist records use
+ * constraint = the p-norm constraint value fval. */
+typedef struct sgld_topopt_local_opts {
+    double rmin;              /* rMin_ */
+    double rhat;              /* rHatMin_ (0 = 8) */
+    double alpha;             /* alphaMin_ (0 = 0.5) */
+    double pnorm;             /* p_ (0 = 16) */
+    double move;              /* move_ (0 = 0.1) */
+    int n_loop;               /* nLoop_ */
+    double min_change;        /* minChange_ (0 = 1e-4) */
+    double max_sharpness;     /* maxSharpness_ (0 = 0.05) */
+    double simp_penalty;      /* SIMPpenalty_ of the modulus (0 = 3) */
+    double penalty;           /* penalty_ of the sensitivity, continued (0 = 3) */
+    double penalty_increment; /* penaltyIncrement_ */
+    int penalty_interval;     /* penaltyUpdateIterations_ (0 = no continuation) */
+    double beta, eta;         /* beta_ (0 = 1), eta_ (0 = 0.5) */
+    double beta_max;          /* pMax_ (0 = 128) */
+    int beta_interval;        /* iterations between beta doublings (0 = 40) */
+    double E0, Emin;          /* modulus_, modulusMin_ (0 = 1, 1e-6) */
+    sgld_solve_opts solve;    /* tol_, maxIT_, precision of the MGPCG solves; tol_ and maxIT_ also
+                                 drive the PDE filter's PCG (TopOpti_PDEFiltering_matrixFree.m:23) */
+} sgld_topopt_local_opts;
+
+int sgld_topopt_local(sgld_ctx *ctx, const sgld_topopt_local_opts *opts, const double *F, double *xphys,
+                      sgld_topopt_iter *hist, int *n_iter);
+
 /* FEA_StressAnalysis.m:17-60 and FEA_ComputePerElementVonMisesStress.m:10-19:
  * nodal Cartesian stress (numNodes x 6, row-major [xx yy zz yz zx xy]), nodal
  * von Mises and per-element von Mises with the reference's final .^(1/2).

@@ -842,3 +842,112 @@ def topopt_global_volume(model: Model, opt: TopOptOptions, history=None):
         sharp = float(4.0 * np.sum(xPhys * (1.0 - xPhys)) / n)               # :102
         hist.append({"loop": loop, "c": c, "vol": vol, "sharp": sharp, "change": change, "g": g, "its": its})
     return xPhys, hist
+
+
+# ---------------------------------------------------------------------------
+# Local-volume-constrained loop (porous infill): src/TopOpti_LocalVolumeConstraint.m
+# ---------------------------------------------------------------------------
+@dataclass
+class LocalOptions:
+    rmin: float = 1.5              # rMin_ (density filter)
+    rhat: float = 8.0              # rHatMin_ (Data_GlobalVariables.m:62), PDE filter of the local volume
+    alpha: float = 0.5             # alphaMin_ = alphaMax_ (Data_GlobalVariables.m:63; Initialize4GradedPorosity)
+    pnorm: float = 16.0            # p_ (Data_GlobalVariables.m:75)
+    move: float = 0.1              # move_
+    n_loop: int = 300              # nLoop_
+    min_change: float = 1.0e-4     # minChange_
+    max_sharpness: float = 0.05    # maxSharpness_
+    simp_penalty: float = 3.0      # SIMPpenalty_ (TopOpti_MaterialInterpolationSIMP.m)
+    penalty: float = 3.0           # penalty_ (TopOpti_DeMaterialInterpolation.m), continued
+    penalty_increment: float = 0.2  # penaltyIncrement_ (Data_GlobalVariables.m:73)
+    penalty_interval: int = 30     # penaltyUpdateIterations_ (:74)
+    beta: float = 1.0              # beta_ (:76)
+    eta: float = 0.5               # eta_ (:77)
+    beta_max: float = 128.0        # pMax_ (:59)
+    beta_interval: int = 40        # TopOpti_LocalVolumeConstraint.m:246
+    E0: float = 1.0                # modulus_
+    Emin: float = 1.0e-6           # modulusMin_
+    tol: float = 1.0e-6            # tol_ (elasticity and PDE-filter PCG)
+    maxit: int = 500               # maxIT_
+    passive: np.ndarray = None     # passiveElements_ (compact 0-based)
+
+
+def heaviside(xt, beta, eta):
+    """TopOpti_DualizeDesignVariable.m:4."""
+    return (np.tanh(beta * eta) + np.tanh(beta * (xt - eta))) / (np.tanh(beta * eta) + np.tanh(beta * (1 - eta)))
+
+
+def heaviside_derivative(xt, beta, eta):
+    """TopOpti_DeDualizeDesignVariable.m:4."""
+    t = np.tanh(beta * (xt - eta))
+    return beta * (1 - t * t) / (np.tanh(beta * eta) + np.tanh(beta * (1 - eta)))
+
+
+def topopt_local_volume(model: Model, opt: LocalOptions, history=None):
+    """TopOpti_LocalVolumeConstraint.m:33-269 (MEX branch, PDE filter matrix-free):
+    solid-domain compliance, then per iteration SIMP E, warm-started MGPCG,
+    normalised compliance and its sensitivity, the p-norm of the PDE-filtered
+    local volume against alpha and its sensitivity, density-filter chain rule
+    through the Heaviside projection, one MMA update (m = 1, passive elements
+    excluded), filter + projection of the new design, beta and penalty
+    continuation.  Returns xPhys and per-iteration records."""
+    from oracle import mma
+
+    l1 = model.levels[0]
+    n = l1.numElements
+    emf, (rx, ry, rz) = l1.eleMapForward, (l1.resX, l1.resY, l1.resZ)
+    Hs = K.density_filter(None, opt.rmin, emf, rx, ry, rz)                       # :37
+    pas = np.zeros(n, bool) if opt.passive is None else np.isin(np.arange(n), opt.passive)
+    act = np.nonzero(~pas)[0]                                                    # :63
+    vol_max = np.full(n, opt.alpha)                                              # :290-301
+    vol_max[pas] = 1.0
+    x = np.full(n, opt.alpha)                                                    # TopOpti_CallTopOpti.m:41-45
+    x[pas] = 1.0
+    beta, penalty = opt.beta, opt.penalty
+    xTilde = x.copy()                                                            # :69
+    xPhys = heaviside(xTilde, beta, opt.eta)                                     # :70
+    # :79-86 compliance of the fully solid domain
+    E = np.full(n, opt.E0)
+    set_modulus(model, E)
+    assemble_stencil(model)
+    U, _ = pcg(lambda u: kbyu(model, u), lambda r: vcycle(model, r), model.F, opt.tol, opt.maxit,
+               x0=np.zeros(l1.numDOFs))
+    c_solid = float(E @ unit_compliance(model, U))
+    loopbeta, loop, change, sharp = 0, 0, 1.0, 1.0
+    hist = [] if history is None else history
+    while loop < opt.n_loop and change > opt.min_change and sharp > opt.max_sharpness:   # :116
+        loopbeta += 1
+        loop += 1
+        E = simp_modulus(xPhys, opt.E0, opt.Emin, opt.simp_penalty)             # :121
+        set_modulus(model, E)
+        assemble_stencil(model)                                                  # :123
+        U, its = pcg(lambda u: kbyu(model, u), lambda r: vcycle(model, r), model.F, opt.tol, opt.maxit, x0=U)
+        ce_norm = unit_compliance(model, U) / c_solid                            # :128, :132
+        c = float(E @ ce_norm) * c_solid                                         # :133-134
+        vol = float(xPhys.sum() / n)                                             # :135
+        dc = -(penalty * (opt.E0 - opt.Emin) * xPhys ** (penalty - 1)) * ce_norm  # :136
+        xh, _ = pde_filter(model, xPhys, opt.rhat, opt.tol, opt.maxit)           # :142
+        s = float(np.sum(xh ** opt.pnorm / vol_max ** opt.pnorm) / n)
+        dfdx_pde = s ** (1.0 / opt.pnorm - 1.0) * (xh ** (opt.pnorm - 1) / vol_max ** opt.pnorm) / n   # :146
+        dx = heaviside_derivative(xTilde, beta, opt.eta)                         # :151
+        dc = K.density_filter(dc * dx / Hs, opt.rmin, emf, rx, ry, rz)           # :153
+        dfdx, _ = pde_filter(model, dfdx_pde, opt.rhat, opt.tol, opt.maxit)      # :162
+        dfdx = K.density_filter(dfdx * dx / Hs, opt.rmin, emf, rx, ry, rz)       # :169
+        fval = s ** (1.0 / opt.pnorm) - 1.0                                      # :179
+        xval = x[act]
+        xmin, xmax = np.maximum(0.0, xval - opt.move), np.minimum(1.0, xval + opt.move)   # :184-185
+        xmma, _, _ = mma.mma_update(1, act.size, xval, xmin, xmax, xval, xval, dc[act], fval, dfdx[act])
+        change = float(np.abs(xmma - xval).max())                                # :191
+        x = np.ones(n)
+        x[act] = xmma                                                            # :192
+        xTilde = K.density_filter(x, opt.rmin, emf, rx, ry, rz) / Hs             # :197
+        xPhys = heaviside(xTilde, beta, opt.eta)                                 # :201
+        xPhys[pas] = 1.0                                                         # :204
+        sharp = float(4.0 * np.sum(xPhys * (1.0 - xPhys)) / n)                   # :205
+        hist.append({"loop": loop, "c": c, "vol": vol, "sharp": sharp, "change": change, "fval": fval,
+                     "its": its, "beta": beta, "penalty": penalty})
+        if beta < opt.beta_max and loopbeta >= opt.beta_interval:               # :246-253
+            beta, loopbeta, change, sharp = 2 * beta, 0, 1.0, 1.0
+        if opt.penalty_interval > 0 and loop % opt.penalty_interval == 0:        # :256-261
+            penalty = min(penalty + opt.penalty_increment, 3.0)
+    return xPhys, hist

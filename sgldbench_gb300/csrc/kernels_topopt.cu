@@ -349,4 +349,99 @@ void launch_fill_active(const Level &l0, double *y, double v, int nb, cudaStream
     k_fill_active<<<nb, TB, 0, s>>>(y, l0.eact, l0.nel, v);
 }
 
+// ---- local-volume loop (TopOpti_LocalVolumeConstraint.m) ------------------------
+// Heaviside projection xp = H(xt) (TopOpti_DualizeDesignVariable.m:4) and, if
+// dx != null, its derivative (TopOpti_DeDualizeDesignVariable.m:4); passive
+// elements are set to 1 (TopOpti_LocalVolumeConstraint.m:204), void to 0
+__global__ void k_heaviside(const double *__restrict__ xt, const uint8_t *__restrict__ eact, int64_t n,
+                            double beta, double eta, double *__restrict__ xp, double *__restrict__ dx) {
+    const double den = tanh(beta * eta) + tanh(beta * (1.0 - eta));
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB) {
+        if (!eact[e]) {
+            if (xp) xp[e] = 0.0;
+            if (dx) dx[e] = 0.0;
+            continue;
+        }
+        const double t = tanh(beta * (xt[e] - eta));
+        if (xp) xp[e] = (eact[e] & EF_PASSIVE) ? 1.0 : (tanh(beta * eta) + t) / den;
+        if (dx) dx[e] = beta * (1.0 - t * t) / den;
+    }
+}
+
+// dcs = dc .* dx ./ Hs with dc = -p (E0 - Emin) xp^(p-1) ce / c_solid
+// (TopOpti_LocalVolumeConstraint.m:132-136, :153)
+__global__ void k_local_sens(const double *__restrict__ xp, const double *__restrict__ ce,
+                             const double *__restrict__ dx, const double *__restrict__ Hs,
+                             const uint8_t *__restrict__ eact, int64_t n, double p, double E0, double Emin,
+                             double inv_csolid, double *__restrict__ dcs) {
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB) {
+        if (!eact[e]) {
+            dcs[e] = 0.0;
+            continue;
+        }
+        const double dc = -(p * (E0 - Emin) * pow(xp[e], p - 1.0)) * ce[e] * inv_csolid;
+        dcs[e] = dc * dx[e] / Hs[e];
+    }
+}
+
+// partial sums of (xh / vmax)^p, vmax = alpha (1 on passive elements)
+__global__ void k_pnorm_sum(const double *__restrict__ xh, const uint8_t *__restrict__ eact, int64_t n, double p,
+                            double alpha, double *__restrict__ part) {
+    double s = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB) {
+        if (!eact[e]) continue;
+        const double vm = (eact[e] & EF_PASSIVE) ? 1.0 : alpha;
+        s += pow(xh[e], p) / pow(vm, p);
+    }
+    s = tblock_sum(s);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// dfdx_pde = (S/N)^(1/p-1) xh^(p-1) / vmax^p / N  (TopOpti_LocalVolumeConstraint.m:146); S on the device
+__global__ void k_pnorm_grad(const double *__restrict__ xh, const uint8_t *__restrict__ eact, int64_t n, double p,
+                             double alpha, const double *__restrict__ S, double N, double *__restrict__ g) {
+    const double f = pow(*S / N, 1.0 / p - 1.0) / N;
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB) {
+        if (!eact[e]) {
+            g[e] = 0.0;
+            continue;
+        }
+        const double vm = (eact[e] & EF_PASSIVE) ? 1.0 : alpha;
+        g[e] = f * pow(xh[e], p - 1.0) / pow(vm, p);
+    }
+}
+
+// y = a .* b ./ c on active elements (b = null: y = a ./ c)
+__global__ void k_mul_div(const double *__restrict__ a, const double *__restrict__ b, const double *__restrict__ c,
+                          const uint8_t *__restrict__ eact, int64_t n, double *__restrict__ y) {
+    for (int64_t e = blockIdx.x * (int64_t)TB + threadIdx.x; e < n; e += (int64_t)gridDim.x * TB)
+        y[e] = eact[e] ? a[e] * (b ? b[e] : 1.0) / c[e] : 0.0;
+}
+
+void launch_heaviside(const Level &l0, const double *xt, double beta, double eta, double *xp, double *dx, int nb,
+                      cudaStream_t s) {
+    ++g_launches;
+    k_heaviside<<<nb, TB, 0, s>>>(xt, l0.eact, l0.nel, beta, eta, xp, dx);
+}
+
+void launch_local_sens(const Level &l0, const double *xp, const double *ce, const double *dx, const double *Hs,
+                       double p, double E0, double Emin, double inv_csolid, double *dcs, int nb, cudaStream_t s) {
+    ++g_launches;
+    k_local_sens<<<nb, TB, 0, s>>>(xp, ce, dx, Hs, l0.eact, l0.nel, p, E0, Emin, inv_csolid, dcs);
+}
+
+void launch_pnorm(const Level &l0, const double *xh, double p, double alpha, double *part, double *S, double N,
+                  double *g, int nb, cudaStream_t s) {
+    g_launches += 2;   // the finalize launch counts itself
+    k_pnorm_sum<<<nb, TB, 0, s>>>(xh, l0.eact, l0.nel, p, alpha, part);
+    launch_finalize_sum(part, nb, S, s);
+    k_pnorm_grad<<<nb, TB, 0, s>>>(xh, l0.eact, l0.nel, p, alpha, S, N, g);
+}
+
+void launch_mul_div(const Level &l0, const double *a, const double *b, const double *c, double *y, int nb,
+                    cudaStream_t s) {
+    ++g_launches;
+    k_mul_div<<<nb, TB, 0, s>>>(a, b, c, l0.eact, l0.nel, y);
+}
+
 }  // namespace sgld

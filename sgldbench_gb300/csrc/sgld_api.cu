@@ -708,7 +708,9 @@ void sgld_destroy(sgld_ctx *ctx) {
         if (a) cudaStreamDestroy(a);
     if (c.solve_graph) cudaGraphExecDestroy(c.solve_graph);
     learned_free(c.lws);
-    for (void *p : {(void *)c.d_blk, (void *)c.d_binfo})
+    for (void *p : {(void *)c.d_blk, (void *)c.d_binfo, (void *)c.t_x, (void *)c.t_xp, (void *)c.t_hs,
+                    (void *)c.t_ce, (void *)c.t_dcs, (void *)c.t_dvs, (void *)c.t_dc, (void *)c.t_dv, (void *)c.t_q,
+                    (void *)c.t_tmp, (void *)c.t_st, (void *)c.t_pde})
         if (p) cudaFree(p);
     delete ctx;
 }

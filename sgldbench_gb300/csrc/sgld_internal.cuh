@@ -73,6 +73,7 @@ struct Ctx {
     double *t_x = nullptr, *t_xp = nullptr, *t_hs = nullptr, *t_ce = nullptr, *t_dcs = nullptr, *t_dvs = nullptr,
            *t_dc = nullptr, *t_dv = nullptr, *t_q = nullptr, *t_tmp = nullptr, *t_st = nullptr;
     double t_rmin = -1.0;
+    double *t_pde = nullptr;   // [7 nnode] PDE-filter PCG work (finest nodes, one value each)
     cudaGraphExec_t factor_graph = nullptr;   // captured factorization of the coarsest matrix
     int64_t factor_graph_launches = 0;
     int trinv_ring = 0;
@@ -198,6 +199,16 @@ void launch_oc_apply(const Level &l0, double *x, const double *q, double move, c
 void launch_max_partials(const double *part, int nb, double *out, cudaStream_t s);
 void launch_div(const Level &l0, const double *a, const double *b, double *y, int nb, cudaStream_t s);
 void launch_fill_active(const Level &l0, double *y, double v, int nb, cudaStream_t s);
+// local-volume loop (kernels_topopt.cu)
+void launch_heaviside(const Level &l0, const double *xt, double beta, double eta, double *xp, double *dx, int nb,
+                      cudaStream_t s);
+void launch_local_sens(const Level &l0, const double *xp, const double *ce, const double *dx, const double *Hs,
+                       double p, double E0, double Emin, double inv_csolid, double *dcs, int nb, cudaStream_t s);
+// S = sum (xh/vmax)^p into *S (device), g = dfdx of the p-norm local volume
+void launch_pnorm(const Level &l0, const double *xh, double p, double alpha, double *part, double *S, double N,
+                  double *g, int nb, cudaStream_t s);
+void launch_mul_div(const Level &l0, const double *a, const double *b, const double *c, double *y, int nb,
+                    cudaStream_t s);
 int launch_mma_gather(const int64_t *var, int64_t nvar, const double *x, const double *dc, const double *dv,
                       double move, double scale, double *xv, double *xmin, double *xmax, double *df0, double *dg,
                       cudaStream_t s);

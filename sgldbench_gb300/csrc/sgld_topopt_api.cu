@@ -221,6 +221,54 @@ extern "C" int sgld_mma_update(sgld_ctx *ctx, int m, int n, const double *xval, 
     return SGLD_OK;
 }
 
+namespace {
+
+// TopOpti_PDEFiltering_matrixFree.m:1-36 on full-grid element fields xe -> ye
+// (device): element -> node (x/8 to each corner), Jacobi-preconditioned PCG on
+// K_pde from 0 (Solving_PreconditionedConjugateGradientSolver.m), node ->
+// element (mean of the 8 corners).  Scratch: its own node vectors, so the
+// elasticity solve's vectors (U, F) survive.
+int pde_filter_dev(sgld_ctx *ctx, double rhat, const double *xe, double *ye, double tol, int maxit, int *iterations) {
+    Ctx &c = ctx->c;
+    const Level &l0 = c.lv[0];
+    const int64_t nn = l0.nnode;
+    if (!c.t_pde) TCK(cudaMalloc((void **)&c.t_pde, 7 * sizeof(double) * (size_t)nn));
+    double *b = c.t_pde, *x = b + nn, *r = x + nn, *z = r + nn, *p = z + nn, *q = p + nn, *dinv = q + nn;
+    double K[64];
+    pde_element_matrix(rhat, K);
+    upload_kpde(K, c.stream);
+    launch_pde_e2n(l0, xe, b, c.stream);
+    launch_pde_diag(l0, dinv, c.stream);
+    const int nbv = reduce_blocks(nn);
+    launch_pcg_scalar(5, c.d_scal, c.d_iflag, c.d_part, 1, tol, maxit, c.stream);
+    launch_dot(b, b, nn, c.d_part, nbv, c.stream);
+    launch_pcg_scalar(0, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
+    TCK(cudaMemsetAsync(x, 0, sizeof(double) * nn, c.stream));
+    TCK(cudaMemcpyAsync(r, b, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c.stream));
+    launch_pde_jacobi(r, dinv, nn, z, c.d_part, nbv, c.stream);
+    launch_pcg_scalar(1, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
+    TCK(cudaMemcpyAsync(p, z, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c.stream));
+    int h_flag[4] = {0, 0, 0, 0};
+    for (int k = 1; k <= maxit; ++k) {
+        const int nb = launch_pde_kbyu(l0, p, q, c.d_part, c.stream);
+        launch_pcg_scalar(2, c.d_scal, c.d_iflag, c.d_part, nb, tol, maxit, c.stream);
+        launch_pcg_update(x, r, p, q, nn, c.d_scal, c.d_iflag, c.d_part, nbv, c.stream);
+        launch_pcg_scalar(3, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
+        TCK(cudaMemcpyAsync(h_flag, c.d_iflag, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.stream));
+        TCK(cudaStreamSynchronize(c.stream));
+        if (h_flag[2]) break;
+        launch_pde_jacobi(r, dinv, nn, z, c.d_part, nbv, c.stream);
+        launch_pcg_scalar(4, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
+        launch_pcg_pupdate(p, z, nn, c.d_scal, c.d_iflag, c.stream);
+    }
+    launch_pde_n2e(l0, x, ye, c.stream);
+    TCK(cudaGetLastError());
+    if (iterations) *iterations = h_flag[0];
+    return SGLD_OK;
+}
+
+}  // namespace
+
 extern "C" int sgld_pde_filter(sgld_ctx *ctx, double rhat, const double *x, double *y, double tol, int maxit,
                                int *iterations) {
     if (!ctx || !x || !y) return SGLD_ERR_ARG;
@@ -229,45 +277,15 @@ extern "C" int sgld_pde_filter(sgld_ctx *ctx, double rhat, const double *x, doub
     int rc = ensure_topo(ctx);
     if (rc) return rc;
     const Level &l0 = c.lv[0];
-    const int64_t ne = (int64_t)c.h_elemap.size(), nn = l0.nnode;
-    double K[64];
-    pde_element_matrix(rhat, K);
-    upload_kpde(K, c.stream);
+    const int64_t ne = (int64_t)c.h_elemap.size();
     TCK(cudaMemcpyAsync(c.d_tmp, x, sizeof(double) * ne, cudaMemcpyHostToDevice, c.stream));
     TCK(cudaMemsetAsync(c.t_tmp, 0, sizeof(double) * l0.nel, c.stream));
     launch_scatter_elems(c.d_elemap, ne, c.d_tmp, c.t_tmp, c.stream);
-    // src on the nodes, Jacobi diagonal, then the reference's PCG from x = 0
-    launch_pde_e2n(l0, c.t_tmp, c.d_b, c.stream);
-    double *dinv = c.d_tmp;
-    launch_pde_diag(l0, dinv, c.stream);
-    const int nbv = reduce_blocks(nn);
-    launch_pcg_scalar(5, c.d_scal, c.d_iflag, c.d_part, 1, tol, maxit, c.stream);
-    launch_dot(c.d_b, c.d_b, nn, c.d_part, nbv, c.stream);
-    launch_pcg_scalar(0, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
-    TCK(cudaMemsetAsync(c.d_x, 0, sizeof(double) * nn, c.stream));
-    TCK(cudaMemcpyAsync(c.d_r, c.d_b, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c.stream));
-    launch_pde_jacobi(c.d_r, dinv, nn, c.d_z, c.d_part, nbv, c.stream);
-    launch_pcg_scalar(1, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
-    TCK(cudaMemcpyAsync(c.d_p, c.d_z, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c.stream));
-    int h_flag[4] = {0, 0, 0, 0};
-    for (int k = 1; k <= maxit; ++k) {
-        const int nb = launch_pde_kbyu(l0, c.d_p, c.d_q, c.d_part, c.stream);
-        launch_pcg_scalar(2, c.d_scal, c.d_iflag, c.d_part, nb, tol, maxit, c.stream);
-        launch_pcg_update(c.d_x, c.d_r, c.d_p, c.d_q, nn, c.d_scal, c.d_iflag, c.d_part, nbv, c.stream);
-        launch_pcg_scalar(3, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
-        TCK(cudaMemcpyAsync(h_flag, c.d_iflag, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.stream));
-        TCK(cudaStreamSynchronize(c.stream));
-        if (h_flag[2]) break;
-        launch_pde_jacobi(c.d_r, dinv, nn, c.d_z, c.d_part, nbv, c.stream);
-        launch_pcg_scalar(4, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
-        launch_pcg_pupdate(c.d_p, c.d_z, nn, c.d_scal, c.d_iflag, c.stream);
-    }
-    launch_pde_n2e(l0, c.d_x, c.t_q, c.stream);
+    if ((rc = pde_filter_dev(ctx, rhat, c.t_tmp, c.t_q, tol, maxit, iterations))) return rc;
     launch_gather_elems(c.d_elemap, ne, c.t_q, c.d_tmp, c.stream);
     TCK(cudaGetLastError());
     TCK(cudaMemcpyAsync(y, c.d_tmp, sizeof(double) * ne, cudaMemcpyDeviceToHost, c.stream));
     TCK(cudaStreamSynchronize(c.stream));
-    if (iterations) *iterations = h_flag[0];
     return SGLD_OK;
 }
 
@@ -495,5 +513,187 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
         TCK(cudaStreamSynchronize(s));
     }
     c.assembled = false;   // E now holds the final design's moduli
+    return SGLD_OK;
+}
+
+// TopOpti_LocalVolumeConstraint.m:33-269 (the porous-infill loop), every field
+// operation on the device; the host runs the MMA dual iteration and the
+// continuation schedule.  Buffers (full element grid): t_x design x, t_tmp
+// xTilde, t_xp xPhys, t_hs filter weight sums, t_ce unit compliance, t_dvs
+// dx = H'(xTilde), t_dcs / t_dc sensitivity before / after the density
+// filter, t_q the PDE-filtered field, t_dv the constraint gradient.
+extern "C" int sgld_topopt_local(sgld_ctx *ctx, const sgld_topopt_local_opts *opts, const double *F,
+                                 double *xphys, sgld_topopt_iter *hist, int *n_iter) {
+    if (!ctx || !opts || !F) return SGLD_ERR_ARG;
+    Ctx &c = ctx->c;
+    if (!c.have_fixed) return tfail(ctx, SGLD_ERR_STATE, "fixed DOFs not set (sgld_set_fixed_dofs)");
+    sgld_topopt_local_opts o = *opts;
+    if (o.rhat == 0) o.rhat = 8.0;
+    if (o.alpha == 0) o.alpha = 0.5;
+    if (o.pnorm == 0) o.pnorm = 16.0;
+    if (o.move == 0) o.move = 0.1;
+    if (o.min_change == 0) o.min_change = 1e-4;
+    if (o.max_sharpness == 0) o.max_sharpness = 0.05;
+    if (o.simp_penalty == 0) o.simp_penalty = 3.0;
+    if (o.penalty == 0) o.penalty = 3.0;
+    if (o.beta == 0) o.beta = 1.0;
+    if (o.eta == 0) o.eta = 0.5;
+    if (o.beta_max == 0) o.beta_max = 128.0;
+    if (o.beta_interval == 0) o.beta_interval = 40;
+    if (o.E0 == 0) o.E0 = 1.0;
+    if (o.Emin == 0) o.Emin = 1e-6;
+    if (o.n_loop < 1 || !(o.alpha > 0.0 && o.alpha <= 1.0) || !(o.pnorm >= 1.0) || !(o.rhat > 0.0))
+        return tfail(ctx, SGLD_ERR_ARG, "n_loop >= 1, alpha in (0, 1], pnorm >= 1, rhat > 0 required");
+    int rc = ensure_topo(ctx);
+    if (rc) return rc;
+    int r = 0;
+    if ((rc = setup_filter(ctx, o.rmin, &r))) return rc;
+    const Level &l0 = c.lv[0];
+    const int64_t ne = (int64_t)c.h_elemap.size(), nn = (int64_t)c.h_nodemap.size();
+    const size_t nv = 3 * (size_t)l0.nnode;
+    const int nb = reduce_blocks(l0.nel);
+    const double N = (double)ne;
+    cudaStream_t s = c.stream;
+    const double pde_tol = o.solve.tol > 0 ? o.solve.tol : 1e-6;
+    const int pde_maxit = o.solve.maxit > 0 ? o.solve.maxit : 500;
+    // design variables: the active elements that are not passive (:63)
+    std::vector<int64_t> var;
+    var.reserve(c.h_elemap.size());
+    for (int64_t e : c.h_elemap)
+        if (!std::binary_search(c.h_passive.begin(), c.h_passive.end(), e)) var.push_back(e);
+    const int64_t nvar = (int64_t)var.size();
+    if (nvar == 0) return tfail(ctx, SGLD_ERR_ARG, "no design variables (every element passive)");
+    const int nbm = mma_blocks(nvar);
+    int64_t *d_var = nullptr;
+    double *mma_buf = nullptr;
+    struct Free {
+        void *a = nullptr, *b = nullptr;
+        ~Free() {
+            if (a) cudaFree(a);
+            if (b) cudaFree(b);
+        }
+    } fr;
+    TCK(cudaMalloc((void **)&d_var, sizeof(int64_t) * nvar));
+    fr.a = d_var;
+    TCK(cudaMemcpyAsync(d_var, var.data(), sizeof(int64_t) * nvar, cudaMemcpyHostToDevice, s));
+    TCK(cudaMalloc((void **)&mma_buf, sizeof(double) * (6 * (size_t)nvar + 2 * (size_t)nbm + 2)));
+    fr.b = mma_buf;
+    double *xv = mma_buf, *xmin = xv + nvar, *xmax = xmin + nvar, *df0 = xmax + nvar, *dg = df0 + nvar,
+           *xo = dg + nvar, *p1 = xo + nvar, *p2 = p1 + nbm, *sums = p2 + nbm;
+    // loads, U = 0
+    TCK(cudaMemsetAsync(c.d_b, 0, sizeof(double) * nv, s));
+    TCK(cudaMemsetAsync(c.d_x, 0, sizeof(double) * nv, s));
+    TCK(cudaMemcpyAsync(c.d_tmp, F, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, s));
+    launch_scatter_nodes(c.d_nodemap, nn, c.d_tmp, c.d_b, s);
+    // x = alpha (passive 1), xTilde = x, xPhys = H(xTilde)  (TopOpti_CallTopOpti.m:41-45, :68-70)
+    launch_fill_active(l0, c.t_x, o.alpha, nb, s);
+    if (!c.h_passive.empty()) launch_set_passive_x(l0, c.t_x, nb, s);
+    TCK(cudaMemcpyAsync(c.t_tmp, c.t_x, sizeof(double) * l0.nel, cudaMemcpyDeviceToDevice, s));
+    double beta = o.beta, penalty = o.penalty;
+    launch_heaviside(l0, c.t_tmp, beta, o.eta, c.t_xp, nullptr, nb, s);
+    sgld_solve_opts so = o.solve;
+    so.use_x0 = 1;
+    so.history = nullptr;
+    // :79-86 compliance of the fully solid domain
+    launch_fill_active(l0, c.E, o.E0, nb, s);
+    c.have_E = true;
+    if ((rc = sgld_assemble(ctx))) return rc;
+    sgld_solve_info si;
+    if ((rc = solve_on_device(ctx, &so, &si))) return rc;
+    int nbc = 0;
+    launch_unit_compliance(l0, c.d_x, c.E, c.t_ce, c.d_part, &nbc, s);
+    launch_finalize_sum(c.d_part, nbc, c.t_st + T_C, s);
+    double c_solid = 0.0;
+    TCK(cudaMemcpyAsync(&c_solid, c.t_st + T_C, sizeof(double), cudaMemcpyDeviceToHost, s));
+    TCK(cudaStreamSynchronize(s));
+    if (!(c_solid > 0.0)) return tfail(ctx, SGLD_ERR_NUMERIC, "compliance of the solid domain is not positive");
+    // E = SIMP(xPhys) for the first iteration, with vol / sharpness sums
+    launch_topo_modulus(l0, c.t_xp, o.simp_penalty, o.E0, o.Emin, c.E, c.d_part, c.d_part2, nb, s);
+    launch_finalize_sum(c.d_part, nb, c.t_st + T_VOL, s);
+    launch_finalize_sum(c.d_part2, nb, c.t_st + T_SHARP, s);
+    cudaEvent_t ev[5];
+    for (auto &e : ev) TCK(cudaEventCreate(&e));
+    double change = 1.0, sharp = 1.0;
+    int loop = 0, loopbeta = 0;
+    while (loop < o.n_loop && change > o.min_change && sharp > o.max_sharpness) {   // :116
+        ++loopbeta;
+        ++loop;
+        double vol = 0.0;
+        TCK(cudaMemcpyAsync(&vol, c.t_st + T_VOL, sizeof(double), cudaMemcpyDeviceToHost, s));
+        TCK(cudaEventRecord(ev[0], s));
+        if ((rc = sgld_assemble(ctx))) return rc;                                   // :123
+        TCK(cudaEventRecord(ev[1], s));
+        if ((rc = solve_on_device(ctx, &so, &si))) return rc;                       // :126
+        TCK(cudaEventRecord(ev[2], s));
+        launch_unit_compliance(l0, c.d_x, c.E, c.t_ce, c.d_part, &nbc, s);         // :128
+        launch_finalize_sum(c.d_part, nbc, c.t_st + T_C, s);                        // :133-134
+        // sensitivity of the normalised compliance through the projection (:136, :151-153)
+        launch_heaviside(l0, c.t_tmp, beta, o.eta, nullptr, c.t_dvs, nb, s);
+        launch_local_sens(l0, c.t_xp, c.t_ce, c.t_dvs, c.t_hs, penalty, o.E0, o.Emin, 1.0 / c_solid, c.t_dcs, nb, s);
+        launch_density_filter(l0, c.t_dcs, r, c.t_dc, s);
+        TCK(cudaEventRecord(ev[3], s));
+        // local volume: x_hat = PDE(xPhys), its p-norm and gradient (:142-146, :162-169)
+        int its_pde = 0;
+        if ((rc = pde_filter_dev(ctx, o.rhat, c.t_xp, c.t_q, pde_tol, pde_maxit, &its_pde))) return rc;
+        launch_pnorm(l0, c.t_q, o.pnorm, o.alpha, c.d_part, c.t_st + 12, N, c.t_dv, nb, s);
+        if ((rc = pde_filter_dev(ctx, o.rhat, c.t_dv, c.t_q, pde_tol, pde_maxit, &its_pde))) return rc;
+        launch_mul_div(l0, c.t_q, c.t_dvs, c.t_hs, c.t_dcs, nb, s);
+        launch_density_filter(l0, c.t_dcs, r, c.t_dv, s);
+        double S = 0.0;
+        TCK(cudaMemcpyAsync(&S, c.t_st + 12, sizeof(double), cudaMemcpyDeviceToHost, s));
+        TCK(cudaStreamSynchronize(s));
+        const double fval = pow(S / N, 1.0 / o.pnorm) - 1.0;                        // :179
+        // MMA (:180-192)
+        launch_mma_gather(d_var, nvar, c.t_x, c.t_dc, c.t_dv, o.move, 1.0, xv, xmin, xmax, df0, dg, s);
+        if ((rc = mma_solve_device(ctx, nvar, xv, xmin, xmax, df0, dg, fval, xo, p1, p2, sums, nullptr))) return rc;
+        if (!c.h_passive.empty()) launch_set_passive_x(l0, c.t_x, nb, s);
+        launch_mma_scatter(d_var, nvar, xo, xv, c.t_x, c.d_part, nbm, s);
+        launch_max_partials(c.d_part, nbm, c.t_st + T_CHANGE, s);
+        // xTilde = filter(x) / Hs, xPhys = H(xTilde), passive 1 (:197-204)
+        launch_density_filter(l0, c.t_x, r, c.t_q, s);
+        launch_mul_div(l0, c.t_q, nullptr, c.t_hs, c.t_tmp, nb, s);
+        launch_heaviside(l0, c.t_tmp, beta, o.eta, c.t_xp, nullptr, nb, s);
+        TCK(cudaEventRecord(ev[4], s));
+        launch_topo_modulus(l0, c.t_xp, o.simp_penalty, o.E0, o.Emin, c.E, c.d_part, c.d_part2, nb, s);   // :121, :205
+        launch_finalize_sum(c.d_part, nb, c.t_st + T_VOL, s);
+        launch_finalize_sum(c.d_part2, nb, c.t_st + T_SHARP, s);
+        TCK(cudaGetLastError());
+        double st[16];
+        TCK(cudaMemcpyAsync(st, c.t_st, sizeof st, cudaMemcpyDeviceToHost, s));
+        TCK(cudaStreamSynchronize(s));
+        change = st[T_CHANGE];
+        sharp = st[T_SHARP] / N;
+        if (hist) {
+            sgld_topopt_iter &h = hist[loop - 1];
+            memset(&h, 0, sizeof h);
+            h.loop = loop;
+            h.cg_iterations = si.iterations;
+            h.inner_iterations = si.inner_iterations;
+            h.compliance = st[T_C];
+            h.volume = vol / N;
+            h.sharpness = sharp;
+            h.change = change;
+            h.constraint = fval;
+            h.t_assemble = elapsed(ev[0], ev[1]) * 1e-3;
+            h.t_solve = elapsed(ev[1], ev[2]) * 1e-3;
+            h.t_opt = elapsed(ev[2], ev[3]) * 1e-3;
+            h.t_filter = elapsed(ev[3], ev[4]) * 1e-3;
+        }
+        if (beta < o.beta_max && loopbeta >= o.beta_interval) {                    // :246-253
+            beta *= 2.0;
+            loopbeta = 0;
+            change = sharp = 1.0;
+        }
+        if (o.penalty_interval > 0 && loop % o.penalty_interval == 0)               // :256-261
+            penalty = std::min(penalty + o.penalty_increment, 3.0);
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (n_iter) *n_iter = loop;
+    if (xphys) {
+        launch_gather_elems(c.d_elemap, ne, c.t_xp, c.d_tmp, s);
+        TCK(cudaMemcpyAsync(xphys, c.d_tmp, sizeof(double) * ne, cudaMemcpyDeviceToHost, s));
+        TCK(cudaStreamSynchronize(s));
+    }
+    c.assembled = false;
     return SGLD_OK;
 }

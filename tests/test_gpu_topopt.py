@@ -150,3 +150,40 @@ def test_simp_loop_optimizer_and_passive(built_lib, optimizer):
         assert abs(a["change"] - b["change"]) <= 1e-5
     assert _rel(xp, xp_o) <= 1e-5
     assert np.all(xp[passive] == 1.0)
+
+
+def test_local_volume_loop_matches_oracle(built_lib):
+    """The porous-infill loop (TopOpti_LocalVolumeConstraint.m): PDE-filtered
+    local volume p-norm constraint, MMA, Heaviside projection, with the beta
+    doubling and the penalty increment both exercised (short intervals), and
+    passive elements.  Both sides solve every MGPCG and PDE filter to 1e-10, so
+    the designs follow the same path: compliance per iteration within 1e-6,
+    the constraint value within 1e-8, final xPhys within 1e-5, passive
+    xPhys exactly 1."""
+    from sgldbench_gb300 import VoxelSolver
+
+    vox = np.ones((8, 16, 8), bool)
+    m = G.build_model(vox, omega=0.6)
+    s = VoxelSolver(vox, omega=0.6)
+    s.set_fixed_dofs(m.levels[0].fixedDOFs)
+    n = m.levels[0].numElements
+    passive = np.arange(3, n, 23)
+    s.set_passive(passive)
+    kw = dict(rmin=1.5, rhat=3.0, alpha=0.6, pnorm=16.0, n_loop=5, penalty=2.8, penalty_increment=0.1,
+              penalty_interval=2, beta_interval=2, tol=1e-10, maxit=2000)
+    opt = G.LocalOptions(passive=passive, **kw)
+    xp_o, hist_o = G.topopt_local_volume(m, opt)
+    xp, hist = s.TopOpti_LocalVolumeConstraint(
+        m.F, rMin=kw["rmin"], rHat=kw["rhat"], alpha=kw["alpha"], p=kw["pnorm"], nLoop=kw["n_loop"],
+        penalty=kw["penalty"], penalty_increment=kw["penalty_increment"], penalty_interval=kw["penalty_interval"],
+        beta_interval=kw["beta_interval"], tol=kw["tol"], maxIT=kw["maxit"])
+    s.set_passive([])
+    assert len(hist) == len(hist_o)
+    assert [h["beta"] for h in hist_o][-1] > 1.0     # the continuation ran
+    for a, b in zip(hist, hist_o):
+        assert abs(a["compliance"] - b["c"]) <= 1e-6 * abs(b["c"])
+        assert abs(a["constraint"] - b["fval"]) <= 1e-8
+        assert abs(a["volume"] - b["vol"]) <= 1e-9
+        assert abs(a["change"] - b["change"]) <= 1e-5
+    assert _rel(xp, xp_o) <= 1e-5
+    assert np.all(xp[passive] == 1.0)

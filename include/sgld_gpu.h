@@ -317,17 +317,27 @@ typedef struct sgld_topopt_iter {
 int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const double *F, const double *x0, double *xphys,
                 sgld_topopt_iter *hist, int *n_iter);
 
-/* Local-volume-constrained loop (porous infill), TopOpti_LocalVolumeConstraint.m:33-269:
- * compliance normalised by the solid domain's, the p-norm of the PDE-filtered
- * (radius rhat) local volume fraction held below alpha
- * (Initialize4GradedPorosity with alphaMax_ = alphaMin_), density filter
- * (rmin) and Heaviside projection (beta, eta) of the design, one MMA update
- * per iteration (passive elements excluded and kept solid), beta doubling
- * every beta_interval iterations up to beta_max, and the sensitivity penalty
- * raised by penalty_increment every penalty_interval iterations (capped at 3).
- * Starts from x = alpha (TopOpti_CallTopOpti.m:41-45).  hist records use
- * constraint = the p-norm constraint value fval. */
-typedef struct sgld_topopt_local_opts {
+/* The projected SIMP loops with MMA, compliance normalised by the solid
+ * domain's, density filter (rmin) and Heaviside projection (beta, eta) of the
+ * design, one MMA update per iteration (passive elements excluded and kept
+ * solid), beta doubling up to beta_max, and the sensitivity penalty raised by
+ * penalty_increment every penalty_interval iterations (capped at 3):
+ *   SGLD_CONS_LOCAL:  TopOpti_LocalVolumeConstraint.m:33-269 (porous infill):
+ *       the p-norm of the PDE-filtered (radius rhat) local volume fraction is
+ *       held below alpha (Initialize4GradedPorosity with alphaMax_ = alphaMin_);
+ *       x starts at alpha (TopOpti_CallTopOpti.m:41-45); beta doubles every
+ *       beta_interval iterations;
+ *   SGLD_CONS_VOLUME: TopOpti_GlobalVolumeConstraint.m:50-228 with
+ *       optimizer_ = 'MMA': sum(xPhys) <= volfrac numElements; x starts at
+ *       volfrac (TopOpti_CallTopOpti.m:34-38); beta doubles every
+ *       beta_interval iterations or once change <= 1e-3.
+ * hist records use constraint = fval of the MMA constraint. */
+#define SGLD_CONS_LOCAL 0
+#define SGLD_CONS_VOLUME 1
+
+typedef struct sgld_topopt_projected_opts {
+    int constraint;           /* SGLD_CONS_LOCAL or SGLD_CONS_VOLUME */
+    double volfrac;           /* V_ (SGLD_CONS_VOLUME) */
     double rmin;              /* rMin_ */
     double rhat;              /* rHatMin_ (0 = 8) */
     double alpha;             /* alphaMin_ (0 = 0.5) */
@@ -346,10 +356,10 @@ typedef struct sgld_topopt_local_opts {
     double E0, Emin;          /* modulus_, modulusMin_ (0 = 1, 1e-6) */
     sgld_solve_opts solve;    /* tol_, maxIT_, precision of the MGPCG solves; tol_ and maxIT_ also
                                  drive the PDE filter's PCG (TopOpti_PDEFiltering_matrixFree.m:23) */
-} sgld_topopt_local_opts;
+} sgld_topopt_projected_opts;
 
-int sgld_topopt_local(sgld_ctx *ctx, const sgld_topopt_local_opts *opts, const double *F, double *xphys,
-                      sgld_topopt_iter *hist, int *n_iter);
+int sgld_topopt_projected(sgld_ctx *ctx, const sgld_topopt_projected_opts *opts, const double *F, double *xphys,
+                          sgld_topopt_iter *hist, int *n_iter);
 
 /* FEA_StressAnalysis.m:17-60 and FEA_ComputePerElementVonMisesStress.m:10-19:
  * nodal Cartesian stress (numNodes x 6, row-major [xx yy zz yz zx xy]), nodal

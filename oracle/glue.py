@@ -849,6 +849,9 @@ def topopt_global_volume(model: Model, opt: TopOptOptions, history=None):
 # ---------------------------------------------------------------------------
 @dataclass
 class LocalOptions:
+    constraint: str = "local"      # "local" (TopOpti_LocalVolumeConstraint.m) or "volume"
+                                   # (TopOpti_GlobalVolumeConstraint.m, optimizer_ = 'MMA')
+    volfrac: float = 0.3           # V_ ("volume")
     rmin: float = 1.5              # rMin_ (density filter)
     rhat: float = 8.0              # rHatMin_ (Data_GlobalVariables.m:62), PDE filter of the local volume
     alpha: float = 0.5             # alphaMin_ = alphaMax_ (Data_GlobalVariables.m:63; Initialize4GradedPorosity)
@@ -884,7 +887,10 @@ def heaviside_derivative(xt, beta, eta):
 
 
 def topopt_local_volume(model: Model, opt: LocalOptions, history=None):
-    """TopOpti_LocalVolumeConstraint.m:33-269 (MEX branch, PDE filter matrix-free):
+    """TopOpti_LocalVolumeConstraint.m:33-269 (MEX branch, PDE filter matrix-free)
+    or, with opt.constraint == "volume", TopOpti_GlobalVolumeConstraint.m:50-228
+    with MMA (volume constraint sum(xPhys) <= V n, x starting at V, beta also
+    doubled once change <= 1e-3):
     solid-domain compliance, then per iteration SIMP E, warm-started MGPCG,
     normalised compliance and its sensitivity, the p-norm of the PDE-filtered
     local volume against alpha and its sensitivity, density-filter chain rule
@@ -901,7 +907,8 @@ def topopt_local_volume(model: Model, opt: LocalOptions, history=None):
     act = np.nonzero(~pas)[0]                                                    # :63
     vol_max = np.full(n, opt.alpha)                                              # :290-301
     vol_max[pas] = 1.0
-    x = np.full(n, opt.alpha)                                                    # TopOpti_CallTopOpti.m:41-45
+    local = opt.constraint == "local"
+    x = np.full(n, opt.alpha if local else opt.volfrac)                          # TopOpti_CallTopOpti.m:34-45
     x[pas] = 1.0
     beta, penalty = opt.beta, opt.penalty
     xTilde = x.copy()                                                            # :69
@@ -926,14 +933,18 @@ def topopt_local_volume(model: Model, opt: LocalOptions, history=None):
         c = float(E @ ce_norm) * c_solid                                         # :133-134
         vol = float(xPhys.sum() / n)                                             # :135
         dc = -(penalty * (opt.E0 - opt.Emin) * xPhys ** (penalty - 1)) * ce_norm  # :136
-        xh, _ = pde_filter(model, xPhys, opt.rhat, opt.tol, opt.maxit)           # :142
-        s = float(np.sum(xh ** opt.pnorm / vol_max ** opt.pnorm) / n)
-        dfdx_pde = s ** (1.0 / opt.pnorm - 1.0) * (xh ** (opt.pnorm - 1) / vol_max ** opt.pnorm) / n   # :146
         dx = heaviside_derivative(xTilde, beta, opt.eta)                         # :151
         dc = K.density_filter(dc * dx / Hs, opt.rmin, emf, rx, ry, rz)           # :153
-        dfdx, _ = pde_filter(model, dfdx_pde, opt.rhat, opt.tol, opt.maxit)      # :162
-        dfdx = K.density_filter(dfdx * dx / Hs, opt.rmin, emf, rx, ry, rz)       # :169
-        fval = s ** (1.0 / opt.pnorm) - 1.0                                      # :179
+        if local:
+            xh, _ = pde_filter(model, xPhys, opt.rhat, opt.tol, opt.maxit)       # :142
+            s = float(np.sum(xh ** opt.pnorm / vol_max ** opt.pnorm) / n)
+            dfdx_pde = s ** (1.0 / opt.pnorm - 1.0) * (xh ** (opt.pnorm - 1) / vol_max ** opt.pnorm) / n   # :146
+            dfdx, _ = pde_filter(model, dfdx_pde, opt.rhat, opt.tol, opt.maxit)  # :162
+            dfdx = K.density_filter(dfdx * dx / Hs, opt.rmin, emf, rx, ry, rz)   # :169
+            fval = s ** (1.0 / opt.pnorm) - 1.0                                  # :179
+        else:   # TopOpti_GlobalVolumeConstraint.m:119, :128-129, :139-141
+            dfdx = K.density_filter(dx / Hs, opt.rmin, emf, rx, ry, rz) / (n * opt.volfrac)
+            fval = float(xPhys.sum()) / (n * opt.volfrac) - 1.0
         xval = x[act]
         xmin, xmax = np.maximum(0.0, xval - opt.move), np.minimum(1.0, xval + opt.move)   # :184-185
         xmma, _, _ = mma.mma_update(1, act.size, xval, xmin, xmax, xval, xval, dc[act], fval, dfdx[act])
@@ -946,7 +957,7 @@ def topopt_local_volume(model: Model, opt: LocalOptions, history=None):
         sharp = float(4.0 * np.sum(xPhys * (1.0 - xPhys)) / n)                   # :205
         hist.append({"loop": loop, "c": c, "vol": vol, "sharp": sharp, "change": change, "fval": fval,
                      "its": its, "beta": beta, "penalty": penalty})
-        if beta < opt.beta_max and loopbeta >= opt.beta_interval:               # :246-253
+        if beta < opt.beta_max and (loopbeta >= opt.beta_interval or (not local and change <= 1e-3)):   # :246 / Global :212
             beta, loopbeta, change, sharp = 2 * beta, 0, 1.0, 1.0
         if opt.penalty_interval > 0 and loop % opt.penalty_interval == 0:        # :256-261
             penalty = min(penalty + opt.penalty_increment, 3.0)

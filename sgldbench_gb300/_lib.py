@@ -44,8 +44,8 @@ class TopOptOpts(C.Structure):
                 ("net_lr", C.c_float)]
 
 
-class TopOptLocalOpts(C.Structure):
-    _fields_ = [("rmin", dbl), ("rhat", dbl), ("alpha", dbl), ("pnorm", dbl), ("move", dbl), ("n_loop", i32),
+class TopOptProjectedOpts(C.Structure):
+    _fields_ = [("constraint", i32), ("volfrac", dbl), ("rmin", dbl), ("rhat", dbl), ("alpha", dbl), ("pnorm", dbl), ("move", dbl), ("n_loop", i32),
                 ("min_change", dbl), ("max_sharpness", dbl), ("simp_penalty", dbl), ("penalty", dbl),
                 ("penalty_increment", dbl), ("penalty_interval", i32), ("beta", dbl), ("eta", dbl),
                 ("beta_max", dbl), ("beta_interval", i32), ("E0", dbl), ("Emin", dbl), ("solve", SolveOpts)]
@@ -109,7 +109,7 @@ SIGNATURES = {
     "sgld_kbyu_dot_noalloc": (i32, [vp, vp, vp, vp, vp]),
     "sgld_density_filter": (i32, [vp, dbl, vp, vp]),
     "sgld_topopt": (i32, [vp, vp, vp, vp, vp, vp, vp]),
-    "sgld_topopt_local": (i32, [vp, vp, vp, vp, vp, vp]),
+    "sgld_topopt_projected": (i32, [vp, vp, vp, vp, vp, vp]),
 }
 
 _lib = None

@@ -516,18 +516,23 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
     return SGLD_OK;
 }
 
-// TopOpti_LocalVolumeConstraint.m:33-269 (the porous-infill loop), every field
-// operation on the device; the host runs the MMA dual iteration and the
+// The projected loops: TopOpti_LocalVolumeConstraint.m:33-269 (porous infill)
+// and TopOpti_GlobalVolumeConstraint.m:50-228 with MMA.  Every field operation
+// runs on the device; the host runs the MMA dual iteration and the
 // continuation schedule.  Buffers (full element grid): t_x design x, t_tmp
 // xTilde, t_xp xPhys, t_hs filter weight sums, t_ce unit compliance, t_dvs
 // dx = H'(xTilde), t_dcs / t_dc sensitivity before / after the density
 // filter, t_q the PDE-filtered field, t_dv the constraint gradient.
-extern "C" int sgld_topopt_local(sgld_ctx *ctx, const sgld_topopt_local_opts *opts, const double *F,
-                                 double *xphys, sgld_topopt_iter *hist, int *n_iter) {
+extern "C" int sgld_topopt_projected(sgld_ctx *ctx, const sgld_topopt_projected_opts *opts, const double *F,
+                                     double *xphys, sgld_topopt_iter *hist, int *n_iter) {
     if (!ctx || !opts || !F) return SGLD_ERR_ARG;
     Ctx &c = ctx->c;
     if (!c.have_fixed) return tfail(ctx, SGLD_ERR_STATE, "fixed DOFs not set (sgld_set_fixed_dofs)");
-    sgld_topopt_local_opts o = *opts;
+    sgld_topopt_projected_opts o = *opts;
+    const bool local = o.constraint == SGLD_CONS_LOCAL;
+    if (!local && o.constraint != SGLD_CONS_VOLUME)
+        return tfail(ctx, SGLD_ERR_ARG, "constraint must be SGLD_CONS_LOCAL or SGLD_CONS_VOLUME");
+    if (!local && !(o.volfrac > 0.0 && o.volfrac <= 1.0)) return tfail(ctx, SGLD_ERR_ARG, "volfrac in (0, 1]");
     if (o.rhat == 0) o.rhat = 8.0;
     if (o.alpha == 0) o.alpha = 0.5;
     if (o.pnorm == 0) o.pnorm = 16.0;
@@ -585,8 +590,8 @@ extern "C" int sgld_topopt_local(sgld_ctx *ctx, const sgld_topopt_local_opts *op
     TCK(cudaMemsetAsync(c.d_x, 0, sizeof(double) * nv, s));
     TCK(cudaMemcpyAsync(c.d_tmp, F, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, s));
     launch_scatter_nodes(c.d_nodemap, nn, c.d_tmp, c.d_b, s);
-    // x = alpha (passive 1), xTilde = x, xPhys = H(xTilde)  (TopOpti_CallTopOpti.m:41-45, :68-70)
-    launch_fill_active(l0, c.t_x, o.alpha, nb, s);
+    // x = alpha or volfrac (passive 1), xTilde = x, xPhys = H(xTilde)  (TopOpti_CallTopOpti.m:34-45)
+    launch_fill_active(l0, c.t_x, local ? o.alpha : o.volfrac, nb, s);
     if (!c.h_passive.empty()) launch_set_passive_x(l0, c.t_x, nb, s);
     TCK(cudaMemcpyAsync(c.t_tmp, c.t_x, sizeof(double) * l0.nel, cudaMemcpyDeviceToDevice, s));
     double beta = o.beta, penalty = o.penalty;
@@ -632,19 +637,29 @@ extern "C" int sgld_topopt_local(sgld_ctx *ctx, const sgld_topopt_local_opts *op
         launch_local_sens(l0, c.t_xp, c.t_ce, c.t_dvs, c.t_hs, penalty, o.E0, o.Emin, 1.0 / c_solid, c.t_dcs, nb, s);
         launch_density_filter(l0, c.t_dcs, r, c.t_dc, s);
         TCK(cudaEventRecord(ev[3], s));
-        // local volume: x_hat = PDE(xPhys), its p-norm and gradient (:142-146, :162-169)
-        int its_pde = 0;
-        if ((rc = pde_filter_dev(ctx, o.rhat, c.t_xp, c.t_q, pde_tol, pde_maxit, &its_pde))) return rc;
-        launch_pnorm(l0, c.t_q, o.pnorm, o.alpha, c.d_part, c.t_st + 12, N, c.t_dv, nb, s);
-        if ((rc = pde_filter_dev(ctx, o.rhat, c.t_dv, c.t_q, pde_tol, pde_maxit, &its_pde))) return rc;
-        launch_mul_div(l0, c.t_q, c.t_dvs, c.t_hs, c.t_dcs, nb, s);
-        launch_density_filter(l0, c.t_dcs, r, c.t_dv, s);
-        double S = 0.0;
-        TCK(cudaMemcpyAsync(&S, c.t_st + 12, sizeof(double), cudaMemcpyDeviceToHost, s));
-        TCK(cudaStreamSynchronize(s));
-        const double fval = pow(S / N, 1.0 / o.pnorm) - 1.0;                        // :179
-        // MMA (:180-192)
-        launch_mma_gather(d_var, nvar, c.t_x, c.t_dc, c.t_dv, o.move, 1.0, xv, xmin, xmax, df0, dg, s);
+        double fval = 0.0, dg_scale = 1.0;
+        if (local) {
+            // local volume: x_hat = PDE(xPhys), its p-norm and gradient (Local...m:142-146, :162-169)
+            int its_pde = 0;
+            if ((rc = pde_filter_dev(ctx, o.rhat, c.t_xp, c.t_q, pde_tol, pde_maxit, &its_pde))) return rc;
+            launch_pnorm(l0, c.t_q, o.pnorm, o.alpha, c.d_part, c.t_st + 12, N, c.t_dv, nb, s);
+            if ((rc = pde_filter_dev(ctx, o.rhat, c.t_dv, c.t_q, pde_tol, pde_maxit, &its_pde))) return rc;
+            launch_mul_div(l0, c.t_q, c.t_dvs, c.t_hs, c.t_dcs, nb, s);
+            launch_density_filter(l0, c.t_dcs, r, c.t_dv, s);
+            double S = 0.0;
+            TCK(cudaMemcpyAsync(&S, c.t_st + 12, sizeof(double), cudaMemcpyDeviceToHost, s));
+            TCK(cudaStreamSynchronize(s));
+            fval = pow(S / N, 1.0 / o.pnorm) - 1.0;                                 // Local...m:179
+        } else {
+            // volume: dv = filter(dx ./ Hs), dfdx = dv / (N V), fval = sum(xPhys) / (N V) - 1
+            // (Global...m:119, :128-129, :139-141)
+            launch_mul_div(l0, c.t_dvs, nullptr, c.t_hs, c.t_dcs, nb, s);
+            launch_density_filter(l0, c.t_dcs, r, c.t_dv, s);
+            dg_scale = 1.0 / (N * o.volfrac);
+            fval = vol / (N * o.volfrac) - 1.0;
+        }
+        // MMA (Local...m:180-192, Global...m:136-150)
+        launch_mma_gather(d_var, nvar, c.t_x, c.t_dc, c.t_dv, o.move, dg_scale, xv, xmin, xmax, df0, dg, s);
         if ((rc = mma_solve_device(ctx, nvar, xv, xmin, xmax, df0, dg, fval, xo, p1, p2, sums, nullptr))) return rc;
         if (!c.h_passive.empty()) launch_set_passive_x(l0, c.t_x, nb, s);
         launch_mma_scatter(d_var, nvar, xo, xv, c.t_x, c.d_part, nbm, s);
@@ -679,7 +694,7 @@ extern "C" int sgld_topopt_local(sgld_ctx *ctx, const sgld_topopt_local_opts *op
             h.t_opt = elapsed(ev[2], ev[3]) * 1e-3;
             h.t_filter = elapsed(ev[3], ev[4]) * 1e-3;
         }
-        if (beta < o.beta_max && loopbeta >= o.beta_interval) {                    // :246-253
+        if (beta < o.beta_max && (loopbeta >= o.beta_interval || (!local && change <= 1e-3))) {   // Local :246, Global :212
             beta *= 2.0;
             loopbeta = 0;
             change = sharp = 1.0;

@@ -418,10 +418,32 @@ class VoxelSolver:
         the PDE-filtered local volume <= alpha, MMA, Heaviside projection with
         beta continuation).  Passive elements (``set_passive``) stay solid.
         Returns (xPhys, history list); history ``constraint`` is fval."""
+        return self._projected(0, 0.0, F, rMin, rHat, alpha, p, nLoop, move, minChange, maxSharpness,
+                               simp_penalty, penalty, penalty_increment, penalty_interval, beta, eta, beta_max,
+                               beta_interval, E0, Emin, tol, maxIT, precision)
+
+    def TopOpti_GlobalVolumeConstraintProjected(self, F, volfrac: float = 0.3, rMin: float = 1.5,
+                                                nLoop: int = 300, move: float = 0.1, minChange: float = 1e-4,
+                                                maxSharpness: float = 0.05, simp_penalty: float = 3.0,
+                                                penalty: float = 3.0, penalty_increment: float = 0.2,
+                                                penalty_interval: int = 30, beta: float = 1.0, eta: float = 0.5,
+                                                beta_max: float = 128.0, beta_interval: int = 40, E0: float = 1.0,
+                                                Emin: float = 1e-6, tol: float = 1e-6, maxIT: int = 500,
+                                                precision: str = "fp64"):
+        """TopOpti_GlobalVolumeConstraint.m (the full loop: Heaviside projection with
+        beta/penalty continuation, solid-normalised compliance) with MMA, on the
+        device.  Returns (xPhys, history list)."""
+        return self._projected(1, volfrac, F, rMin, 8.0, 0.5, 16.0, nLoop, move, minChange, maxSharpness,
+                               simp_penalty, penalty, penalty_increment, penalty_interval, beta, eta, beta_max,
+                               beta_interval, E0, Emin, tol, maxIT, precision)
+
+    def _projected(self, constraint, volfrac, F, rMin, rHat, alpha, p, nLoop, move, minChange, maxSharpness,
+                   simp_penalty, penalty, penalty_increment, penalty_interval, beta, eta, beta_max, beta_interval,
+                   E0, Emin, tol, maxIT, precision):
         Fv = self._vec(F, self.numDOFs)
         so = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=1, precision=_precision(precision), inner_its=0,
                          history=None, profile=0, inner_tol=0.0)
-        o = L.TopOptLocalOpts(rmin=rMin, rhat=rHat, alpha=alpha, pnorm=p, move=move, n_loop=nLoop,
+        o = L.TopOptProjectedOpts(constraint=constraint, volfrac=volfrac, rmin=rMin, rhat=rHat, alpha=alpha, pnorm=p, move=move, n_loop=nLoop,
                               min_change=minChange, max_sharpness=maxSharpness, simp_penalty=simp_penalty,
                               penalty=penalty, penalty_increment=penalty_increment,
                               penalty_interval=penalty_interval, beta=beta, eta=eta, beta_max=beta_max,
@@ -429,7 +451,7 @@ class VoxelSolver:
         xp = np.zeros(self.numElements)
         hist = (L.TopOptIter * nLoop)()
         nit = C.c_int()
-        self._check(self.lib.sgld_topopt_local(self.ctx, C.byref(o), _p(Fv), _p(xp), hist, C.byref(nit)))
+        self._check(self.lib.sgld_topopt_projected(self.ctx, C.byref(o), _p(Fv), _p(xp), hist, C.byref(nit)))
         return xp, [{k: getattr(hist[i], k) for k, _ in L.TopOptIter._fields_} for i in range(nit.value)]
 
     def TopOpti_GlobalVolumeConstraint(self, F, volfrac: float = 0.3, rMin: float = 1.5, nLoop: int = 60,

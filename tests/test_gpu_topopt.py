@@ -187,3 +187,29 @@ def test_local_volume_loop_matches_oracle(built_lib):
         assert abs(a["change"] - b["change"]) <= 1e-5
     assert _rel(xp, xp_o) <= 1e-5
     assert np.all(xp[passive] == 1.0)
+
+
+def test_projected_volume_loop_matches_oracle(built_lib):
+    """TopOpti_GlobalVolumeConstraint.m's full loop with MMA (Heaviside projection,
+    beta and penalty continuation, solid-normalised compliance) against the
+    oracle, same tolerances as the local-volume loop."""
+    from sgldbench_gb300 import VoxelSolver
+
+    vox = np.ones((8, 16, 8), bool)
+    m = G.build_model(vox, omega=0.6)
+    s = VoxelSolver(vox, omega=0.6)
+    s.set_fixed_dofs(m.levels[0].fixedDOFs)
+    kw = dict(volfrac=0.4, rmin=1.5, n_loop=5, penalty=2.8, penalty_increment=0.1, penalty_interval=2,
+              beta_interval=3, tol=1e-10, maxit=2000)
+    xp_o, hist_o = G.topopt_local_volume(m, G.LocalOptions(constraint="volume", **kw))
+    xp, hist = s.TopOpti_GlobalVolumeConstraintProjected(
+        m.F, volfrac=kw["volfrac"], rMin=kw["rmin"], nLoop=kw["n_loop"], penalty=kw["penalty"],
+        penalty_increment=kw["penalty_increment"], penalty_interval=kw["penalty_interval"],
+        beta_interval=kw["beta_interval"], tol=kw["tol"], maxIT=kw["maxit"])
+    assert len(hist) == len(hist_o)
+    assert [h["beta"] for h in hist_o][-1] > 1.0
+    for a, b in zip(hist, hist_o):
+        assert abs(a["compliance"] - b["c"]) <= 1e-6 * abs(b["c"])
+        assert abs(a["constraint"] - b["fval"]) <= 1e-8
+        assert abs(a["change"] - b["change"]) <= 1e-5
+    assert _rel(xp, xp_o) <= 1e-5

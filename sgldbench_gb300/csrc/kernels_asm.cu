@@ -536,11 +536,11 @@ __global__ void __launch_bounds__(TI_THREADS) k_trinv_tiles(const float2 *__rest
             const int ca = c0 + gp, cb = ca + 1;
             if (ca < n && i >= ca) {
                 M[(int64_t)i + (int64_t)n * ca] = df_to(x0);
-                M32[(int64_t)i + (int64_t)n * ca] = x0.hi;
+                if (M32) M32[(int64_t)i + (int64_t)n * ca] = x0.hi;
             }
             if (cb < n && i >= cb) {
                 M[(int64_t)i + (int64_t)n * cb] = df_to(x1);
-                M32[(int64_t)i + (int64_t)n * cb] = x1.hi;
+                if (M32) M32[(int64_t)i + (int64_t)n * cb] = x1.hi;
             }
         }
         // the transpose into the upper triangle (M^T, column-major), staged
@@ -555,7 +555,7 @@ __global__ void __launch_bounds__(TI_THREADS) k_trinv_tiles(const float2 *__rest
             if (ii < n && cc < n && ii > cc) {
                 const float2 v = rhs[rr * TI_G + g];
                 M[(int64_t)cc + (int64_t)n * ii] = (double)v.x + (double)v.y;
-                M32[(int64_t)cc + (int64_t)n * ii] = v.x;
+                if (M32) M32[(int64_t)cc + (int64_t)n * ii] = v.x;
             }
         }
         __syncthreads();
@@ -563,6 +563,82 @@ __global__ void __launch_bounds__(TI_THREADS) k_trinv_tiles(const float2 *__rest
 }
 
 size_t trinv_smem_bytes(int R) { return sizeof(float2) * ((size_t)R * TI_G + 32 * (TI_KC + 1) + 32 * TI_G); }
+
+// The same column sweep in FP32 (the hi words of the double-float band and
+// block inverses, FP32 FMA accumulation), writing only the FP32 copy M32 that
+// the FP32 V-cycle of the mixed-precision solves applies.  Its rounding error
+// only perturbs that preconditioner: the coarse apply M32' (M32 r) stays
+// symmetric positive semi-definite for any M32, and the outer solve still
+// converges on the FP64 residual.
+__global__ void __launch_bounds__(TI_THREADS) k_trinv_tiles32(const float2 *__restrict__ LB,
+                                                              const float2 *__restrict__ D, int n, int b, int R,
+                                                              float *__restrict__ M32) {
+    extern __shared__ float tsm32[];
+    float *ring = tsm32;                      // [R][TI_G]
+    float *Lt = ring + (int64_t)R * TI_G;     // [32][TI_KC + 1]
+    float *rhs = Lt + 32 * (TI_KC + 1);       // [32][TI_G]
+    const int t = threadIdx.x, r = t & 31, gp = (t >> 5) * 2;
+    const int c0 = blockIdx.x * TI_G;
+    for (int idx = t; idx < R * TI_G; idx += TI_THREADS) ring[idx] = 0.f;
+    __syncthreads();
+    for (int i0 = c0 & ~31; i0 < n; i0 += 32) {
+        float a0 = 0.f, a1 = 0.f;
+        const int kbeg = max(0, i0 - b);
+        for (int kc = kbeg; kc < i0; kc += TI_KC) {
+            const int kn = min(TI_KC, i0 - kc);
+            for (int idx = t; idx < 32 * TI_KC; idx += TI_THREADS) {
+                const int rr = idx & 31, kk = idx >> 5, i = i0 + rr, k = kc + kk;
+                Lt[rr * (TI_KC + 1) + kk] = (kk < kn && i < n && i - k <= b) ? band_at(LB, b, i, k).x : 0.f;
+            }
+            __syncthreads();
+#pragma unroll 8
+            for (int kk = 0; kk < kn; ++kk) {
+                const float l = Lt[r * (TI_KC + 1) + kk];
+                const float2 m = *reinterpret_cast<const float2 *>(ring + (int64_t)((kc + kk) & (R - 1)) * TI_G + gp);
+                a0 = fmaf(l, m.x, a0);
+                a1 = fmaf(l, m.y, a1);
+            }
+            __syncthreads();
+        }
+        const int i = i0 + r;
+        {
+            float e0 = -a0, e1 = -a1;
+            if (i == c0 + gp) e0 += 1.f;
+            if (i == c0 + gp + 1) e1 += 1.f;
+            rhs[r * TI_G + gp] = e0;
+            rhs[r * TI_G + gp + 1] = e1;
+        }
+        __syncthreads();
+        float x0 = 0.f, x1 = 0.f;
+        const float2 *dblk = D + (int64_t)(i0 >> 5) * 1024 + r;
+#pragma unroll 8
+        for (int q = 0; q < 32; ++q) {
+            const float d = q <= r ? dblk[q * 32].x : 0.f;
+            x0 = fmaf(d, rhs[q * TI_G + gp], x0);
+            x1 = fmaf(d, rhs[q * TI_G + gp + 1], x1);
+        }
+        float *slot = ring + (int64_t)(i & (R - 1)) * TI_G + gp;
+        slot[0] = x0;
+        slot[1] = x1;
+        if (i < n) {
+            const int ca = c0 + gp, cb = ca + 1;
+            if (ca < n && i >= ca) M32[(int64_t)i + (int64_t)n * ca] = x0;
+            if (cb < n && i >= cb) M32[(int64_t)i + (int64_t)n * cb] = x1;
+        }
+        __syncthreads();
+        rhs[r * TI_G + gp] = x0;
+        rhs[r * TI_G + gp + 1] = x1;
+        __syncthreads();
+        for (int idx = t; idx < 32 * TI_G; idx += TI_THREADS) {
+            const int g = idx % TI_G, rr = idx / TI_G;
+            const int cc = c0 + g, ii = i0 + rr;
+            if (ii < n && cc < n && ii > cc) M32[(int64_t)cc + (int64_t)n * ii] = rhs[rr * TI_G + g];
+        }
+        __syncthreads();
+    }
+}
+
+size_t trinv32_smem_bytes(int R) { return sizeof(float) * ((size_t)R * TI_G + 32 * (TI_KC + 1) + 32 * TI_G); }
 
 // Enqueues the whole factorization (band Cholesky, L^-1, FP32 copy); no host
 // synchronisation, so the sequence is captured once into a CUDA graph.
@@ -594,11 +670,27 @@ static void factor_enqueue(Ctx &c, int *d_info) {
     k_band_cols<<<(unsigned)(((int64_t)n * (b + 1) + 255) / 256), 256, 0, c.stream>>>(A, n, b, LB, rd);
     ++g_launches;
     k_block_inverse<<<nblk, 32, 0, c.stream>>>(LB, rd, n, b, D);
-    cudaMemsetAsync(c.d_Ainv, 0, sizeof(double) * (size_t)n * n, c.stream);
     cudaMemsetAsync(c.d_Ainv32, 0, sizeof(float) * (size_t)n * n, c.stream);
     ++g_launches;
+    k_trinv_tiles32<<<(n + TI_G - 1) / TI_G, TI_THREADS, trinv32_smem_bytes(c.trinv_ring), c.stream>>>(
+        LB, D, n, b, c.trinv_ring, c.d_Ainv32);
+}
+
+// The FP64 copy M of L^-1 (double-float sweep), for the FP64 V-cycle; made on
+// first use after each factorization.
+int ensure_coarse_m64(Ctx &c) {
+    if (c.m64_valid || c.ncf == 0) return 0;
+    const int n = c.ncf, b = c.cband;
+    const int nblk = (n + NB - 1) / NB;
+    const float2 *LB = reinterpret_cast<const float2 *>(c.d_LB), *D = LB + (int64_t)n * (b + 1) + n;
+    (void)nblk;
+    if (cudaMemsetAsync(c.d_Ainv, 0, sizeof(double) * (size_t)n * n, c.stream) != cudaSuccess) return -1;
+    ++g_launches;
     k_trinv_tiles<<<(n + TI_G - 1) / TI_G, TI_THREADS, c.trinv_smem, c.stream>>>(LB, D, n, b, c.trinv_ring,
-                                                                                 c.d_Ainv, c.d_Ainv32);
+                                                                                 c.d_Ainv, nullptr);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+    c.m64_valid = true;
+    return 0;
 }
 
 // Cholesky of the dense coarsest matrix in d_Ac (lower, in place) and
@@ -614,6 +706,8 @@ int coarse_factor_invert(Ctx &c) {
         const size_t smem = trinv_smem_bytes(R);
         if (smem > 220 * 1024) return -2;
         cudaFuncSetAttribute(k_trinv_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_trinv_tiles32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)trinv32_smem_bytes(R));
         c.trinv_ring = R;
         c.trinv_smem = smem;
         const int64_t before = g_launches;
@@ -631,6 +725,7 @@ int coarse_factor_invert(Ctx &c) {
     }
     if (cudaGraphLaunch(c.factor_graph, c.stream) != cudaSuccess) return -1;
     g_launches += c.factor_graph_launches;
+    c.m64_valid = false;
     int info = 0;
     cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
     cudaStreamSynchronize(c.stream);

@@ -282,6 +282,7 @@ bool skip_level2_ks(const Ctx &c) { return c.L > 2 && c.lv[1].span == 2; }
 int vcycle_dev(sgld_ctx *ctx, const double *r, double *z, double *partial, int *nb) {
     Ctx &c = ctx->c;
     const int L = c.L;
+    if (ensure_coarse_m64(c)) return fail(ctx, SGLD_ERR_CUDA, "FP64 coarse inverse: CUDA error");
     const double *rf = r;
     for (int l = 1; l < L; ++l) {
         launch_restrict<double>(c.lv[l - 1], c.lv[l], rf, c.lv[l].r, c.stream);

@@ -78,6 +78,7 @@ struct Ctx {
     int64_t factor_graph_launches = 0;
     int trinv_ring = 0;
     size_t trinv_smem = 0;
+    bool m64_valid = false;         // d_Ainv holds L^-1 of the current factorization (made on first use)
     double *d_cpart = nullptr;      // [CSPLIT*ncf] GEMV partials
     // templates for the level-2 Galerkin assembly
     double *d_H = nullptr;          // [2 (8 + 64) * 576] templates for span 2, span 4, then both as
@@ -256,7 +257,8 @@ void launch_asm_templates(const Level &coarse, int S, const double *E, const dou
 void launch_diag_templates(const Level &coarse, const double *E, const double *H2, double *diag, cudaStream_t s);
 void launch_asm_coarse(const Level &coarse, const Level &fine, double *Ks, cudaStream_t s);
 void launch_coarse_dense(const Level &lc, int ncf, const int *cfree_pos_of_dof, double *A, cudaStream_t s);
-int coarse_factor_invert(Ctx &c);  // returns 0 or error
+int coarse_factor_invert(Ctx &c);
+int ensure_coarse_m64(Ctx &c);   // FP64 L^-1 for the FP64 V-cycle (0 or -1 on a CUDA error)  // returns 0 or error
 void launch_coarse_apply_f64(const Ctx &c, const double *rc, double *xc, cudaStream_t s);
 void launch_coarse_apply_f32(const Ctx &c, const float *rc, float *xc, cudaStream_t s);
 

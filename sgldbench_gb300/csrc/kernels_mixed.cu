@@ -33,16 +33,28 @@ __device__ double msum_partials(const double *__restrict__ part, int nb) {
 }
 
 // inner scalars (FP64 storage): rho = z.s of the last iteration, alpha, beta,
-// r0 = s.s at entry, the iteration count of this inner solve and the total
-// over the outer solve (reset by the host at the start of each solve)
-enum { IS_RHO = 0, IS_ALPHA = 1, IS_BETA = 2, IS_R0 = 3, IS_IT = 4 };
+// r0 = s.s at entry, the iteration count of this inner solve, the current
+// iteration cap, whether the last inner solve stopped at that cap short of
+// its tolerance, and (slot 8) the total over the outer solve (reset by the
+// host at the start of each solve)
+enum { IS_RHO = 0, IS_ALPHA = 1, IS_BETA = 2, IS_R0 = 3, IS_IT = 4, IS_KCAP = 5, IS_CAPHIT = 6, IS_TOT = 8 };
 
-// op 0: r0 = sum, rho = 0, it = 0; op 1: alpha = rho / sum;
-// op 2: beta = sum / rho (0 on the first iteration, rho = 0), rho = sum
-__global__ void k_icg_scalar(int op, double *__restrict__ sc, const double *__restrict__ part, int nb) {
+// op 0 (entry of an inner solve): r0 = sum, rho = 0, it = 0, and the cap:
+// kbase at the first inner solve of an outer solve, doubled (up to klimit)
+// after an inner solve that hit its cap without reaching its tolerance;
+// op 1: alpha = rho / sum;  op 2: beta = sum / rho (0 on the first iteration,
+// rho = 0), rho = sum
+__global__ void k_icg_scalar(int op, double *__restrict__ sc, const double *__restrict__ part, int nb, int kbase,
+                             int klimit) {
     const double s = msum_partials(part, nb);
     if (threadIdx.x != 0) return;
     if (op == 0) {
+        if (sc[IS_TOT] == 0.0) {
+            sc[IS_KCAP] = (double)kbase;
+        } else if (sc[IS_CAPHIT] != 0.0) {
+            sc[IS_KCAP] = fmin(2.0 * sc[IS_KCAP], (double)klimit);
+        }
+        sc[IS_CAPHIT] = 0.0;
         sc[IS_R0] = s;
         sc[IS_RHO] = 0.0;
         sc[IS_IT] = 0.0;
@@ -69,11 +81,14 @@ __global__ void k_icg_cond(cudaGraphConditionalHandle h, double *__restrict__ sc
     const double it = sc[IS_IT] + 1.0;
     sc[IS_IT] = it;
     *total += 1.0;
-    bool more = it < (double)kmax;
-    if (more && eta_min > 0.0) {
+    const double cap = eta_min > 0.0 ? sc[IS_KCAP] : (double)kmax;
+    bool more = it < cap;
+    if (eta_min > 0.0) {
         const double relres = outer[3], tol = outer[15];
         const double eta = (relres > 0.0) ? fmax(eta_min, 0.5 * tol / relres) : eta_min;
-        more = ss > eta * eta * sc[IS_R0];
+        const bool above = ss > eta * eta * sc[IS_R0];
+        if (!more && above) sc[IS_CAPHIT] = 1.0;
+        more = more && above;
     }
     cudaGraphSetConditional(h, more ? 1u : 0u);
 }
@@ -117,11 +132,14 @@ __global__ void k_icg_cond_flag(int *flag, double *__restrict__ sc, const double
     const double it = sc[IS_IT] + 1.0;
     sc[IS_IT] = it;
     *total += 1.0;
-    bool more = it < (double)kmax;
-    if (more && eta_min > 0.0) {
+    const double cap = eta_min > 0.0 ? sc[IS_KCAP] : (double)kmax;
+    bool more = it < cap;
+    if (eta_min > 0.0) {
         const double relres = outer[3], tol = outer[15];
         const double eta = (relres > 0.0) ? fmax(eta_min, 0.5 * tol / relres) : eta_min;
-        more = ss > eta * eta * sc[IS_R0];
+        const bool above = ss > eta * eta * sc[IS_R0];
+        if (!more && above) sc[IS_CAPHIT] = 1.0;
+        more = more && above;
     }
     *flag = more ? 1 : 0;
 }
@@ -168,9 +186,9 @@ int launch_icg_init(const float *r, float *s, float *e, float *d, int64_t n, dou
     return nb;
 }
 
-void launch_icg_scalar(int op, double *sc, const double *part, int nb, cudaStream_t s) {
+void launch_icg_scalar(int op, double *sc, const double *part, int nb, cudaStream_t s, int kbase, int klimit) {
     ++g_launches;
-    k_icg_scalar<<<1, MB, 0, s>>>(op, sc, part, nb);
+    k_icg_scalar<<<1, MB, 0, s>>>(op, sc, part, nb, kbase, klimit);
 }
 
 // The FP32 vectors are separate allocations (256-byte aligned), so the

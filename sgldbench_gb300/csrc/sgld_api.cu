@@ -363,6 +363,14 @@ static cudaGraph_t capturing_graph(cudaStream_t s) {
 // Captures one inner solve: entry kernels on s (capturing), then a while node
 // whose body (one CG iteration) is captured on stream sb.  *entry / *body
 // receive the kernel launches of each part.
+// Inner iteration caps: an inner solve with a tolerance (eta > 0) starts the
+// outer solve with at most kmax iterations; after one that stops at its cap
+// short of its tolerance the cap doubles, up to 16 kmax.  On a badly
+// conditioned system the restarts of a short inner solve would otherwise
+// multiply the outer iterations (and the inner ones with them).  A fixed
+// iteration count (eta <= 0) keeps kmax.
+static int inner_cap_limit(int kmax, double eta) { return eta > 0.0 ? 16 * kmax : kmax; }
+
 static int capture_inner(sgld_ctx *ctx, cudaStream_t s, cudaStream_t sb, int kmax, double eta, int64_t *entry,
                          int64_t *body_n) {
     Ctx &c = ctx->c;
@@ -372,7 +380,7 @@ static int capture_inner(sgld_ctx *ctx, cudaStream_t s, cudaStream_t sb, int kma
     CK(cudaGraphConditionalHandleCreate(&h, capturing_graph(s), 1, cudaGraphCondAssignDefault));
     int64_t before = g_launches;
     const int nbi = launch_icg_init(c.d_r32, c.d_s32, c.d_e32, c.d_d32, nv, c.d_part2, s);
-    launch_icg_scalar(0, c.d_isc, c.d_part2, nbi, s);
+    launch_icg_scalar(0, c.d_isc, c.d_part2, nbi, s, kmax, inner_cap_limit(kmax, eta));
     launch_set_cond(h, 1u, s);   // re-arm: the loop may sit in another loop's body
     *entry = g_launches - before;
     cudaGraph_t body = nullptr;
@@ -382,10 +390,10 @@ static int capture_inner(sgld_ctx *ctx, cudaStream_t s, cudaStream_t sb, int kma
     CK(cudaStreamBeginCaptureToGraph(sb, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     int nb = 0;
     vcycle_dev32(ctx, c.d_s32, c.d_z32, c.d_part2, &nb, sb);
-    launch_icg_scalar(2, c.d_isc, c.d_part2, nb, sb);
+    launch_icg_scalar(2, c.d_isc, c.d_part2, nb, sb, 0, 0);
     launch_icg_dupdate(c.d_e32, c.d_d32, c.d_z32, nv, c.d_isc, sb);
     launch_kbyu_f32(l0, c.d_E32, c.d_d32, c.d_t32, c.d_part2, &nb, sb);
-    launch_icg_scalar(1, c.d_isc, c.d_part2, nb, sb);
+    launch_icg_scalar(1, c.d_isc, c.d_part2, nb, sb, 0, 0);
     nb = launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.d_part2, sb);
     launch_icg_cond(h, c.d_isc, c.d_part2, nb, kmax, eta, c.d_scal, c.d_isc + IS_TOTAL, sb);
     CK(cudaStreamEndCapture(sb, &body));
@@ -427,14 +435,15 @@ static int inner_run_host(sgld_ctx *ctx, int kmax, double eta) {
     const int64_t nv = 3 * l0.nnode;
     int *d_flag = c.d_iflag + 12;
     const int nbi = launch_icg_init(c.d_r32, c.d_s32, c.d_e32, c.d_d32, nv, c.d_part2, c.stream);
-    launch_icg_scalar(0, c.d_isc, c.d_part2, nbi, c.stream);
-    for (int it = 0; it < kmax; ++it) {
+    launch_icg_scalar(0, c.d_isc, c.d_part2, nbi, c.stream, kmax, inner_cap_limit(kmax, eta));
+    const int kl = inner_cap_limit(kmax, eta);
+    for (int it = 0; it < kl; ++it) {
         int nb = 0;
         vcycle_dev32(ctx, c.d_s32, c.d_z32, c.d_part2, &nb);
-        launch_icg_scalar(2, c.d_isc, c.d_part2, nb, c.stream);
+        launch_icg_scalar(2, c.d_isc, c.d_part2, nb, c.stream, 0, 0);
         launch_icg_dupdate(c.d_e32, c.d_d32, c.d_z32, nv, c.d_isc, c.stream);
         launch_kbyu_f32(l0, c.d_E32, c.d_d32, c.d_t32, c.d_part2, &nb, c.stream);
-        launch_icg_scalar(1, c.d_isc, c.d_part2, nb, c.stream);
+        launch_icg_scalar(1, c.d_isc, c.d_part2, nb, c.stream, 0, 0);
         nb = launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.d_part2, c.stream);
         launch_icg_cond_flag(d_flag, c.d_isc, c.d_part2, nb, kmax, eta, c.d_scal, c.d_isc + IS_TOTAL, c.stream);
         int more = 0;

@@ -156,7 +156,9 @@ void init_kbyu_df_attributes();
 void launch_kbyu_df(const Level &l0, const double *E, const double *u, double *y, double *partial_dot,
                     int *nblocks_out, cudaStream_t s);
 // mixed-precision solve (kernels_mixed.cu)
-void launch_icg_scalar(int op, double *sc, const double *part, int nb, cudaStream_t s);
+// op 0 also sets the inner iteration cap (kbase at an outer solve's first inner solve,
+// doubled up to klimit after a capped inner solve that missed its tolerance)
+void launch_icg_scalar(int op, double *sc, const double *part, int nb, cudaStream_t s, int kbase, int klimit);
 int launch_icg_update(float *e, float *s, const float *d, const float *t, int64_t n, const double *sc,
                       double *part, cudaStream_t st);
 void launch_icg_cond(cudaGraphConditionalHandle h, double *sc, const double *part, int nb, int kmax,

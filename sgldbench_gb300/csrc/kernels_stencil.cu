@@ -530,8 +530,8 @@ static int kbyu_x2_zc(int NZ) {
 }
 
 int kbyu_f32_zc(const Level &l) { return l.kx_zc > 0 ? l.kx_zc : kbyu_x2_zc(l.nz + 1); }
-// tile width in x: 16 unless the tuner chose 8
-int kbyu_f32_tx(const Level &l) { return l.kx_tx == 8 ? 8 : 16; }
+// tile width in x: 8 unless the tuner chose 16
+int kbyu_f32_tx(const Level &l) { return l.kx_tx == 16 ? 16 : 8; }
 
 static dim3 kbyu_x2_grid(const Level &l) {
     const int NZ = l.nz + 1;

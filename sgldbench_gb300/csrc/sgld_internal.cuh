@@ -31,7 +31,7 @@ struct Level {
     int nx = 0, ny = 0, nz = 0;   // elements
     int span = 1;                 // coarsening factor from the next finer level
     int kx_zc = 0;                // node layers per CTA of the FP32 K*u (0 = default rule; set by the tuner)
-    int kx_tx = 0;                // x width of the FP32 K*u tile, 8 or 16 (0 = 16; set by the tuner)
+    int kx_tx = 0;                // x width of the FP32 K*u tile, 8 or 16 (0 = 8; set by the tuner)
     int64_t nel = 0, nnode = 0;   // full-grid counts
     int64_t nel_active = 0, nnode_active = 0;
     uint8_t *eact = nullptr;      // [nel] element non-empty

@@ -176,6 +176,113 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
     } else if (!strcmp(cmd, "filter")) {
         plhs[0] = mxCreateDoubleMatrix(nel, 1, mxREAL);
         check(sgld_density_filter(g_ctx, mxGetScalar(prhs[2]), dvec(prhs[1], nel, "x"), mxGetPr(plhs[0])));
+    } else if (!strcmp(cmd, "principal")) {
+        // [ps, dir] = ('principal', U): FEA_ComputePrincipalStress.m per node (numNodes x 12),
+        // Common_ExtractDominantDirectionsFromPrincipalStressDirections.m per element (numElements x 3)
+        const size_t nn = ndof / 3;
+        std::vector<double> ps(12 * nn), dir(3 * nel);
+        check(sgld_principal_stress(g_ctx, dvec(prhs[1], ndof, "U"), ps.data(), dir.data()));
+        plhs[0] = mxCreateDoubleMatrix(nn, 12, mxREAL);
+        for (size_t i = 0; i < nn; ++i)
+            for (int k = 0; k < 12; ++k) mxGetPr(plhs[0])[i + nn * k] = ps[12 * i + k];
+        if (nlhs > 1) {
+            plhs[1] = mxCreateDoubleMatrix(nel, 3, mxREAL);
+            for (size_t i = 0; i < nel; ++i)
+                for (int k = 0; k < 3; ++k) mxGetPr(plhs[1])[i + nel * k] = dir[3 * i + k];
+        }
+    } else if (!strcmp(cmd, "pdefilter")) {
+        // [y, its] = ('pdefilter', x, rHatMin, tol, maxIT): TopOpti_PDEFiltering_matrixFree.m
+        if (nrhs < 5) mexErrMsgIdAndTxt("sgld:arg", "pdefilter needs x, rHatMin, tol, maxIT");
+        plhs[0] = mxCreateDoubleMatrix(nel, 1, mxREAL);
+        int its = 0;
+        check(sgld_pde_filter(g_ctx, mxGetScalar(prhs[2]), dvec(prhs[1], nel, "x"), mxGetPr(plhs[0]),
+                              mxGetScalar(prhs[3]), (int)mxGetScalar(prhs[4]), &its));
+        if (nlhs > 1) plhs[1] = mxCreateDoubleScalar(its);
+    } else if (!strcmp(cmd, "passive")) {
+        // ('passive', passiveElements_): 1-based element indices, as MATLAB holds them
+        const size_t np = mxGetNumberOfElements(prhs[1]);
+        const double *p = np ? mxGetPr(prhs[1]) : nullptr;
+        std::vector<int64_t> e(np);
+        for (size_t i = 0; i < np; ++i) {
+            if (!(p[i] >= 1.0 && p[i] <= (double)nel)) mexErrMsgIdAndTxt("sgld:arg", "passive element out of range");
+            e[i] = (int64_t)p[i] - 1;
+        }
+        check(sgld_set_passive(g_ctx, (int64_t)np, e.data()));
+    } else if (!strcmp(cmd, "mma")) {
+        // [xmma, xold1, xold2] = ('mma', m, n, xval, xmin, xmax, xold1, xold2, df0dx, fval, dfdx): MMA_mex.cpp
+        if (nrhs < 11) mexErrMsgIdAndTxt("sgld:arg", "mma needs m, n, xval, xmin, xmax, xold1, xold2, df0dx, fval, dfdx");
+        const int mm = (int)mxGetScalar(prhs[1]), n = (int)mxGetScalar(prhs[2]);
+        if (mm < 1 || n < 1) mexErrMsgIdAndTxt("sgld:arg", "m and n must be positive");
+        const size_t un = (size_t)n;
+        plhs[0] = mxCreateDoubleMatrix(un, 1, mxREAL);
+        mxArray *o1 = mxCreateDoubleMatrix(un, 1, mxREAL), *o2 = mxCreateDoubleMatrix(un, 1, mxREAL);
+        check(sgld_mma_update(g_ctx, mm, n, dvec(prhs[3], un, "xval"), dvec(prhs[4], un, "xmin"),
+                              dvec(prhs[5], un, "xmax"), dvec(prhs[6], un, "xold1"), dvec(prhs[7], un, "xold2"),
+                              dvec(prhs[8], un, "df0dx"), dvec(prhs[9], (size_t)mm, "fval"),
+                              dvec(prhs[10], un * mm, "dfdx"), mxGetPr(plhs[0]), mxGetPr(o1), mxGetPr(o2)));
+        if (nlhs > 1) plhs[1] = o1; else mxDestroyArray(o1);
+        if (nlhs > 2) plhs[2] = o2; else mxDestroyArray(o2);
+    } else if (!strcmp(cmd, "topopt") || !strcmp(cmd, "topopt_local")) {
+        // [xPhys, hist] = ('topopt', F, V, rMin, nLoop, tol, maxIT[, 'OC'|'MMA'])
+        //   TopOpti_GlobalVolumeConstraint_Tmp.m;
+        // [xPhys, hist] = ('topopt_local', F, alphaMin, rMin, rHatMin, p, nLoop, tol, maxIT)
+        //   TopOpti_LocalVolumeConstraint.m.
+        // hist: one row per iteration [compliance volume sharpness change constraint iterations]
+        const bool local = cmd[6] == '_';
+        if (nrhs < (local ? 9 : 7)) mexErrMsgIdAndTxt("sgld:arg", "too few arguments for %s", cmd);
+        const double *F = dvec(prhs[1], ndof, "F");
+        sgld_solve_opts so;
+        memset(&so, 0, sizeof so);
+        so.precision = SGLD_PREC_FP64;
+        int nloop = 0, nit = 0;
+        std::vector<sgld_topopt_iter> hist;
+        plhs[0] = mxCreateDoubleMatrix(nel, 1, mxREAL);
+        if (local) {
+            sgld_topopt_projected_opts o;
+            memset(&o, 0, sizeof o);
+            o.constraint = SGLD_CONS_LOCAL;
+            o.alpha = mxGetScalar(prhs[2]);
+            o.rmin = mxGetScalar(prhs[3]);
+            o.rhat = mxGetScalar(prhs[4]);
+            o.pnorm = mxGetScalar(prhs[5]);
+            nloop = o.n_loop = (int)mxGetScalar(prhs[6]);
+            so.tol = mxGetScalar(prhs[7]);
+            so.maxit = (int)mxGetScalar(prhs[8]);
+            o.penalty_increment = 0.2;    // penaltyIncrement_ (Data_GlobalVariables.m:73)
+            o.penalty_interval = 30;      // penaltyUpdateIterations_ (:74)
+            o.solve = so;
+            if (nloop < 1) mexErrMsgIdAndTxt("sgld:arg", "nLoop must be positive");
+            hist.resize((size_t)nloop);
+            check(sgld_topopt_projected(g_ctx, &o, F, mxGetPr(plhs[0]), hist.data(), &nit));
+        } else {
+            sgld_topopt_opts o;
+            memset(&o, 0, sizeof o);
+            o.volfrac = mxGetScalar(prhs[2]);
+            o.rmin = mxGetScalar(prhs[3]);
+            nloop = o.n_loop = (int)mxGetScalar(prhs[4]);
+            so.tol = mxGetScalar(prhs[5]);
+            so.maxit = (int)mxGetScalar(prhs[6]);
+            o.solve = so;
+            if (nrhs > 7) {
+                char opt[8] = {0};
+                mxGetString(prhs[7], opt, sizeof opt);
+                if (!strcmp(opt, "MMA")) o.optimizer = SGLD_OPT_MMA;
+                else if (strcmp(opt, "OC")) mexErrMsgIdAndTxt("sgld:arg", "optimizer must be 'OC' or 'MMA'");
+            }
+            if (nloop < 1) mexErrMsgIdAndTxt("sgld:arg", "nLoop must be positive");
+            hist.resize((size_t)nloop);
+            check(sgld_topopt(g_ctx, &o, F, nullptr, mxGetPr(plhs[0]), hist.data(), &nit));
+        }
+        if (nlhs > 1) {
+            plhs[1] = mxCreateDoubleMatrix((size_t)nit, 6, mxREAL);
+            double *h = mxGetPr(plhs[1]);
+            for (int i = 0; i < nit; ++i) {
+                const sgld_topopt_iter &r = hist[(size_t)i];
+                const double row[6] = {r.compliance, r.volume, r.sharpness, r.change, r.constraint,
+                                       (double)r.cg_iterations};
+                for (int k = 0; k < 6; ++k) h[i + (size_t)nit * k] = row[k];
+            }
+        }
     } else {
         mexErrMsgIdAndTxt("sgld:arg", "unknown command '%s'", cmd);
     }

@@ -80,6 +80,65 @@ def test_gateway_solve_path(gateway):
         M.call("sgld_gpu_mex", 1, "kbyu", u)
 
 
+def test_gateway_callers(gateway):
+    """The gateway's commands for the callers around the solve, driven as MATLAB
+    would: principal stresses, the PDE filter, MMA and the two SIMP loops
+    (with passive elements given as 1-based indices), against the oracle."""
+    from oracle import mma as OM
+
+    M = gateway
+    vox = np.ones((8, 16, 8), bool)
+    m = G.build_model(vox, omega=0.6)
+    _, nlev0, padded, _ = G.voxel_discretization(vox)
+    M.call("sgld_gpu_mex", 1, "create", padded, float(nlev0), 1.0, 0.3, 1.0, 0.6)
+    l1 = m.levels[0]
+    n = l1.numElements
+    rng = np.random.default_rng(3)
+    E = rng.uniform(0.3, 1.0, n)
+    G.set_modulus(m, E)
+    G.assemble_stencil(m)
+    M.call("sgld_gpu_mex", 0, "fixed", l1.fixedDOFs)
+    M.call("sgld_gpu_mex", 0, "modulus", E)
+    M.call("sgld_gpu_mex", 0, "assemble")
+    U_o, _ = G.solve(m, tol=1e-10, maxIT=2000)
+    ps, dirs = M.call("sgld_gpu_mex", 2, "principal", U_o)
+    s_o, _ = G.stress_analysis(m, U_o)
+    ps_o = G.principal_stress(s_o)
+    assert ps.shape == (l1.numNodes, 12) and dirs.shape == (n, 3)
+    lam = ps[:, [0, 4, 8]]
+    assert _rel(lam, ps_o[:, [0, 4, 8]]) <= 1e-9
+    x = rng.random(n)
+    y, its = M.call("sgld_gpu_mex", 2, "pdefilter", x, 3.0, 1e-10, 1000.0)
+    y_o, its_o = G.pde_filter(m, x, 3.0, tol=1e-10, maxIT=1000)
+    assert _rel(y.ravel(), y_o) <= 1e-9 and abs(int(np.asarray(its).ravel()[0]) - its_o) <= 1
+    nv = 50
+    xv = rng.uniform(0.2, 0.8, nv)
+    xmin, xmax = np.maximum(0, xv - 0.1), np.minimum(1, xv + 0.1)
+    df0, dg = -rng.random(nv), rng.random(nv) / nv
+    out = M.call("sgld_gpu_mex", 3, "mma", 1.0, float(nv), xv, xmin, xmax, xv, xv, df0, np.array([0.05]), dg)
+    x_o, _, _ = OM.mma_update(1, nv, xv, xmin, xmax, xv, xv, df0, 0.05, dg)
+    assert _rel(out[0].ravel(), x_o) <= 1e-10
+    # the _Tmp loop with MMA and passive elements, and the local-volume loop
+    passive = np.arange(0, n, 17)
+    M.call("sgld_gpu_mex", 0, "passive", (passive + 1).astype(float))
+    xp, hist = M.call("sgld_gpu_mex", 2, "topopt", m.F, 0.3, 1.5, 4.0, 1e-10, 2000.0, "MMA")
+    xp_o, hist_o = G.topopt_global_volume(m, G.TopOptOptions(n_loop=4, tol=1e-10, maxit=2000, Emin=1e-6,
+                                                             optimizer="MMA", passive=passive))
+    assert hist.shape == (len(hist_o), 6)
+    assert _rel(hist[:, 0], np.array([h["c"] for h in hist_o])) <= 1e-6
+    assert _rel(xp.ravel(), xp_o) <= 1e-5 and np.all(xp.ravel()[passive] == 1.0)
+    xl, hl = M.call("sgld_gpu_mex", 2, "topopt_local", m.F, 0.6, 1.5, 3.0, 16.0, 3.0, 1e-10, 2000.0)
+    xl_o, hl_o = G.topopt_local_volume(m, G.LocalOptions(rmin=1.5, rhat=3.0, alpha=0.6, n_loop=3, tol=1e-10,
+                                                         maxit=2000, passive=passive))
+    assert _rel(hl[:, 0], np.array([h["c"] for h in hl_o])) <= 1e-6
+    assert np.abs(hl[:, 4] - np.array([h["fval"] for h in hl_o])).max() <= 1e-8
+    assert _rel(xl.ravel(), xl_o) <= 1e-5
+    M.call("sgld_gpu_mex", 0, "passive", np.zeros(0))
+    with pytest.raises(mexcall.MexError):
+        M.call("sgld_gpu_mex", 0, "passive", np.array([float(n + 1)]))
+    M.call("sgld_gpu_mex", 0, "destroy")
+
+
 def test_harness_config0(built_lib):
     from sgldbench_gb300 import build as B
 

@@ -88,7 +88,17 @@ typedef struct sgld_solve_info {
     double kbyu_seconds;   /* profile: summed device time of the outer K*u launches */
     int kbyu_launches;     /* profile: number of those launches */
     double precond_seconds;/* profile: summed device time of the preconditioner applications */
+    int fallback;          /* SGLD_PREC_MIXED(_DF): 1 if the mixed solve failed (not converged,
+                              a non-finite residual, or a true residual above 100 tol) and the
+                              answer comes from the reference-form FP64 solve rerun from the
+                              same start; the other fields then describe that FP64 solve */
 } sgld_solve_info;
+
+/* Test hook (no counterpart in the reference): corrupts, on the host side of
+ * the next solve, the data of the FP32 inner operator so that a mixed solve
+ * fails and its fallback runs.  kind 1: the FP32 copy of the moduli gets a
+ * NaN (until the next sgld_assemble).  kind 0: no-op.  Faults no GPU. */
+int sgld_inject_fault(sgld_ctx *ctx, int kind);
 
 /* The CUDA stream every call of this context runs on (a cudaStream_t). */
 void *sgld_get_stream(const sgld_ctx *ctx);

@@ -34,7 +34,7 @@ class SolveOpts(C.Structure):
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", i32), ("converged", i32), ("relres", dbl), ("true_relres", dbl),
                 ("inner_iterations", i32), ("seconds", dbl), ("kbyu_seconds", dbl), ("kbyu_launches", i32),
-                ("precond_seconds", dbl)]
+                ("precond_seconds", dbl), ("fallback", i32)]
 
 
 class TopOptOpts(C.Structure):
@@ -97,6 +97,7 @@ SIGNATURES = {
     "sgld_kernel_launches": (i64, []),
     "sgld_time_op": (i32, [vp, i32, i32, vp]),
     "sgld_kbyu_tile": (i32, [vp, vp, vp]),
+    "sgld_inject_fault": (i32, [vp, i32]),
     "sgld_net_create": (i32, [i32, i32, i32, i32, i32, i32, vp, C.c_ulonglong, vp]),
     "sgld_net_destroy": (None, [vp]),
     "sgld_net_last_error": (C.c_char_p, [vp]),

@@ -6,6 +6,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
+#include <limits>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -517,11 +519,40 @@ int pcg_mixed_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info
 static int run_solve_graph(sgld_ctx *ctx, int nrhs, bool staged, const sgld_solve_opts *o, sgld_solve_info *infos);
 static int ensure_block_buffers(sgld_ctx *ctx, int nrhs);
 
+// A mixed solve that did not converge, met a non-finite residual or whose
+// true residual drifted above 100 tol is not trusted: the reference-form FP64
+// solve reruns from the same start and its answer is returned
+// (info->fallback = 1).  Plain FP64 MGPCG stays the judge.
+bool mixed_failed(const sgld_solve_info &i, double tol) {
+    return !i.converged || !std::isfinite(i.true_relres) || !std::isfinite(i.relres) || i.true_relres > 100.0 * tol;
+}
+
 int solve_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
     if (o->maxit < 1 || !(o->tol >= 0.0)) return fail(ctx, SGLD_ERR_ARG, "maxit must be >= 1 and tol >= 0");
-    if (o->precision == SGLD_PREC_MIXED || o->precision == SGLD_PREC_MIXED_DF) return pcg_mixed_dev(ctx, o, info);
-    if (o->precision != SGLD_PREC_FP64) return fail(ctx, SGLD_ERR_ARG, "unknown precision mode");
-    return pcg_dev(ctx, o, info);
+    const bool mixed = o->precision == SGLD_PREC_MIXED || o->precision == SGLD_PREC_MIXED_DF;
+    if (!mixed && o->precision != SGLD_PREC_FP64) return fail(ctx, SGLD_ERR_ARG, "unknown precision mode");
+    sgld_solve_info local;
+    if (!info) info = &local;
+    memset(info, 0, sizeof *info);
+    if (!mixed) return pcg_dev(ctx, o, info);
+    Ctx &c = ctx->c;
+    const size_t nv = 3 * (size_t)c.lv[0].nnode;
+    if (o->use_x0) {
+        if (!c.d_x0) CK(dalloc(&c.d_x0, nv));
+        CK(cudaMemcpyAsync(c.d_x0, c.d_x, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c.stream));
+    }
+    int rc = pcg_mixed_dev(ctx, o, info);
+    if (rc) return rc;
+    if (!mixed_failed(*info, o->tol)) return SGLD_OK;
+    if (o->use_x0)
+        CK(cudaMemcpyAsync(c.d_x, c.d_x0, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c.stream));
+    else
+        CK(cudaMemsetAsync(c.d_x, 0, sizeof(double) * nv, c.stream));
+    sgld_solve_opts o64 = *o;
+    o64.precision = SGLD_PREC_FP64;
+    if ((rc = pcg_dev(ctx, &o64, info))) return rc;
+    info->fallback = 1;
+    return SGLD_OK;
 }
 
 }  // namespace
@@ -718,7 +749,7 @@ void sgld_destroy(sgld_ctx *ctx) {
         if (a) cudaStreamDestroy(a);
     if (c.solve_graph) cudaGraphExecDestroy(c.solve_graph);
     learned_free(c.lws);
-    for (void *p : {(void *)c.d_blk, (void *)c.d_binfo, (void *)c.t_x, (void *)c.t_xp, (void *)c.t_hs,
+    for (void *p : {(void *)c.d_x0, (void *)c.d_blk, (void *)c.d_binfo, (void *)c.t_x, (void *)c.t_xp, (void *)c.t_hs,
                     (void *)c.t_ce, (void *)c.t_dcs, (void *)c.t_dvs, (void *)c.t_dc, (void *)c.t_dv, (void *)c.t_q,
                     (void *)c.t_tmp, (void *)c.t_st, (void *)c.t_pde})
         if (p) cudaFree(p);
@@ -726,6 +757,16 @@ void sgld_destroy(sgld_ctx *ctx) {
 }
 
 int sgld_num_levels(const sgld_ctx *ctx) { return ctx ? ctx->c.L : -1; }
+
+int sgld_inject_fault(sgld_ctx *ctx, int kind) {
+    if (!ctx || kind < 0 || kind > 1) return SGLD_ERR_ARG;
+    if (kind == 0) return SGLD_OK;
+    Ctx &c = ctx->c;
+    if (!c.assembled || c.h_elemap.empty()) return fail(ctx, SGLD_ERR_STATE, "inject after sgld_assemble");
+    const float nan = std::numeric_limits<float>::quiet_NaN();
+    CK(cudaMemcpy(c.d_E32 + c.h_elemap[c.h_elemap.size() / 2], &nan, sizeof(float), cudaMemcpyHostToDevice));
+    return SGLD_OK;
+}
 
 int sgld_kbyu_tile(const sgld_ctx *ctx, int *tile_x, int *z_chunk) {
     if (!ctx || ctx->c.L < 1) return SGLD_ERR_ARG;
@@ -1178,9 +1219,29 @@ int sgld_solve_block(sgld_ctx *ctx, int nrhs, const double *F, double *U, const 
         const size_t bytes = sizeof(double) * (size_t)nrhs * nd;
         CK(cudaMemcpyAsync(c.d_blk, F, bytes, cudaMemcpyHostToDevice, c.stream));
         if (o->use_x0) CK(cudaMemcpyAsync(c.d_blk + (size_t)nrhs * nd, U, bytes, cudaMemcpyHostToDevice, c.stream));
+        std::vector<double> u0;   // starts of the cases, for a fallback
+        if (o->use_x0) u0.assign(U, U + (size_t)nrhs * nd);
+        std::vector<sgld_solve_info> local;
+        if (!info) {
+            local.resize((size_t)nrhs);
+            info = local.data();
+        }
+        for (int j = 0; j < nrhs; ++j) memset(info + j, 0, sizeof *info);
         if ((rc = run_solve_graph(ctx, nrhs, true, o, info))) return rc;
         CK(cudaMemcpyAsync(U, c.d_blk + (size_t)nrhs * nd, bytes, cudaMemcpyDeviceToHost, c.stream));
         CK(cudaStreamSynchronize(c.stream));
+        // cases whose mixed solve failed: the reference-form FP64 solve from the same start
+        for (int j = 0; j < nrhs; ++j) {
+            if (!mixed_failed(info[j], o->tol)) continue;
+            sgld_solve_opts o64 = *o;
+            o64.precision = SGLD_PREC_FP64;
+            if (o->use_x0)
+                std::copy(u0.begin() + (size_t)j * nd, u0.begin() + (size_t)(j + 1) * nd, U + (size_t)j * nd);
+            else
+                std::fill(U + (size_t)j * nd, U + (size_t)(j + 1) * nd, 0.0);
+            if ((rc = sgld_pcg(ctx, F + (size_t)j * nd, U + (size_t)j * nd, &o64, info + j))) return rc;
+            info[j].fallback = 1;
+        }
         return SGLD_OK;
     }
     for (int j = 0; j < nrhs; ++j)

@@ -111,6 +111,7 @@ struct Ctx {
     double inner_graph_eta = -1.0;
     int64_t inner_entry_launches = 0, inner_body_launches = 0;
     struct LearnedWS *lws = nullptr;   // learned warm start of the SIMP loop (sgld_learned.cu)
+    double *d_x0 = nullptr;            // [3*nnode] start of a mixed solve, kept for its FP64 fallback
     cudaStream_t stream = nullptr;
     std::string err;
     int device = 0;

@@ -71,7 +71,7 @@ def _info_dict(info) -> dict:
     return {"its": info.iterations, "converged": bool(info.converged), "relres": info.relres,
             "true_relres": info.true_relres, "inner_its": info.inner_iterations, "seconds": info.seconds,
             "kbyu_seconds": info.kbyu_seconds, "kbyu_launches": info.kbyu_launches,
-            "precond_seconds": info.precond_seconds}
+            "precond_seconds": info.precond_seconds, "fallback": bool(info.fallback)}
 
 
 def kernel_launches() -> int:
@@ -297,6 +297,11 @@ class VoxelSolver:
         ms = C.c_double()
         self._check(self.lib.sgld_time_op(self.ctx, self.OPS[op], int(reps), C.byref(ms)))
         return ms.value
+
+    def inject_fault(self, kind: int = 1):
+        """Test hook: kind 1 puts a NaN into the FP32 inner operator's moduli (until
+        the next assembly), so that a mixed solve fails and falls back to FP64."""
+        self._check(self.lib.sgld_inject_fault(self.ctx, int(kind)))
 
     def kbyu_tile(self) -> dict:
         """Tile of the FP32 K*u on the finest level (x width, node layers per CTA)."""

@@ -109,3 +109,34 @@ def test_mixed_adaptive_inner_stop(graded):
         res[eta] = info
     assert res[1e-2]["its"] >= res[1e-4]["its"]
     assert res[1e-2]["inner_its"] / res[1e-2]["its"] < res[1e-4]["inner_its"] / res[1e-4]["its"]
+
+
+def test_mixed_fallback_to_fp64(built_lib):
+    """Failure detection: a NaN planted on the host in the FP32 inner operator's
+    moduli makes the mixed solve fail; the library detects it (non-finite
+    residual) and returns the reference-form FP64 solve from the same start,
+    flagged as a fallback, identical to a plain FP64 solve.  The block path does
+    the same per load case.  After the next assembly the mixed solve is clean."""
+    import numpy as np
+
+    from sgldbench_gb300 import VoxelSolver
+    from sgldbench_gb300 import domains as D
+
+    vox = D.cuboid(32, 16, 16)
+    s = VoxelSolver(vox, num_levels=3, non_dyadic=0, omega=0.6, pad=False)
+    F, fixed = D.cantilever3(vox, s.nodMapBack(1))
+    s.set_fixed_dofs(fixed)
+    s.set_modulus(np.random.default_rng(0).uniform(0.2, 1.0, s.numElements))
+    s.Solving_AssembleFEAstencil()
+    U64, i64 = s.pcg(F, tol=1e-8, maxIT=500, precision="fp64")
+    s.inject_fault(1)
+    Um, im = s.pcg(F, tol=1e-8, maxIT=500, precision="mixed_df")
+    assert im["fallback"] and im["converged"]
+    assert im["its"] == i64["its"] and np.array_equal(Um, U64)
+    Ub, ib = s.solve_block(np.stack([F, 2 * F]), tol=1e-8, maxIT=500, precision="mixed_df")
+    assert all(i["fallback"] and i["converged"] for i in ib)
+    assert np.array_equal(Ub[0], U64)
+    s.Solving_AssembleFEAstencil()
+    Uc, ic = s.pcg(F, tol=1e-8, maxIT=500, precision="mixed_df")
+    assert not ic["fallback"] and ic["converged"]
+    assert np.linalg.norm(Uc - U64) <= 1e-6 * np.linalg.norm(U64)

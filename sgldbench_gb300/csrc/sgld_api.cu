@@ -534,6 +534,7 @@ int solve_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
     sgld_solve_info local;
     if (!info) info = &local;
     memset(info, 0, sizeof *info);
+    NvtxRange range(mixed ? "solve mixed" : "solve fp64");
     if (!mixed) return pcg_dev(ctx, o, info);
     Ctx &c = ctx->c;
     const size_t nv = 3 * (size_t)c.lv[0].nnode;
@@ -550,6 +551,7 @@ int solve_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
         CK(cudaMemsetAsync(c.d_x, 0, sizeof(double) * nv, c.stream));
     sgld_solve_opts o64 = *o;
     o64.precision = SGLD_PREC_FP64;
+    NvtxRange fb("fp64 fallback");
     if ((rc = pcg_dev(ctx, &o64, info))) return rc;
     info->fallback = 1;
     return SGLD_OK;
@@ -1000,6 +1002,7 @@ static int tune_kbyu_f32(sgld_ctx *ctx) {
 }
 
 int sgld_assemble(sgld_ctx *ctx) {
+    NvtxRange range("sgld_assemble");
     int rc = check_ready(ctx);
     if (rc) return rc;
     Ctx &c = ctx->c;

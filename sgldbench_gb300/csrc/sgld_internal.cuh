@@ -11,12 +11,22 @@
 //   * inactive nodes hold exact zeros, inactive elements have modulus 0.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <string>
 #include <vector>
 
 namespace sgld {
+
+// NVTX range for the phases of a call (assembly, solves, SIMP iterations);
+// free unless a profiler is attached
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // node flag bits
 enum : uint8_t { NF_ACTIVE = 1, NF_FIXX = 2, NF_FIXY = 4, NF_FIXZ = 8 };

@@ -174,6 +174,7 @@ int mnorm_to(sgld_ctx *ctx, const double *r, double *out) {
 // may replace c.d_x by the better start.
 int learned_before_solve(sgld_ctx *ctx, LearnedWS *w, int mode, double E0, int *used, int *accepted,
                          double *ratio, double *ext_ratio) {
+    NvtxRange range("learned start");
     Ctx &c = ctx->c;
     cudaStream_t s = c.stream;
     const Level &l0 = c.lv[0], &ll = c.lv[w->level];
@@ -272,6 +273,7 @@ int learned_after_solve(sgld_ctx *ctx, LearnedWS *w, int mode, int steps, float 
     const Level &l0 = c.lv[0], &ll = c.lv[w->level];
     const int64_t nv = 3 * l0.nnode;
     *loss = 0.0;
+    NvtxRange range("learned training");
     const bool had_features = w->have_prev;
     // d_prev = U_k - U_{k-1}
     LCK(cudaMemcpyAsync(w->d_prev, c.d_x, sizeof(double) * nv, cudaMemcpyDeviceToDevice, s));

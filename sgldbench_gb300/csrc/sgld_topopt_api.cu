@@ -411,6 +411,7 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
     int loop = 0;
     while (loop < o.n_loop && change > o.min_change && sharp > o.max_sharpness) {   // :47
         ++loop;
+        NvtxRange iter_range("SIMP iteration");
         double vol = 0.0;
         TCK(cudaMemcpyAsync(&vol, c.t_st + T_VOL, sizeof(double), cudaMemcpyDeviceToHost, s));
         launch_oc_scalar(0, c.t_st, c.t_st + T_VOL, 1, nact, o.volfrac, s);        // g (:83), bisection bounds
@@ -623,6 +624,7 @@ extern "C" int sgld_topopt_projected(sgld_ctx *ctx, const sgld_topopt_projected_
     while (loop < o.n_loop && change > o.min_change && sharp > o.max_sharpness) {   // :116
         ++loopbeta;
         ++loop;
+        NvtxRange iter_range("projected SIMP iteration");
         double vol = 0.0;
         TCK(cudaMemcpyAsync(&vol, c.t_st + T_VOL, sizeof(double), cudaMemcpyDeviceToHost, s));
         TCK(cudaEventRecord(ev[0], s));

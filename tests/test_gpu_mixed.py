@@ -140,3 +140,29 @@ def test_mixed_fallback_to_fp64(built_lib):
     Uc, ic = s.pcg(F, tol=1e-8, maxIT=500, precision="mixed_df")
     assert not ic["fallback"] and ic["converged"]
     assert np.linalg.norm(Uc - U64) <= 1e-6 * np.linalg.norm(U64)
+
+
+def test_run_to_run_determinism(built_lib):
+    """Every reduction is two-stage in a fixed order and no kernel uses atomics
+    for sums, so repeated solves are bitwise identical (FP64, mixed, block)."""
+    import numpy as np
+
+    from sgldbench_gb300 import VoxelSolver
+    from sgldbench_gb300 import domains as D
+
+    vox = D.cuboid(32, 16, 16)
+    s = VoxelSolver(vox, num_levels=3, non_dyadic=0, omega=0.6, pad=False)
+    F, fixed = D.cantilever3(vox, s.nodMapBack(1))
+    s.set_fixed_dofs(fixed)
+    s.set_modulus(np.random.default_rng(1).uniform(0.1, 1.0, s.numElements))
+    s.Solving_AssembleFEAstencil()
+    for prec in ("fp64", "mixed_df"):
+        U1, i1 = s.pcg(F, tol=1e-8, maxIT=500, precision=prec)
+        U2, i2 = s.pcg(F, tol=1e-8, maxIT=500, precision=prec)
+        assert np.array_equal(U1, U2) and i1["its"] == i2["its"] and i1["inner_its"] == i2["inner_its"]
+    Ub1, _ = s.solve_block(np.stack([F, -F]), tol=1e-8, maxIT=500, precision="mixed_df")
+    Ub2, _ = s.solve_block(np.stack([F, -F]), tol=1e-8, maxIT=500, precision="mixed_df")
+    assert np.array_equal(Ub1, Ub2)
+    s.Solving_AssembleFEAstencil()
+    U3, _ = s.pcg(F, tol=1e-8, maxIT=500, precision="mixed_df")
+    assert np.array_equal(U3, U1)

@@ -297,6 +297,16 @@ typedef struct sgld_topopt_opts {
     int net_level;         /* MATLAB level index of the network's grid (0 = 3, clamped to [1, levels]) */
     int net_train_steps;   /* Adam steps after each solve (0 = 4) */
     float net_lr;          /* Adam learning rate (0 = 1e-3) */
+    /* Checkpoint / resume (no counterpart in the reference's global loop, which
+     * cannot resume).  A loop stopped after k iterations and restarted with
+     * x0 = its design x (x_out), xphys0 = its xPhys, U0 = its displacement
+     * and loop0 = k runs the same iterations k+1.. as an uninterrupted loop,
+     * bit for bit (the OC and MMA updates keep no state between iterations;
+     * a learned warm start, if on, starts a fresh network). */
+    const double *xphys0;  /* NULL: xPhys starts as x (TopOpti_CallTopOpti.m); else numElements */
+    const double *U0;      /* NULL: U = 0; else numDOFs, the warm start of the first solve */
+    int loop0;             /* iterations already run: numbering continues, n_loop is the total */
+    double *x_out;         /* NULL or numElements: the final design variables x */
 } sgld_topopt_opts;
 
 #define SGLD_OPT_OC 0
@@ -322,10 +332,14 @@ typedef struct sgld_topopt_iter {
 } sgld_topopt_iter;
 
 /* x0: initial design (NULL = volfrac everywhere, TopOpti_CallTopOpti.m:34);
- * xphys: final filtered design (numElements); hist: n_loop records; *n_iter:
- * iterations run.  Leaves the last displacement in the context. */
+ * xphys: final filtered design (numElements); hist: n_loop - loop0 records;
+ * *n_iter: iterations run by this call.  Leaves the last displacement in the
+ * context (sgld_topopt_displacement reads it). */
 int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const double *F, const double *x0, double *xphys,
                 sgld_topopt_iter *hist, int *n_iter);
+
+/* The displacement the last SIMP loop ended with (numDOFs), e.g. for a checkpoint. */
+int sgld_topopt_displacement(sgld_ctx *ctx, double *U);
 
 /* The projected SIMP loops with MMA, compliance normalised by the solid
  * domain's, density filter (rmin) and Heaviside projection (beta, eta) of the

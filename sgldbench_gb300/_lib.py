@@ -41,7 +41,7 @@ class TopOptOpts(C.Structure):
     _fields_ = [("volfrac", dbl), ("rmin", dbl), ("move", dbl), ("n_loop", i32), ("min_change", dbl),
                 ("max_sharpness", dbl), ("penalty", dbl), ("E0", dbl), ("Emin", dbl), ("solve", SolveOpts),
                 ("optimizer", i32), ("learned", i32), ("net_level", i32), ("net_train_steps", i32),
-                ("net_lr", C.c_float)]
+                ("net_lr", C.c_float), ("xphys0", vp), ("U0", vp), ("loop0", i32), ("x_out", vp)]
 
 
 class TopOptProjectedOpts(C.Structure):
@@ -110,6 +110,7 @@ SIGNATURES = {
     "sgld_kbyu_dot_noalloc": (i32, [vp, vp, vp, vp, vp]),
     "sgld_density_filter": (i32, [vp, dbl, vp, vp]),
     "sgld_topopt": (i32, [vp, vp, vp, vp, vp, vp, vp]),
+    "sgld_topopt_displacement": (i32, [vp, vp]),
     "sgld_topopt_projected": (i32, [vp, vp, vp, vp, vp, vp]),
 }
 

@@ -349,7 +349,17 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
     } else {
         launch_fill_active(l0, c.t_x, o.volfrac, nb, s);
     }
-    TCK(cudaMemcpyAsync(c.t_xp, c.t_x, sizeof(double) * l0.nel, cudaMemcpyDeviceToDevice, s));
+    if (o.xphys0) {   // resume: the checkpoint's filtered design
+        TCK(cudaMemsetAsync(c.t_xp, 0, sizeof(double) * l0.nel, s));
+        TCK(cudaMemcpyAsync(c.d_tmp, o.xphys0, sizeof(double) * ne, cudaMemcpyHostToDevice, s));
+        launch_scatter_elems(c.d_elemap, ne, c.d_tmp, c.t_xp, s);
+    } else {
+        TCK(cudaMemcpyAsync(c.t_xp, c.t_x, sizeof(double) * l0.nel, cudaMemcpyDeviceToDevice, s));
+    }
+    if (o.U0) {       // resume: the checkpoint's displacement as the first warm start
+        TCK(cudaMemcpyAsync(c.d_tmp, o.U0, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, s));
+        launch_scatter_nodes(c.d_nodemap, nn, c.d_tmp, c.d_x, s);
+    }
     launch_topo_modulus(l0, c.t_xp, o.penalty, o.E0, o.Emin, c.E, c.d_part, c.d_part2, nb, s);
     launch_finalize_sum(c.d_part, nb, c.t_st + T_VOL, s);
     launch_finalize_sum(c.d_part2, nb, c.t_st + T_SHARP, s);
@@ -408,7 +418,8 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
     so.use_x0 = 1;
     so.history = nullptr;
     double change = 1.0, sharp = 1.0;
-    int loop = 0;
+    const int loop0 = o.loop0 > 0 ? o.loop0 : 0;
+    int loop = loop0;
     while (loop < o.n_loop && change > o.min_change && sharp > o.max_sharpness) {   // :47
         ++loop;
         NvtxRange iter_range("SIMP iteration");
@@ -482,7 +493,7 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
         change = st[T_CHANGE];
         sharp = st[T_SHARP] / nact;
         if (hist) {
-            sgld_topopt_iter &h = hist[loop - 1];
+            sgld_topopt_iter &h = hist[loop - 1 - loop0];
             h.loop = loop;
             h.cg_iterations = si.iterations;
             h.compliance = st[T_C];
@@ -507,7 +518,12 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
     }
     for (auto &e : ev) cudaEventDestroy(e);
     for (auto &e : evn) cudaEventDestroy(e);
-    if (n_iter) *n_iter = loop;
+    if (n_iter) *n_iter = loop - loop0;
+    if (o.x_out) {
+        launch_gather_elems(c.d_elemap, ne, c.t_x, c.d_tmp, s);
+        TCK(cudaMemcpyAsync(o.x_out, c.d_tmp, sizeof(double) * ne, cudaMemcpyDeviceToHost, s));
+        TCK(cudaStreamSynchronize(s));
+    }
     if (xphys) {
         launch_gather_elems(c.d_elemap, ne, c.t_xp, c.d_tmp, s);
         TCK(cudaMemcpyAsync(xphys, c.d_tmp, sizeof(double) * ne, cudaMemcpyDeviceToHost, s));
@@ -712,5 +728,15 @@ extern "C" int sgld_topopt_projected(sgld_ctx *ctx, const sgld_topopt_projected_
         TCK(cudaStreamSynchronize(s));
     }
     c.assembled = false;
+    return SGLD_OK;
+}
+
+extern "C" int sgld_topopt_displacement(sgld_ctx *ctx, double *U) {
+    if (!ctx || !U) return SGLD_ERR_ARG;
+    Ctx &c = ctx->c;
+    const int64_t nn = (int64_t)c.h_nodemap.size();
+    launch_gather_nodes(c.d_nodemap, nn, c.d_x, c.d_tmp, c.stream);
+    TCK(cudaMemcpyAsync(U, c.d_tmp, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost, c.stream));
+    TCK(cudaStreamSynchronize(c.stream));
     return SGLD_OK;
 }

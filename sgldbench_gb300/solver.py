@@ -465,14 +465,18 @@ class VoxelSolver:
                                        tol: float = 1e-6, maxIT: int = 500, precision: str = "fp64",
                                        inner_its: int = 0, x0=None, inner_tol: float = 0.0,
                                        optimizer: str = "OC", learned: int = 0, net_level: int = 0,
-                                       net_train_steps: int = 0, net_lr: float = 0.0):
-        """The whole SIMP loop on the device.  Returns (xPhys, history list).
+                                       net_train_steps: int = 0, net_lr: float = 0.0, resume=None,
+                                       return_state: bool = False):
+        """The whole SIMP loop on the device.  Returns (xPhys, history list), and
+        with return_state=True also the loop state {"loop", "x", "xPhys", "U"}
+        (what ``sgldbench_gb300.checkpoint`` saves).
 
         learned=1 turns on the learned warm start (a U-Net on the grid of
         level ``net_level`` trained online on the loop's solves, combined with
         the previous displacement change); learned=2 uses the previous change
         alone.  The solves still run to ``tol``, so only iteration counts
-        change."""
+        change.  resume=state continues a loop from its state (x0 is then
+        ignored); nLoop stays the total iteration cap."""
         Fv = self._vec(F, self.numDOFs)
         so = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=1,
                          precision=_precision(precision),
@@ -486,6 +490,15 @@ class VoxelSolver:
         xp = np.zeros(self.numElements)
         hist = (L.TopOptIter * nLoop)()
         nit = C.c_int()
+        keep = []
+        if resume is not None:
+            x0 = resume["x"]
+            xph0 = self._vec(resume["xPhys"], self.numElements)
+            U0 = self._vec(resume["U"], self.numDOFs)
+            keep += [xph0, U0]
+            o.xphys0, o.U0, o.loop0 = _p(xph0), _p(U0), int(resume["loop"])
+        xout = np.zeros(self.numElements)
+        o.x_out = _p(xout)
         x0v = self._vec(x0, self.numElements) if x0 is not None else None
         self._check(self.lib.sgld_topopt(self.ctx, C.byref(o), _p(Fv), _p(x0v) if x0v is not None else None,
                                          _p(xp), hist, C.byref(nit)))
@@ -493,4 +506,9 @@ class VoxelSolver:
         for i in range(nit.value):
             h = hist[i]
             recs.append({k: getattr(h, k) for k, _ in L.TopOptIter._fields_})
-        return xp, recs
+        if not return_state:
+            return xp, recs
+        U = np.zeros(self.numDOFs)
+        self._check(self.lib.sgld_topopt_displacement(self.ctx, _p(U)))
+        loop = (int(resume["loop"]) if resume is not None else 0) + nit.value
+        return xp, recs, {"loop": loop, "x": xout, "xPhys": xp.copy(), "U": U}

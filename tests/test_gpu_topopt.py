@@ -213,3 +213,28 @@ def test_projected_volume_loop_matches_oracle(built_lib):
         assert abs(a["constraint"] - b["fval"]) <= 1e-8
         assert abs(a["change"] - b["change"]) <= 1e-5
     assert _rel(xp, xp_o) <= 1e-5
+
+
+@pytest.mark.parametrize("optimizer", ["OC", "MMA"])
+def test_simp_loop_checkpoint_resume(built_lib, tmp_path, optimizer):
+    """A loop stopped after 3 iterations, saved to a checkpoint file, loaded and
+    resumed to 7 runs iterations 4-7 exactly as the uninterrupted 7-iteration
+    loop does: same history, bitwise-equal final xPhys."""
+    from sgldbench_gb300 import VoxelSolver
+    from sgldbench_gb300 import checkpoint as CK
+
+    vox = np.ones((8, 16, 8), bool)
+    m = G.build_model(vox, omega=0.6)
+    s = VoxelSolver(vox, omega=0.6)
+    s.set_fixed_dofs(m.levels[0].fixedDOFs)
+    kw = dict(volfrac=0.3, rMin=1.5, tol=1e-8, maxIT=2000, optimizer=optimizer, precision="mixed_df")
+    xp_full, h_full = s.TopOpti_GlobalVolumeConstraint(m.F, nLoop=7, **kw)
+    _, h_a, st = s.TopOpti_GlobalVolumeConstraint(m.F, nLoop=3, return_state=True, **kw)
+    p = str(tmp_path / "loop.ckpt")
+    CK.save(p, st)
+    xp_b, h_b = s.TopOpti_GlobalVolumeConstraint(m.F, nLoop=7, resume=CK.load(p), **kw)
+    assert [h["loop"] for h in h_a + h_b] == list(range(1, 8))
+    for a, b in zip(h_a + h_b, h_full):
+        assert a["compliance"] == b["compliance"] and a["change"] == b["change"]
+        assert a["cg_iterations"] == b["cg_iterations"]
+    assert np.array_equal(xp_b, xp_full)

@@ -100,3 +100,24 @@ def test_boundary_conditions_follow_apply_boundary_condition():
     F_ref = G.apply_boundary_condition(l1, fixing, loading)
     assert np.array_equal(fixed, l1.fixedDOFs)
     assert np.array_equal(F, F_ref)
+
+
+def test_checkpoint_roundtrip(tmp_path):
+    """The checkpoint format stores the loop state exactly and rejects foreign files."""
+    import numpy as np
+    import pytest
+
+    from sgldbench_gb300 import checkpoint as CK
+
+    rng = np.random.default_rng(0)
+    st = {"loop": 7, "x": rng.random(100), "xPhys": rng.random(100), "U": rng.standard_normal(303)}
+    p = str(tmp_path / "state.ckpt")
+    CK.save(p, st)
+    back = CK.load(p)
+    assert back["loop"] == 7
+    for k in ("x", "xPhys", "U"):
+        assert np.array_equal(back[k], st[k])
+    bad = tmp_path / "bad.ckpt"
+    bad.write_bytes(b"NOTACKPT" + bytes(40))
+    with pytest.raises(ValueError):
+        CK.load(str(bad))

@@ -276,6 +276,7 @@ __global__ void k_coarse_dense(const double *__restrict__ Ks, const uint8_t *__r
 void launch_coarse_dense(const Level &lc, int ncf, const int *rows_and_pos, double *A, cudaStream_t s) {
     const int *rows = rows_and_pos;
     const int *pos = rows_and_pos + ncf;
+    if (ncf == 0) return;   // every coarsest DOF fixed: nothing to factor
     cudaMemsetAsync(A, 0, sizeof(double) * (size_t)ncf * ncf, s);
     ++g_launches;
     k_coarse_dense<<<(ncf + 127) / 128, 128, 0, s>>>(lc.Ks, lc.eact, lc.ny, lc.nx, lc.nz, rows, pos, ncf, A);

@@ -535,9 +535,22 @@ int solve_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
     if (!info) info = &local;
     memset(info, 0, sizeof *info);
     NvtxRange range(mixed ? "solve mixed" : "solve fp64");
-    if (!mixed) return pcg_dev(ctx, o, info);
     Ctx &c = ctx->c;
     const size_t nv = 3 * (size_t)c.lv[0].nnode;
+    {   // a zero load has the solution 0 (the reference's PCG would divide by ||b|| = 0)
+        const int nbv = reduce_blocks((int64_t)nv);
+        launch_dot(c.d_b, c.d_b, (int64_t)nv, c.d_part, nbv, c.stream);
+        launch_finalize_sum(c.d_part, nbv, c.d_scal + 31, c.stream);
+        double bb = 0.0;
+        CK(cudaMemcpyAsync(&bb, c.d_scal + 31, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaStreamSynchronize(c.stream));
+        if (bb == 0.0) {
+            CK(cudaMemsetAsync(c.d_x, 0, sizeof(double) * nv, c.stream));
+            info->converged = 1;
+            return SGLD_OK;
+        }
+    }
+    if (!mixed) return pcg_dev(ctx, o, info);
     if (o->use_x0) {
         if (!c.d_x0) CK(dalloc(&c.d_x0, nv));
         CK(cudaMemcpyAsync(c.d_x0, c.d_x, sizeof(double) * nv, cudaMemcpyDeviceToDevice, c.stream));
@@ -1233,9 +1246,17 @@ int sgld_solve_block(sgld_ctx *ctx, int nrhs, const double *F, double *U, const 
         if ((rc = run_solve_graph(ctx, nrhs, true, o, info))) return rc;
         CK(cudaMemcpyAsync(U, c.d_blk + (size_t)nrhs * nd, bytes, cudaMemcpyDeviceToHost, c.stream));
         CK(cudaStreamSynchronize(c.stream));
-        // cases whose mixed solve failed: the reference-form FP64 solve from the same start
+        // cases whose mixed solve failed: a zero load has the solution 0; any other
+        // case reruns as the reference-form FP64 solve from the same start
         for (int j = 0; j < nrhs; ++j) {
             if (!mixed_failed(info[j], o->tol)) continue;
+            const double *Fj = F + (size_t)j * nd;
+            if (std::all_of(Fj, Fj + nd, [](double v) { return v == 0.0; })) {
+                std::fill(U + (size_t)j * nd, U + (size_t)(j + 1) * nd, 0.0);
+                memset(info + j, 0, sizeof *info);
+                info[j].converged = 1;
+                continue;
+            }
             sgld_solve_opts o64 = *o;
             o64.precision = SGLD_PREC_FP64;
             if (o->use_x0)

@@ -56,10 +56,11 @@ def parse():
     ap.add_argument("--levels", type=int, default=5)
     ap.add_argument("--maxit", type=int, default=2000)
     ap.add_argument("--inner-its", type=int, default=0,
-                    help="cap on the FP32 inner CG iterations per outer step of the mixed solves (0 = library "
-                         "default); exact count when --inner-tol is 0 and this is > 0")
+                    help="initial cap on the FP32 inner CG iterations per outer step of the mixed solves (0 = "
+                         "library default 64, doubled after a capped inner solve up to 16x); exact count when "
+                         "--inner-tol is 0 and this is > 0")
     ap.add_argument("--inner-tol", type=float, default=0.0,
-                    help="inner CG stops at ||s|| <= inner_tol ||r|| (0 = library default 1e-3)")
+                    help="inner CG stops at ||s|| <= inner_tol ||r|| (0 = library default 3e-4)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-iters", type=int, default=5, help="PCG iterations in the CPU sample")
     return ap.parse_args()

@@ -64,9 +64,10 @@ typedef struct sgld_solve_opts {
     int maxit;             /* iteration cap (maxIT_) */
     int use_x0;            /* 1: x holds the initial guess (Solving_CG_GMGS.m:7 warm start) */
     int precision;         /* SGLD_PREC_* */
-    int inner_its;         /* SGLD_PREC_MIXED(_DF): cap on the FP32 inner CG iterations per outer
-                              step (0 = 64); with inner_tol == 0 and inner_its > 0, exactly
-                              inner_its iterations */
+    int inner_its;         /* SGLD_PREC_MIXED(_DF): initial cap on the FP32 inner CG iterations per
+                              outer step (0 = 64); the cap doubles after an inner solve that stops
+                              at it short of its tolerance, up to 16 inner_its.  With inner_tol
+                              == 0 and inner_its > 0: exactly inner_its iterations, no doubling */
     double *history;       /* optional host buffer [maxit]: relative residual per iteration */
     int profile;           /* 1: time the K*u and preconditioner launches with CUDA events
                               (the SpMV / PtV split of QuickAccess/zTmp_Benchmarking_SpMV.m:63-111) */

@@ -20,6 +20,15 @@
  * layout) and do not copy through the host.  Device memory belongs to the
  * context.  A context is not thread-safe; use one per host thread.
  *
+ * Every entry point that touches the GPU first makes the context's device
+ * (sgld_options.device) current, and leaves it current.  The element matrix
+ * lives in constant memory, one copy per device shared by the contexts on it:
+ * when a call reaches a context whose matrix (Poisson ratio, cell size,
+ * sgld_set_ke) differs from the one held, the library waits for the device to
+ * go idle and uploads the context's own.  Contexts of different materials on
+ * one device may therefore be called in turn, but not from concurrent threads;
+ * contexts of equal matrices may.
+ *
  * Every function returns SGLD_OK (0) or an error code; sgld_last_error()
  * gives the message.  No exceptions cross the ABI.
  */
@@ -140,7 +149,10 @@ int sgld_kbyu_tile(const sgld_ctx *ctx, int *tile_x, int *z_chunk);
  * that array's address (once per device, the context's device must be
  * current); make that first call before any stream capture.  Every call
  * shares the array, so calls that overlap on the GPU (other streams, other
- * contexts on the same device) race; serialise them.  Grids needing more than
+ * contexts on the same device) race; serialise them.  The call uploads no
+ * constants: if the device holds another context's element matrix, it returns
+ * SGLD_ERR_STATE, and any other call on this context (before the capture)
+ * binds the matrix again.  Grids needing more than
  * SGLD_NOALLOC_MAX_CTAS CTAs (on the order of 1e8 nodes; each CTA covers a
  * 31 x 7 x 16 node block) are rejected with SGLD_ERR_ARG. */
 #define SGLD_NOALLOC_MAX_CTAS 32768

@@ -16,6 +16,7 @@
 //    and turns two sequential solves into parallel mat-vecs.
 #include <math.h>
 
+#include <atomic>
 #include <vector>
 
 #include "sgld_internal.cuh"
@@ -27,8 +28,17 @@ namespace sgld {
 // upper triangle (row <= col) and mirror them.
 __constant__ unsigned char c_pr[300], c_pc[300];
 
+// The tables below are the same for every context; each device gets them once.
+static std::atomic<bool> g_pairs_done[kMaxDevices], g_weights_done[kMaxDevices];
+
+static int current_device() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return dev;
+}
+
 static void upload_pairs(cudaStream_t s) {
-    static bool done = false;
+    std::atomic<bool> &done = g_pairs_done[current_device()];
     if (done) return;
     unsigned char pr[300], pc[300];
     int k = 0;
@@ -205,7 +215,7 @@ __global__ void __launch_bounds__(320) k_asm_coarse(const double *__restrict__ K
 }
 
 void launch_asm_coarse(const Level &coarse, const Level &fine, double *Ks, cudaStream_t s) {
-    static bool uploaded = false;
+    std::atomic<bool> &uploaded = g_weights_done[current_device()];
     upload_pairs(s);
     if (!uploaded) {
         const int cdy[8] = {1, 1, 0, 0, 1, 1, 0, 0}, cdx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, cdz[8] = {0, 0, 0, 0, 1, 1, 1, 1};

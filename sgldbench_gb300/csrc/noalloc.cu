@@ -23,7 +23,6 @@ using namespace sgld;
 static __device__ __align__(256) double g_noalloc_partial[SGLD_NOALLOC_MAX_CTAS];
 
 namespace {
-constexpr int kMaxDevices = 64;
 double *g_partial_addr[kMaxDevices] = {};   // device address of the array, per device
 }  // namespace
 
@@ -44,6 +43,11 @@ extern "C" int sgld_kbyu_dot_noalloc(sgld_ctx *ctx, const double *d_u, double *d
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev != c.device || dev < 0 || dev >= kMaxDevices) {
         c.err = "sgld_kbyu_dot_noalloc: the context's device must be current";
+        return SGLD_ERR_STATE;
+    }
+    if (!kh_bound(c)) {   // uploading here could break a capture, so the caller binds first
+        c.err = "sgld_kbyu_dot_noalloc: the device holds another context's element matrix; call any other "
+                "entry point of this context (e.g. sgld_kbyu_device) first";
         return SGLD_ERR_STATE;
     }
     if (!g_partial_addr[dev]) {   // once per device: host code needs the array's device address

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <limits>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -268,9 +269,7 @@ int setup_templates(sgld_ctx *ctx) {
     }
     CK(dalloc(&c.d_H, 2 * nh));
     CK(cudaMemcpy(c.d_H, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
-    upload_kh(c.Kh, c.stream);
-    upload_kh_df(c.Kh, c.stream);
-    return SGLD_OK;
+    return bind_ctx(ctx);   // uploads c.Kh unless the device already holds an equal matrix
 }
 
 const double *templates(const Ctx &c, int S) { return S == 2 ? c.d_H : c.d_H + 8 * 576; }
@@ -481,6 +480,7 @@ int inner_run(sgld_ctx *ctx, int kmax, double eta) {
 
 int check_ready(sgld_ctx *ctx) {
     if (!ctx) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     if (!ctx->c.have_fixed) return fail(ctx, SGLD_ERR_STATE, "fixed DOFs not set (sgld_set_fixed_dofs)");
     if (!ctx->c.have_E) return fail(ctx, SGLD_ERR_STATE, "element moduli not set (sgld_set_modulus)");
     return SGLD_OK;
@@ -572,6 +572,37 @@ int solve_dev(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
 
 }  // namespace
 
+namespace sgld {
+namespace {
+std::mutex g_bind_mu;
+bool g_kh_valid[kMaxDevices] = {};
+double g_kh_held[kMaxDevices][KH_NNZ];   // the element matrix in each device's constants
+}  // namespace
+
+int bind_ctx(sgld_ctx *ctx) {
+    Ctx &c = ctx->c;
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    if (dev != c.device) CK(cudaSetDevice(c.device));
+    std::lock_guard<std::mutex> lock(g_bind_mu);
+    if (g_kh_valid[c.device] && memcmp(g_kh_held[c.device], c.Kh, sizeof c.Kh) == 0) return SGLD_OK;
+    // another context's matrix is held: its queued kernels still read it
+    if (g_kh_valid[c.device]) CK(cudaDeviceSynchronize());
+    g_kh_valid[c.device] = false;
+    upload_kh(c.Kh, c.stream);
+    upload_kh_df(c.Kh, c.stream);
+    CK(cudaStreamSynchronize(c.stream));
+    memcpy(g_kh_held[c.device], c.Kh, sizeof c.Kh);
+    g_kh_valid[c.device] = true;
+    return SGLD_OK;
+}
+
+bool kh_bound(const Ctx &c) {
+    std::lock_guard<std::mutex> lock(g_bind_mu);
+    return g_kh_valid[c.device] && memcmp(g_kh_held[c.device], c.Kh, sizeof c.Kh) == 0;
+}
+}  // namespace sgld
+
 // =============================================================================
 extern "C" {
 
@@ -653,6 +684,7 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
         lv.nnode = (int64_t)(nx + 1) * (ny + 1) * (nz + 1);
     }
     *out = ctx;
+    if (c.device < 0 || c.device >= kMaxDevices) return fail(ctx, SGLD_ERR_ARG, "device ordinal out of range");
     if (cudaSetDevice(c.device) != cudaSuccess) return fail(ctx, SGLD_ERR_CUDA, "cudaSetDevice failed");
     CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
     for (auto &a : c.aux) CK(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
@@ -744,6 +776,9 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
 void sgld_destroy(sgld_ctx *ctx) {
     if (!ctx) return;
     Ctx &c = ctx->c;
+    int dev = -1;   // the buffers and streams belong to the context's device
+    if (c.device >= 0 && c.device < kMaxDevices && cudaGetDevice(&dev) == cudaSuccess && dev != c.device)
+        cudaSetDevice(c.device);
     for (Level &l : c.lv) {
         for (void *p : {(void *)l.eact, (void *)l.nflag, (void *)l.diag, (void *)l.idiag, (void *)l.idiag32, (void *)l.Ks, (void *)l.r,
                         (void *)l.x, (void *)l.r32, (void *)l.x32})
@@ -838,6 +873,7 @@ int sgld_set_ke(sgld_ctx *ctx, const double *Ke) {
 
 int sgld_set_fixed_dofs(sgld_ctx *ctx, const uint8_t *fixed) {
     if (!ctx || !fixed) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     Ctx &c = ctx->c;
     Level &l0 = c.lv[0];
     for (int64_t n = 0; n < l0.nnode; ++n) l0.h_nflag[n] &= NF_ACTIVE;
@@ -947,6 +983,7 @@ int sgld_get_free_dofs(const sgld_ctx *ctx, int level, uint8_t *free_mask) {
 
 int sgld_set_modulus_device(sgld_ctx *ctx, const double *d_E) {
     if (!ctx || !d_E) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     Ctx &c = ctx->c;
     CK(cudaMemsetAsync(c.E, 0, sizeof(double) * c.lv[0].nel, c.stream));
     launch_scatter_elems(c.d_elemap, (int64_t)c.h_elemap.size(), d_E, c.E, c.stream);
@@ -959,6 +996,7 @@ int sgld_set_modulus_device(sgld_ctx *ctx, const double *d_E) {
 
 int sgld_set_modulus(sgld_ctx *ctx, const double *E) {
     if (!ctx || !E) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     Ctx &c = ctx->c;
     CK(cudaMemcpyAsync(c.d_tmp, E, sizeof(double) * c.h_elemap.size(), cudaMemcpyHostToDevice, c.stream));
     return sgld_set_modulus_device(ctx, c.d_tmp);
@@ -1061,6 +1099,7 @@ int sgld_assemble(sgld_ctx *ctx) {
 int sgld_get_diag(const sgld_ctx *cctx, int level, double *diag) {
     auto *ctx = const_cast<sgld_ctx *>(cctx);
     if (!ctx || !diag || level < 1 || level >= ctx->c.L) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     const Level &l = ctx->c.lv[level - 1];
     std::vector<double> full(3 * l.nnode);
     CK(cudaMemcpy(full.data(), l.diag, sizeof(double) * full.size(), cudaMemcpyDeviceToHost));
@@ -1073,6 +1112,7 @@ int sgld_get_diag(const sgld_ctx *cctx, int level, double *diag) {
 int sgld_get_ks(const sgld_ctx *cctx, int level, double *Ks) {
     auto *ctx = const_cast<sgld_ctx *>(cctx);
     if (!ctx || !Ks || level < 2 || level > ctx->c.L) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     Ctx &c = ctx->c;
     if (!c.assembled) return fail(ctx, SGLD_ERR_STATE, "stencil not assembled (sgld_assemble)");
     Level &l = c.lv[level - 1];
@@ -1149,6 +1189,7 @@ static int level_vec_to_host(sgld_ctx *ctx, int l, const double *d_full, double 
 
 int sgld_restrict(sgld_ctx *ctx, int ii, const double *rf, double *rc_out) {
     if (!ctx || !rf || !rc_out || ii < 2 || ii > ctx->c.L) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     Ctx &c = ctx->c;
     const int l = ii - 1;
     int rc;
@@ -1161,6 +1202,7 @@ int sgld_restrict(sgld_ctx *ctx, int ii, const double *rf, double *rc_out) {
 
 int sgld_interpolate(sgld_ctx *ctx, int ii, const double *xc, double *xf) {
     if (!ctx || !xc || !xf || ii < 2 || ii > ctx->c.L) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     Ctx &c = ctx->c;
     const int l = ii - 1;
     int rc;

@@ -191,6 +191,18 @@ void launch_narrow(const double *a, float *b, int64_t n, cudaStream_t st);
 struct sgld_solve_opts;
 struct sgld_solve_info;
 namespace sgld {
+// Devices a process can bind contexts on (ordinals 0 .. kMaxDevices-1).
+constexpr int kMaxDevices = 64;
+// Every entry point that touches the device binds its context first
+// (sgld_api.cu): the context's device becomes current, and the element
+// matrix's Hadamard blocks in __constant__ memory (one copy per device, shared
+// by all contexts on it) become this context's.  A context whose matrix differs
+// from the one held waits for the device to go idle before the upload, so
+// contexts of different materials may alternate from one thread; contexts of
+// equal matrices never re-upload and may run concurrently.
+int bind_ctx(sgld_ctx *ctx);
+// true if the constants on the current device hold c's element matrix
+bool kh_bound(const Ctx &c);
 // PCG on the context's own full-grid vectors d_b / d_x (sgld_api.cu)
 int solve_on_device(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info);
 // FP64 additive V-cycle z = M r on full-grid vectors; with partial, the CTA

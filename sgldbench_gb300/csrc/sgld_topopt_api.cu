@@ -64,6 +64,7 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 
 extern "C" int sgld_density_filter(sgld_ctx *ctx, double rmin, const double *x, double *y) {
     if (!ctx || !y) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     Ctx &c = ctx->c;
     int rc = ensure_topo(ctx);
     if (rc) return rc;
@@ -186,6 +187,7 @@ extern "C" int sgld_mma_update(sgld_ctx *ctx, int m, int n, const double *xval, 
                                const double *fval, const double *dfdx, double *xnew, double *xold1_out,
                                double *xold2_out) {
     if (!ctx) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     if (m != 1) return tfail(ctx, SGLD_ERR_ARG, "sgld_mma_update supports one constraint (m = 1)");
     if (n < 1 || !xval || !xmin || !xmax || !xold1 || !df0dx || !fval || !dfdx || !xnew)
         return tfail(ctx, SGLD_ERR_ARG, "null argument or n < 1");
@@ -272,6 +274,7 @@ int pde_filter_dev(sgld_ctx *ctx, double rhat, const double *xe, double *ye, dou
 extern "C" int sgld_pde_filter(sgld_ctx *ctx, double rhat, const double *x, double *y, double tol, int maxit,
                                int *iterations) {
     if (!ctx || !x || !y) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     Ctx &c = ctx->c;
     if (!(rhat > 0.0) || maxit < 1 || !(tol >= 0.0)) return tfail(ctx, SGLD_ERR_ARG, "rhat > 0, maxit >= 1, tol >= 0");
     int rc = ensure_topo(ctx);
@@ -291,6 +294,7 @@ extern "C" int sgld_pde_filter(sgld_ctx *ctx, double rhat, const double *x, doub
 
 extern "C" int sgld_set_passive(sgld_ctx *ctx, int64_t n, const int64_t *elements) {
     if (!ctx || n < 0 || (n > 0 && !elements)) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     Ctx &c = ctx->c;
     const int64_t ne = (int64_t)c.h_elemap.size();
     std::vector<int64_t> full((size_t)n);
@@ -316,6 +320,7 @@ extern "C" int sgld_set_passive(sgld_ctx *ctx, int64_t n, const int64_t *element
 extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const double *F, const double *x0,
                            double *xphys, sgld_topopt_iter *hist, int *n_iter) {
     if (!ctx || !opts || !F) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     Ctx &c = ctx->c;
     if (!c.have_fixed) return tfail(ctx, SGLD_ERR_STATE, "fixed DOFs not set (sgld_set_fixed_dofs)");
     sgld_topopt_opts o = *opts;
@@ -543,6 +548,7 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
 extern "C" int sgld_topopt_projected(sgld_ctx *ctx, const sgld_topopt_projected_opts *opts, const double *F,
                                      double *xphys, sgld_topopt_iter *hist, int *n_iter) {
     if (!ctx || !opts || !F) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     Ctx &c = ctx->c;
     if (!c.have_fixed) return tfail(ctx, SGLD_ERR_STATE, "fixed DOFs not set (sgld_set_fixed_dofs)");
     sgld_topopt_projected_opts o = *opts;
@@ -733,6 +739,7 @@ extern "C" int sgld_topopt_projected(sgld_ctx *ctx, const sgld_topopt_projected_
 
 extern "C" int sgld_topopt_displacement(sgld_ctx *ctx, double *U) {
     if (!ctx || !U) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
     Ctx &c = ctx->c;
     const int64_t nn = (int64_t)c.h_nodemap.size();
     launch_gather_nodes(c.d_nodemap, nn, c.d_x, c.d_tmp, c.stream);

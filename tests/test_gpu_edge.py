@@ -7,7 +7,8 @@
 * no DOF fixed (a floating body): the coarsest matrix is singular and the
   library reports SGLD_ERR_NUMERIC instead of iterating;
 * the smallest domain, one 2x2x2 voxel block on 2 levels, against the oracle;
-* an empty block (nrhs = 0) is covered in test_gpu_block.py.
+* an empty block (nrhs = 0) is covered in test_gpu_block.py;
+* two live contexts of different materials, called in turn.
 """
 import numpy as np
 import pytest
@@ -81,3 +82,52 @@ def test_single_voxel_block(built_lib):
     U, info = s.pcg(m.F, tol=1e-10, maxIT=100)
     assert info["converged"] and abs(info["its"] - its_o) <= 1
     assert np.linalg.norm(U - U_o) <= 1e-8 * np.linalg.norm(U_o)
+
+
+def test_contexts_of_different_materials_alternate(built_lib, monkeypatch):
+    """The element matrix sits in device constant memory shared by all contexts
+    on a device.  Two live contexts with different Poisson ratios, called in
+    turn, must each apply their own matrix: K*u and the FP64 and mixed solves
+    match bit for bit what each context gives when it runs alone (with the
+    default FP32 tile, so that both runs use the same one)."""
+    from sgldbench_gb300 import VoxelSolver
+    from sgldbench_gb300 import domains as D
+
+    monkeypatch.setenv("SGLD_AUTOTUNE", "0")
+    vox = D.cuboid(16, 8, 8)
+
+    def make(nu):
+        s = VoxelSolver(vox, num_levels=2, non_dyadic=0, omega=0.6, pad=False, poisson_ratio=nu)
+        F, fixed = D.cantilever3(vox, s.nodMapBack(1))
+        s.set_fixed_dofs(fixed)
+        s.set_modulus(np.ones(s.numElements))
+        s.Solving_AssembleFEAstencil()
+        return s, F
+
+    u = np.random.default_rng(1).standard_normal(3 * 17 * 9 * 9)
+
+    def run(s, F):
+        y = s.Solving_KbyU_MatrixFree(u[: F.size])
+        U, _ = s.pcg(F, tol=1e-8, maxIT=200)
+        Um, _ = s.pcg(F, tol=1e-8, maxIT=200, precision="mixed")
+        return y, U, Um
+
+    a, Fa = make(0.3)
+    alone_a = run(a, Fa)
+    a.close()
+    b, Fb = make(0.45)
+    alone_b = run(b, Fb)
+    b.close()
+
+    a, Fa = make(0.3)
+    b, Fb = make(0.45)   # created last: its matrix is the one held
+    for _ in range(2):
+        got_a = run(a, Fa)
+        got_b = run(b, Fb)
+        for x, y in zip(got_a, alone_a):
+            assert np.array_equal(x, y)
+        for x, y in zip(got_b, alone_b):
+            assert np.array_equal(x, y)
+    assert not np.allclose(alone_a[0], alone_b[0])
+    a.close()
+    b.close()

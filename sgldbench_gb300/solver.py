@@ -244,16 +244,16 @@ class VoxelSolver:
         optional float64 array of numDOFs entries to receive x (for example
         page-locked host memory)."""
         bv = self._vec(b, self.numDOFs)
+        # without x0 the library starts from zero on the device and never reads x;
+        # it writes every entry of x on return
         if out is not None:
             if out.dtype != np.float64 or out.size != self.numDOFs or not out.flags.c_contiguous:
                 raise ValueError("out must be a contiguous float64 array of numDOFs entries")
             x = out
-            if x0 is None:
-                x[...] = 0.0
-            else:
+            if x0 is not None:
                 x[...] = self._vec(x0, self.numDOFs)
         else:
-            x = np.zeros_like(bv) if x0 is None else self._vec(x0, self.numDOFs).copy()
+            x = np.empty_like(bv) if x0 is None else self._vec(x0, self.numDOFs).copy()
         hist = np.zeros(maxIT) if history else None
         o = L.SolveOpts(tol=tol, maxit=maxIT, use_x0=int(x0 is not None),
                         precision=_precision(precision),

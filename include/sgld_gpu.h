@@ -113,8 +113,9 @@ int sgld_inject_fault(sgld_ctx *ctx, int kind);
 /* The CUDA stream every call of this context runs on (a cudaStream_t). */
 void *sgld_get_stream(const sgld_ctx *ctx);
 
-/* Total number of CUDA kernels this library has launched in the process
- * (a host-side counter; no counterpart in the reference, used for accounting). */
+/* Number of CUDA kernels this library has launched from the calling thread
+ * (a host-side counter, one per kernel, graph nodes included; no counterpart
+ * in the reference, used for accounting). */
 int64_t sgld_kernel_launches(void);
 
 /* Times `reps` back-to-back applications of one internal operator on the

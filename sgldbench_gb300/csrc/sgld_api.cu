@@ -18,7 +18,7 @@
 
 using namespace sgld;
 
-int64_t sgld::g_launches = 0;
+thread_local int64_t sgld::g_launches = 0;
 
 namespace {
 

@@ -149,8 +149,10 @@ int learned_before_solve(sgld_ctx *ctx, LearnedWS *w, int mode, double E0, int *
                          double *ratio, double *ext_ratio);
 int learned_after_solve(sgld_ctx *ctx, LearnedWS *w, int mode, int steps, float lr, double *loss);
 
-// number of kernels this library has launched (host-side counter, one per launch)
-extern int64_t g_launches;
+// number of kernels this library has launched from the calling thread
+// (host-side counter, one per launch; per thread, so that the launches counted
+// while a thread captures a graph are exactly that graph's)
+extern thread_local int64_t g_launches;
 
 // ---- launchers (kernels_*.cu) ------------------------------------------------
 void upload_kh(const double *Kh, cudaStream_t s);

@@ -75,7 +75,7 @@ def _info_dict(info) -> dict:
 
 
 def kernel_launches() -> int:
-    """Kernels the CUDA library has launched so far in this process."""
+    """Kernels the CUDA library has launched so far from the calling thread."""
     return int(L.load().sgld_kernel_launches())
 
 

@@ -7,7 +7,8 @@ per-CTA scratch is a static device array instead of context memory.  This
 test calls it through the C ABI twice in a row (the shared scratch keeps the
 previous call's contents) and checks y and u.y against the existing entry
 point sgld_kbyu, with the tolerance of the other K*u parity tests (1e-13
-relative for y, 1e-12 for the dot product).  It is collected last so that a
+relative for y, 1e-12 for the dot product), and that it refuses to run while
+the device holds another context's element matrix.  It is collected last so that a
 run that stops at the first failure has run every other test first.
 """
 import ctypes
@@ -63,4 +64,23 @@ def test_kbyu_dot_noalloc_matches_kbyu(built_lib):
         assert not torch.isnan(y_full).any()     # inactive nodes are written too (zeros)
         d_ref = float(u @ y_ref)
         assert abs(dot.item() - d_ref) <= 1e-12 * abs(d_ref)
+    # another material's context takes the device's constant-memory element
+    # matrix; the allocation-free call uploads nothing, so it refuses until a
+    # regular call on its own context binds the matrix again
+    other = VoxelSolver(vox, non_dyadic=0, omega=0.6, poisson_ratio=0.45)
+    other.set_fixed_dofs(fixed)
+    other.set_modulus(np.ones(other.numElements))
+    other.Solving_KbyU_MatrixFree(np.ones(other.numDOFs))
+
+    def call():
+        return lib.sgld_kbyu_dot_noalloc(s.ctx, ctypes.c_void_p(u_full.data_ptr()),
+                                         ctypes.c_void_p(y_full.data_ptr()), ctypes.c_void_p(dot.data_ptr()),
+                                         ctypes.c_void_p(s.stream))
+
+    assert call() == _lib.SGLD_OK + 3
+    y_ref = s.Solving_KbyU_MatrixFree(u)
+    assert call() == _lib.SGLD_OK, lib.sgld_last_error(s.ctx)
+    torch.cuda.synchronize()
+    assert _rel(y_full[idx].cpu().numpy(), y_ref) <= 1e-13
+    other.close()
     s.close()

@@ -75,3 +75,17 @@ def test_domain_bc_matches_oracle_cantilever():
     F, fixed = D.cantilever3(padded, m.levels[0].nodMapBack, nelx=m.nelx)
     assert np.array_equal(F, m.F)
     assert np.array_equal(fixed, m.levels[0].fixedDOFs)
+
+
+def test_create_rejects_device_ordinal_out_of_range(built_lib):
+    """The per-device tables hold 64 devices; other ordinals are an argument
+    error, reported before any CUDA call (so it needs no GPU)."""
+    from sgldbench_gb300 import VoxelSolver, _lib
+
+    for dev in (-1, 64):
+        try:
+            VoxelSolver(np.ones((8, 16, 8), bool), device=dev)
+        except _lib.SgldError as e:
+            assert e.code == 1 and "device" in str(e)
+        else:
+            raise AssertionError(f"device {dev} accepted")

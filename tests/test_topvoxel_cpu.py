@@ -121,3 +121,8 @@ def test_checkpoint_roundtrip(tmp_path):
     bad.write_bytes(b"NOTACKPT" + bytes(40))
     with pytest.raises(ValueError):
         CK.load(str(bad))
+    good = (tmp_path / "state.ckpt").read_bytes()
+    cut = tmp_path / "cut.ckpt"
+    cut.write_bytes(good[:-8])          # last U entry missing
+    with pytest.raises(ValueError):
+        CK.load(str(cut))

@@ -427,8 +427,9 @@ int sgld_principal_stress(sgld_ctx *ctx, const double *U, double *ps_node, doubl
  * convolution W[taps][cin][cout] then b[cout], convolutions in the order
  * a_0, b_0, .., a_{L-1}, b_{L-1}, u_{L-2}, m_{L-2}, .., u_0, m_0, head.
  * levels in [1, 4]; widths NULL = {16, 32, 48, 64}; channel counts are
- * multiples of 4 up to 64 (in_channels too).  The network uses its own CUDA
- * stream on the current device. */
+ * multiples of 4 up to 64 (in_channels too).  The network lives on the device
+ * current at sgld_net_create, with its own CUDA stream there; every later call
+ * makes that device current again. */
 typedef struct sgld_net sgld_net;
 
 int sgld_net_create(int ny, int nx, int nz, int in_channels, int out_channels, int levels, const int *widths,

@@ -251,6 +251,7 @@ struct sgld_net {
     Net n;
     std::string err;
     bool own_stream = false;
+    int device = 0;   // the device current at sgld_net_create; its stream and buffers live there
 };
 
 namespace {
@@ -265,6 +266,14 @@ int nfail(sgld_net *h, int code, const std::string &m) {
         cudaError_t e_ = (x);                                                                        \
         if (e_ != cudaSuccess) return nfail(h, SGLD_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
     } while (0)
+
+// every entry point runs on the network's own device
+int net_bind(sgld_net *h) {
+    int dev = -1;
+    NCK(cudaGetDevice(&dev));
+    if (dev != h->device) NCK(cudaSetDevice(h->device));
+    return SGLD_OK;
+}
 
 // host [V][cin] FP32 -> the network's BF16 input
 int upload_input(sgld_net *h, const float *x) {
@@ -303,6 +312,7 @@ int sgld_net_create(int ny, int nx, int nz, int in_channels, int out_channels, i
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return SGLD_ERR_CUDA;
     sgld_net *h = new sgld_net();
+    h->device = dev;
     cudaStream_t s = nullptr;
     if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
         delete h;
@@ -322,6 +332,7 @@ int sgld_net_create(int ny, int nx, int nz, int in_channels, int out_channels, i
 
 void sgld_net_destroy(sgld_net *h) {
     if (!h) return;
+    net_bind(h);
     if (h->n.s) cudaStreamSynchronize(h->n.s);
     net_free(h->n);
     if (h->own_stream && h->n.s) cudaStreamDestroy(h->n.s);
@@ -334,6 +345,7 @@ int64_t sgld_net_num_params(const sgld_net *h) { return h ? h->n.nparam : -1; }
 
 int sgld_net_get_params(sgld_net *h, float *w) {
     if (!h || !w) return SGLD_ERR_ARG;
+    if (int rc = net_bind(h)) return rc;
     NCK(cudaMemcpyAsync(w, h->n.w, sizeof(float) * h->n.nparam, cudaMemcpyDeviceToHost, h->n.s));
     NCK(cudaStreamSynchronize(h->n.s));
     return SGLD_OK;
@@ -341,6 +353,7 @@ int sgld_net_get_params(sgld_net *h, float *w) {
 
 int sgld_net_set_params(sgld_net *h, const float *w) {
     if (!h || !w) return SGLD_ERR_ARG;
+    if (int rc = net_bind(h)) return rc;
     Net &n = h->n;
     NCK(cudaMemcpyAsync(n.w, w, sizeof(float) * n.nparam, cudaMemcpyHostToDevice, n.s));
     net_to_bf16(n.w, n.wb, n.nparam, n.s);
@@ -353,6 +366,7 @@ int sgld_net_set_params(sgld_net *h, const float *w) {
 
 int sgld_net_forward(sgld_net *h, const float *x, float *y) {
     if (!h || !x || !y) return SGLD_ERR_ARG;
+    if (int rc = net_bind(h)) return rc;
     Net &n = h->n;
     int rc = upload_input(h, x);
     if (rc) return rc;
@@ -365,6 +379,7 @@ int sgld_net_forward(sgld_net *h, const float *x, float *y) {
 
 int sgld_net_grad(sgld_net *h, const float *x, const float *target, const float *mask, double *loss, float *grad) {
     if (!h || !x || !target) return SGLD_ERR_ARG;
+    if (int brc = net_bind(h)) return brc;
     Net &n = h->n;
     int rc = upload_input(h, x);
     if (!rc) rc = upload_target(h, target, mask);
@@ -382,6 +397,7 @@ int sgld_net_grad(sgld_net *h, const float *x, const float *target, const float 
 int sgld_net_train_step(sgld_net *h, const float *x, const float *target, const float *mask, float lr,
                         double *loss) {
     if (!h || !x || !target || !(lr > 0.f)) return SGLD_ERR_ARG;
+    if (int brc = net_bind(h)) return brc;
     Net &n = h->n;
     int rc = upload_input(h, x);
     if (!rc) rc = upload_target(h, target, mask);

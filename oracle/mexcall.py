@@ -56,6 +56,8 @@ class MexLib:
         L.shim_data.restype = vp
         L.shim_data.argtypes = [vp]
         L.shim_destroy.argtypes = [vp]
+        if hasattr(L, "shim_run_at_exit"):   # absent from libraries built before the shim had it
+            L.shim_run_at_exit.argtypes = []
         L.shim_call.restype = C.c_int
         L.shim_call.argtypes = [vp, C.c_int, vp, C.c_int, vp, C.c_char_p, C.c_size_t]
 
@@ -110,6 +112,11 @@ class MexLib:
         raw = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(np.ctypeslib.as_ctypes_type(dt))),
                                     shape=(max(n, 1),))[:n].copy()
         return raw.reshape(shape, order="F")
+
+    def clear(self):
+        """What MATLAB's `clear mex` does to the loaded file: runs the function
+        it registered with mexAtExit."""
+        self.lib.shim_run_at_exit()
 
     # -- call ---------------------------------------------------------------
     def call(self, name: str, nlhs: int, *args):

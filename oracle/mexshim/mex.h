@@ -21,6 +21,9 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]);
 void mexErrMsgIdAndTxt(const char *id, const char *fmt, ...);
 void mexWarnMsgIdAndTxt(const char *id, const char *fmt, ...);
 int mexPrintf(const char *fmt, ...);
+/* Registers the function MATLAB calls when the MEX file is cleared; the shim
+ * runs it from shim_run_at_exit(). */
+int mexAtExit(void (*exit_fcn)(void));
 #ifdef __cplusplus
 }
 #endif

@@ -169,6 +169,11 @@ int mexPrintf(const char *fmt, ...) {
     va_end(ap);
     return r;
 }
+static void (*g_exit_fcn)(void) = nullptr;
+int mexAtExit(void (*exit_fcn)(void)) {
+    g_exit_fcn = exit_fcn;
+    return 0;
+}
 
 /* ---- helpers for ctypes callers ---- */
 mxArray *shim_new_numeric(int cls, size_t m, size_t n, const void *src) {
@@ -211,6 +216,12 @@ size_t shim_ndim(const mxArray *a) { return a->dims.size(); }
 size_t shim_dim(const mxArray *a, size_t i) { return i < a->dims.size() ? a->dims[i] : 1; }
 void *shim_data(const mxArray *a) { return a->data; }
 void shim_destroy(mxArray *a) { mxDestroyArray(a); }
+/* what `clear mex` does to a loaded MEX file: run its mexAtExit function once */
+void shim_run_at_exit(void) {
+    void (*f)(void) = g_exit_fcn;
+    g_exit_fcn = nullptr;
+    if (f) f();
+}
 
 typedef void (*mex_entry_t)(int, mxArray **, int, const mxArray **);
 int shim_call(mex_entry_t fn, int nlhs, mxArray **plhs, int nrhs, const mxArray **prhs, char *err,

@@ -34,6 +34,13 @@
 
 static sgld_ctx *g_ctx = nullptr;
 
+// MATLAB calls this when the MEX file is cleared (clear mex, clear all) or
+// exits, so that the context's device memory goes with it
+static void release_ctx(void) {
+    if (g_ctx) sgld_destroy(g_ctx);
+    g_ctx = nullptr;
+}
+
 static void check(int rc) {
     if (rc != SGLD_OK) mexErrMsgIdAndTxt("sgld:gpu", "%s", g_ctx ? sgld_last_error(g_ctx) : "no context");
 }
@@ -82,8 +89,8 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
         if (nrhs > 4) o.poisson_ratio = mxGetScalar(prhs[4]);
         if (nrhs > 5) o.cell_size = mxGetScalar(prhs[5]);
         if (nrhs > 6) o.omega = mxGetScalar(prhs[6]);
-        if (g_ctx) sgld_destroy(g_ctx);
-        g_ctx = nullptr;
+        release_ctx();
+        mexAtExit(release_ctx);
         const int rc = sgld_create((int)d[0], (int)d[1], (int)d[2], solid.data(), &o, &g_ctx);
         if (rc != SGLD_OK) {
             const char *m = g_ctx ? sgld_last_error(g_ctx) : "create failed";
@@ -98,8 +105,7 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
         return;
     }
     if (!strcmp(cmd, "destroy")) {
-        if (g_ctx) sgld_destroy(g_ctx);
-        g_ctx = nullptr;
+        release_ctx();
         return;
     }
     need_ctx();

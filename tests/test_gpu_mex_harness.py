@@ -154,3 +154,18 @@ def test_harness_config0(built_lib):
     U_o, its_o = G.solve(m, tol=1e-6, maxIT=500)
     assert abs(rec["iterations"] - its_o) <= 1
     assert abs(rec["compliance"] - G.compliance(m, U_o)) <= 1e-6 * G.compliance(m, U_o)
+
+
+def test_gateway_clear_releases_context(gateway):
+    """`clear mex` runs the gateway's mexAtExit function, which destroys the
+    context: the next command that needs one is refused until 'create'."""
+    M = gateway
+    vox = np.ones((8, 16, 8), bool)
+    _, nlev0, padded, _ = G.voxel_discretization(vox)
+    M.call("sgld_gpu_mex", 1, "create", padded, float(nlev0), 1.0, 0.3, 1.0, 0.6)
+    M.clear()
+    with pytest.raises(mexcall.MexError, match="create"):
+        M.call("sgld_gpu_mex", 0, "assemble")
+    M.call("sgld_gpu_mex", 1, "create", padded, float(nlev0), 1.0, 0.3, 1.0, 0.6)
+    M.call("sgld_gpu_mex", 0, "destroy")
+    M.clear()   # nothing left to release

@@ -8,7 +8,7 @@
 // timings and the compliance.
 //
 //   sgld_harness [--size NX NY NZ] [--levels L] [--nondyadic 0|1] [--omega W]
-//                [--tol T] [--maxit N] [--precision fp64|mixed] [--graded SEED] [--repeat R]
+//                [--tol T] [--maxit N] [--precision fp64|mixed|mixed_df] [--graded SEED] [--repeat R]
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -78,14 +78,24 @@ int main(int argc, char **argv) {
         } else if (!strcmp(argv[i], "--maxit") && i + 1 < argc) {
             maxit = atoi(argv[++i]);
         } else if (!strcmp(argv[i], "--precision") && i + 1 < argc) {
-            precision = !strcmp(argv[++i], "mixed") ? SGLD_PREC_MIXED : SGLD_PREC_FP64;
+            const char *p = argv[++i];
+            if (!strcmp(p, "fp64")) {
+                precision = SGLD_PREC_FP64;
+            } else if (!strcmp(p, "mixed")) {
+                precision = SGLD_PREC_MIXED;
+            } else if (!strcmp(p, "mixed_df")) {
+                precision = SGLD_PREC_MIXED_DF;
+            } else {
+                fprintf(stderr, "sgld_harness: unknown precision %s (fp64, mixed or mixed_df)\n", p);
+                return 2;
+            }
         } else if (!strcmp(argv[i], "--graded") && i + 1 < argc) {
             graded = atoi(argv[++i]);
         } else if (!strcmp(argv[i], "--repeat") && i + 1 < argc) {
             repeat = atoi(argv[++i]);
         } else {
             fprintf(stderr, "usage: %s [--size NX NY NZ] [--levels L] [--nondyadic 0|1] [--omega W] [--tol T] "
-                            "[--maxit N] [--precision fp64|mixed] [--graded SEED] [--repeat R]\n", argv[0]);
+                            "[--maxit N] [--precision fp64|mixed|mixed_df] [--graded SEED] [--repeat R]\n", argv[0]);
             return 2;
         }
     }
@@ -99,9 +109,9 @@ int main(int argc, char **argv) {
     if (sgld_create(ny, nx, nz, solid.data(), &o, &ctx) != SGLD_OK) die(ctx, "sgld_create");
     int res[3], span;
     int64_t ne = 0, nn = 0;
-    sgld_level_info(ctx, 1, res, &span, &ne, &nn);
+    if (sgld_level_info(ctx, 1, res, &span, &ne, &nn) != SGLD_OK) die(ctx, "sgld_level_info");
     std::vector<int64_t> nodes(nn);
-    sgld_node_map(ctx, 1, nodes.data());
+    if (sgld_node_map(ctx, 1, nodes.data()) != SGLD_OK) die(ctx, "sgld_node_map");
     // boundary conditions: solid cuboid -> every node is active, compact = full order
     std::vector<uint8_t> fixed(3 * nn, 0);
     std::vector<double> F(3 * nn, 0.0);
@@ -139,7 +149,8 @@ int main(int argc, char **argv) {
     printf("{\"grid\": [%d, %d, %d], \"dofs\": %lld, \"levels\": %d, \"precision\": \"%s\", \"iterations\": %d, "
            "\"converged\": %d, \"relres\": %.6e, \"true_relres\": %.6e, \"solve_s\": %.6f, \"wall_s\": %.6f, "
            "\"compliance\": %.12e}\n",
-           nx, ny, nz, (long long)(3 * nn), sgld_num_levels(ctx), precision == SGLD_PREC_MIXED ? "mixed" : "fp64",
+           nx, ny, nz, (long long)(3 * nn), sgld_num_levels(ctx),
+           precision == SGLD_PREC_MIXED ? "mixed" : precision == SGLD_PREC_MIXED_DF ? "mixed_df" : "fp64",
            info.iterations, info.converged, info.relres, info.true_relres, info.seconds, best, c);
     sgld_destroy(ctx);
     return info.converged ? 0 : 3;

@@ -154,6 +154,12 @@ def test_harness_config0(built_lib):
     U_o, its_o = G.solve(m, tol=1e-6, maxIT=500)
     assert abs(rec["iterations"] - its_o) <= 1
     assert abs(rec["compliance"] - G.compliance(m, U_o)) <= 1e-6 * G.compliance(m, U_o)
+    # the headline mode from the command line: same compliance to 1e-6
+    out = subprocess.run([exe, "--size", "64", "32", "32", "--levels", "4", "--nondyadic", "1", "--omega", "0.6",
+                          "--tol", "1e-6", "--precision", "mixed_df"], capture_output=True, text=True, check=True)
+    mix = json.loads(out.stdout.strip().splitlines()[-1])
+    assert mix["precision"] == "mixed_df" and mix["converged"] == 1 and mix["true_relres"] < 1e-6
+    assert abs(mix["compliance"] - G.compliance(m, U_o)) <= 1e-6 * G.compliance(m, U_o)
 
 
 def test_gateway_clear_releases_context(gateway):

@@ -282,14 +282,21 @@ def run_ours(args):
     E_h = torch.from_numpy(E).pin_memory().numpy()
     F_h = torch.from_numpy(F).pin_memory().numpy()
     U_h = torch.zeros(F.size, dtype=torch.float64).pin_memory().numpy()
+    def step_e2e():
+        s.set_modulus(E_h)
+        s.Solving_AssembleFEAstencil()
+        return s.pcg(F_h, tol=TOL, maxIT=args.maxit, precision=args.precision, inner_its=args.inner_its,
+                     inner_tol=args.inner_tol, out=U_h)
+
+    # warm-up of the host-buffer path too: its first calls pay one-time costs
+    # (pinned-buffer registration lookups, the host entry point's first solve)
+    for _ in range(max(args.warmup, 0)):
+        step_e2e()
     e2e = []
     for _ in range(args.steps):
         torch.cuda.synchronize()
         t0.record(stream)
-        s.set_modulus(E_h)
-        s.Solving_AssembleFEAstencil()
-        U_h, inf = s.pcg(F_h, tol=TOL, maxIT=args.maxit, precision=args.precision, inner_its=args.inner_its,
-                         inner_tol=args.inner_tol, out=U_h)
+        U_h, inf = step_e2e()
         t1.record(stream)
         torch.cuda.synchronize()
         e2e.append(t0.elapsed_time(t1) / 1e3)
@@ -328,7 +335,7 @@ def run_ours(args):
                       "kbyu_s": pinfo["kbyu_seconds"], "precond_s": pinfo["precond_seconds"]},
             "true_relres": infos[-1]["true_relres"], "converged": infos[-1]["converged"],
             "e2e": {"value": float(np.mean(e2e)), "unit": "s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h)},
+                    "d2h_bytes_per_step": int(d2h), "samples": [round(v, 6) for v in e2e]},
             "gpu_launches": int(round(launches)), "roofline": roofline, "clocks": clocks}
     if fp64:
         line["plain_fp64"] = fp64

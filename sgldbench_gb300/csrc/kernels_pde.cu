@@ -7,19 +7,19 @@
 //
 // Kernels are node-centric gathers on the full grid (deterministic: every
 // output is written by one thread summing in a fixed order).  The element
-// matrix sits in constant memory in the reference's corner order j (offsets
+// matrix Kp (row-major 8 x 8, in the context's own device buffer, since it
+// depends on the call's radius) is in the reference's corner order j (offsets
 // (dy, dx, dz) = (1,0,0),(1,1,0),(0,1,0),(0,0,0),(1,0,1),(1,1,1),(0,1,1),(0,0,1)).
 #include "sgld_internal.cuh"
 
 namespace sgld {
 
-__constant__ double c_Kp[64];   // row-major 8 x 8
 __constant__ int c_pdy[8] = {1, 1, 0, 0, 1, 1, 0, 0};
 __constant__ int c_pdx[8] = {0, 1, 1, 0, 0, 1, 1, 0};
 __constant__ int c_pdz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
 
-void upload_kpde(const double *K, cudaStream_t s) {
-    cudaMemcpyToSymbolAsync(c_Kp, K, sizeof(double) * 64, 0, cudaMemcpyHostToDevice, s);
+void upload_kpde(const double *K, double *d_kp, cudaStream_t s) {
+    cudaMemcpyAsync(d_kp, K, sizeof(double) * 64, cudaMemcpyHostToDevice, s);
 }
 
 // node n is corner j of element (iy - dy_j, ix - dx_j, iz - dz_j)
@@ -48,7 +48,7 @@ __global__ void k_pde_e2n(const double *__restrict__ xe, const uint8_t *__restri
 
 // y = K_pde u (scalar field), optional partial sums of u.y per CTA
 __global__ void k_pde_kbyu(const double *__restrict__ u, const uint8_t *__restrict__ eact, int ny, int nx, int nz,
-                           double *__restrict__ y, double *__restrict__ partial) {
+                           const double *__restrict__ Kp, double *__restrict__ y, double *__restrict__ partial) {
     const int NY = ny + 1, NX = nx + 1;
     const int64_t nn = (int64_t)NY * NX * (nz + 1);
     const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -63,7 +63,7 @@ __global__ void k_pde_kbyu(const double *__restrict__ u, const uint8_t *__restri
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 const int64_t m = (int64_t)(ey + c_pdy[k]) + (int64_t)NY * ((ex + c_pdx[k]) + (int64_t)NX * (ez + c_pdz[k]));
-                s += c_Kp[8 * j + k] * u[m];
+                s += Kp[8 * j + k] * u[m];
             }
             acc += s;
         }
@@ -85,7 +85,8 @@ __global__ void k_pde_kbyu(const double *__restrict__ u, const uint8_t *__restri
 }
 
 // dinv_n = 1 / sum of diag(K_pde) over the active elements at n (0 where none)
-__global__ void k_pde_diag(const uint8_t *__restrict__ eact, int ny, int nx, int nz, double *__restrict__ dinv) {
+__global__ void k_pde_diag(const uint8_t *__restrict__ eact, int ny, int nx, int nz, const double *__restrict__ Kp,
+                           double *__restrict__ dinv) {
     const int NY = ny + 1, NX = nx + 1;
     const int64_t nn = (int64_t)NY * NX * (nz + 1);
     const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -94,7 +95,7 @@ __global__ void k_pde_diag(const uint8_t *__restrict__ eact, int ny, int nx, int
     double d = 0.0;
     for (int j = 0; j < 8; ++j) {
         const int64_t e = corner_elem(iy, ix, iz, j, ny, nx, nz);
-        if (e >= 0 && eact[e]) d += c_Kp[9 * j];
+        if (e >= 0 && eact[e]) d += Kp[9 * j];
     }
     dinv[n] = d > 0.0 ? 1.0 / d : 0.0;
 }
@@ -143,15 +144,15 @@ void launch_pde_e2n(const Level &l0, const double *xe, double *yn, cudaStream_t 
     ++g_launches;
     k_pde_e2n<<<nblk(l0.nnode, 256), 256, 0, s>>>(xe, l0.eact, l0.ny, l0.nx, l0.nz, yn);
 }
-int launch_pde_kbyu(const Level &l0, const double *u, double *y, double *partial, cudaStream_t s) {
+int launch_pde_kbyu(const Level &l0, const double *Kp, const double *u, double *y, double *partial, cudaStream_t s) {
     ++g_launches;
     const unsigned nb = nblk(l0.nnode, 256);
-    k_pde_kbyu<<<nb, 256, 0, s>>>(u, l0.eact, l0.ny, l0.nx, l0.nz, y, partial);
+    k_pde_kbyu<<<nb, 256, 0, s>>>(u, l0.eact, l0.ny, l0.nx, l0.nz, Kp, y, partial);
     return (int)nb;
 }
-void launch_pde_diag(const Level &l0, double *dinv, cudaStream_t s) {
+void launch_pde_diag(const Level &l0, const double *Kp, double *dinv, cudaStream_t s) {
     ++g_launches;
-    k_pde_diag<<<nblk(l0.nnode, 256), 256, 0, s>>>(l0.eact, l0.ny, l0.nx, l0.nz, dinv);
+    k_pde_diag<<<nblk(l0.nnode, 256), 256, 0, s>>>(l0.eact, l0.ny, l0.nx, l0.nz, Kp, dinv);
 }
 void launch_pde_jacobi(const double *r, const double *dinv, int64_t n, double *z, double *partial, int nb,
                        cudaStream_t s) {

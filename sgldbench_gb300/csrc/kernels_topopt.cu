@@ -17,9 +17,11 @@
 namespace sgld {
 
 constexpr int FW_MAX = 7;   // box side up to 7 (rmin <= 4)
-__constant__ double c_fw[FW_MAX * FW_MAX * FW_MAX];
 
-void upload_filter_weights(double rmin, int *radius, cudaStream_t s) {
+// The weights go to the context's own device buffer d_w (FW_MAX^3 doubles), not
+// to constant memory shared by the device, so that contexts filtering with
+// different radii do not overwrite each other's.
+void upload_filter_weights(double rmin, int *radius, double *d_w, cudaStream_t s) {
     const int r = (int)ceil(rmin) - 1;
     const int side = 2 * r + 1;
     double w[FW_MAX * FW_MAX * FW_MAX];
@@ -29,13 +31,13 @@ void upload_filter_weights(double rmin, int *radius, cudaStream_t s) {
                 const double d = rmin - sqrt((double)(dx * dx + dy * dy + dz * dz));
                 w[(dz + r) * side * side + (dx + r) * side + (dy + r)] = d > 0.0 ? d : 0.0;
             }
-    cudaMemcpyToSymbolAsync(c_fw, w, sizeof(double) * side * side * side, 0, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_w, w, sizeof(double) * side * side * side, cudaMemcpyHostToDevice, s);
     *radius = r;
 }
 
 // y_e = sum_{e2 in box, active} w(e - e2) x_e2   (x == nullptr: the weight sums Hs)
 __global__ void k_density_filter(const double *__restrict__ x, const uint8_t *__restrict__ eact, int ny, int nx,
-                                 int nz, int r, double *__restrict__ y) {
+                                 int nz, int r, const double *__restrict__ fw, double *__restrict__ y) {
     const int pl = blockIdx.x * blockDim.x + threadIdx.x;
     if (pl >= ny * nx) return;
     const int jj = pl % ny, ii = pl / ny, kk = blockIdx.y;
@@ -51,16 +53,16 @@ __global__ void k_density_filter(const double *__restrict__ x, const uint8_t *__
             for (int j2 = max(jj - r, 0); j2 <= min(jj + r, ny - 1); ++j2) {
                 const int64_t e2 = (int64_t)j2 + (int64_t)ny * (i2 + (int64_t)nx * k2);
                 if (!eact[e2]) continue;
-                const double w = c_fw[(k2 - kk + r) * side * side + (i2 - ii + r) * side + (j2 - jj + r)];
+                const double w = fw[(k2 - kk + r) * side * side + (i2 - ii + r) * side + (j2 - jj + r)];
                 acc += x ? w * x[e2] : w;
             }
     y[e] = acc;
 }
 
-void launch_density_filter(const Level &l0, const double *x, int r, double *y, cudaStream_t s) {
+void launch_density_filter(const Level &l0, const double *x, int r, const double *fw, double *y, cudaStream_t s) {
     const dim3 g((unsigned)((l0.ny * l0.nx + 255) / 256), (unsigned)l0.nz);
     ++g_launches;
-    k_density_filter<<<g, 256, 0, s>>>(x, l0.eact, l0.ny, l0.nx, l0.nz, r, y);
+    k_density_filter<<<g, 256, 0, s>>>(x, l0.eact, l0.ny, l0.nx, l0.nz, r, fw, y);
 }
 
 constexpr int TB = 256;

@@ -801,7 +801,7 @@ void sgld_destroy(sgld_ctx *ctx) {
     learned_free(c.lws);
     for (void *p : {(void *)c.d_x0, (void *)c.d_blk, (void *)c.d_binfo, (void *)c.t_x, (void *)c.t_xp, (void *)c.t_hs,
                     (void *)c.t_ce, (void *)c.t_dcs, (void *)c.t_dvs, (void *)c.t_dc, (void *)c.t_dv, (void *)c.t_q,
-                    (void *)c.t_tmp, (void *)c.t_st, (void *)c.t_pde})
+                    (void *)c.t_tmp, (void *)c.t_st, (void *)c.t_pde, (void *)c.t_fw, (void *)c.t_kp})
         if (p) cudaFree(p);
     delete ctx;
 }

@@ -84,6 +84,8 @@ struct Ctx {
            *t_dc = nullptr, *t_dv = nullptr, *t_q = nullptr, *t_tmp = nullptr, *t_st = nullptr;
     double t_rmin = -1.0;
     double *t_pde = nullptr;   // [7 nnode] PDE-filter PCG work (finest nodes, one value each)
+    double *t_fw = nullptr;    // [7^3] density-filter weights of the last radius
+    double *t_kp = nullptr;    // [64] PDE-filter element matrix of the last radius
     cudaGraphExec_t factor_graph = nullptr;   // captured factorization of the coarsest matrix
     int64_t factor_graph_launches = 0;
     int trinv_ring = 0;
@@ -211,8 +213,8 @@ int solve_on_device(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *in
 // partials of z.r (nb of them) for launch_finalize_sum
 int vcycle_f64(sgld_ctx *ctx, const double *r, double *z, double *partial, int *nb);
 // SIMP loop (kernels_topopt.cu)
-void upload_filter_weights(double rmin, int *radius, cudaStream_t s);
-void launch_density_filter(const Level &l0, const double *x, int r, double *y, cudaStream_t s);
+void upload_filter_weights(double rmin, int *radius, double *d_w, cudaStream_t s);
+void launch_density_filter(const Level &l0, const double *x, int r, const double *fw, double *y, cudaStream_t s);
 void launch_topo_modulus(const Level &l0, const double *xp, double p, double E0, double Emin, double *E,
                          double *pv, double *ps, int nb, cudaStream_t s);
 void launch_topo_sens(const Level &l0, const double *xp, const double *ce, const double *Hs, double p, double E0,
@@ -251,10 +253,10 @@ void launch_stress(const Level &l0, const double *E, const double *u, const doub
 void launch_elem_vm(const Level &l0, const double *nodal6, double *vm_elem_full, cudaStream_t s);
 void launch_principal(const Level &l0, const double *s6, double *ps_node, double *dir_elem, cudaStream_t s);
 // PDE density filter (kernels_pde.cu)
-void upload_kpde(const double *K, cudaStream_t s);
+void upload_kpde(const double *K, double *d_kp, cudaStream_t s);
 void launch_pde_e2n(const Level &l0, const double *xe, double *yn, cudaStream_t s);
-int launch_pde_kbyu(const Level &l0, const double *u, double *y, double *partial, cudaStream_t s);
-void launch_pde_diag(const Level &l0, double *dinv, cudaStream_t s);
+int launch_pde_kbyu(const Level &l0, const double *Kp, const double *u, double *y, double *partial, cudaStream_t s);
+void launch_pde_diag(const Level &l0, const double *Kp, double *dinv, cudaStream_t s);
 void launch_pde_jacobi(const double *r, const double *dinv, int64_t n, double *z, double *partial, int nb,
                        cudaStream_t s);
 void launch_pde_n2e(const Level &l0, const double *t, double *xe, cudaStream_t s);

@@ -45,9 +45,10 @@ int setup_filter(sgld_ctx *ctx, double rmin, int *radius) {
     Ctx &c = ctx->c;
     if (!(rmin > 0.0) || (int)ceil(rmin) - 1 > 3) return tfail(ctx, SGLD_ERR_ARG, "rmin must be in (0, 4]");
     int r = 0;
-    upload_filter_weights(rmin, &r, c.stream);
+    if (!c.t_fw) TCK(cudaMalloc((void **)&c.t_fw, sizeof(double) * 7 * 7 * 7));
+    upload_filter_weights(rmin, &r, c.t_fw, c.stream);
     if (c.t_rmin != rmin) {
-        launch_density_filter(c.lv[0], nullptr, r, c.t_hs, c.stream);
+        launch_density_filter(c.lv[0], nullptr, r, c.t_fw, c.t_hs, c.stream);
         c.t_rmin = rmin;
     }
     *radius = r;
@@ -76,7 +77,7 @@ extern "C" int sgld_density_filter(sgld_ctx *ctx, double rmin, const double *x, 
         TCK(cudaMemcpyAsync(c.d_tmp, x, sizeof(double) * ne, cudaMemcpyHostToDevice, c.stream));
         TCK(cudaMemsetAsync(c.t_tmp, 0, sizeof(double) * l0.nel, c.stream));
         launch_scatter_elems(c.d_elemap, ne, c.d_tmp, c.t_tmp, c.stream);
-        launch_density_filter(l0, c.t_tmp, r, c.t_q, c.stream);
+        launch_density_filter(l0, c.t_tmp, r, c.t_fw, c.t_q, c.stream);
         launch_gather_elems(c.d_elemap, ne, c.t_q, c.d_tmp, c.stream);
     } else {
         launch_gather_elems(c.d_elemap, ne, c.t_hs, c.d_tmp, c.stream);
@@ -238,9 +239,10 @@ int pde_filter_dev(sgld_ctx *ctx, double rhat, const double *xe, double *ye, dou
     double *b = c.t_pde, *x = b + nn, *r = x + nn, *z = r + nn, *p = z + nn, *q = p + nn, *dinv = q + nn;
     double K[64];
     pde_element_matrix(rhat, K);
-    upload_kpde(K, c.stream);
+    if (!c.t_kp) TCK(cudaMalloc((void **)&c.t_kp, sizeof(double) * 64));
+    upload_kpde(K, c.t_kp, c.stream);
     launch_pde_e2n(l0, xe, b, c.stream);
-    launch_pde_diag(l0, dinv, c.stream);
+    launch_pde_diag(l0, c.t_kp, dinv, c.stream);
     const int nbv = reduce_blocks(nn);
     launch_pcg_scalar(5, c.d_scal, c.d_iflag, c.d_part, 1, tol, maxit, c.stream);
     launch_dot(b, b, nn, c.d_part, nbv, c.stream);
@@ -252,7 +254,7 @@ int pde_filter_dev(sgld_ctx *ctx, double rhat, const double *xe, double *ye, dou
     TCK(cudaMemcpyAsync(p, z, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c.stream));
     int h_flag[4] = {0, 0, 0, 0};
     for (int k = 1; k <= maxit; ++k) {
-        const int nb = launch_pde_kbyu(l0, p, q, c.d_part, c.stream);
+        const int nb = launch_pde_kbyu(l0, c.t_kp, p, q, c.d_part, c.stream);
         launch_pcg_scalar(2, c.d_scal, c.d_iflag, c.d_part, nb, tol, maxit, c.stream);
         launch_pcg_update(x, r, p, q, nn, c.d_scal, c.d_iflag, c.d_part, nbv, c.stream);
         launch_pcg_scalar(3, c.d_scal, c.d_iflag, c.d_part, nbv, tol, maxit, c.stream);
@@ -451,8 +453,8 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
         launch_finalize_sum(c.d_part, nbc, c.t_st + T_C, s);
         launch_topo_sens(l0, c.t_xp, c.t_ce, c.t_hs, o.penalty, o.E0, o.Emin, c.t_dcs, c.t_dvs, nb, s);   // :66
         TCK(cudaEventRecord(ev[3], s));
-        launch_density_filter(l0, c.t_dcs, r, c.t_dc, s);                          // :76
-        launch_density_filter(l0, c.t_dvs, r, c.t_dv, s);                          // :77
+        launch_density_filter(l0, c.t_dcs, r, c.t_fw, c.t_dc, s);                          // :76
+        launch_density_filter(l0, c.t_dvs, r, c.t_fw, c.t_dv, s);                          // :77
         cudaEvent_t evf;
         TCK(cudaEventCreate(&evf));
         TCK(cudaEventRecord(evf, s));
@@ -485,7 +487,7 @@ extern "C" int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const do
         cudaEvent_t evo;
         TCK(cudaEventCreate(&evo));
         TCK(cudaEventRecord(evo, s));
-        launch_density_filter(l0, c.t_x, r, c.t_tmp, s);                           // :99
+        launch_density_filter(l0, c.t_x, r, c.t_fw, c.t_tmp, s);                           // :99
         launch_div(l0, c.t_tmp, c.t_hs, c.t_xp, nb, s);
         TCK(cudaEventRecord(ev[4], s));
         launch_topo_modulus(l0, c.t_xp, o.penalty, o.E0, o.Emin, c.E, c.d_part, c.d_part2, nb, s);   // :52, :102
@@ -659,7 +661,7 @@ extern "C" int sgld_topopt_projected(sgld_ctx *ctx, const sgld_topopt_projected_
         // sensitivity of the normalised compliance through the projection (:136, :151-153)
         launch_heaviside(l0, c.t_tmp, beta, o.eta, nullptr, c.t_dvs, nb, s);
         launch_local_sens(l0, c.t_xp, c.t_ce, c.t_dvs, c.t_hs, penalty, o.E0, o.Emin, 1.0 / c_solid, c.t_dcs, nb, s);
-        launch_density_filter(l0, c.t_dcs, r, c.t_dc, s);
+        launch_density_filter(l0, c.t_dcs, r, c.t_fw, c.t_dc, s);
         TCK(cudaEventRecord(ev[3], s));
         double fval = 0.0, dg_scale = 1.0;
         if (local) {
@@ -669,7 +671,7 @@ extern "C" int sgld_topopt_projected(sgld_ctx *ctx, const sgld_topopt_projected_
             launch_pnorm(l0, c.t_q, o.pnorm, o.alpha, c.d_part, c.t_st + 12, N, c.t_dv, nb, s);
             if ((rc = pde_filter_dev(ctx, o.rhat, c.t_dv, c.t_q, pde_tol, pde_maxit, &its_pde))) return rc;
             launch_mul_div(l0, c.t_q, c.t_dvs, c.t_hs, c.t_dcs, nb, s);
-            launch_density_filter(l0, c.t_dcs, r, c.t_dv, s);
+            launch_density_filter(l0, c.t_dcs, r, c.t_fw, c.t_dv, s);
             double S = 0.0;
             TCK(cudaMemcpyAsync(&S, c.t_st + 12, sizeof(double), cudaMemcpyDeviceToHost, s));
             TCK(cudaStreamSynchronize(s));
@@ -678,7 +680,7 @@ extern "C" int sgld_topopt_projected(sgld_ctx *ctx, const sgld_topopt_projected_
             // volume: dv = filter(dx ./ Hs), dfdx = dv / (N V), fval = sum(xPhys) / (N V) - 1
             // (Global...m:119, :128-129, :139-141)
             launch_mul_div(l0, c.t_dvs, nullptr, c.t_hs, c.t_dcs, nb, s);
-            launch_density_filter(l0, c.t_dcs, r, c.t_dv, s);
+            launch_density_filter(l0, c.t_dcs, r, c.t_fw, c.t_dv, s);
             dg_scale = 1.0 / (N * o.volfrac);
             fval = vol / (N * o.volfrac) - 1.0;
         }
@@ -689,7 +691,7 @@ extern "C" int sgld_topopt_projected(sgld_ctx *ctx, const sgld_topopt_projected_
         launch_mma_scatter(d_var, nvar, xo, xv, c.t_x, c.d_part, nbm, s);
         launch_max_partials(c.d_part, nbm, c.t_st + T_CHANGE, s);
         // xTilde = filter(x) / Hs, xPhys = H(xTilde), passive 1 (:197-204)
-        launch_density_filter(l0, c.t_x, r, c.t_q, s);
+        launch_density_filter(l0, c.t_x, r, c.t_fw, c.t_q, s);
         launch_mul_div(l0, c.t_q, nullptr, c.t_hs, c.t_tmp, nb, s);
         launch_heaviside(l0, c.t_tmp, beta, o.eta, c.t_xp, nullptr, nb, s);
         TCK(cudaEventRecord(ev[4], s));

@@ -131,3 +131,53 @@ def test_contexts_of_different_materials_alternate(built_lib, monkeypatch):
     assert not np.allclose(alone_a[0], alone_b[0])
     a.close()
     b.close()
+
+
+def test_contexts_of_one_material_in_threads(built_lib, monkeypatch):
+    """Contexts of equal element matrices may be used from concurrent host
+    threads (ctypes releases the GIL during each call).  Two contexts run a
+    mixed solve, a density filter and a PDE filter with different radii at the
+    same time; every result matches the same calls made one after another."""
+    import threading
+
+    from sgldbench_gb300 import VoxelSolver
+    from sgldbench_gb300 import domains as D
+
+    monkeypatch.setenv("SGLD_AUTOTUNE", "0")
+    vox = D.cuboid(32, 16, 16)
+    rng = np.random.default_rng(4)
+
+    def make(seed):
+        s = VoxelSolver(vox, num_levels=3, non_dyadic=0, omega=0.6, pad=False)
+        F, fixed = D.cantilever3(vox, s.nodMapBack(1))
+        s.set_fixed_dofs(fixed)
+        s.set_modulus(np.random.default_rng(seed).uniform(0.2, 1.0, s.numElements))
+        s.Solving_AssembleFEAstencil()
+        return s, F
+
+    x = rng.random(32 * 16 * 16)
+    jobs = [(make(1), 1.5, 2.0), (make(2), 3.0, 4.0)]
+
+    def work(job):
+        (s, F), rmin, rhat = job
+        U, _ = s.pcg(F, tol=1e-8, maxIT=300, precision="mixed")
+        return U, s.TopOpti_PerformDensityFiltering(x, rmin), s.TopOpti_PDEFiltering(x, rhat, tol=1e-10)[0]
+
+    alone = [work(j) for j in jobs]
+    for _ in range(3):
+        got = [None, None]
+
+        def run(i):
+            got[i] = work(jobs[i])
+
+        ts = [threading.Thread(target=run, args=(i,)) for i in range(2)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        for g, a in zip(got, alone):
+            assert g is not None
+            for u, v in zip(g, a):
+                assert np.array_equal(u, v)
+    for (s, _), _, _ in jobs:
+        s.close()

@@ -171,6 +171,13 @@ int sgld_reference_num_levels(int64_t num_voxels, int64_t coarsest_resolution_co
  * Solving_BuildingMeshHierarchy.m:9-165 (coarse levels). */
 int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_options *opts, sgld_ctx **out);
 void sgld_destroy(sgld_ctx *ctx);
+/* Solving_BuildingMeshHierarchy.m:1-175 as a call of its own: rebuilds the
+ * context's coarse levels for num_levels / non_dyadic (the numLevels_ and
+ * nonDyadic_ globals it reads) from the context's own voxel grid, keeping
+ * its material, omega and any Ke set by sgld_set_ke.  As after sgld_create,
+ * fixed DOFs, moduli and passive elements must then be set again.  On error
+ * the context is unchanged. */
+int sgld_build_hierarchy(sgld_ctx *ctx, int num_levels, int non_dyadic);
 const char *sgld_last_error(const sgld_ctx *ctx);
 
 /* Sizes of level `level` (1 = finest, as meshHierarchy_(level)). */
@@ -225,6 +232,14 @@ int sgld_interpolate(sgld_ctx *ctx, int ii, const double *x_coarse, double *x_fi
 /* Solving_Vcycle.m:1-52: z = M^-1 r (additive multilevel Jacobi + coarsest solve). */
 int sgld_vcycle(sgld_ctx *ctx, const double *r, double *z);
 
+/* K*u and the V-cycle at a chosen precision (SGLD_PREC_*), the operators the
+ * solve modes use: FP64 (the reference form; = sgld_kbyu / sgld_vcycle);
+ * SGLD_PREC_MIXED: K*u in FP32 on FP32 copies of u and the moduli, the FP32
+ * V-cycle; SGLD_PREC_MIXED_DF: K*u in double-float (= sgld_kbyu_df), the FP32
+ * V-cycle.  Inputs and outputs stay FP64 compact vectors. */
+int sgld_kbyu_prec(sgld_ctx *ctx, const double *u, double *y, int precision);
+int sgld_vcycle_prec(sgld_ctx *ctx, const double *r, double *z, int precision);
+
 /* Solving_PreconditionedConjugateGradientSolver.m:1-37 with AtX = KbyU and
  * PtV = Vcycle (as Solving_CG_GMGS.m:7 binds them).  x: in = initial guess when
  * opts->use_x0, out = solution. */
@@ -242,6 +257,12 @@ int sgld_pcg(sgld_ctx *ctx, const double *b, double *x, const sgld_solve_opts *o
  * another. */
 int sgld_solve_block(sgld_ctx *ctx, int nrhs, const double *F, double *U, const sgld_solve_opts *opts,
                      sgld_solve_info *info);
+/* Solving_CG_GMGS.m:1-9 for nrhs load cases with plain arguments: sgld_solve_block
+ * from U = 0 with tol, maxit and precision; its[j] and relres[j] (either may be
+ * NULL) receive case j's iteration count and relative residual, as the
+ * reference's `its` and the final ||r||/||b||. */
+int sgld_solve(sgld_ctx *ctx, int nrhs, const double *F, double *U, double tol, int maxit, int precision, int *its,
+               double *relres);
 int sgld_pcg_device(sgld_ctx *ctx, const double *d_b, double *d_x, const sgld_solve_opts *opts,
                     sgld_solve_info *info);
 
@@ -404,6 +425,9 @@ int sgld_topopt_projected(sgld_ctx *ctx, const sgld_topopt_projected_opts *opts,
  * von Mises and per-element von Mises with the reference's final .^(1/2).
  * Any output may be NULL. */
 int sgld_stress(sgld_ctx *ctx, const double *U, double *nodal_stress, double *vm_node, double *vm_elem);
+/* The von Mises part of sgld_stress alone: per element (numElements) and per
+ * node (numNodes); either may be NULL. */
+int sgld_vonmises(sgld_ctx *ctx, const double *U, double *vm_elem, double *vm_node);
 
 /* Principal stresses of the nodal Cartesian stress field of U
  * (FEA_ComputePrincipalStress.m:1-8 per node): ps_node is numNodes x 12,

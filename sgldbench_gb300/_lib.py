@@ -80,6 +80,9 @@ SIGNATURES = {
     "sgld_get_ks": (i32, [vp, i32, vp]),
     "sgld_kbyu": (i32, [vp, vp, vp]),
     "sgld_kbyu_df": (i32, [vp, vp, vp]),
+    "sgld_kbyu_prec": (i32, [vp, vp, vp, i32]),
+    "sgld_vcycle_prec": (i32, [vp, vp, vp, i32]),
+    "sgld_build_hierarchy": (i32, [vp, i32, i32]),
     "sgld_kbyu_device": (i32, [vp, vp, vp]),
     "sgld_restrict": (i32, [vp, i32, vp, vp]),
     "sgld_interpolate": (i32, [vp, i32, vp, vp]),
@@ -87,8 +90,10 @@ SIGNATURES = {
     "sgld_pcg": (i32, [vp, vp, vp, vp, vp]),
     "sgld_pcg_device": (i32, [vp, vp, vp, vp, vp]),
     "sgld_solve_block": (i32, [vp, i32, vp, vp, vp, vp]),
+    "sgld_solve": (i32, [vp, i32, vp, vp, dbl, i32, i32, vp, vp]),
     "sgld_compliance": (i32, [vp, vp, vp, vp]),
     "sgld_stress": (i32, [vp, vp, vp, vp, vp]),
+    "sgld_vonmises": (i32, [vp, vp, vp, vp]),
     "sgld_principal_stress": (i32, [vp, vp, vp, vp]),
     "sgld_pde_filter": (i32, [vp, dbl, vp, vp, dbl, i32, vp]),
     "sgld_mma_update": (i32, [vp, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),

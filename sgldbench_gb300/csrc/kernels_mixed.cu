@@ -331,4 +331,14 @@ void launch_narrow(const double *a, float *b, int64_t n, cudaStream_t st) {
     k_narrow<<<reduce_blocks(n), MB, 0, st>>>(a, b, n);
 }
 
+// r64 = (double) r32
+__global__ void k_widen(const float *__restrict__ a, double *__restrict__ b, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)MB + threadIdx.x; i < n; i += (int64_t)gridDim.x * MB) b[i] = (double)a[i];
+}
+
+void launch_widen(const float *a, double *b, int64_t n, cudaStream_t st) {
+    ++g_launches;
+    k_widen<<<reduce_blocks(n), MB, 0, st>>>(a, b, n);
+}
+
 }  // namespace sgld

@@ -1417,6 +1417,89 @@ int sgld_principal_stress(sgld_ctx *ctx, const double *U, double *ps_node, doubl
     return SGLD_OK;
 }
 
+int sgld_kbyu_prec(sgld_ctx *ctx, const double *u, double *y, int precision) {
+    if (precision == SGLD_PREC_FP64) return sgld_kbyu(ctx, u, y);
+    if (precision == SGLD_PREC_MIXED_DF) return sgld_kbyu_df(ctx, u, y);
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (precision != SGLD_PREC_MIXED) return fail(ctx, SGLD_ERR_ARG, "unknown precision mode");
+    if (!u || !y) return fail(ctx, SGLD_ERR_ARG, "null vector");
+    Ctx &c = ctx->c;
+    const Level &l0 = c.lv[0];
+    const int64_t nv = 3 * l0.nnode;
+    if ((rc = upload_nodes(ctx, u, c.d_p))) return rc;
+    launch_cast_f32(c.E, c.d_E32, l0.nel, c.stream);
+    launch_narrow(c.d_p, c.d_r32, nv, c.stream);
+    launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, c.stream);
+    launch_widen(c.d_t32, c.d_q, nv, c.stream);
+    CKL();
+    return download_nodes(ctx, c.d_q, y);
+}
+
+int sgld_vcycle_prec(sgld_ctx *ctx, const double *r, double *z, int precision) {
+    if (precision == SGLD_PREC_FP64) return sgld_vcycle(ctx, r, z);
+    int rc = check_assembled(ctx);
+    if (rc) return rc;
+    if (precision != SGLD_PREC_MIXED && precision != SGLD_PREC_MIXED_DF)
+        return fail(ctx, SGLD_ERR_ARG, "unknown precision mode");
+    if (!r || !z) return fail(ctx, SGLD_ERR_ARG, "null vector");
+    Ctx &c = ctx->c;
+    const int64_t nv = 3 * c.lv[0].nnode;
+    if ((rc = upload_nodes(ctx, r, c.d_p))) return rc;
+    launch_narrow(c.d_p, c.d_r32, nv, c.stream);
+    if ((rc = vcycle_dev32(ctx, c.d_r32, c.d_z32, nullptr, nullptr))) return rc;
+    launch_widen(c.d_z32, c.d_z, nv, c.stream);
+    CKL();
+    return download_nodes(ctx, c.d_z, z);
+}
+
+int sgld_build_hierarchy(sgld_ctx *ctx, int num_levels, int non_dyadic) {
+    if (!ctx) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
+    Ctx &c = ctx->c;
+    const Level &l0 = c.lv[0];
+    sgld_options o;
+    sgld_default_options(&o);
+    o.num_levels = num_levels;
+    o.non_dyadic = non_dyadic;
+    o.poisson_ratio = c.nu;
+    o.cell_size = c.cell;
+    o.omega = c.omega;
+    o.device = c.device;
+    sgld_ctx *fresh = nullptr;
+    int rc = sgld_create(l0.ny, l0.nx, l0.nz, l0.h_eact.data(), &o, &fresh);
+    if (rc == SGLD_OK && memcmp(fresh->c.Ke, c.Ke, sizeof c.Ke) != 0) rc = sgld_set_ke(fresh, c.Ke);
+    if (rc != SGLD_OK) {
+        c.err = fresh ? fresh->c.err : std::string("sgld_build_hierarchy: create failed");
+        sgld_destroy(fresh);
+        return rc;
+    }
+    std::swap(*ctx, *fresh);   // the handle keeps its address; the old levels go with `fresh`
+    sgld_destroy(fresh);
+    return bind_ctx(ctx);
+}
+
+int sgld_solve(sgld_ctx *ctx, int nrhs, const double *F, double *U, double tol, int maxit, int precision, int *its,
+               double *relres) {
+    sgld_solve_opts o;
+    memset(&o, 0, sizeof o);
+    o.tol = tol;
+    o.maxit = maxit;
+    o.precision = precision;
+    std::vector<sgld_solve_info> infos((size_t)std::max(nrhs, 1));
+    const int rc = sgld_solve_block(ctx, nrhs, F, U, &o, infos.data());
+    if (rc) return rc;
+    for (int i = 0; i < nrhs; ++i) {
+        if (its) its[i] = infos[i].iterations;
+        if (relres) relres[i] = infos[i].relres;
+    }
+    return SGLD_OK;
+}
+
+int sgld_vonmises(sgld_ctx *ctx, const double *U, double *vm_elem, double *vm_node) {
+    return sgld_stress(ctx, U, nullptr, vm_node, vm_elem);
+}
+
 }  // extern "C"
 
 // =============================================================================

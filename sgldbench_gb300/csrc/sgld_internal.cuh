@@ -191,6 +191,7 @@ void launch_widen_dots(const float *e, const float *d, const double *sc, double 
 void launch_flex_beta(double *scal, const int *iflag, const double *p1, const double *p2, int nb, int first,
                       cudaStream_t st);
 void launch_narrow(const double *a, float *b, int64_t n, cudaStream_t st);
+void launch_widen(const float *a, double *b, int64_t n, cudaStream_t st);
 }  // namespace sgld
 struct sgld_solve_opts;
 struct sgld_solve_info;

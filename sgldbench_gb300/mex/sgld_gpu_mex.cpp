@@ -9,9 +9,12 @@
  *        FEA_VoxelBasedDiscretization.m + Solving_BuildingMeshHierarchy.m (padded grid)
  *   sgld_gpu_mex('fixed', fixedDOFs)            FEA_SetupVoxelBased.m:13-26 (logical numDOFs)
  *   sgld_gpu_mex('modulus', eleModulus)         meshHierarchy_(1).eleModulus
+ *   nLev = sgld_gpu_mex('hierarchy', numLevels[, nonDyadic])
+ *                                               Solving_BuildingMeshHierarchy.m (rebuild)
  *   sgld_gpu_mex('assemble')                    Solving_AssembleFEAstencil.m
- *   y = sgld_gpu_mex('kbyu', u)                 Solving_KbyU_MatrixFree.m
- *   z = sgld_gpu_mex('vcycle', r)               Solving_Vcycle.m
+ *   y = sgld_gpu_mex('kbyu', u[, precision])    Solving_KbyU_MatrixFree.m
+ *   z = sgld_gpu_mex('vcycle', r[, precision])  Solving_Vcycle.m
+ *       precision as for pcg: the operator that solve mode applies
  *   [U, its] = sgld_gpu_mex('pcg', F, tol, maxIT[, U0[, 'fp64' | 'mixed' | 'mixed64']])
  *       'mixed' = SGLD_PREC_MIXED_DF, 'mixed64' = SGLD_PREC_MIXED
  *                                               Solving_PreconditionedConjugateGradientSolver.m
@@ -43,6 +46,18 @@ static void release_ctx(void) {
 
 static void check(int rc) {
     if (rc != SGLD_OK) mexErrMsgIdAndTxt("sgld:gpu", "%s", g_ctx ? sgld_last_error(g_ctx) : "no context");
+}
+
+// 'fp64' (the reference form), 'mixed' (FP32 inner operators with the
+// double-float outer K*u) or 'mixed64' (FP32 inner, FP64 outer) -> SGLD_PREC_*
+static int precision_arg(const mxArray *a) {
+    char mode[16] = {0};
+    mxGetString(a, mode, sizeof mode);
+    if (!strcmp(mode, "fp64")) return SGLD_PREC_FP64;
+    if (!strcmp(mode, "mixed")) return SGLD_PREC_MIXED_DF;
+    if (!strcmp(mode, "mixed64")) return SGLD_PREC_MIXED;
+    mexErrMsgIdAndTxt("sgld:arg", "precision must be 'fp64', 'mixed' or 'mixed64'");
+    return SGLD_PREC_FP64;
 }
 
 static void need_ctx() {
@@ -126,10 +141,19 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
         check(sgld_set_modulus(g_ctx, dvec(prhs[1], nel, "eleModulus")));
     } else if (!strcmp(cmd, "assemble")) {
         check(sgld_assemble(g_ctx));
+    } else if (!strcmp(cmd, "hierarchy")) {
+        // Solving_BuildingMeshHierarchy() for numLevels_ / nonDyadic_; fixed DOFs
+        // and moduli are set again afterwards
+        if (nrhs < 2) mexErrMsgIdAndTxt("sgld:arg", "hierarchy needs numLevels [, nonDyadic]");
+        check(sgld_build_hierarchy(g_ctx, (int)mxGetScalar(prhs[1]), nrhs > 2 ? (int)mxGetScalar(prhs[2]) : 0));
+        if (nlhs > 0) plhs[0] = mxCreateDoubleScalar(sgld_num_levels(g_ctx));
     } else if (!strcmp(cmd, "kbyu") || !strcmp(cmd, "vcycle")) {
+        // optional third argument: the operator of a solve mode (precision_arg)
         const double *u = dvec(prhs[1], ndof, "vector");
+        const int prec = nrhs > 2 ? precision_arg(prhs[2]) : SGLD_PREC_FP64;
         plhs[0] = mxCreateDoubleMatrix(ndof, 1, mxREAL);
-        check(cmd[0] == 'k' ? sgld_kbyu(g_ctx, u, mxGetPr(plhs[0])) : sgld_vcycle(g_ctx, u, mxGetPr(plhs[0])));
+        check(cmd[0] == 'k' ? sgld_kbyu_prec(g_ctx, u, mxGetPr(plhs[0]), prec)
+                            : sgld_vcycle_prec(g_ctx, u, mxGetPr(plhs[0]), prec));
     } else if (!strcmp(cmd, "pcg")) {
         if (nrhs < 4) mexErrMsgIdAndTxt("sgld:arg", "pcg needs F, tol, maxIT");
         const double *F = dvec(prhs[1], ndof, "F");
@@ -143,13 +167,7 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
             memcpy(mxGetPr(plhs[0]), dvec(prhs[4], ndof, "U0"), ndof * sizeof(double));
             o.use_x0 = 1;
         }
-        if (nrhs > 5) {
-            char mode[16] = {0};
-            mxGetString(prhs[5], mode, sizeof mode);
-            if (!strcmp(mode, "mixed")) o.precision = SGLD_PREC_MIXED_DF;
-            else if (!strcmp(mode, "mixed64")) o.precision = SGLD_PREC_MIXED;
-            else if (strcmp(mode, "fp64")) mexErrMsgIdAndTxt("sgld:arg", "precision must be 'fp64', 'mixed' or 'mixed64'");
-        }
+        if (nrhs > 5) o.precision = precision_arg(prhs[5]);
         sgld_solve_info info;
         check(sgld_pcg(g_ctx, F, mxGetPr(plhs[0]), &o, &info));
         if (nlhs > 1) plhs[1] = mxCreateDoubleScalar(info.iterations);

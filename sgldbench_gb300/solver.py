@@ -207,10 +207,15 @@ class VoxelSolver:
             raise ValueError(f"vector must have {n} entries, got {a.size}")
         return a
 
-    def Solving_KbyU_MatrixFree(self, uVec) -> np.ndarray:
+    def Solving_KbyU_MatrixFree(self, uVec, precision: str = "fp64") -> np.ndarray:
+        """K u; ``precision`` 'mixed' applies the FP32 operator of the inner
+        solve, 'mixed_df' the double-float one (sgld_kbyu_prec)."""
         u = self._vec(uVec, self.numDOFs)
         y = np.zeros_like(u)
-        self._check(self.lib.sgld_kbyu(self.ctx, _p(u), _p(y)))
+        if precision == "fp64":
+            self._check(self.lib.sgld_kbyu(self.ctx, _p(u), _p(y)))
+        else:
+            self._check(self.lib.sgld_kbyu_prec(self.ctx, _p(u), _p(y), _precision(precision)))
         return y
 
     def kbyu_double_float(self, uVec) -> np.ndarray:
@@ -232,11 +237,23 @@ class VoxelSolver:
         self._check(self.lib.sgld_interpolate(self.ctx, ii, _p(x), _p(out)))
         return out
 
-    def Solving_Vcycle(self, r) -> np.ndarray:
+    def Solving_Vcycle(self, r, precision: str = "fp64") -> np.ndarray:
+        """z = M^-1 r; ``precision`` 'mixed' / 'mixed_df' applies the FP32 V-cycle
+        of the inner solve (sgld_vcycle_prec)."""
         rv = self._vec(r, self.numDOFs)
         z = np.zeros_like(rv)
-        self._check(self.lib.sgld_vcycle(self.ctx, _p(rv), _p(z)))
+        if precision == "fp64":
+            self._check(self.lib.sgld_vcycle(self.ctx, _p(rv), _p(z)))
+        else:
+            self._check(self.lib.sgld_vcycle_prec(self.ctx, _p(rv), _p(z), _precision(precision)))
         return z
+
+    def Solving_BuildingMeshHierarchy(self, num_levels: int, non_dyadic: int = 0):
+        """Rebuilds the coarse levels for another level count (sgld_build_hierarchy).
+        Fixed DOFs and moduli must be set again afterwards."""
+        self._check(self.lib.sgld_build_hierarchy(self.ctx, int(num_levels), int(non_dyadic)))
+        self.numLevels = int(self.lib.sgld_num_levels(self.ctx))
+        self.levels = [self.level_info(i + 1) for i in range(self.numLevels)]
 
     def pcg(self, b, tol: float = 1e-3, maxIT: int = 500, x0=None, precision: str = "fp64",
             inner_its: int = 0, history: bool = False, inner_tol: float = 0.0, out=None):
@@ -347,6 +364,26 @@ class VoxelSolver:
         c = C.c_double()
         self._check(self.lib.sgld_compliance(self.ctx, _p(u), _p(ce), C.byref(c)))
         return ce, c.value
+
+    def solve(self, F, tol: float = 1e-6, maxIT: int = 500, precision: str = "fp64"):
+        """sgld_solve: F is (nrhs, numDOFs) or one vector; returns (U, its, relres)
+        with one entry per load case."""
+        Fb = np.ascontiguousarray(np.asarray(F, dtype=np.float64).reshape(-1, self.numDOFs))
+        nrhs = Fb.shape[0]
+        U = np.empty_like(Fb)
+        its = np.zeros(nrhs, np.int32)
+        relres = np.zeros(nrhs)
+        self._check(self.lib.sgld_solve(self.ctx, nrhs, _p(Fb), _p(U), float(tol), int(maxIT),
+                                        _precision(precision), _p(its), _p(relres)))
+        return U, its, relres
+
+    def vonmises(self, U):
+        """sgld_vonmises: (per-element von Mises, per-node von Mises)."""
+        u = self._vec(U, self.numDOFs)
+        vme = np.zeros(self.numElements)
+        vmn = np.zeros(self.numNodes)
+        self._check(self.lib.sgld_vonmises(self.ctx, _p(u), _p(vme), _p(vmn)))
+        return vme, vmn
 
     def FEA_StressAnalysis(self, U):
         """Returns (cartesianStressField numNodes x 6, vonMises per node,

@@ -4,7 +4,8 @@
   oracle's MEX API stand-in and driven the way MATLAB calls it (mxArrays in,
   mxArrays out): create / fixed / modulus / assemble / kbyu / vcycle / pcg /
   compliance / stress / filter, checked against the oracle, and its error
-  behaviour (mexErrMsgIdAndTxt) on bad input.
+  behaviour (mexErrMsgIdAndTxt) on bad input; the callers' commands; kbyu and
+  vcycle with a precision argument and the hierarchy rebuild; clear mex.
 * The standalone harness (sgldbench_gb300/harness/sgld_harness.cpp) on config 0.
 """
 import json
@@ -175,3 +176,37 @@ def test_gateway_clear_releases_context(gateway):
     M.call("sgld_gpu_mex", 1, "create", padded, float(nlev0), 1.0, 0.3, 1.0, 0.6)
     M.call("sgld_gpu_mex", 0, "destroy")
     M.clear()   # nothing left to release
+
+
+def test_gateway_precision_and_hierarchy(gateway):
+    """'kbyu' / 'vcycle' with a precision argument give the library's
+    operators of that solve mode; 'hierarchy' rebuilds the levels."""
+    from sgldbench_gb300 import VoxelSolver
+
+    M = gateway
+    vox = np.ones((8, 16, 8), bool)
+    m = G.build_model(vox, omega=0.6)
+    _, nlev0, padded, _ = G.voxel_discretization(vox)
+    assert int(np.asarray(M.call("sgld_gpu_mex", 1, "create", padded, float(nlev0), 0.0, 0.3, 1.0, 0.6)).ravel()[0]) == nlev0
+    l1 = m.levels[0]
+    E = np.random.default_rng(5).uniform(0.3, 1.0, l1.numElements)
+    s = VoxelSolver(padded, num_levels=nlev0, non_dyadic=0, omega=0.6, pad=False)
+    M.call("sgld_gpu_mex", 0, "fixed", l1.fixedDOFs)
+    M.call("sgld_gpu_mex", 0, "modulus", E)
+    M.call("sgld_gpu_mex", 0, "assemble")
+    s.set_fixed_dofs(l1.fixedDOFs)
+    s.set_modulus(E)
+    s.Solving_AssembleFEAstencil()
+    u = np.random.default_rng(6).standard_normal(s.numDOFs)
+    for mode, prec in (("fp64", "fp64"), ("mixed", "mixed_df"), ("mixed64", "mixed")):
+        y = M.call("sgld_gpu_mex", 1, "kbyu", u, mode).ravel()
+        assert np.array_equal(y, s.Solving_KbyU_MatrixFree(u, prec))
+        z = M.call("sgld_gpu_mex", 1, "vcycle", u, mode).ravel()
+        assert np.array_equal(z, s.Solving_Vcycle(u, prec))
+    with pytest.raises(mexcall.MexError, match="precision"):
+        M.call("sgld_gpu_mex", 1, "kbyu", u, "half")
+    assert int(np.asarray(M.call("sgld_gpu_mex", 1, "hierarchy", 2.0)).ravel()[0]) == 2
+    with pytest.raises(mexcall.MexError):
+        M.call("sgld_gpu_mex", 1, "hierarchy", 1.0)
+    s.close()
+    M.call("sgld_gpu_mex", 0, "destroy")

@@ -148,18 +148,33 @@ def cpu_time_to_solve(vox, E, levels, its_full, sample_iters, steps=1, warmup=0)
     m = G.build_model(vox, non_dyadic=0, omega=OMEGA, num_levels=levels)
     t_setup = time.perf_counter() - t0
     G.set_modulus(m, E)
+    spent = {"kbyu": 0.0, "vcycle": 0.0}
+
+    def timed(name, fn):
+        def call(v):
+            t = time.perf_counter()
+            out = fn(v)
+            spent[name] += time.perf_counter() - t
+            return out
+        return call
+
+    AtX = timed("kbyu", lambda u: G.kbyu(m, u))
+    PtV = timed("vcycle", lambda r: G.vcycle(m, r))
     times = []
     for k in range(warmup + steps):
         t0 = time.perf_counter()
         G.assemble_stencil(m)
+        spent["kbyu"] = spent["vcycle"] = 0.0
         t1 = time.perf_counter()
-        G.pcg(lambda u: G.kbyu(m, u), lambda r: G.vcycle(m, r), m.F, 0.0, sample_iters)
+        G.pcg(AtX, PtV, m.F, 0.0, sample_iters)
         t2 = time.perf_counter()
         if k >= warmup:
-            times.append((t1 - t0, (t2 - t1) / sample_iters))
-    t_asm = float(np.mean([a for a, _ in times]))
-    t_it = float(np.mean([b for _, b in times]))
-    return {"seconds": t_asm + t_it * its_full, "assemble_s": t_asm, "iter_s": t_it, "setup_s": t_setup,
+            times.append((t1 - t0, (t2 - t1) / sample_iters, spent["kbyu"] / sample_iters,
+                          spent["vcycle"] / sample_iters))
+    t_asm, t_it, t_kbyu, t_vc = (float(np.mean([t[i] for t in times])) for i in range(4))
+    # the SpMV / PtV / rest split of QuickAccess/zTmp_Benchmarking_SpMV.m:63-111, per iteration
+    return {"seconds": t_asm + t_it * its_full, "assemble_s": t_asm, "iter_s": t_it, "kbyu_s": t_kbyu,
+            "vcycle_s": t_vc, "glue_s": t_it - t_kbyu - t_vc, "setup_s": t_setup,
             "levels": m.numLevels, "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))}
 
 

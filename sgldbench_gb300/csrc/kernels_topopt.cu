@@ -5,9 +5,9 @@
 //
 // Element fields live on the finest level's full element grid (inactive = 0).
 // The filter weights max(0, rmin - |d|) depend only on the offset d, so they
-// are formed once on the host with the reference's expression and kept in
-// constant memory; the kernel sums over the box in the reference's loop
-// order (z outer, x, y inner).
+// are formed once on the host with the reference's expression and kept in a
+// small device buffer of the context; the kernel sums over the box in the
+// reference's loop order (z outer, x, y inner).
 #include <math.h>
 
 #include <algorithm>

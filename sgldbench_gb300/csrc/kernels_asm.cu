@@ -37,6 +37,11 @@ static int current_device() {
     return dev;
 }
 
+void forget_asm_tables(int dev) {
+    g_pairs_done[dev] = false;
+    g_weights_done[dev] = false;
+}
+
 static void upload_pairs(cudaStream_t s) {
     std::atomic<bool> &done = g_pairs_done[current_device()];
     if (done) return;

@@ -8,6 +8,8 @@
 // scratch (one partial sum per CTA of the K*u grid) lives in the file-scope
 // device array below, which every GPU that loads this library holds until the
 // process exits.  The call itself allocates nothing.
+#include <atomic>
+
 #include "../../include/sgld_gpu.h"
 #include "sgld_internal.cuh"
 
@@ -23,8 +25,10 @@ using namespace sgld;
 static __device__ __align__(256) double g_noalloc_partial[SGLD_NOALLOC_MAX_CTAS];
 
 namespace {
-double *g_partial_addr[kMaxDevices] = {};   // device address of the array, per device
+std::atomic<double *> g_partial_addr[kMaxDevices];   // device address of the array, per device
 }  // namespace
+
+void sgld::forget_noalloc_scratch(int dev) { g_partial_addr[dev] = nullptr; }
 
 extern "C" int sgld_kbyu_dot_noalloc(sgld_ctx *ctx, const double *d_u, double *d_y, double *d_dot, void *stream) {
     if (!ctx || !d_u || !d_y || !d_dot) return SGLD_ERR_ARG;

@@ -576,6 +576,7 @@ namespace sgld {
 namespace {
 std::mutex g_bind_mu;
 bool g_kh_valid[kMaxDevices] = {};
+bool g_kh_stale[kMaxDevices] = {};      // upload again even if the record matches (after a create)
 double g_kh_held[kMaxDevices][KH_NNZ];   // the element matrix in each device's constants
 }  // namespace
 
@@ -585,16 +586,28 @@ int bind_ctx(sgld_ctx *ctx) {
     CK(cudaGetDevice(&dev));
     if (dev != c.device) CK(cudaSetDevice(c.device));
     std::lock_guard<std::mutex> lock(g_bind_mu);
-    if (g_kh_valid[c.device] && memcmp(g_kh_held[c.device], c.Kh, sizeof c.Kh) == 0) return SGLD_OK;
-    // another context's matrix is held: its queued kernels still read it
-    if (g_kh_valid[c.device]) CK(cudaDeviceSynchronize());
+    const bool same = g_kh_valid[c.device] && memcmp(g_kh_held[c.device], c.Kh, sizeof c.Kh) == 0;
+    if (same && !g_kh_stale[c.device]) return SGLD_OK;
+    // another context's matrix is held: its queued kernels still read it.  (Rewriting
+    // the same values under running kernels is harmless.)
+    if (g_kh_valid[c.device] && !same) CK(cudaDeviceSynchronize());
     g_kh_valid[c.device] = false;
     upload_kh(c.Kh, c.stream);
     upload_kh_df(c.Kh, c.stream);
     CK(cudaStreamSynchronize(c.stream));
     memcpy(g_kh_held[c.device], c.Kh, sizeof c.Kh);
     g_kh_valid[c.device] = true;
+    g_kh_stale[c.device] = false;
     return SGLD_OK;
+}
+
+void forget_device_tables(int dev) {
+    {
+        std::lock_guard<std::mutex> lock(g_bind_mu);
+        g_kh_stale[dev] = true;
+    }
+    forget_asm_tables(dev);
+    forget_noalloc_scratch(dev);
 }
 
 bool kh_bound(const Ctx &c) {
@@ -686,6 +699,7 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
     *out = ctx;
     if (c.device < 0 || c.device >= kMaxDevices) return fail(ctx, SGLD_ERR_ARG, "device ordinal out of range");
     if (cudaSetDevice(c.device) != cudaSuccess) return fail(ctx, SGLD_ERR_CUDA, "cudaSetDevice failed");
+    forget_device_tables(c.device);   // the device may have been reset since the last create
     CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
     for (auto &a : c.aux) CK(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
     // element / node activity per level (host)

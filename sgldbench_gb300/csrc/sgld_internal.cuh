@@ -208,6 +208,14 @@ constexpr int kMaxDevices = 64;
 int bind_ctx(sgld_ctx *ctx);
 // true if the constants on the current device hold c's element matrix
 bool kh_bound(const Ctx &c);
+// sgld_create calls this for its device: a device reset (cudaDeviceReset, or
+// MATLAB's reset(gpuDevice)) clears every __constant__ table and module
+// address, while the host-side records of what each device holds survive it.
+// Creation therefore uploads the element matrix again and makes the assembly
+// tables and the allocation-free scratch address be set up anew on first use.
+void forget_device_tables(int dev);
+void forget_asm_tables(int dev);       // kernels_asm.cu
+void forget_noalloc_scratch(int dev);  // noalloc.cu
 // PCG on the context's own full-grid vectors d_b / d_x (sgld_api.cu)
 int solve_on_device(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info);
 // FP64 additive V-cycle z = M r on full-grid vectors; with partial, the CTA

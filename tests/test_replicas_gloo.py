@@ -31,7 +31,9 @@ def _worker(rank, world, port, out):
 def test_aggregate_two_ranks():
     port = _free_port()
     world = 2
-    with mp.Manager() as mgr:
+    # the manager's server process is spawned too: forking a process that already
+    # runs threads (torch's) can deadlock the child
+    with mp.get_context("spawn").Manager() as mgr:
         out = mgr.dict()
         mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)

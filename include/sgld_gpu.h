@@ -110,7 +110,9 @@ typedef struct sgld_solve_info {
  * NaN (until the next sgld_assemble).  kind 0: no-op.  Faults no GPU. */
 int sgld_inject_fault(sgld_ctx *ctx, int kind);
 
-/* The CUDA stream every call of this context runs on (a cudaStream_t). */
+/* The CUDA stream every call of this context runs on (a cudaStream_t).  No
+ * counterpart in the reference, whose solve runs on the host: it lets a caller
+ * order its own device work after the library's. */
 void *sgld_get_stream(const sgld_ctx *ctx);
 
 /* Number of CUDA kernels this library has launched from the calling thread
@@ -180,12 +182,16 @@ void sgld_destroy(sgld_ctx *ctx);
 int sgld_build_hierarchy(sgld_ctx *ctx, int num_levels, int non_dyadic);
 const char *sgld_last_error(const sgld_ctx *ctx);
 
-/* Sizes of level `level` (1 = finest, as meshHierarchy_(level)). */
+/* Sizes of level `level` (1 = finest, as meshHierarchy_(level)): resY/resX/resZ,
+ * spanWidth, numElements and numNodes as FEA_VoxelBasedDiscretization.m:56-82
+ * (level 1) and Solving_BuildingMeshHierarchy.m:24-34,104-122 set them; the
+ * level count is numLevels_ (Solving_BuildingMeshHierarchy.m:13). */
 int sgld_level_info(const sgld_ctx *ctx, int level, int res_yxz[3], int *span, int64_t *num_elements,
                     int64_t *num_nodes);
 int sgld_num_levels(const sgld_ctx *ctx);
 /* 1-based full-grid indices of the compact nodes / elements of a level
- * (nodMapBack / eleMapBack of that level, in that level's own grid). */
+ * (nodMapBack / eleMapBack of that level, in that level's own grid:
+ * FEA_VoxelBasedDiscretization.m:63,81, Solving_BuildingMeshHierarchy.m:104,122). */
 int sgld_node_map(const sgld_ctx *ctx, int level, int64_t *map);
 int sgld_element_map(const sgld_ctx *ctx, int level, int64_t *map);
 
@@ -199,7 +205,8 @@ int sgld_set_ke(sgld_ctx *ctx, const double *Ke);
  * FEA_ApplyBoundaryCondition.m:37-41; also derives the coarse masks as
  * FEA_SetupVoxelBased.m:13-26 does. */
 int sgld_set_fixed_dofs(sgld_ctx *ctx, const uint8_t *fixed);
-/* Coarse-level free-DOF mask of `level` (numDOFs of that level). */
+/* Coarse-level free-DOF mask of `level` (numDOFs of that level): meshHierarchy_(level).freeDOFs
+ * of FEA_SetupVoxelBased.m:13-19 as a mask. */
 int sgld_get_free_dofs(const sgld_ctx *ctx, int level, uint8_t *free_mask);
 
 /* Element moduli (numElements): meshHierarchy_(1).eleModulus
@@ -210,9 +217,10 @@ int sgld_set_modulus_device(sgld_ctx *ctx, const double *d_E);
 /* Solving_AssembleFEAstencil.m:7-135: Galerkin coarse element matrices, Jacobi
  * diagonals, coarsest-level factorization. */
 int sgld_assemble(sgld_ctx *ctx);
-/* Jacobi diagonal diagK of `level` (1..L-1), compact numDOFs. */
+/* Jacobi diagonal diagK of `level` (1..L-1), compact numDOFs (Solving_AssembleFEAstencil.m:24-96). */
 int sgld_get_diag(const sgld_ctx *ctx, int level, double *diag);
-/* Galerkin element matrices Ks of coarse `level` (2..L), 24 x 24 x numElements. */
+/* Galerkin element matrices Ks of coarse `level` (2..L), 24 x 24 x numElements
+ * (Solving_AssembleFEAstencil.m:33-58). */
 int sgld_get_ks(const sgld_ctx *ctx, int level, double *Ks);
 
 /* Solving_KbyU_MatrixFree.m:1-41 (Solving_KbyU_MatrixFree_mex.cpp:6-138): y = K u,
@@ -373,7 +381,8 @@ typedef struct sgld_topopt_iter {
 int sgld_topopt(sgld_ctx *ctx, const sgld_topopt_opts *opts, const double *F, const double *x0, double *xphys,
                 sgld_topopt_iter *hist, int *n_iter);
 
-/* The displacement the last SIMP loop ended with (numDOFs), e.g. for a checkpoint. */
+/* The displacement the last SIMP loop ended with (numDOFs), e.g. for a checkpoint: the
+ * global U_ that the next Solving_CG_GMGS.m:7 would warm-start from. */
 int sgld_topopt_displacement(sgld_ctx *ctx, double *U);
 
 /* The projected SIMP loops with MMA, compliance normalised by the solid
@@ -425,8 +434,9 @@ int sgld_topopt_projected(sgld_ctx *ctx, const sgld_topopt_projected_opts *opts,
  * von Mises and per-element von Mises with the reference's final .^(1/2).
  * Any output may be NULL. */
 int sgld_stress(sgld_ctx *ctx, const double *U, double *nodal_stress, double *vm_node, double *vm_elem);
-/* The von Mises part of sgld_stress alone: per element (numElements) and per
- * node (numNodes); either may be NULL. */
+/* The von Mises part of sgld_stress alone (FEA_ComputePerElementVonMisesStress.m:10-19,
+ * FEA_ComputeVonMisesStress.m:1-7): per element (numElements) and per node
+ * (numNodes); either may be NULL. */
 int sgld_vonmises(sgld_ctx *ctx, const double *U, double *vm_elem, double *vm_node);
 
 /* Principal stresses of the nodal Cartesian stress field of U
@@ -462,15 +472,19 @@ void sgld_net_destroy(sgld_net *net);
 const char *sgld_net_last_error(const sgld_net *net);
 int64_t sgld_net_num_params(const sgld_net *net);
 int sgld_net_get_params(sgld_net *net, float *params);
-/* also resets the Adam moments and step count */
+/* also resets the Adam moments and step count (no reference counterpart, as for
+ * every sgld_net_* call) */
 int sgld_net_set_params(sgld_net *net, const float *params);
-/* x [V][in_channels] (rounded to BF16 on upload) -> y [V][out_channels] */
+/* x [V][in_channels] (rounded to BF16 on upload) -> y [V][out_channels]; no reference
+ * counterpart */
 int sgld_net_forward(sgld_net *net, const float *x, float *y);
 /* loss = sum_v mask_v |y_v - target_v|^2 / (out_channels sum_v mask_v) (mask NULL = 1)
- * and its gradient with respect to every parameter (grad may be NULL) */
+ * and its gradient with respect to every parameter (grad may be NULL); no reference
+ * counterpart */
 int sgld_net_grad(sgld_net *net, const float *x, const float *target, const float *mask, double *loss,
                   float *grad);
-/* sgld_net_grad followed by one Adam step (beta 0.9, 0.999, eps 1e-8); loss before the step */
+/* sgld_net_grad followed by one Adam step (beta 0.9, 0.999, eps 1e-8); loss before the
+ * step; no reference counterpart */
 int sgld_net_train_step(sgld_net *net, const float *x, const float *target, const float *mask, float lr,
                         double *loss);
 

@@ -1,25 +1,30 @@
 #!/usr/bin/env python
-"""MGPCG time-to-solve on one GB300 (SGLDBench's solve path).
+"""MGPCG time-to-solve on one GB300 (SGLDBench's solve path): the large stress
+analysis with a learned start for held-out load cases.
 
-Workload (default): the SIMP-graded 256 x 128 x 128 cantilever -- a solid
-cuboid of 4,194,304 voxels (12,830,211 DOFs), densities = seeded U[0,1) noise
-Gaussian-smoothed (sigma 2 voxels) and mapped to [1e-3, 1], E = 1e-9 +
-rho^3 (1 - 1e-9), nu = 0.3, all nodes at x = 0 fixed, a unit -z load spread
-over the x = max bottom edge, 5 dyadic multigrid levels, damped Jacobi
-omega = 0.6, PCG to relative residual 1e-6.  Synthetic, seeded inputs stand
-in for the reference's voxelized models.
+Workload (default): a 1024 x 512 x 512 voxel box holding a seeded random
+smooth shape -- the sum of 64 Gaussian blobs thresholded to keep ~30 % of the
+voxels, largest face-connected component (about 231 M DOFs) -- E = 1, nu = 0.3,
+all nodes of the lowest 4 voxel layers fixed, 7 dyadic multigrid levels, damped
+Jacobi omega = 0.6, PCG to relative residual 1e-6.  Load cases are perturbed
+versions of one surface load (a unit force spread over the boundary nodes
+within 10 voxels of a centre; the centre moves by up to 8 voxels and the
+direction turns by up to 30 degrees between cases).  Synthetic, seeded inputs
+stand in for the reference's voxelized models.
 
-One step = one full solve for a given modulus field: set E, assemble the
-Galerkin hierarchy and the coarsest factor, run PCG to 1e-6.  `value` is the
-device time per step with E and F already in HBM, for the mixed-precision
-solve (FP64 flexible PCG, FP32 inner CG with the FP32 V-cycle, double-float
-outer K*u) unless --precision says otherwise; `plain_fp64` is the reference
-form (FP64 PCG, FP64 V-cycle) timed the same way right after; `e2e` is the
-headline solve through the public C ABI with host buffers (E and F copied in,
-U copied out).
+Protocol: 20 training cases are solved first and teach the learned start
+(sgld_cases_*: a K-orthonormal basis of their solutions and a coarse-level
+U-Net trained on the corrections the solves found); then each step solves one
+held-out case from the learned start with the mixed-precision solve (FP64
+flexible PCG, FP32 inner CG with the FP32 V-cycle, double-float outer K*u).
+`value` is the device time per held-out solve with the loads resident in HBM;
+`e2e` the same through the host-buffer C ABI call (load copied in, U copied
+out); `plain_fp64` the reference form (FP64 PCG and V-cycle from zero) on the
+same case; `learned` compares the held-out cases' starts (zero, basis only,
+basis + network).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--precision fp64|mixed|mixed_df] [--size NX NY NZ]
+                  [--size NX NY NZ] [--levels L] [--train T]
 
 Under torchrun (N > 1) every rank solves its own replica on its own GPU (the
 solve path has no data-parallel split; replicas only) and rank 0 reports.
@@ -44,47 +49,67 @@ TOL = 1e-6
 OMEGA = 0.6
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", choices=["fp64", "mixed", "mixed_df"], default="mixed_df")
-    ap.add_argument("--fp64-steps", type=int, default=2, help="plain FP64 solves timed beside the headline")
-    ap.add_argument("--size", type=int, nargs=3, default=[256, 128, 128], metavar=("NX", "NY", "NZ"))
-    ap.add_argument("--levels", type=int, default=5)
-    ap.add_argument("--maxit", type=int, default=2000)
-    ap.add_argument("--inner-its", type=int, default=0,
-                    help="initial cap on the FP32 inner CG iterations per outer step of the mixed solves (0 = "
-                         "library default 64, doubled after a capped inner solve up to 16x); exact count when "
-                         "--inner-tol is 0 and this is > 0")
-    ap.add_argument("--inner-tol", type=float, default=0.0,
-                    help="inner CG stops at ||s|| <= inner_tol ||r|| (0 = library default 3e-4)")
+    ap.add_argument("--size", type=int, nargs=3, default=[1024, 512, 512], metavar=("NX", "NY", "NZ"))
+    ap.add_argument("--levels", type=int, default=7)
+    ap.add_argument("--fill", type=float, default=0.3)
+    ap.add_argument("--blobs", type=int, default=64)
+    ap.add_argument("--train", type=int, default=20, help="training load cases solved before the held-out ones")
+    ap.add_argument("--held-out", type=int, default=20, help="distinct held-out load cases (steps cycle over them)")
+    ap.add_argument("--precision", choices=["mixed", "mixed_df"], default="mixed_df")
+    ap.add_argument("--maxit", type=int, default=20000)
+    ap.add_argument("--fp64-steps", type=int, default=1, help="plain FP64 solves timed beside the headline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-iters", type=int, default=5, help="PCG iterations in the CPU sample")
-    return ap.parse_args()
+    ap.add_argument("--cpu-iters", type=int, default=5, help="PCG iterations per CPU sample")
+    return ap.parse_args(argv)
 
 
-def workload(nx, ny, nz):
+def patch_scale(args):
+    """Patch radius and centre shift in voxels (10 and 8 at 1024 voxels in x)."""
+    f = args.size[0] / 1024.0
+    return max(10.0 * f, 2.5), max(8.0 * f, 2.0)
+
+
+def workload(args):
     from sgldbench_gb300 import domains as D
 
-    vox = D.cuboid(nx, ny, nz)
-    rho = D.graded_density(nx, ny, nz, seed=0, sigma=2.0, rho_min=1e-3)
-    E = D.simp_modulus(rho, E0=1.0, Emin=1e-9, p=3.0)
-    return vox, E
-
-
-def workload_config(args):
     nx, ny, nz = args.size
-    return {"workload": f"SIMP-graded cantilever {nx}x{ny}x{nz} voxels (config 1)", "grid": [nx, ny, nz],
-            "levels": args.levels, "dyadic": True, "omega": OMEGA, "tol": TOL, "precision": args.precision,
-            "inner_its": args.inner_its, "inner_tol": args.inner_tol,
-            "l2": "inputs larger than L2 (each DOF vector > 100 MB at the default size)"}
+    return D.gaussian_blobs(nx, ny, nz, seed=0, n_blobs=args.blobs, fill=args.fill)
+
+
+def load_cases(vox, nodes, args):
+    from sgldbench_gb300 import domains as D
+
+    radius, shift = patch_scale(args)
+    kw = dict(base_seed=0, radius=radius, shift=shift, max_angle_deg=30.0)
+    train = D.perturbed_patch_cases(vox, nodes, args.train, seed=1, **kw)
+    held = D.perturbed_patch_cases(vox, nodes, args.held_out, seed=2, **kw)
+    return train, held
+
+
+def workload_config(args, extra=None):
+    nx, ny, nz = args.size
+    radius, shift = patch_scale(args)
+    cfg = {"workload": f"stress analysis of {args.blobs} thresholded Gaussian blobs in a {nx}x{ny}x{nz} voxel box "
+                       f"(~{args.fill:.0%} solid), learned start for held-out perturbed load cases",
+           "grid": [nx, ny, nz], "levels": args.levels, "dyadic": True, "omega": OMEGA, "tol": TOL,
+           "precision": args.precision, "train_cases": args.train, "held_out_cases": args.held_out,
+           "load": f"unit force over boundary nodes within {radius:g} voxels of a centre moved by up to {shift:g} "
+                   "voxels, direction turned by up to 30 degrees", "fixed": "lowest 4 voxel layers",
+           "l2": "inputs larger than L2 (each DOF vector > 1 GB)"}
+    if extra:
+        cfg.update(extra)
+    return cfg
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks / throttle reasons sampled every 500 ms while running
+    (started before the warm-up, so that its start-up is not in a timed step)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -94,11 +119,12 @@ class ClockSampler:
         self.idx = gpu_index
         self.proc = None
         self.lines = []
+        self.marks = []
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                          "--format=csv,noheader,nounits", "-lms", "500"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -107,7 +133,11 @@ class ClockSampler:
 
     def _read(self):
         for ln in self.proc.stdout:
-            self.lines.append(ln.strip())
+            self.lines.append((time.monotonic(), ln.strip()))
+
+    def mark(self):
+        """Start of a timed region; summary() keeps samples after the first mark."""
+        self.marks.append(time.monotonic())
 
     def stop(self):
         if self.proc is None:
@@ -117,11 +147,12 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
+        t0 = self.marks[0] if self.marks else 0.0
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for t, ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
+            if t < t0 or len(parts) < 9:
                 continue
             try:
                 sm.append(float(parts[1]))
@@ -132,22 +163,48 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "interval_ms": 500}
 
 
 # ---------------------------------------------------------------------------
-# CPU path (oracle): restated reference, timed on a bounded sample
+# CPU path (oracle): the restated reference on a bounded sample of the workload
 # ---------------------------------------------------------------------------
-def cpu_time_to_solve(vox, E, levels, its_full, sample_iters, steps=1, warmup=0):
+def crop_of(vox, args):
+    """The CPU sample's model: a window of the workload's box, a quarter of
+    each extent (at least 32 voxels, at most the extent), centred in x and y
+    and resting on z = 0 so that it holds fixed layers, reduced to its largest
+    face-connected component.  Returns (voxels, levels)."""
+    from sgldbench_gb300 import domains as D
+
+    ny, nx, nz = vox.shape
+    cy, cx, cz = (min(n, max(n // 4, 32)) for n in (ny, nx, nz))
+    y0, x0 = (ny - cy) // 2, (nx - cx) // 2
+    crop = D._largest_component(vox[y0:y0 + cy, x0:x0 + cx, :cz].copy())
+    levels = max(2, args.levels - int(round(np.log2(nx / cx))))
+    return crop, levels
+
+
+def cpu_sample(vox, args, iterations, steps=1, warmup=0):
     """Times the oracle (C + numpy restatement of the reference's MEX kernels
-    and MATLAB glue) on the host cores: assembly + `sample_iters` PCG
-    iterations, extrapolated to `its_full` iterations.  Returns a dict."""
+    and MATLAB glue) on the host cores: per step, assembly + args.cpu_iters PCG
+    iterations of the reference (FP64) algorithm on the crop of crop_of(); the
+    time to solve the whole workload is extrapolated by the ratio of active
+    elements and to `iterations` iterations.  Returns a dict."""
     from oracle import glue as G
+    from sgldbench_gb300 import domains as D
 
+    crop, levels = crop_of(vox, args)
+    ne_full, ne_crop = int(vox.sum()), int(crop.sum())
     t0 = time.perf_counter()
-    m = G.build_model(vox, non_dyadic=0, omega=OMEGA, num_levels=levels)
+    # the crop's own fixed DOFs (its lowest 4 layers) and one load on its boundary
+    l1 = G.voxel_discretization(crop, 50000, levels)[0]
+    fixed = D.fix_bottom_layers(crop, l1.nodMapBack, layers=4)
+    m = G.build_model_fixed(crop, fixed, non_dyadic=0, omega=OMEGA, num_levels=levels)
+    case = D.perturbed_patch_cases(crop, m.levels[0].nodMapBack, 1, seed=2, base_seed=0,
+                                   radius=min(10.0, crop.shape[1] / 8), shift=2.0)[0]
+    m.F = D.dense_load(m.levels[0].numNodes, case)
     t_setup = time.perf_counter() - t0
-    G.set_modulus(m, E)
+    G.set_modulus(m, np.ones(m.levels[0].numElements))
     spent = {"kbyu": 0.0, "vcycle": 0.0}
 
     def timed(name, fn):
@@ -160,22 +217,26 @@ def cpu_time_to_solve(vox, E, levels, its_full, sample_iters, steps=1, warmup=0)
 
     AtX = timed("kbyu", lambda u: G.kbyu(m, u))
     PtV = timed("vcycle", lambda r: G.vcycle(m, r))
-    times = []
+    rec = []
     for k in range(warmup + steps):
         t0 = time.perf_counter()
         G.assemble_stencil(m)
         spent["kbyu"] = spent["vcycle"] = 0.0
         t1 = time.perf_counter()
-        G.pcg(AtX, PtV, m.F, 0.0, sample_iters)
+        G.pcg(AtX, PtV, m.F, 0.0, args.cpu_iters)
         t2 = time.perf_counter()
         if k >= warmup:
-            times.append((t1 - t0, (t2 - t1) / sample_iters, spent["kbyu"] / sample_iters,
-                          spent["vcycle"] / sample_iters))
-    t_asm, t_it, t_kbyu, t_vc = (float(np.mean([t[i] for t in times])) for i in range(4))
-    # the SpMV / PtV / rest split of QuickAccess/zTmp_Benchmarking_SpMV.m:63-111, per iteration
-    return {"seconds": t_asm + t_it * its_full, "assemble_s": t_asm, "iter_s": t_it, "kbyu_s": t_kbyu,
-            "vcycle_s": t_vc, "glue_s": t_it - t_kbyu - t_vc, "setup_s": t_setup,
-            "levels": m.numLevels, "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))}
+            rec.append((t1 - t0, (t2 - t1) / args.cpu_iters, spent["kbyu"] / args.cpu_iters,
+                        spent["vcycle"] / args.cpu_iters))
+    t_asm, t_it, t_kbyu, t_vc = (float(np.mean([r[i] for r in rec])) for i in range(4))
+    scale = ne_full / ne_crop
+    seconds = (t_asm + t_it * iterations) * scale
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"seconds": seconds, "extrapolated": True, "sampled_iterations": args.cpu_iters, "iterations": iterations,
+            "scale_active_elements": scale, "crop_voxels": list(crop.shape), "crop_active_elements": ne_crop,
+            "crop_levels": m.numLevels, "assemble_s": t_asm, "iter_s": t_it, "kbyu_s": t_kbyu, "vcycle_s": t_vc,
+            "glue_s": t_it - t_kbyu - t_vc, "crop_setup_s": t_setup, "cores": cores,
+            "split": "per-iteration K*u / V-cycle / rest, as QuickAccess/zTmp_Benchmarking_SpMV.m:63-111"}
 
 
 def run_reference(args):
@@ -183,38 +244,28 @@ def run_reference(args):
     if rank != 0:
         return
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
-    nx, ny, nz = args.size
-    vox, E = workload(nx, ny, nz)
-    its_full = _known_iterations(args)
-    r = cpu_time_to_solve(vox, E, args.levels, its_full, args.cpu_iters, steps=args.steps,
-                          warmup=min(args.warmup, 1))
+    from sgldbench_gb300.workloads import fp64_iterations
+
+    vox = workload(args)
+    its, provenance = fp64_iterations(args.size, args.levels, args.fill, args.blobs)
+    r = cpu_sample(vox, args, its, steps=args.steps, warmup=min(args.warmup, 1))
     from oracle import mexcall
 
     kind = "reference" if mexcall.ref_lib() is not None else "port"
+    sample = (f"per step: oracle assembly + {args.cpu_iters} PCG iterations of the reference (FP64) algorithm on a "
+              f"{'x'.join(map(str, r['crop_voxels']))} crop of the box ({r['crop_active_elements']} active "
+              f"elements), scaled by the active-element ratio {r['scale_active_elements']:.1f} and to {its} "
+              f"iterations ({provenance})")
     line = {"impl": "reference", "metric": METRIC, "value": r["seconds"], "unit": "s", "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["seconds"] * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded graded-density cuboid)", "config": workload_config(args),
+            "data": "synthetic (seeded Gaussian-blob shape, perturbed surface loads)",
+            "config": workload_config(args),
             "cpu_baseline": {"value": r["seconds"], "unit": "s", "cores": r["cores"], "kind": kind,
-                             "sample": f"assembly + {args.cpu_iters} PCG iterations per step, "
-                                       f"extrapolated to {its_full} iterations"},
+                             "sample": sample, "extrapolated": True},
             "e2e": {"value": r["seconds"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "detail": r}
     print(json.dumps(line), flush=True)
-
-
-def _known_iterations(args):
-    """Iteration count of the FP64 solve of this workload.  The GPU solve and the
-    oracle run the same algorithm (equal counts in the parity tests), and a full
-    oracle solve does not fit a bounded CPU sample, so the count recorded from
-    the GPU run (profiles/iterations.json) is used to extrapolate."""
-    path = os.path.join(ROOT, "profiles", "iterations.json")
-    key = "x".join(map(str, args.size)) + f"_L{args.levels}"
-    try:
-        with open(path) as f:
-            return int(json.load(f)[key])
-    except (OSError, KeyError, ValueError):
-        return 100
 
 
 # ---------------------------------------------------------------------------
@@ -223,173 +274,172 @@ def _known_iterations(args):
 def run_ours(args):
     import torch
 
-    from sgldbench_gb300 import VoxelSolver, replicas
+    from sgldbench_gb300 import LoadCases, VoxelSolver, replicas
     from sgldbench_gb300 import domains as D
     from sgldbench_gb300.solver import kernel_launches
 
     rank, world, local = replicas.dist_env()
     torch.cuda.set_device(local)
     replicas.init("nccl")
-    nx, ny, nz = args.size
-    vox, E = workload(nx, ny, nz)
+    dev = torch.device("cuda", local)
+    t_host = time.perf_counter()
+    vox = workload(args)
     s = VoxelSolver(vox, num_levels=args.levels, non_dyadic=0, omega=OMEGA, device=local, pad=False)
     nodes = s.nodMapBack(1)
-    F, fixed = D.cantilever3(vox, nodes)
+    fixed = D.fix_bottom_layers(vox, nodes, layers=4)
     s.set_fixed_dofs(fixed)
-    dev = torch.device("cuda", local)
-    E_d = torch.from_numpy(E).to(dev)
-    F_d = torch.from_numpy(F).to(dev)
-    U_d = torch.zeros_like(F_d)
+    s.set_modulus(np.ones(s.numElements))
+    s.Solving_AssembleFEAstencil()
+    train, held = load_cases(vox, nodes, args)
+    nn, nd = s.numNodes, s.numDOFs
+    t_host = time.perf_counter() - t_host
     stream = torch.cuda.ExternalStream(s.stream, device=dev)
 
-    def step(profile=False):
-        s.set_modulus_device(E_d.data_ptr())
-        s.Solving_AssembleFEAstencil()
-        return s.pcg_device(F_d.data_ptr(), U_d.data_ptr(), TOL, args.maxit, precision=args.precision,
-                            inner_its=args.inner_its, inner_tol=args.inner_tol, profile=profile)
+    def dev_load(case):
+        f = torch.zeros(nd, dtype=torch.float64, device=dev)
+        sel, v = case
+        f.view(-1, 3)[torch.from_numpy(sel).to(dev)] = torch.tensor(v, dtype=torch.float64, device=dev)
+        return f
 
-    for _ in range(max(args.warmup, 0)):
-        info = step()
     sampler = ClockSampler(local)
     sampler.start()
+    # training: the learned start sees the training cases one after another
+    lc = LoadCases(s, max_basis=args.train, net_level=0, train_steps=8)
+    U_d = torch.empty(nd, dtype=torch.float64, device=dev)
+    t0 = time.perf_counter()
+    train_rec = []
+    for case in train:
+        F_d = dev_load(case)
+        info, st = lc.solve_device(F_d.data_ptr(), U_d.data_ptr(), mode="learned", train=True, tol=TOL,
+                                   maxIT=args.maxit, precision=args.precision)
+        train_rec.append((info["its"], info["inner_its"], st["t_solve"], st["t_train"], st["net_loss"]))
+        del F_d
+    t_train = time.perf_counter() - t0
+    held_d = [dev_load(c) for c in held]
+    torch.cuda.synchronize()
+
+    def step(j):
+        return lc.solve_device(held_d[j % len(held_d)].data_ptr(), U_d.data_ptr(), mode="learned", tol=TOL,
+                               maxIT=args.maxit, precision=args.precision)
+
+    for k in range(max(args.warmup, 0)):
+        step(k)
     replicas.barrier()
     torch.cuda.synchronize()
+    sampler.mark()
     l0 = kernel_launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    infos = []
-    for _ in range(args.steps):
-        infos.append(step())
+    recs = []
+    for k in range(args.steps):
+        recs.append(step(k))
     e1.record(stream)
     torch.cuda.synchronize()
     launches = (kernel_launches() - l0) / max(args.steps, 1)
-    clocks = sampler.stop()
     t_step = e0.elapsed_time(e1) / 1e3 / args.steps
     replicas.barrier()
     torch.cuda.synchronize()
-    # the slowest replica's time per solve; every rank solved `steps` replicas
     t_step, solves = replicas.aggregate(t_step, args.steps, device=dev)
-    its = infos[-1]["its"]
-    # split: one profiled solve (outer K*u launches timed with events on the library stream)
-    pinfo = step(profile=True)
-    # the reference form, same workload, timed the same way (device events)
+    # end to end through the host-buffer C ABI call: the load copied in from
+    # page-locked memory, U copied out, every step
+    F_pin = torch.zeros(nd, dtype=torch.float64).pin_memory().numpy()
+    U_pin = torch.zeros(nd, dtype=torch.float64).pin_memory().numpy()
+    t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2e = []
+    for k in range(-1, args.steps):   # one warm-up call of the host path
+        D.dense_load(nn, held[max(k, 0) % len(held)], out=F_pin)
+        torch.cuda.synchronize()
+        t0e.record(stream)
+        lc.solve(F_pin, mode="learned", tol=TOL, maxIT=args.maxit, precision=args.precision, out=U_pin)
+        t1e.record(stream)
+        torch.cuda.synchronize()
+        if k >= 0:
+            e2e.append(t0e.elapsed_time(t1e) / 1e3)
+    clocks = sampler.stop()
+    # the starts compared on the first held-out cases (untimed): zero, basis only, basis + network
+    cmp = {"zero": [], "basis": [], "learned": []}
+    for j in range(min(2, len(held))):
+        for mode in ("zero", "basis", "learned"):
+            info, st = lc.solve_device(held_d[j].data_ptr(), U_d.data_ptr(), mode=mode, tol=TOL, maxIT=args.maxit,
+                                       precision=args.precision, diagnostics=True)
+            cmp[mode].append({"its": info["its"], "inner_its": info["inner_its"], "seconds": st["t_start"] +
+                              st["t_solve"], "start_ratio": st["start_ratio"], "net_accepted": st["net_accepted"]})
+    U_mx = U_d.clone()   # case 0, learned start
+    # the reference form on case 0: FP64 PCG with the FP64 V-cycle from zero
     fp64 = None
-    if args.precision != "fp64" and args.fp64_steps > 0:
-        def step64():
-            s.set_modulus_device(E_d.data_ptr())
-            s.Solving_AssembleFEAstencil()
-            return s.pcg_device(F_d.data_ptr(), U_d.data_ptr(), TOL, args.maxit, precision="fp64")
-        step64()
+    if args.fp64_steps > 0:
+        U64_d = torch.empty_like(U_d)
+        s.pcg_device(held_d[0].data_ptr(), U64_d.data_ptr(), TOL, 3, precision="fp64")   # one-time set-up
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         f0.record(stream)
         for _ in range(args.fp64_steps):
-            i64 = step64()
+            i64 = s.pcg_device(held_d[0].data_ptr(), U64_d.data_ptr(), TOL, args.maxit, precision="fp64")
         f1.record(stream)
         torch.cuda.synchronize()
         t64 = f0.elapsed_time(f1) / 1e3 / args.fp64_steps
         fp64 = {"value": t64, "unit": "s", "iterations": i64["its"], "true_relres": i64["true_relres"],
-                "steps": args.fp64_steps, "speedup_of_headline": t64 / t_step}
-    # end to end through the public API with host buffers (page-locked, as a
-    # caller streaming load cases would hold them)
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    E_h = torch.from_numpy(E).pin_memory().numpy()
-    F_h = torch.from_numpy(F).pin_memory().numpy()
-    U_h = torch.zeros(F.size, dtype=torch.float64).pin_memory().numpy()
-    def step_e2e():
-        s.set_modulus(E_h)
-        s.Solving_AssembleFEAstencil()
-        return s.pcg(F_h, tol=TOL, maxIT=args.maxit, precision=args.precision, inner_its=args.inner_its,
-                     inner_tol=args.inner_tol, out=U_h)
+                "steps": args.fp64_steps, "speedup_of_headline": t64 / t_step,
+                "speedup_of_e2e": t64 / float(np.mean(e2e))}
+        # errors of the mixed + learned answer of case 0 against the FP64 one
+        U64 = U64_d.cpu().numpy()
+        Um = U_mx.cpu().numpy()
+        F0 = D.dense_load(nn, held[0])
+        c64, cm = float(F0 @ U64), float(F0 @ Um)
+        _, _, vm64 = s.FEA_StressAnalysis(U64)
+        _, _, vmm = s.FEA_StressAnalysis(Um)
+        fp64["error_of_headline_vs_fp64"] = {
+            "compliance_rel": abs(cm - c64) / abs(c64),
+            "displacement_rel_l2": float(np.linalg.norm(Um - U64) / np.linalg.norm(U64)),
+            "von_mises_elem_rel_max": float(np.abs(vmm - vm64).max() / np.abs(vm64).max()),
+            "note": "both solves at relative residual 1e-6 on their true residual"}
+    # roofline of the dominant kernel: the FP32 K*u of the inner CG
+    from sgldbench_gb300 import roofline as R
 
-    # warm-up of the host-buffer path too: its first calls pay one-time costs
-    # (pinned-buffer registration lookups, the host entry point's first solve)
-    for _ in range(max(args.warmup, 0)):
-        step_e2e()
-    e2e = []
-    for _ in range(args.steps):
-        torch.cuda.synchronize()
-        t0.record(stream)
-        U_h, inf = step_e2e()
-        t1.record(stream)
-        torch.cuda.synchronize()
-        e2e.append(t0.elapsed_time(t1) / 1e3)
-    h2d = E.nbytes + F.nbytes
-    d2h = U_h.nbytes
-    ndof = s.numDOFs
-    # roofline of the dominant kernel: the K*u of the solve's inner loop
-    NN = (nx + 1) * (ny + 1) * (nz + 1)
-    NE = nx * ny * nz
-    peaks = _peaks()
-    if args.precision == "fp64":
-        kname, kbytes = "k_kbyu<double> (FP64 K*u)", NN * (3 * 8 * 2 + 1) + NE * 8
-        kb_avg = pinfo["kbyu_seconds"] / max(pinfo["kbyu_launches"], 1)
-        how = "CUDA events around every K*u launch of one solve on the library stream"
-        note = "FP64 K*u is FP64-issue-bound on GB300 (ncu: FP64 pipe ~84 % busy)"
-    else:
-        kname, kbytes = "k_kbyu_x2 (FP32 K*u of the inner CG, f32x2 packed)", NN * (3 * 4 * 2 + 1) + NE * 4
-        kb_avg = s.time_op("kbyu32", 20) * 1e-3
-        how = ("CUDA events around 20 back-to-back launches on the library stream (sgld_time_op) right after "
-               "the timed region; inside the timed region the kernel runs in the inner CG's graph")
-        note = ("FP32 K*u is issue/latency-bound, not HBM-bound; the HBM fraction is reported against the "
-                "measured copy bandwidth. Autotuned tile: %s" % json.dumps(s.kbyu_tile()))
-    achieved = kbytes / kb_avg / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": _ncu_traffic(args.precision),
-                "kernel": kname, "avg_launch_ms": kb_avg * 1e3, "launch_timing": how,
-                "algorithmic_bytes_per_launch": kbytes, "peak_source": peaks["source"],
-                "dense_equiv_tflops": 1152.0 * NE / kb_avg / 1e12, "note": note}
+    rl = R.kbyu_f32_roofline(s, vox, reps=20)
+    free, total = torch.cuda.mem_get_info()
+    inner = [r["inner_its"] for r in recs]
+    outer = [r["its"] for r in recs]
     line = {"metric": METRIC, "value": t_step, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": {"fp64": "f64", "mixed": "f64+f32", "mixed_df": "f64+f32+df32"}[args.precision],
-            "data": "synthetic (seeded graded-density cuboid)", "config": workload_config(args),
-            "iterations": its, "dof": ndof, "dof_it_per_s": world * ndof * its / t_step,
+            "vs_baseline": None, "dtype": {"mixed": "f64+f32", "mixed_df": "f64+f32+df32"}[args.precision],
+            "data": "synthetic (seeded Gaussian-blob shape, perturbed surface loads)",
+            "config": workload_config(args, {"dofs": nd, "active_fraction": float(vox.mean())}),
+            "iterations": {"outer": outer, "inner": inner},
+            "dof_it_per_s": {"outer": world * nd * float(np.mean(outer)) / t_step,
+                             "inner": world * nd * float(np.mean(inner)) / t_step},
             "replica_solves_per_s": solves / (t_step * args.steps),
-            "split": {"pcg_s": infos[-1]["seconds"], "assemble_s": t_step - infos[-1]["seconds"],
-                      "kbyu_s": pinfo["kbyu_seconds"], "precond_s": pinfo["precond_seconds"]},
-            "true_relres": infos[-1]["true_relres"], "converged": infos[-1]["converged"],
-            "e2e": {"value": float(np.mean(e2e)), "unit": "s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "samples": [round(v, 6) for v in e2e]},
-            "gpu_launches": int(round(launches)), "roofline": roofline, "clocks": clocks}
+            "converged": all(r["converged"] for r in recs),
+            "max_true_relres": max(r["true_relres"] for r in recs),
+            "fallbacks": sum(int(r["fallback"]) for r in recs),
+            "e2e": {"value": float(np.mean(e2e)), "unit": "s", "h2d_bytes_per_step": 8 * nd,
+                    "d2h_bytes_per_step": 8 * nd, "samples": [round(v, 4) for v in e2e]},
+            "gpu_launches": int(round(launches)), "roofline": rl, "clocks": clocks,
+            "learned": {"train_cases": len(train), "basis": lc.basis_size,
+                        "train_s_wall": t_train,
+                        "train": [{"its": a, "inner_its": b, "t_solve": c, "t_train": d, "net_loss": e}
+                                  for a, b, c, d, e in train_rec],
+                        "held_out_compare": cmp,
+                        "start": "energy-optimal combination of the training solutions' basis plus the "
+                                 "coarse-level network's correction when it lowers r'Mr"},
+            "memory_bytes": int(total - free), "host_setup_s": t_host}
     if fp64:
         line["plain_fp64"] = fp64
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and fp64:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
-        its_ref = fp64["iterations"] if fp64 else (its if args.precision == "fp64" else _known_iterations(args))
-        r = cpu_time_to_solve(vox, E, args.levels, its_ref, args.cpu_iters, steps=1, warmup=0)
-        line["cpu_baseline"] = {"value": r["seconds"], "unit": "s", "cores": r["cores"], "kind": "port",
-                                "sample": f"oracle assembly + {args.cpu_iters} PCG iterations of the reference "
-                                          f"(FP64) algorithm, extrapolated to its {its_ref} iterations",
-                                "detail": r}
+        r = cpu_sample(vox, args, fp64["iterations"])
+        line["cpu_baseline"] = {
+            "value": r["seconds"], "unit": "s", "cores": r["cores"], "kind": "port", "extrapolated": True,
+            "sample": (f"oracle assembly + {args.cpu_iters} PCG iterations of the reference (FP64) algorithm on a "
+                       f"{'x'.join(map(str, r['crop_voxels']))} crop of the box, scaled by the active-element ratio "
+                       f"{r['scale_active_elements']:.1f} and to the {fp64['iterations']} iterations of the "
+                       "reference-form solve of the same case in this run"),
+            "detail": r}
     if rank == 0:
         print(json.dumps(line), flush=True)
+    lc.close()
     s.close()
     replicas.shutdown()
-
-
-def _peaks():
-    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    try:
-        with open(p) as f:
-            d = json.load(f)
-        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured (MEASURED_PEAKS.json)"}
-    except (OSError, KeyError, ValueError):
-        return {"hbm_gbs": 6800.0, "source": "fallback"}
-
-
-def _ncu_traffic(precision):
-    """DRAM bytes per launch of the roofline kernel from the committed ncu
-    capture (profiles/kbyu_traffic.json), if recorded."""
-    p = os.path.join(ROOT, "profiles", "kbyu_traffic.json")
-    try:
-        with open(p) as f:
-            d = json.load(f)
-    except (OSError, ValueError):
-        return None
-    if precision == "fp64":
-        return d.get("dram_bytes_per_launch_full")
-    return d.get("k_kbyu_x2", {}).get("dram_bytes_per_launch")
 
 
 def main():

@@ -89,7 +89,9 @@ typedef struct sgld_solve_opts {
 
 typedef struct sgld_solve_info {
     int iterations;        /* outer iterations, as the reference's `its` */
-    int converged;         /* 1 if relres < tol */
+    int converged;         /* SGLD_PREC_FP64: 1 if relres < tol, the reference's own stopping test
+                              (Solving_PreconditionedConjugateGradientSolver.m:22).  Mixed modes:
+                              1 only if true_relres <= tol as well */
     double relres;         /* recursive residual norm / ||b|| at exit */
     double true_relres;    /* ||b - K x|| / ||b|| recomputed at exit (FP64 vectors; K x by the
                               precision mode's outer operator) */
@@ -99,15 +101,24 @@ typedef struct sgld_solve_info {
     int kbyu_launches;     /* profile: number of those launches */
     double precond_seconds;/* profile: summed device time of the preconditioner applications */
     int fallback;          /* SGLD_PREC_MIXED(_DF): 1 if the mixed solve failed (not converged,
-                              a non-finite residual, or a true residual above 100 tol) and the
-                              answer comes from the reference-form FP64 solve rerun from the
-                              same start; the other fields then describe that FP64 solve */
+                              a non-finite residual, or a true residual still above tol after
+                              its residual replacements) and the answer comes from the
+                              reference-form FP64 solve rerun from the same start; the other
+                              fields then describe that FP64 solve */
+    int replacements;      /* SGLD_PREC_MIXED(_DF): residual replacements made.  When the
+                              recurrence met tol but the recomputed true residual is above tol,
+                              the outer PCG restarts from x with r = b - K x (at most 3 times);
+                              their iterations are included in `iterations` and `seconds` */
 } sgld_solve_info;
 
 /* Test hook (no counterpart in the reference): corrupts, on the host side of
- * the next solve, the data of the FP32 inner operator so that a mixed solve
- * fails and its fallback runs.  kind 1: the FP32 copy of the moduli gets a
- * NaN (until the next sgld_assemble).  kind 0: no-op.  Faults no GPU. */
+ * the next solve, data of a mixed solve so that its failure handling runs.
+ * kind 1: the FP32 copy of the moduli gets a NaN (until the next
+ * sgld_assemble), so the mixed solve fails and its FP64 fallback runs.
+ * kind 2: the next single-load mixed solve's iterate is scaled by (1 + 1e-3)
+ * after its recurrence has met tol, as a drifted recurrence would leave it, so
+ * its true residual is above tol and residual replacement runs.  kind 0:
+ * no-op.  Faults no GPU. */
 int sgld_inject_fault(sgld_ctx *ctx, int kind);
 
 /* The CUDA stream every call of this context runs on (a cudaStream_t).  No
@@ -487,6 +498,49 @@ int sgld_net_grad(sgld_net *net, const float *x, const float *target, const floa
  * step; no reference counterpart */
 int sgld_net_train_step(sgld_net *net, const float *x, const float *target, const float *mask, float lr,
                         double *loss);
+
+/* ---- learned start for a sequence of load cases on one model -----------------
+ * No counterpart in the reference, which solves every new load case from
+ * U_ = 0 (Solving_CG_GMGS.m:7; GUIs/Mtd_StructuralRobustnessExploration.m:119
+ * re-solves per rotated load).  The object learns from the solves it is given
+ * for training: a K-orthonormal basis of their solutions (FP32, compact DOF
+ * order, at most max_basis <= 32 vectors) and, with net_level >= 0, a U-Net on a
+ * coarse level trained on (residual left by the basis start -> correction the
+ * solve found) pairs.  A new case starts from the energy-optimal combination of
+ * the basis, plus the network's correction when that lowers r'Mr (M = the FP64
+ * V-cycle).  The solve then runs to its tolerance on the true residual like any
+ * other, so the start changes iteration counts, never the converged answer.
+ * net_level: MATLAB level index of the network's grid, 0 = the finest level of
+ * at most 110K nodes, -1 = no network.  train_steps: Adam steps per training
+ * case.  Memory: max_basis * numDOFs * 4 bytes plus four full-grid FP64 vectors. */
+typedef struct sgld_cases sgld_cases;
+
+typedef struct sgld_cases_stats {
+    int diagnostics;     /* in: 1 = also measure the starts' sqrt(r'Mr) ratios (two FP64 V-cycles) */
+    int basis;           /* basis vectors the start was formed from */
+    int net_used;        /* the network's correction was evaluated ... */
+    int net_accepted;    /* ... and kept (it lowered r'Mr) */
+    double net_ratio;    /* sqrt(r'Mr) with the kept correction / without it */
+    double basis_ratio;  /* diagnostics: sqrt(r'Mr) of the basis start / of the zero start */
+    double start_ratio;  /* diagnostics: the same for the start used */
+    double net_loss;     /* training loss after this case's Adam steps */
+    double t_start;      /* device seconds forming the start (CUDA events) */
+    double t_solve;      /* device seconds of the solve */
+    double t_train;      /* device seconds adding the case to the basis and training */
+} sgld_cases_stats;
+
+int sgld_cases_create(sgld_ctx *ctx, int max_basis, int net_level, int train_steps, sgld_cases **out);
+void sgld_cases_destroy(sgld_cases *cases);
+int sgld_cases_basis_size(const sgld_cases *cases);
+/* Solves one load case (F, U: compact host vectors as sgld_pcg) with the
+ * context's assembled stencil and opts (use_x0 is ignored).  mode 0: zero start;
+ * 1: the basis start; 2: the basis start and the network's correction.  train:
+ * afterwards add the solution to the basis and train the network on the case. */
+int sgld_cases_solve(sgld_cases *cases, const double *F, double *U, const sgld_solve_opts *opts, int mode,
+                     int train, sgld_solve_info *info, sgld_cases_stats *stats);
+/* the same with compact device vectors */
+int sgld_cases_solve_device(sgld_cases *cases, const double *d_F, double *d_U, const sgld_solve_opts *opts,
+                            int mode, int train, sgld_solve_info *info, sgld_cases_stats *stats);
 
 #ifdef __cplusplus
 }

@@ -9,7 +9,7 @@ REF=${SGLD_REFERENCE:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 SRC="$REF/src/MEXfuncs"
-[ -d "$SRC" ] || { echo "reference sources not found at $SRC" >&2; exit 2; }
+[ -d "$SRC" ] || { echo "reference sources not found at $SRC (set SGLD_REFERENCE)" >&2; exit 2; }
 mkdir -p "$OUT/obj"
 CXX=${CXX:-g++}
 FLAGS="-O3 -fopenmp -fPIC -std=c++17 -w -I$HERE/mexshim"
@@ -29,4 +29,6 @@ OBJS="$OBJS $OUT/obj/MMA_mex.o $OUT/obj/MMAseq.o"
 $CXX $FLAGS -c "$HERE/mexshim/mexshim.cpp" -o "$OUT/obj/mexshim.o" &
 wait
 $CXX -shared -fopenmp -o "$OUT/libref_mex.so" $OBJS "$OUT/obj/mexshim.o"
+# record where the checkout is, for the tests that read its data files
+(cd "$REF" && pwd) > "$OUT/REFERENCE_ROOT"
 echo "built $OUT/libref_mex.so"

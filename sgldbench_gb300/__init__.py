@@ -5,6 +5,6 @@ The compute path is the CUDA library ``libsgld_gb300.so`` (C ABI in
 Importing the package does not load the library; constructing a solver does,
 and fails loudly when it is not built.
 """
-from .solver import VoxelSolver, pad_voxels, reference_num_levels, simp_modulus  # noqa: F401
+from .solver import LoadCases, VoxelSolver, pad_voxels, reference_num_levels, simp_modulus  # noqa: F401
 
-__all__ = ["VoxelSolver", "pad_voxels", "reference_num_levels", "simp_modulus"]
+__all__ = ["LoadCases", "VoxelSolver", "pad_voxels", "reference_num_levels", "simp_modulus"]

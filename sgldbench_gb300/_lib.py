@@ -34,7 +34,13 @@ class SolveOpts(C.Structure):
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", i32), ("converged", i32), ("relres", dbl), ("true_relres", dbl),
                 ("inner_iterations", i32), ("seconds", dbl), ("kbyu_seconds", dbl), ("kbyu_launches", i32),
-                ("precond_seconds", dbl), ("fallback", i32)]
+                ("precond_seconds", dbl), ("fallback", i32), ("replacements", i32)]
+
+
+class CasesStats(C.Structure):
+    _fields_ = [("diagnostics", i32), ("basis", i32), ("net_used", i32), ("net_accepted", i32), ("net_ratio", dbl),
+                ("basis_ratio", dbl), ("start_ratio", dbl), ("net_loss", dbl), ("t_start", dbl), ("t_solve", dbl),
+                ("t_train", dbl)]
 
 
 class TopOptOpts(C.Structure):
@@ -117,6 +123,11 @@ SIGNATURES = {
     "sgld_topopt": (i32, [vp, vp, vp, vp, vp, vp, vp]),
     "sgld_topopt_displacement": (i32, [vp, vp]),
     "sgld_topopt_projected": (i32, [vp, vp, vp, vp, vp, vp]),
+    "sgld_cases_create": (i32, [vp, i32, i32, i32, vp]),
+    "sgld_cases_destroy": (None, [vp]),
+    "sgld_cases_basis_size": (i32, [vp]),
+    "sgld_cases_solve": (i32, [vp, vp, vp, vp, i32, i32, vp, vp]),
+    "sgld_cases_solve_device": (i32, [vp, vp, vp, vp, i32, i32, vp, vp]),
 }
 
 _lib = None

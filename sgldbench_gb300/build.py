@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsgld_gb300.so")
-SOURCES = ["kernels_stencil.cu", "kernels_mg.cu", "kernels_asm.cu", "kernels_vec.cu", "kernels_mixed.cu", "kernels_topopt.cu", "kernels_df.cu", "kernels_principal.cu", "kernels_pde.cu", "kernels_mma.cu", "kernels_net.cu", "sgld_net.cu", "sgld_learned.cu", "noalloc.cu",
+SOURCES = ["kernels_stencil.cu", "kernels_mg.cu", "kernels_asm.cu", "kernels_vec.cu", "kernels_mixed.cu", "kernels_topopt.cu", "kernels_df.cu", "kernels_principal.cu", "kernels_pde.cu", "kernels_mma.cu", "kernels_net.cu", "sgld_net.cu", "sgld_learned.cu", "noalloc.cu", "kernels_cases.cu", "sgld_cases.cu",
            "sgld_api.cu", "sgld_topopt_api.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -80,7 +80,7 @@ def build_mex_gateway(mex_include: str, out: str) -> str:
     """Compiles the MEX gateway (mex/sgld_gpu_mex.cpp) against the mex.h found
     in `mex_include`, with its entry point renamed to sgld_gpu_mex, into the
     shared object `out` linked to the library.  MATLAB users build it with
-    `mex` instead."""
+    MATLAB's own `mex` command instead."""
     lib = build()
     src = os.path.join(HERE, "mex", "sgld_gpu_mex.cpp")
     extra = [os.path.join(mex_include, f) for f in os.listdir(mex_include) if f.endswith(".cpp")]

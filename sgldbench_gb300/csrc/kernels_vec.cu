@@ -161,6 +161,14 @@ void launch_residual(double *r, const double *b, const double *Ax, int64_t n, cu
     k_residual<<<reduce_blocks(n), VB, 0, s>>>(r, b, Ax, n);
 }
 
+__global__ void k_scale(double *__restrict__ x, double a, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)VB + threadIdx.x; i < n; i += (int64_t)gridDim.x * VB) x[i] *= a;
+}
+void launch_scale(double *x, double a, int64_t n, cudaStream_t s) {
+    ++g_launches;
+    k_scale<<<reduce_blocks(n), VB, 0, s>>>(x, a, n);
+}
+
 __global__ void k_cast_f32(const double *__restrict__ a, float *__restrict__ b, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)VB + threadIdx.x; i < n; i += (int64_t)gridDim.x * VB) b[i] = (float)a[i];
 }

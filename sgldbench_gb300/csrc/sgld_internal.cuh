@@ -124,6 +124,8 @@ struct Ctx {
     int64_t inner_entry_launches = 0, inner_body_launches = 0;
     struct LearnedWS *lws = nullptr;   // learned warm start of the SIMP loop (sgld_learned.cu)
     double *d_x0 = nullptr;            // [3*nnode] start of a mixed solve, kept for its FP64 fallback
+    bool fault_drift = false;          // test hook (sgld_inject_fault kind 2): perturb the next mixed
+                                       // solve's iterate before its true residual is checked
     cudaStream_t stream = nullptr;
     std::string err;
     int device = 0;
@@ -309,6 +311,7 @@ void launch_pcg_update(double *x, double *r, const double *p, const double *q, i
 void launch_pcg_pupdate(double *p, const double *z, int64_t n, const double *scal, const int *iflag,
                         cudaStream_t s);
 void launch_residual(double *r, const double *b, const double *Ax, int64_t n, cudaStream_t s);
+void launch_scale(double *x, double a, int64_t n, cudaStream_t s);
 void launch_pcg_scalar(int op, double *scal, int *iflag, const double *partial, int nb, double tol, int maxit,
                        cudaStream_t s);
 void launch_mask_fixed(const Level &l0, double *v, cudaStream_t s);

@@ -194,3 +194,55 @@ def patch_loads(voxels: np.ndarray, nodMapBack: np.ndarray, nrhs: int, seed: int
         f[sel] = v / len(sel)
         out[k] = f.reshape(-1)
     return out
+
+
+def perturbed_patch_cases(voxels: np.ndarray, nodMapBack: np.ndarray, n: int, seed: int = 0, base_seed: int = 0,
+                          radius: float = 10.0, shift: float = 8.0, max_angle_deg: float = 30.0,
+                          exclude_below: int = 4):
+    """n perturbed versions of one load case (a unit force spread evenly over
+    the boundary nodes within `radius` of a boundary node), as a list of
+    (compact node indices, force per node (3,)).  The base case's centre node
+    and direction come from `base_seed`; each perturbed case moves the centre
+    to a random boundary node within `shift` voxels of the base centre and
+    turns the direction by a random rotation of at most `max_angle_deg`
+    degrees; cases from another `seed` are held-out cases of the same
+    distribution.  The reference's robustness study turns its loads by Euler
+    angles (GUIs/Mtd_StructuralRobustnessExploration.m, UpdateButtonPushed);
+    here the patch moves as well, so that a case is not a combination of
+    others."""
+    ny, nx, _ = voxels.shape
+    ix, iy, iz = node_coords(nodMapBack, ny, nx)
+    bnd = np.nonzero(boundary_nodes(voxels, nodMapBack) & (iz > iz.min() + exclude_below))[0]
+    base = np.random.default_rng(base_seed)
+    c0 = bnd[base.integers(len(bnd))]
+    d0 = base.standard_normal(3)
+    d0 /= np.linalg.norm(d0)
+    near = bnd[((ix[bnd] - ix[c0]) ** 2 + (iy[bnd] - iy[c0]) ** 2 + (iz[bnd] - iz[c0]) ** 2) <= shift ** 2]
+    rng = np.random.default_rng(seed)
+    cases = []
+    for _ in range(n):
+        c = near[rng.integers(len(near))]
+        sel = bnd[((ix[bnd] - ix[c]) ** 2 + (iy[bnd] - iy[c]) ** 2 + (iz[bnd] - iz[c]) ** 2) <= radius ** 2]
+        axis = rng.standard_normal(3)
+        axis /= np.linalg.norm(axis)
+        ang = np.deg2rad(max_angle_deg) * rng.random()
+        # Rodrigues' rotation of d0 about `axis` by `ang`
+        v = d0 * np.cos(ang) + np.cross(axis, d0) * np.sin(ang) + axis * (axis @ d0) * (1.0 - np.cos(ang))
+        cases.append((sel, v / len(sel)))
+    return cases
+
+
+def dense_load(num_nodes: int, case, out: np.ndarray | None = None) -> np.ndarray:
+    """The load vector (3 num_nodes,) of one (nodes, force per node) case."""
+    f = np.zeros(3 * num_nodes) if out is None else out
+    if out is not None:
+        f[...] = 0.0
+    sel, v = case
+    f.reshape(-1, 3)[sel] = v
+    return f
+
+
+def perturbed_patch_loads(voxels: np.ndarray, nodMapBack: np.ndarray, n: int, **kw) -> np.ndarray:
+    """perturbed_patch_cases as a dense (n, numDOFs) array."""
+    nn = len(nodMapBack)
+    return np.stack([dense_load(nn, c) for c in perturbed_patch_cases(voxels, nodMapBack, n, **kw)])

@@ -1,0 +1,57 @@
+"""Roofline figures of the solve's dominant kernel, the FP32 K*u of the inner
+CG (k_kbyu_x2), for bench.py and kernel_bench.py.
+
+Algorithmic bytes per launch follow the operator's own data (per active node:
+u read and y written, 3 FP32 values each, plus one flag byte; per active
+element: its FP32 modulus), the same count the reference's K*u kernel would
+have to move (src/MEXfuncs/Solving_KbyU_MatrixFree_mex.cpp:53-138 reads u, E
+and writes y).  The launch time is measured live with CUDA events on the
+library's stream (sgld_time_op).  The DRAM traffic of a launch comes from an
+ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) recorded below with
+the command that produced it; captures on a case smaller than the workload are
+scaled by the full-grid node count, which the kernel's traffic follows.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+# ncu DRAM bytes per full-grid node of one k_kbyu_x2 launch, by workload kind
+# (filled from the captures summarised under profiles/)
+DRAM_BYTES_PER_GRID_NODE: dict = {}
+
+
+def peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured (MEASURED_PEAKS.json)"}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6800.0, "source": "fallback (6.8 TB/s, one earlier GB300 measurement)"}
+
+
+def kbyu_f32_bytes(active_nodes: int, active_elements: int) -> int:
+    return active_nodes * (3 * 4 * 2 + 1) + active_elements * 4
+
+
+def kbyu_f32_roofline(s, voxels=None, reps: int = 20, kind: str = "blobs") -> dict:
+    """Roofline record of k_kbyu_x2 on solver s (assembled)."""
+    nn, ne = s.numNodes, s.numElements
+    alg = kbyu_f32_bytes(nn, ne)
+    ms = s.time_op("kbyu32", reps)
+    p = peaks()
+    achieved = alg / (ms * 1e-3) / 1e9
+    ry, rx, rz = s.resY, s.resX, s.resZ
+    grid_nodes = (ry + 1) * (rx + 1) * (rz + 1)
+    per = DRAM_BYTES_PER_GRID_NODE.get(kind)
+    return {"bound": "hbm", "achieved": achieved, "peak": p["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / p["hbm_gbs"], "traffic": None if per is None else per * grid_nodes,
+            "kernel": "k_kbyu_x2 (FP32 K*u of the inner CG)", "avg_launch_ms": ms,
+            "launch_timing": f"CUDA events around {reps} back-to-back launches on the library stream "
+                             "(sgld_time_op) after the timed region; inside it the kernel runs in the inner CG's "
+                             "graph", "algorithmic_bytes_per_launch": alg,
+            "algorithmic_bytes": "active nodes x (3 x 4 B in + 3 x 4 B out + 1 B flags) + active elements x 4 B",
+            "active_nodes": nn, "active_elements": ne, "grid_nodes": grid_nodes,
+            "peak_source": p["source"], "tile": s.kbyu_tile()}

@@ -71,7 +71,8 @@ def _info_dict(info) -> dict:
     return {"its": info.iterations, "converged": bool(info.converged), "relres": info.relres,
             "true_relres": info.true_relres, "inner_its": info.inner_iterations, "seconds": info.seconds,
             "kbyu_seconds": info.kbyu_seconds, "kbyu_launches": info.kbyu_launches,
-            "precond_seconds": info.precond_seconds, "fallback": bool(info.fallback)}
+            "precond_seconds": info.precond_seconds, "fallback": bool(info.fallback),
+            "replacements": info.replacements}
 
 
 def kernel_launches() -> int:
@@ -317,7 +318,10 @@ class VoxelSolver:
 
     def inject_fault(self, kind: int = 1):
         """Test hook: kind 1 puts a NaN into the FP32 inner operator's moduli (until
-        the next assembly), so that a mixed solve fails and falls back to FP64."""
+        the next assembly), so that a mixed solve fails and falls back to FP64;
+        kind 2 scales the next single-load mixed solve's converged iterate by
+        1 + 1e-3 before its true residual is checked, so that residual
+        replacement runs."""
         self._check(self.lib.sgld_inject_fault(self.ctx, int(kind)))
 
     def kbyu_tile(self) -> dict:
@@ -549,3 +553,68 @@ class VoxelSolver:
         self._check(self.lib.sgld_topopt_displacement(self.ctx, _p(U)))
         loop = (int(resume["loop"]) if resume is not None else 0) + nit.value
         return xp, recs, {"loop": loop, "x": xout, "xPhys": xp.copy(), "U": U}
+
+
+class LoadCases:
+    """Learned start for a sequence of load cases on one VoxelSolver
+    (sgld_cases_* of the C ABI; no counterpart in the reference, which starts
+    every new load case from zero).  Training cases add their solutions to a
+    K-orthonormal basis and train a coarse-level U-Net on the correction the
+    solve found beyond the basis start; a new case starts from the basis
+    projection (mode 1) plus the network's correction when it lowers r'Mr
+    (mode 2).  Every solve still runs to its tolerance on the true residual."""
+
+    MODES = {"zero": 0, "basis": 1, "learned": 2}
+
+    def __init__(self, solver: VoxelSolver, max_basis: int = 20, net_level: int = 0, train_steps: int = 8):
+        self.s = solver
+        self.lib = solver.lib
+        h = C.c_void_p()
+        solver._check(self.lib.sgld_cases_create(solver.ctx, int(max_basis), int(net_level), int(train_steps),
+                                                  C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sgld_cases_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def basis_size(self) -> int:
+        return int(self.lib.sgld_cases_basis_size(self.h))
+
+    def _opts(self, tol, maxIT, precision, inner_its, inner_tol):
+        return L.SolveOpts(tol=tol, maxit=maxIT, use_x0=0, precision=_precision(precision), inner_its=inner_its,
+                           history=None, profile=0, inner_tol=inner_tol)
+
+    @staticmethod
+    def _stats(st) -> dict:
+        return {k: getattr(st, k) for k, _ in L.CasesStats._fields_ if k != "diagnostics"}
+
+    def solve(self, F, mode: str = "learned", train: bool = False, tol: float = 1e-6, maxIT: int = 5000,
+              precision: str = "mixed_df", inner_its: int = 0, inner_tol: float = 0.0, diagnostics: bool = False,
+              out=None):
+        """One load case from host vectors.  Returns (U, info dict, stats dict)."""
+        bv = self.s._vec(F, self.s.numDOFs)
+        x = np.empty_like(bv) if out is None else out
+        o = self._opts(tol, maxIT, precision, inner_its, inner_tol)
+        info, st = L.SolveInfo(), L.CasesStats(diagnostics=int(diagnostics))
+        self.s._check(self.lib.sgld_cases_solve(self.h, _p(bv), _p(x), C.byref(o), self.MODES[mode], int(train),
+                                                C.byref(info), C.byref(st)))
+        return x, _info_dict(info), self._stats(st)
+
+    def solve_device(self, F_ptr: int, U_ptr: int, mode: str = "learned", train: bool = False, tol: float = 1e-6,
+                     maxIT: int = 5000, precision: str = "mixed_df", inner_its: int = 0, inner_tol: float = 0.0,
+                     diagnostics: bool = False):
+        """One load case from compact device vectors.  Returns (info dict, stats dict)."""
+        o = self._opts(tol, maxIT, precision, inner_its, inner_tol)
+        info, st = L.SolveInfo(), L.CasesStats(diagnostics=int(diagnostics))
+        self.s._check(self.lib.sgld_cases_solve_device(self.h, C.c_void_p(F_ptr), C.c_void_p(U_ptr), C.byref(o),
+                                                       self.MODES[mode], int(train), C.byref(info), C.byref(st)))
+        return _info_dict(info), self._stats(st)

@@ -31,7 +31,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-REF = os.environ.get("SGLD_REFERENCE", "/root/reference")
+from oracle.refpath import reference_root  # noqa: E402
+
+REF = reference_root()
+if REF is None:
+    sys.exit("reference checkout not found: set SGLD_REFERENCE to its root")
 
 
 def _parse_matrix(text: str) -> np.ndarray:

@@ -4,7 +4,7 @@ the solid mask and the passive mask bit-packed in the file's column-major
 voxel order, the fixations and the loads.  The GPU tests cannot read the
 reference checkout, so they load this compact copy.
 
-    python tests/golden/make_topvoxel_fixture.py /root/reference/data/part_R256.TopVoxel
+    python tests/golden/make_topvoxel_fixture.py $SGLD_REFERENCE/data/part_R256.TopVoxel
 """
 import os
 import sys

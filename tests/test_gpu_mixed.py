@@ -33,7 +33,7 @@ def test_mixed_converges_true_residual(graded):
     m, s, U_ref = graded
     U, info = s.pcg(m.F, tol=1e-6, maxIT=500, precision="mixed")
     assert info["converged"]
-    assert info["true_relres"] < 1.05e-6
+    assert info["true_relres"] <= 1e-6
     _, c = s.TopOpti_ComputeUnitCompliance(U)
     c_ref = G.compliance(m, U_ref)
     assert abs(c - c_ref) / abs(c_ref) <= 1e-6
@@ -82,13 +82,13 @@ def test_mixed_df_converges_like_mixed(graded):
     m, s, U_ref = graded
     U, info = s.pcg(m.F, tol=1e-6, maxIT=500, precision="mixed_df")
     _, imx = s.pcg(m.F, tol=1e-6, maxIT=500, precision="mixed")
-    assert info["converged"] and info["true_relres"] < 1.05e-6
+    assert info["converged"] and info["true_relres"] <= 1e-6
     assert abs(info["its"] - imx["its"]) <= 1
     _, c = s.TopOpti_ComputeUnitCompliance(U)
     c_ref = G.compliance(m, U_ref)
     assert abs(c - c_ref) / abs(c_ref) <= 1e-6
     U9, info9 = s.pcg(m.F, tol=1e-9, maxIT=500, precision="mixed_df")
-    assert info9["converged"] and info9["true_relres"] < 2e-9
+    assert info9["converged"] and info9["true_relres"] <= 1e-9
     assert np.linalg.norm(U9 - U_ref) / np.linalg.norm(U_ref) <= 1e-5
 
 
@@ -102,7 +102,7 @@ def test_mixed_adaptive_inner_stop(graded):
     res = {}
     for eta in (0.0, 1e-2, 1e-4):
         U, info = s.pcg(m.F, tol=1e-6, maxIT=500, precision="mixed_df", inner_tol=eta)
-        assert info["converged"] and info["true_relres"] < 1.05e-6
+        assert info["converged"] and info["true_relres"] <= 1e-6
         assert 0 < info["inner_its"] <= 64 * info["its"]
         _, c = s.TopOpti_ComputeUnitCompliance(U)
         assert abs(c - c_ref) / abs(c_ref) <= 1e-6
@@ -140,6 +140,44 @@ def test_mixed_fallback_to_fp64(built_lib):
     Uc, ic = s.pcg(F, tol=1e-8, maxIT=500, precision="mixed_df")
     assert not ic["fallback"] and ic["converged"]
     assert np.linalg.norm(Uc - U64) <= 1e-6 * np.linalg.norm(U64)
+
+
+def test_mixed_residual_replacement(built_lib):
+    """A mixed solve counts as converged only on its true residual.  An iterate
+    that drifted after the recurrence met tol (planted on the host:
+    sgld_inject_fault kind 2 scales x by 1 + 1e-3) has a true residual above
+    tol; the outer PCG then restarts from x with r = b - K x and the answer
+    meets tol on the residual recomputed independently with the FP64 K*u.  A
+    clean solve makes no replacement; the block path restarts such a case too."""
+    import numpy as np
+
+    from sgldbench_gb300 import VoxelSolver
+    from sgldbench_gb300 import domains as D
+
+    vox = D.cuboid(32, 16, 16)
+    s = VoxelSolver(vox, num_levels=3, non_dyadic=0, omega=0.6, pad=False)
+    F, fixed = D.cantilever3(vox, s.nodMapBack(1))
+    s.set_fixed_dofs(fixed)
+    s.set_modulus(np.random.default_rng(3).uniform(0.2, 1.0, s.numElements))
+    s.Solving_AssembleFEAstencil()
+    U_ref, _ = s.pcg(F, tol=1e-11, maxIT=2000, precision="fp64")
+    tol = 1e-6
+    U0, i0 = s.pcg(F, tol=tol, maxIT=500, precision="mixed_df")
+    assert i0["converged"] and i0["replacements"] == 0 and not i0["fallback"]
+    for prec in ("mixed_df", "mixed"):
+        s.inject_fault(2)
+        U, info = s.pcg(F, tol=tol, maxIT=500, precision=prec)
+        assert info["replacements"] >= 1 and not info["fallback"], info
+        assert info["converged"] and info["true_relres"] <= tol, info
+        assert info["its"] > i0["its"]
+        r = F - s.Solving_KbyU_MatrixFree(U)
+        assert np.linalg.norm(r) / np.linalg.norm(F) <= 1.0001 * tol
+        _, c = s.TopOpti_ComputeUnitCompliance(U)
+        _, c_ref = s.TopOpti_ComputeUnitCompliance(U_ref)
+        assert abs(c - c_ref) <= 1e-6 * abs(c_ref)
+    U1, i1 = s.pcg(F, tol=tol, maxIT=500, precision="mixed_df")
+    assert i1["replacements"] == 0 and np.array_equal(U1, U0)
+    s.close()
 
 
 def test_run_to_run_determinism(built_lib):

@@ -12,11 +12,13 @@ import numpy as np
 import pytest
 
 from oracle import glue as G
+from oracle.refpath import reference_root
 from sgldbench_gb300 import topvoxel as T
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURE = os.path.join(HERE, "golden", "part_R256_model.npz")
-REF_FILE = "/root/reference/data/part_R256.TopVoxel"
+_REF = reference_root()
+REF_FILE = os.path.join(_REF, "data", "part_R256.TopVoxel") if _REF else ""
 
 
 def test_fixture_counts():
@@ -31,7 +33,7 @@ def test_fixture_counts():
     assert flat[m.passive - 1].all()
 
 
-@pytest.mark.skipif(not os.path.exists(REF_FILE), reason="reference checkout not present")
+@pytest.mark.skipif(not os.path.exists(REF_FILE), reason="reference checkout not found (SGLD_REFERENCE)")
 def test_reader_matches_fixture():
     a = T.read_topvoxel(REF_FILE)
     b = T.model_from_npz(FIXTURE)

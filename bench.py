@@ -148,6 +148,8 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         t0 = self.marks[0] if self.marks else 0.0
+        if not any(t >= t0 for t, _ in self.lines):   # a timed region shorter than the interval
+            t0 = 0.0
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for t, ln in self.lines:
@@ -312,7 +314,8 @@ def run_ours(args):
         F_d = dev_load(case)
         info, st = lc.solve_device(F_d.data_ptr(), U_d.data_ptr(), mode="learned", train=True, tol=TOL,
                                    maxIT=args.maxit, precision=args.precision)
-        train_rec.append((info["its"], info["inner_its"], st["t_solve"], st["t_train"], st["net_loss"]))
+        train_rec.append((info["its"], info["inner_its"], st["t_solve"], st["t_train"], st["net_loss_before"],
+                          st["net_loss"]))
         del F_d
     t_train = time.perf_counter() - t0
     held_d = [dev_load(c) for c in held]
@@ -332,7 +335,7 @@ def run_ours(args):
     e0.record(stream)
     recs = []
     for k in range(args.steps):
-        recs.append(step(k))
+        recs.append(step(k)[0])
     e1.record(stream)
     torch.cuda.synchronize()
     launches = (kernel_launches() - l0) / max(args.steps, 1)
@@ -358,13 +361,20 @@ def run_ours(args):
     clocks = sampler.stop()
     # the starts compared on the first held-out cases (untimed): zero, basis only, basis + network
     cmp = {"zero": [], "basis": [], "learned": []}
+    U_mx = None
     for j in range(min(2, len(held))):
         for mode in ("zero", "basis", "learned"):
             info, st = lc.solve_device(held_d[j].data_ptr(), U_d.data_ptr(), mode=mode, tol=TOL, maxIT=args.maxit,
                                        precision=args.precision, diagnostics=True)
             cmp[mode].append({"its": info["its"], "inner_its": info["inner_its"], "seconds": st["t_start"] +
                               st["t_solve"], "start_ratio": st["start_ratio"], "net_accepted": st["net_accepted"]})
-    U_mx = U_d.clone()   # case 0, learned start
+            if j == 0 and mode == "learned":
+                U_mx = U_d.clone()   # case 0 from the learned start, the headline's answer
+    gain = {m: float(np.mean([r["inner_its"] for r in cmp[m]])) for m in cmp}
+    net_gain = {"inner_its_basis_only": gain["basis"], "inner_its_with_network": gain["learned"],
+                "inner_its_zero_start": gain["zero"],
+                "network_vs_basis": gain["basis"] / gain["learned"] if gain["learned"] else None,
+                "learned_vs_zero": gain["zero"] / gain["learned"] if gain["learned"] else None}
     # the reference form on case 0: FP64 PCG with the FP64 V-cycle from zero
     fp64 = None
     if args.fp64_steps > 0:
@@ -417,9 +427,9 @@ def run_ours(args):
             "gpu_launches": int(round(launches)), "roofline": rl, "clocks": clocks,
             "learned": {"train_cases": len(train), "basis": lc.basis_size,
                         "train_s_wall": t_train,
-                        "train": [{"its": a, "inner_its": b, "t_solve": c, "t_train": d, "net_loss": e}
-                                  for a, b, c, d, e in train_rec],
-                        "held_out_compare": cmp,
+                        "train": [{"its": a, "inner_its": b, "t_solve": c, "t_train": d, "net_loss_before": e,
+                                   "net_loss": f} for a, b, c, d, e, f in train_rec],
+                        "held_out_compare": cmp, "gain": net_gain,
                         "start": "energy-optimal combination of the training solutions' basis plus the "
                                  "coarse-level network's correction when it lowers r'Mr"},
             "memory_bytes": int(total - free), "host_setup_s": t_host}

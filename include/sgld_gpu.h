@@ -503,7 +503,7 @@ int sgld_net_train_step(sgld_net *net, const float *x, const float *target, cons
  * No counterpart in the reference, which solves every new load case from
  * U_ = 0 (Solving_CG_GMGS.m:7; GUIs/Mtd_StructuralRobustnessExploration.m:119
  * re-solves per rotated load).  The object learns from the solves it is given
- * for training: a K-orthonormal basis of their solutions (FP32, compact DOF
+ * for training: a K-orthonormal basis of their solutions (FP64, compact DOF
  * order, at most max_basis <= 32 vectors) and, with net_level >= 0, a U-Net on a
  * coarse level trained on (residual left by the basis start -> correction the
  * solve found) pairs.  A new case starts from the energy-optimal combination of
@@ -512,7 +512,8 @@ int sgld_net_train_step(sgld_net *net, const float *x, const float *target, cons
  * other, so the start changes iteration counts, never the converged answer.
  * net_level: MATLAB level index of the network's grid, 0 = the finest level of
  * at most 110K nodes, -1 = no network.  train_steps: Adam steps per training
- * case.  Memory: max_basis * numDOFs * 4 bytes plus four full-grid FP64 vectors. */
+ * case.  Memory: max_basis * numDOFs * 8 bytes plus four full-grid FP64 vectors.
+ * Destroy it before its context. */
 typedef struct sgld_cases sgld_cases;
 
 typedef struct sgld_cases_stats {
@@ -523,7 +524,8 @@ typedef struct sgld_cases_stats {
     double net_ratio;    /* sqrt(r'Mr) with the kept correction / without it */
     double basis_ratio;  /* diagnostics: sqrt(r'Mr) of the basis start / of the zero start */
     double start_ratio;  /* diagnostics: the same for the start used */
-    double net_loss;     /* training loss after this case's Adam steps */
+    double net_loss_before;  /* train: loss on this case's sample before its Adam steps */
+    double net_loss;     /* train: loss on this case's sample after them */
     double t_start;      /* device seconds forming the start (CUDA events) */
     double t_solve;      /* device seconds of the solve */
     double t_train;      /* device seconds adding the case to the basis and training */

@@ -39,7 +39,7 @@ class SolveInfo(C.Structure):
 
 class CasesStats(C.Structure):
     _fields_ = [("diagnostics", i32), ("basis", i32), ("net_used", i32), ("net_accepted", i32), ("net_ratio", dbl),
-                ("basis_ratio", dbl), ("start_ratio", dbl), ("net_loss", dbl), ("t_start", dbl), ("t_solve", dbl),
+                ("basis_ratio", dbl), ("start_ratio", dbl), ("net_loss_before", dbl), ("net_loss", dbl), ("t_start", dbl), ("t_solve", dbl),
                 ("t_train", dbl)]
 
 

@@ -3,11 +3,13 @@
 // the basis, and storing a new basis vector.
 //
 // The basis lives in the compact DOF order (active nodes only, node-major
-// [ux uy uz]) in FP32, so a model with 30 % active voxels stores 3.5x less
+// [ux uy uz]) in FP64, so a model with 30 % active voxels stores 3.5x less
 // than on the full grid; nodal vectors of the solver live on the full grid,
 // and DOF n of the compact order is full-grid entry 3 map[n / 3] + n % 3.
-// Every pass reads each basis vector once (HBM-bound: 4 bytes per DOF per
-// basis vector plus 8 bytes per DOF of the solver vector).
+// FP64, because a start rounded to FP32 leaves a high-frequency residual near
+// 1e-3 of ||F|| that the solve must then remove.  Every pass reads each basis
+// vector once (HBM-bound: 8 bytes per DOF per basis vector plus the solver
+// vector's 8 bytes per DOF).
 #include "sgld_internal.cuh"
 
 namespace sgld {
@@ -21,7 +23,7 @@ __device__ __forceinline__ int64_t full_index(const int64_t *map, int64_t n) {
 }
 
 // part[i * gridDim.x + block] = sum over this block's DOFs of W_i[n] v(n)
-__global__ void __launch_bounds__(CB_THREADS) k_basis_dots(const float *__restrict__ W, int k, int64_t nd,
+__global__ void __launch_bounds__(CB_THREADS) k_basis_dots(const double *__restrict__ W, int k, int64_t nd,
                                                            const double *__restrict__ v,
                                                            const int64_t *__restrict__ map,
                                                            double *__restrict__ part) {
@@ -32,7 +34,7 @@ __global__ void __launch_bounds__(CB_THREADS) k_basis_dots(const float *__restri
         const double vn = v[full_index(map, n)];
 #pragma unroll
         for (int i = 0; i < CB_MAXK; ++i)
-            if (i < k) acc[i] += (double)W[(int64_t)i * nd + n] * vn;
+            if (i < k) acc[i] += W[(int64_t)i * nd + n] * vn;
     }
     __shared__ double red[CB_THREADS / 32][CB_MAXK];
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -65,7 +67,7 @@ __global__ void k_basis_finalize(const double *__restrict__ part, int nb, int k,
 }
 
 // x(n) = beta x(n) + alpha sum_i coef[i] W_i[n] on the full grid
-__global__ void __launch_bounds__(CB_THREADS) k_basis_combine(const float *__restrict__ W, int k, int64_t nd,
+__global__ void __launch_bounds__(CB_THREADS) k_basis_combine(const double *__restrict__ W, int k, int64_t nd,
                                                               const double *__restrict__ coef, double alpha,
                                                               double beta, double *__restrict__ x,
                                                               const int64_t *__restrict__ map) {
@@ -74,7 +76,7 @@ __global__ void __launch_bounds__(CB_THREADS) k_basis_combine(const float *__res
     __syncthreads();
     for (int64_t n = blockIdx.x * (int64_t)CB_THREADS + threadIdx.x; n < nd; n += (int64_t)gridDim.x * CB_THREADS) {
         double s = 0.0;
-        for (int i = 0; i < k; ++i) s += c[i] * (double)W[(int64_t)i * nd + n];
+        for (int i = 0; i < k; ++i) s += c[i] * W[(int64_t)i * nd + n];
         const int64_t f = full_index(map, n);
         x[f] = (beta == 0.0 ? 0.0 : beta * x[f]) + alpha * s;
     }
@@ -82,9 +84,9 @@ __global__ void __launch_bounds__(CB_THREADS) k_basis_combine(const float *__res
 
 // Wk[n] = scale * w(n)
 __global__ void k_basis_store(const double *__restrict__ w, const int64_t *__restrict__ map, int64_t nd,
-                              double scale, float *__restrict__ Wk) {
+                              double scale, double *__restrict__ Wk) {
     for (int64_t n = blockIdx.x * (int64_t)CB_THREADS + threadIdx.x; n < nd; n += (int64_t)gridDim.x * CB_THREADS)
-        Wk[n] = (float)(scale * w[full_index(map, n)]);
+        Wk[n] = scale * w[full_index(map, n)];
 }
 
 static int basis_blocks(int64_t nd) {
@@ -96,7 +98,7 @@ int basis_max() { return CB_MAXK; }
 int basis_partials(int64_t nd) { return basis_blocks(nd); }
 
 // out[0..k) = scale * W_i . v  (part: k * basis_partials(nd) doubles)
-void launch_basis_dots(const float *W, int k, int64_t nd, const double *v, const int64_t *map, double *part,
+void launch_basis_dots(const double *W, int k, int64_t nd, const double *v, const int64_t *map, double *part,
                        double scale, double *out, cudaStream_t s) {
     if (k <= 0) return;
     const int nb = basis_blocks(nd);
@@ -105,13 +107,13 @@ void launch_basis_dots(const float *W, int k, int64_t nd, const double *v, const
     k_basis_finalize<<<k, 32, 0, s>>>(part, nb, k, scale, out);
 }
 
-void launch_basis_combine(const float *W, int k, int64_t nd, const double *coef, double alpha, double beta,
+void launch_basis_combine(const double *W, int k, int64_t nd, const double *coef, double alpha, double beta,
                           double *x, const int64_t *map, cudaStream_t s) {
     ++g_launches;
     k_basis_combine<<<basis_blocks(nd), CB_THREADS, 0, s>>>(W, k, nd, coef, alpha, beta, x, map);
 }
 
-void launch_basis_store(const double *w, const int64_t *map, int64_t nd, double scale, float *Wk, cudaStream_t s) {
+void launch_basis_store(const double *w, const int64_t *map, int64_t nd, double scale, double *Wk, cudaStream_t s) {
     ++g_launches;
     k_basis_store<<<basis_blocks(nd), CB_THREADS, 0, s>>>(w, map, nd, scale, Wk);
 }

@@ -7,7 +7,7 @@
 // The object learns from the solves it is given for training:
 //   * a basis W of the training solutions, K-orthonormal (W_i' K W_j = d_ij,
 //     classical Gram-Schmidt applied twice, K by the double-float K*u), stored
-//     in FP32 in the compact DOF order;
+//     in FP64 in the compact DOF order;
 //   * a U-Net (sgld_net.cuh) on a coarse multigrid level, trained on the
 //     training solves' own pairs: features of the residual that the basis
 //     start leaves, r0 = F - K x_b, with the basis start x_b, the log-modulus
@@ -31,11 +31,11 @@
 namespace sgld {
 int basis_max();
 int basis_partials(int64_t nd);
-void launch_basis_dots(const float *W, int k, int64_t nd, const double *v, const int64_t *map, double *part,
+void launch_basis_dots(const double *W, int k, int64_t nd, const double *v, const int64_t *map, double *part,
                        double scale, double *out, cudaStream_t s);
-void launch_basis_combine(const float *W, int k, int64_t nd, const double *coef, double alpha, double beta,
+void launch_basis_combine(const double *W, int k, int64_t nd, const double *coef, double alpha, double beta,
                           double *x, const int64_t *map, cudaStream_t s);
-void launch_basis_store(const double *w, const int64_t *map, int64_t nd, double scale, float *Wk, cudaStream_t s);
+void launch_basis_store(const double *w, const int64_t *map, int64_t nd, double scale, double *Wk, cudaStream_t s);
 }  // namespace sgld
 
 using namespace sgld;
@@ -44,7 +44,7 @@ struct sgld_cases {
     sgld_ctx *ctx = nullptr;
     int kmax = 0, k = 0;
     int64_t nd = 0;                       // compact DOFs
-    float *W = nullptr;                   // [kmax][nd] K-orthonormal basis, compact order
+    double *W = nullptr;                  // [kmax][nd] K-orthonormal basis, compact order
     double *d_coef = nullptr;             // [2 * CB_MAXK] projection coefficients
     double *d_bpart = nullptr;            // basis dot partials
     double *d_xb = nullptr, *d_r0 = nullptr, *d_w = nullptr, *d_kw = nullptr;   // full-grid FP64
@@ -248,6 +248,11 @@ int net_train(sgld_cases *cs, int steps, float lr, sgld_cases_stats *st) {
     net_target(cs->d_ec, ll.nflag, cs->Vc, se, cs->ts[slot], cs->ms[slot], s);
     cs->head = (cs->head + 1) % ring;
     if (cs->nsamp < ring) ++cs->nsamp;
+    // the new sample's loss before training (the network as it stood for this case)
+    cs->net.X.a = cs->xs[slot];
+    net_forward(cs->net);
+    net_loss(cs->net, cs->ts[slot], cs->ms[slot]);
+    CCK(cudaMemcpyAsync(&st->net_loss_before, cs->net.d_loss, sizeof(double), cudaMemcpyDeviceToHost, s));
     // most recent sample first, then back through the ring
     for (int k = 0; k < steps; ++k) {
         const int i = (slot - (k % cs->nsamp) + ring) % ring;
@@ -258,6 +263,10 @@ int net_train(sgld_cases *cs, int steps, float lr, sgld_cases_stats *st) {
         net_adam_step(cs->net, lr);
     }
     cs->ready = true;
+    // and after
+    cs->net.X.a = cs->xs[slot];
+    net_forward(cs->net);
+    net_loss(cs->net, cs->ts[slot], cs->ms[slot]);
     CCK(cudaGetLastError());
     CCK(cudaMemcpyAsync(&st->net_loss, cs->net.d_loss, sizeof(double), cudaMemcpyDeviceToHost, s));
     CCK(cudaStreamSynchronize(s));

@@ -149,9 +149,9 @@ int sgld_kbyu_tile(const sgld_ctx *ctx, int *tile_x, int *z_chunk);
 /* Allocation-free K*u with its dot product (no counterpart in the reference).
  *
  * For callers that must not allocate device memory when they apply the
- * operator: a stream being captured into a CUDA graph, a real-time loop whose
- * device memory budget is fixed at start-up, or a plugin in a process whose
- * device memory belongs to another framework's caching allocator.  Enqueues,
+ * operator: a real-time loop whose device memory budget is fixed at start-up,
+ * or a plugin in a process whose device memory belongs to another framework's
+ * caching allocator.  Enqueues,
  * on `stream` (a cudaStream_t; NULL = the legacy default stream),
  *     d_y = K d_u (fixed DOFs of d_y set to 0)   and   *d_dot = d_u . d_y,
  * for the context's current moduli.  d_u and d_y are device arrays in the
@@ -161,12 +161,11 @@ int sgld_kbyu_tile(const sgld_ctx *ctx, int *tile_x, int *z_chunk);
  * array of SGLD_NOALLOC_MAX_CTAS doubles (256 KiB) that every GPU loading this
  * library holds until the process exits.  The first call on a device looks up
  * that array's address (once per device, the context's device must be
- * current); make that first call before any stream capture.  Every call
- * shares the array, so calls that overlap on the GPU (other streams, other
- * contexts on the same device) race; serialise them.  The call uploads no
- * constants: if the device holds another context's element matrix, it returns
- * SGLD_ERR_STATE, and any other call on this context (before the capture)
- * binds the matrix again.  Grids needing more than
+ * current).  Every call shares the array, so calls that overlap on the GPU
+ * (other streams, other contexts on the same device) race; serialise them.
+ * The call uploads no constants: if the device holds another context's
+ * element matrix, it returns SGLD_ERR_STATE, and any other call on this
+ * context binds the matrix again.  Grids needing more than
  * SGLD_NOALLOC_MAX_CTAS CTAs (on the order of 1e8 nodes; each CTA covers a
  * 31 x 7 x 16 node block) are rejected with SGLD_ERR_ARG. */
 #define SGLD_NOALLOC_MAX_CTAS 32768

@@ -100,7 +100,8 @@ template <bool DOT>
 __global__ void __launch_bounds__(DT_THREADS) k_kbyu_df(const double *__restrict__ u, double *__restrict__ y,
                                                         const double *__restrict__ E,
                                                         const uint8_t *__restrict__ nflag, int ny, int nx, int nz,
-                                                        double *__restrict__ partial) {
+                                                        double *__restrict__ partial,
+                                                        const uint8_t *__restrict__ tiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     df *su = reinterpret_cast<df *>(smem_raw);   // [2][DT_NL*3] node layers (hi, lo)
     df *so = su + 2 * DT_NL * 3;                 // [24][DT_THREADS]
@@ -113,6 +114,20 @@ __global__ void __launch_bounds__(DT_THREADS) k_kbyu_df(const double *__restrict
     const bool owner = (ty < DT_Y - 1) && (tx < DT_X - 1) && gny < NY && gnx < NX;
     const int ey = y0 - 1 + ty, ex = x0 - 1 + tx;
     const bool ein = ey >= 0 && ey < ny && ex >= 0 && ex < nx;
+    if (tiles && !tiles[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)]) {
+        // no active element in the CTA's box: its nodes are inactive, K*u is zero there
+        if (owner) {
+            const int64_t node0 = (int64_t)gny + (int64_t)NY * gnx;
+            for (int z = z0; z < zend; ++z) {
+                double *o = y + 3 * (node0 + (int64_t)NY * NX * z);
+                o[0] = 0.0;
+                o[1] = 0.0;
+                o[2] = 0.0;
+            }
+        }
+        if (DOT && tid == 0) partial[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = 0.0;
+        return;
+    }
     int soff[DT_SV];
 #pragma unroll
     for (int k = 0; k < DT_SV; ++k) {
@@ -226,9 +241,11 @@ void launch_kbyu_df(const Level &l0, const double *E, const double *u, double *y
     if (nblocks_out) *nblocks_out = (int)(g.x * g.y * g.z);
     ++g_launches;
     if (partial_dot)
-        k_kbyu_df<true><<<g, DT_THREADS, kbyu_df_smem(), s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, partial_dot);
+        k_kbyu_df<true><<<g, DT_THREADS, kbyu_df_smem(), s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, partial_dot,
+                                                             l0.tiles16);
     else
-        k_kbyu_df<false><<<g, DT_THREADS, kbyu_df_smem(), s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, nullptr);
+        k_kbyu_df<false><<<g, DT_THREADS, kbyu_df_smem(), s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, nullptr,
+                                                              l0.tiles16);
 }
 
 }  // namespace sgld

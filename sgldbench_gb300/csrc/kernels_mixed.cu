@@ -271,6 +271,93 @@ void launch_icg_dupdate(float *e, float *d, const float *w, int64_t n, const dou
     k_icg_dupdate<<<reduce_blocks(n), MB, 0, st>>>(e, d, w, n, sc);
 }
 
+// ---- the same two updates over the active runs only -------------------------
+// On a grid with inactive regions the inner CG's vectors are exactly zero
+// outside the active bricks (32 y x 8 x x 8 z nodes holding an active node):
+// the inner solve's entry kernel and the K*u write every node, and these
+// updates keep zeros zero.  So the updates may visit only the bricks'
+// y-runs (runs[i] = first DOF | floats << 40, at most 96 floats each): a
+// warp per run, lanes over its floats.  Sums visit the runs in a fixed order.
+constexpr int RUN_SHIFT = 40;
+constexpr int64_t RUN_MASK = (int64_t(1) << RUN_SHIFT) - 1;
+
+__global__ void __launch_bounds__(MB) k_icg_update_runs(float *__restrict__ s, const float *__restrict__ t,
+                                                        const int64_t *__restrict__ runs, int64_t nruns,
+                                                        const double *__restrict__ sc, double *__restrict__ part) {
+    const float a = (float)sc[IS_ALPHA];
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = (int64_t)blockIdx.x * (MB / 32) + (threadIdx.x >> 5), nw = (int64_t)gridDim.x * (MB / 32);
+    float acc = 0.f;
+    for (int64_t r = w0; r < nruns; r += nw) {
+        const int64_t rv = runs[r];
+        const int64_t b = rv & RUN_MASK;
+        const int len = (int)(rv >> RUN_SHIFT);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int j = lane + 32 * k;
+            if (j < len) {
+                const float v = fmaf(-a, t[b + j], s[b + j]);
+                s[b + j] = v;
+                acc = fmaf(v, v, acc);
+            }
+        }
+    }
+    if (part) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        __shared__ double wred[MB / 32];
+        if (lane == 0) wred[threadIdx.x >> 5] = (double)acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tt = 0.0;
+            for (int k = 0; k < MB / 32; ++k) tt += wred[k];
+            part[blockIdx.x] = tt;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(MB) k_icg_dupdate_runs(float *__restrict__ e, float *__restrict__ d,
+                                                         const float *__restrict__ w,
+                                                         const int64_t *__restrict__ runs, int64_t nruns,
+                                                         const double *__restrict__ sc) {
+    const float a = (float)sc[IS_ALPHA], bt = (float)sc[IS_BETA];
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = (int64_t)blockIdx.x * (MB / 32) + (threadIdx.x >> 5), nw = (int64_t)gridDim.x * (MB / 32);
+    for (int64_t r = w0; r < nruns; r += nw) {
+        const int64_t rv = runs[r];
+        const int64_t b = rv & RUN_MASK;
+        const int len = (int)(rv >> RUN_SHIFT);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int j = lane + 32 * k;
+            if (j < len) {
+                const float dv = d[b + j];
+                e[b + j] = fmaf(a, dv, e[b + j]);
+                d[b + j] = fmaf(bt, dv, w[b + j]);
+            }
+        }
+    }
+}
+
+static int run_blocks(int64_t nruns) {
+    const int64_t b = (nruns + MB / 32 - 1) / (MB / 32);
+    return (int)(b < 1216 ? (b > 0 ? b : 1) : 1216);   // 152 SMs x 8 CTAs
+}
+
+int launch_icg_update_runs(float *s, const float *t, const int64_t *runs, int64_t nruns, const double *sc,
+                           double *part, cudaStream_t st) {
+    ++g_launches;
+    const int nb = run_blocks(nruns);
+    k_icg_update_runs<<<nb, MB, 0, st>>>(s, t, runs, nruns, sc, part);
+    return nb;
+}
+
+void launch_icg_dupdate_runs(float *e, float *d, const float *w, const int64_t *runs, int64_t nruns,
+                             const double *sc, cudaStream_t st) {
+    ++g_launches;
+    k_icg_dupdate_runs<<<run_blocks(nruns), MB, 0, st>>>(e, d, w, runs, nruns, sc);
+}
+
 // z64 = e32 + alpha d32 (the last iteration's deferred step; masked at fixed
 // DOFs by construction), partials of z.r and z.q
 __global__ void k_widen_dots(const float *__restrict__ e, const float *__restrict__ d,

@@ -152,12 +152,61 @@ __device__ __forceinline__ void async_copy(T *dst, const T *src) {
 __device__ __forceinline__ void async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// A CTA whose element box holds no active element: every node it owns is
+// inactive and its K*u is exactly zero, so it writes zeros (no loads, no
+// element work) and a zero dot partial.  The whole CTA takes this branch.
+template <typename T>
+__device__ __forceinline__ void skip_tile(T *__restrict__ y, bool owner, int gny, int gnx, int NY, int NX, int z0,
+                                          int zend, double *__restrict__ partial) {
+    if (owner) {
+        const int64_t node0 = (int64_t)gny + (int64_t)NY * gnx;
+        for (int z = z0; z < zend; ++z) {
+            T *o = y + 3 * (node0 + (int64_t)NY * NX * z);
+            o[0] = T(0);
+            o[1] = T(0);
+            o[2] = T(0);
+        }
+    }
+    if (partial && threadIdx.x == 0) partial[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = 0.0;
+}
+
+// Active-tile map of a z-marching K*u grid g whose CTAs own (TY-1) x (TX-1)
+// node columns and zc node layers: a CTA is active iff an element of its box
+// -- elements y0-1 .. y0+TY-2, x0-1 .. x0+TX-2, z0-1 .. z0+zc (a superset of
+// what any of the kernels reads) -- is active.  One warp per CTA.
+__global__ void k_tile_map(const uint8_t *__restrict__ eact, int ny, int nx, int nz, int TY, int TX, int zc,
+                           dim3 g, uint8_t *__restrict__ out) {
+    const int64_t ntile = (int64_t)g.x * g.y * g.z;
+    const int64_t t = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (t >= ntile) return;
+    const int lane = threadIdx.x & 31;
+    const int bx = (int)(t % g.x), by = (int)((t / g.x) % g.y), bz = (int)(t / ((int64_t)g.x * g.y));
+    const int y0 = bx * (TY - 1) - 1, x0 = by * (TX - 1) - 1, z0 = bz * zc - 1;
+    bool act = false;
+    for (int ly = lane; ly < TY; ly += 32) {
+        const int ey = y0 + ly;
+        if (ey < 0 || ey >= ny) continue;
+        for (int ex = max(x0, 0); ex < min(x0 + TX, nx); ++ex)
+            for (int ez = max(z0, 0); ez < min(z0 + zc + 2, nz); ++ez)
+                act |= eact[ey + (int64_t)ny * (ex + (int64_t)nx * ez)] != 0;
+    }
+    act = __any_sync(0xffffffffu, act);
+    if (lane == 0) out[t] = act ? 1 : 0;
+}
+
+static void make_tile_map(const Level &l, int TY, int TX, int zc, dim3 g, uint8_t *out, cudaStream_t s) {
+    const int64_t ntile = (int64_t)g.x * g.y * g.z;
+    ++g_launches;
+    k_tile_map<<<(unsigned)((ntile + 3) / 4), 128, 0, s>>>(l.eact, l.ny, l.nx, l.nz, TY, TX, zc, g, out);
+}
+
 // y = K u on the full grid; y at fixed DOFs is 0.  When DOT, also writes
 // sum(u .* y) of this CTA's nodes to partial[block].
 template <typename T, bool DOT>
 __global__ void __launch_bounds__(KT_THREADS) k_kbyu(const T *__restrict__ u, T *__restrict__ y,
                                                      const T *__restrict__ E, const uint8_t *__restrict__ nflag,
-                                                     int ny, int nx, int nz, double *__restrict__ partial) {
+                                                     int ny, int nx, int nz, double *__restrict__ partial,
+                                                     const uint8_t *__restrict__ tiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *su = reinterpret_cast<T *>(smem_raw);      // [3][KT_NL*3] ring of node layers
     T *so = su + 3 * KT_NL * 3;                   // [24][KT_THREADS]
@@ -170,6 +219,10 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu(const T *__restrict__ u, T 
     const bool owner = (ty < KT_Y - 1) && (tx < KT_X - 1) && gny < NY && gnx < NX;
     const int ey = y0 - 1 + ty, ex = x0 - 1 + tx;
     const bool ein = ey >= 0 && ey < ny && ex >= 0 && ex < nx;
+    if (tiles && !tiles[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)]) {
+        skip_tile(y, owner, gny, gnx, NY, NX, z0, zend, DOT ? partial : nullptr);
+        return;
+    }
     T acc0 = T(0), acc1 = T(0), acc2 = T(0);
     T dot = T(0);
 
@@ -379,7 +432,8 @@ __device__ __forceinline__ int xslot(int z) { return (z + KX_RING) % KX_RING; }
 template <int TX, bool DOT>
 __global__ void __launch_bounds__(KT_Y * TX, 1024 / (KT_Y * TX))
     k_kbyu_x2(const float *__restrict__ u, float *__restrict__ y, const float *__restrict__ E,
-              const uint8_t *__restrict__ nflag, int ny, int nx, int nz, int zc, double *__restrict__ partial) {
+              const uint8_t *__restrict__ nflag, int ny, int nx, int nz, int zc, double *__restrict__ partial,
+              const uint8_t *__restrict__ tiles) {
     using G = KxTile<TX>;
     constexpr int KT_X = TX, KT_THREADS = G::THREADS, KT_NL = G::NL, KT_SV = G::SV;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -396,6 +450,10 @@ __global__ void __launch_bounds__(KT_Y * TX, 1024 / (KT_Y * TX))
     const bool owner = (ty < KT_Y - 1) && (tx < KT_X - 1) && gny < NY && gnx < NX;
     const int ey = y0 - 1 + ty, ex = x0 - 1 + tx;
     const bool ein = ey >= 0 && ey < ny && ex >= 0 && ex < nx;
+    if (tiles && !tiles[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)]) {
+        skip_tile(y, owner, gny, gnx, NY, NX, z0, zend, DOT ? partial : nullptr);
+        return;
+    }
     int soff[KT_SV];
 #pragma unroll
     for (int k = 0; k < KT_SV; ++k) {
@@ -565,7 +623,7 @@ static void kbyu_launch(const Level &l0, const T *E, const T *u, T *y, double *p
     dim3 g = kbyu_grid(l0);
     if (nb) *nb = (int)(g.x * g.y * g.z);
     ++g_launches;
-    k_kbyu<T, DOT><<<g, KT_THREADS, smem, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, partial);
+    k_kbyu<T, DOT><<<g, KT_THREADS, smem, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, partial, l0.tiles16);
 }
 
 void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *y, double *partial_dot,
@@ -579,22 +637,54 @@ void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *
 void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
                      int *nblocks_out, cudaStream_t s) {
     const dim3 g = kbyu_x2_grid(l0);
-    const int zc = kbyu_f32_zc(l0);
+    const int zc = kbyu_f32_zc(l0), tx = kbyu_f32_tx(l0);
     if (nblocks_out) *nblocks_out = (int)(g.x * g.y * g.z);
     ++g_launches;
-    if (kbyu_f32_tx(l0) == 8) {
+    // the tile map only when it was made for this tile
+    const uint8_t *tiles = (l0.tiles_x2 && l0.tiles_x2_tx == tx && l0.tiles_x2_zc == zc) ? l0.tiles_x2 : nullptr;
+    if (tx == 8) {
         using G = KxTile<8>;
         if (partial_dot)
-            k_kbyu_x2<8, true><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, partial_dot);
+            k_kbyu_x2<8, true><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, partial_dot,
+                                                              tiles);
         else
-            k_kbyu_x2<8, false><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr);
+            k_kbyu_x2<8, false><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr,
+                                                               tiles);
     } else {
         using G = KxTile<16>;
         if (partial_dot)
-            k_kbyu_x2<16, true><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, partial_dot);
+            k_kbyu_x2<16, true><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc,
+                                                               partial_dot, tiles);
         else
-            k_kbyu_x2<16, false><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr);
+            k_kbyu_x2<16, false><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr,
+                                                                tiles);
     }
+}
+
+int update_kbyu_tiles(Level &l0, cudaStream_t s) {
+    cudaError_t e = cudaSuccess;
+    const dim3 g16 = kbyu_grid(l0);
+    if (!l0.tiles16) {
+        e = cudaMalloc((void **)&l0.tiles16, (size_t)g16.x * g16.y * g16.z);
+        if (e != cudaSuccess) return (int)e;
+        make_tile_map(l0, KT_Y, KT_X, KT_ZC, g16, l0.tiles16, s);
+    }
+    const int tx = kbyu_f32_tx(l0), zc = kbyu_f32_zc(l0);
+    if (l0.tiles_x2 && l0.tiles_x2_tx == tx && l0.tiles_x2_zc == zc) return 0;
+    const dim3 g = kbyu_x2_grid(l0);
+    const int64_t n = (int64_t)g.x * g.y * g.z;
+    if (n > l0.tiles_x2_cap) {
+        if (l0.tiles_x2) cudaFree(l0.tiles_x2);
+        l0.tiles_x2 = nullptr;
+        l0.tiles_x2_cap = 0;
+        e = cudaMalloc((void **)&l0.tiles_x2, (size_t)n);
+        if (e != cudaSuccess) return (int)e;
+        l0.tiles_x2_cap = n;
+    }
+    make_tile_map(l0, KT_Y, tx, zc, g, l0.tiles_x2, s);
+    l0.tiles_x2_tx = tx;
+    l0.tiles_x2_zc = zc;
+    return (int)cudaGetLastError();
 }
 
 int kbyu_num_blocks(const Level &l0) {

@@ -1,10 +1,9 @@
 // Allocation-free K*u with the p.Kp dot product.
 //
 // Some callers cannot allocate device memory at the moment they need the
-// operator: a stream that is being captured into a CUDA graph, a real-time
-// solver loop in a host application that fixes its device memory budget at
-// start-up, or a plugin whose process hands all device memory to another
-// framework's caching allocator.  sgld_kbyu_dot_noalloc serves them: its only
+// operator: a real-time solver loop in a host application that fixes its
+// device memory budget at start-up, or a plugin whose process hands all
+// device memory to another framework's caching allocator.  sgld_kbyu_dot_noalloc serves them: its only
 // scratch (one partial sum per CTA of the K*u grid) lives in the file-scope
 // device array below, which every GPU that loads this library holds until the
 // process exits.  The call itself allocates nothing.
@@ -49,7 +48,7 @@ extern "C" int sgld_kbyu_dot_noalloc(sgld_ctx *ctx, const double *d_u, double *d
         c.err = "sgld_kbyu_dot_noalloc: the context's device must be current";
         return SGLD_ERR_STATE;
     }
-    if (!kh_bound(c)) {   // uploading here could break a capture, so the caller binds first
+    if (!kh_bound(c)) {   // the call changes no device state besides its outputs and scratch
         c.err = "sgld_kbyu_dot_noalloc: the device holds another context's element matrix; call any other "
                 "entry point of this context (e.g. sgld_kbyu_device) first";
         return SGLD_ERR_STATE;

@@ -237,6 +237,7 @@ int fail(sgld_ctx *ctx, int code, const std::string &msg) {
     return code;
 }
 
+
 #define CK(x)                                                                                            \
     do {                                                                                                 \
         cudaError_t e_ = (x);                                                                            \
@@ -248,6 +249,40 @@ int fail(sgld_ctx *ctx, int code, const std::string &msg) {
         cudaError_t e_ = cudaGetLastError();                                                             \
         if (e_ != cudaSuccess) return fail(ctx, SGLD_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
     } while (0)
+
+// The finest level's active runs (Level::runs): the y-runs of every brick of
+// 32 (y) x 8 (x) x 8 (z) nodes that holds an active node, in address order.
+// Left empty when more than 85 % of the bricks are active (a solid box),
+// where the flat float4 kernels stream faster.
+int build_active_runs(sgld_ctx *ctx) {
+    Level &l0 = ctx->c.lv[0];
+    const int NY = l0.ny + 1, NX = l0.nx + 1, NZ = l0.nz + 1;
+    const int by = (NY + 31) / 32, bx = (NX + 7) / 8, bz = (NZ + 7) / 8;
+    std::vector<uint8_t> brick((size_t)by * bx * bz, 0);
+    for (int z = 0; z < NZ; ++z)
+        for (int x = 0; x < NX; ++x) {
+            const uint8_t *f = l0.h_nflag.data() + (size_t)NY * (x + (size_t)NX * z);
+            for (int y = 0; y < NY; ++y)
+                if (f[y] & NF_ACTIVE) brick[(size_t)(y / 32) + by * ((size_t)(x / 8) + (size_t)bx * (z / 8))] = 1;
+        }
+    size_t nact = 0;
+    for (uint8_t b : brick) nact += b;
+    if (nact > 0.85 * (double)brick.size()) return SGLD_OK;
+    std::vector<int64_t> runs;
+    runs.reserve(nact * 64);
+    for (int z = 0; z < NZ; ++z)
+        for (int x = 0; x < NX; ++x)
+            for (int yb = 0; yb < by; ++yb) {
+                if (!brick[(size_t)yb + by * ((size_t)(x / 8) + (size_t)bx * (z / 8))]) continue;
+                const int y0 = 32 * yb, len = 3 * std::min(32, NY - y0);
+                const int64_t first = 3 * ((int64_t)y0 + (int64_t)NY * (x + (int64_t)NX * z));
+                runs.push_back(first | ((int64_t)len << 40));
+            }
+    l0.nruns = (int64_t)runs.size();
+    CK(dalloc(&l0.runs, runs.size()));
+    CK(cudaMemcpy(l0.runs, runs.data(), sizeof(int64_t) * runs.size(), cudaMemcpyHostToDevice));
+    return SGLD_OK;
+}
 
 int setup_templates(sgld_ctx *ctx) {
     Ctx &c = ctx->c;
@@ -392,10 +427,14 @@ static int capture_inner(sgld_ctx *ctx, cudaStream_t s, cudaStream_t sb, int kma
     int nb = 0;
     vcycle_dev32(ctx, c.d_s32, c.d_z32, c.d_part2, &nb, sb);
     launch_icg_scalar(2, c.d_isc, c.d_part2, nb, sb, 0, 0);
-    launch_icg_dupdate(c.d_e32, c.d_d32, c.d_z32, nv, c.d_isc, sb);
+    if (l0.runs)
+        launch_icg_dupdate_runs(c.d_e32, c.d_d32, c.d_z32, l0.runs, l0.nruns, c.d_isc, sb);
+    else
+        launch_icg_dupdate(c.d_e32, c.d_d32, c.d_z32, nv, c.d_isc, sb);
     launch_kbyu_f32(l0, c.d_E32, c.d_d32, c.d_t32, c.d_part2, &nb, sb);
     launch_icg_scalar(1, c.d_isc, c.d_part2, nb, sb, 0, 0);
-    nb = launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.d_part2, sb);
+    nb = l0.runs ? launch_icg_update_runs(c.d_s32, c.d_t32, l0.runs, l0.nruns, c.d_isc, c.d_part2, sb)
+                 : launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.d_part2, sb);
     launch_icg_cond(h, c.d_isc, c.d_part2, nb, kmax, eta, c.d_scal, c.d_isc + IS_TOTAL, sb);
     CK(cudaStreamEndCapture(sb, &body));
     *body_n = g_launches - before;
@@ -442,10 +481,14 @@ static int inner_run_host(sgld_ctx *ctx, int kmax, double eta) {
         int nb = 0;
         vcycle_dev32(ctx, c.d_s32, c.d_z32, c.d_part2, &nb);
         launch_icg_scalar(2, c.d_isc, c.d_part2, nb, c.stream, 0, 0);
-        launch_icg_dupdate(c.d_e32, c.d_d32, c.d_z32, nv, c.d_isc, c.stream);
+        if (l0.runs)
+            launch_icg_dupdate_runs(c.d_e32, c.d_d32, c.d_z32, l0.runs, l0.nruns, c.d_isc, c.stream);
+        else
+            launch_icg_dupdate(c.d_e32, c.d_d32, c.d_z32, nv, c.d_isc, c.stream);
         launch_kbyu_f32(l0, c.d_E32, c.d_d32, c.d_t32, c.d_part2, &nb, c.stream);
         launch_icg_scalar(1, c.d_isc, c.d_part2, nb, c.stream, 0, 0);
-        nb = launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.d_part2, c.stream);
+        nb = l0.runs ? launch_icg_update_runs(c.d_s32, c.d_t32, l0.runs, l0.nruns, c.d_isc, c.d_part2, c.stream)
+                     : launch_icg_update(c.d_e32, c.d_s32, c.d_d32, c.d_t32, nv, c.d_isc, c.d_part2, c.stream);
         launch_icg_cond_flag(d_flag, c.d_isc, c.d_part2, nb, kmax, eta, c.d_scal, c.d_isc + IS_TOTAL, c.stream);
         int more = 0;
         CK(cudaMemcpyAsync(&more, d_flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
@@ -822,6 +865,7 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
         }
     }
     if (c.lv[0].nel_active == 0) return fail(ctx, SGLD_ERR_ARG, "the voxel grid has no solid voxel");
+    if (int rc = build_active_runs(ctx)) return rc;
     c.h_nodemap = ctx->nodemaps[0];
     c.h_elemap = ctx->elemaps[0];
     CK(dalloc(&c.d_nodemap, c.h_nodemap.size()));
@@ -864,7 +908,8 @@ void sgld_destroy(sgld_ctx *ctx) {
         cudaSetDevice(c.device);
     for (Level &l : c.lv) {
         for (void *p : {(void *)l.eact, (void *)l.nflag, (void *)l.diag, (void *)l.idiag, (void *)l.idiag32, (void *)l.Ks, (void *)l.r,
-                        (void *)l.x, (void *)l.r32, (void *)l.x32})
+                        (void *)l.x, (void *)l.r32, (void *)l.x32, (void *)l.tiles16, (void *)l.tiles_x2,
+                        (void *)l.runs})
             if (p) cudaFree(p);
     }
     for (void *p : {(void *)c.d_nodemap, (void *)c.d_elemap, (void *)c.E, (void *)c.d_E32, (void *)c.d_b,
@@ -1102,7 +1147,10 @@ static int tune_kbyu_f32(sgld_ctx *ctx) {
     if (c.kbyu_tuned) return SGLD_OK;
     c.kbyu_tuned = true;
     const char *v = getenv("SGLD_AUTOTUNE");
-    if (v && strcmp(v, "0") == 0) return SGLD_OK;
+    if (v && strcmp(v, "0") == 0) {
+        if (update_kbyu_tiles(l0, c.stream)) return fail(ctx, SGLD_ERR_CUDA, "K*u tile maps");
+        return SGLD_OK;
+    }
     const int NZ = l0.nz + 1;
     std::vector<int> cand;
     for (int zc : {7, 9, 11, 15, 21, 31, 47})
@@ -1118,6 +1166,7 @@ static int tune_kbyu_f32(sgld_ctx *ctx) {
         for (int zc : cand) {
             l0.kx_tx = tx;
             l0.kx_zc = zc;
+            if (update_kbyu_tiles(l0, c.stream)) return fail(ctx, SGLD_ERR_CUDA, "K*u tile maps");
             launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, c.stream);
             CK(cudaEventRecord(a, c.stream));
             for (int r = 0; r < 3; ++r) launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, c.stream);
@@ -1135,6 +1184,7 @@ static int tune_kbyu_f32(sgld_ctx *ctx) {
     cudaEventDestroy(b);
     l0.kx_tx = best_tx;
     l0.kx_zc = best_zc;
+    if (update_kbyu_tiles(l0, c.stream)) return fail(ctx, SGLD_ERR_CUDA, "K*u tile maps");
     CKL();
     return SGLD_OK;
 }

@@ -45,6 +45,19 @@ struct Level {
     int64_t nel = 0, nnode = 0;   // full-grid counts
     int64_t nel_active = 0, nnode_active = 0;
     uint8_t *eact = nullptr;      // [nel] element non-empty
+    // active-tile maps of the finest level's K*u launches (one byte per CTA:
+    // 0 = no active element in the CTA's element box, so every node it owns
+    // is inactive and its result is zero): the 32 x 8 x 16-layer grid of the
+    // FP64 and double-float kernels, and the FP32 kernel's grid for the tile
+    // (tiles_x2_tx, tiles_x2_zc) it was made for
+    uint8_t *tiles16 = nullptr, *tiles_x2 = nullptr;
+    // finest level: the y-runs of the active bricks (32 y x 8 x x 8 z nodes
+    // holding an active node), each first DOF | floats << 40, in address order;
+    // empty when nearly every brick is active (then the flat kernels run)
+    int64_t *runs = nullptr;
+    int64_t nruns = 0;
+    int tiles_x2_tx = 0, tiles_x2_zc = 0;
+    int64_t tiles_x2_cap = 0;
     uint8_t *nflag = nullptr;     // [nnode] NF_* bits
     double *diag = nullptr;       // [3*nnode] Jacobi diagonal (levels 1..L-1)
     double *idiag = nullptr;      // [3*nnode] 1 / diag on active nodes, 0 elsewhere
@@ -162,6 +175,8 @@ extern thread_local int64_t g_launches;
 void upload_kh(const double *Kh, cudaStream_t s);
 void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *y, double *partial_dot,
                      int *nblocks_out, cudaStream_t s);
+// (re)makes l0's active-tile maps for its current FP32 tile; 0 or a CUDA error
+int update_kbyu_tiles(Level &l0, cudaStream_t s);
 void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
                      int *nblocks_out, cudaStream_t s);
 void init_kernel_attributes();
@@ -187,6 +202,11 @@ void launch_set_cond(cudaGraphConditionalHandle h, unsigned v, cudaStream_t s);
 void launch_icg_cond_flag(int *flag, double *sc, const double *part, int nb, int kmax, double eta_min,
                           const double *outer, double *total, cudaStream_t s);
 void launch_icg_dupdate(float *e, float *d, const float *w, int64_t n, const double *sc, cudaStream_t st);
+// the same updates over the finest level's active runs (Level::runs)
+int launch_icg_update_runs(float *s, const float *t, const int64_t *runs, int64_t nruns, const double *sc,
+                           double *part, cudaStream_t st);
+void launch_icg_dupdate_runs(float *e, float *d, const float *w, const int64_t *runs, int64_t nruns,
+                             const double *sc, cudaStream_t st);
 void launch_widen_dots(const float *e, const float *d, const double *sc, double *z, const double *r,
                        const double *q, int64_t n, double *p1,
                        double *p2, int nb, cudaStream_t st);

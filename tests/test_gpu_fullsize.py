@@ -9,8 +9,11 @@
 * One iteration of the SIMP loop (TopOpti_GlobalVolumeConstraint_Tmp.m) on
   the same 256 x 128 x 128 cantilever: compliance, volume, change, sharpness
   and xPhys against the oracle's loop.
-* The real model data/part_R256.TopVoxel (1.85 M voxels, 5 levels): FP64 and
-  mixed solves against the oracle's FP64 solve of the same system.
+* The real model data/part_R256.TopVoxel (1.85 M voxels): FP64 and mixed
+  solves against the oracle's FP64 solve of the same system, on 5 dyadic
+  levels and on the reference's own default hierarchy (coarsestResolution-
+  Control_ = 50000 and nonDyadic_ = 1, Data_GlobalVariables.m:13-15: 4 levels,
+  a 4:1 first step, a 10 x 16 x 7-element coarsest grid).
 
 The oracle (C + numpy restatement of the reference) takes about half a
 minute of host time per solve at these sizes.
@@ -125,3 +128,41 @@ def test_part_mixed_matches_oracle(part):
     _, c = s.TopOpti_ComputeUnitCompliance(U)
     assert abs(c - c_ref) / abs(c_ref) <= 1e-6
     assert np.linalg.norm(U - U_c) / np.linalg.norm(U_c) <= 1e-4
+
+
+@pytest.fixture(scope="module")
+def part_default(built_lib):
+    """part_R256 with the reference's default level rule and first step."""
+    from sgldbench_gb300 import VoxelSolver
+    from sgldbench_gb300 import topvoxel as T
+
+    tv = T.model_from_npz(os.path.join(HERE, "golden", "part_R256_model.npz"))
+    s = VoxelSolver(tv.voxels, omega=0.6)   # num_levels from the reference rule, non_dyadic = 1
+    fixed, F = T.boundary_conditions(tv, s)
+    m = G.build_model_fixed(s.voxels, fixed, omega=0.6)
+    assert m.numLevels == s.numLevels == 4
+    for i, lv in enumerate(m.levels, 1):
+        info = s.levels[i - 1]
+        assert (info["resX"], info["resY"], info["resZ"]) == (lv.resX, lv.resY, lv.resZ)
+    m.F = F
+    E = np.ones(s.numElements)
+    G.set_modulus(m, E)
+    G.assemble_stencil(m)
+    s.set_fixed_dofs(fixed)
+    s.set_modulus(E)
+    s.Solving_AssembleFEAstencil()
+    U_o, its_o = G.solve(m, tol=1e-6, maxIT=5000)
+    yield m, s, U_o, its_o
+    s.close()
+
+
+def test_part_default_hierarchy_matches_oracle(part_default):
+    m, s, U_o, its_o = part_default
+    U, info = s.pcg(m.F, tol=1e-6, maxIT=5000)
+    assert info["converged"]
+    assert abs(info["its"] - its_o) <= 1, (info["its"], its_o)
+    assert np.linalg.norm(U - U_o) / np.linalg.norm(U_o) <= 1e-8
+    Um, im = s.pcg(m.F, tol=1e-6, maxIT=5000, precision="mixed_df")
+    assert im["converged"] and im["true_relres"] <= 1e-6
+    c_o = float(m.F @ U_o)
+    assert abs(float(m.F @ Um) - c_o) <= 1e-5 * abs(c_o)

@@ -1,8 +1,8 @@
 """GPU test of the allocation-free entry point sgld_kbyu_dot_noalloc.
 
 Callers that cannot allocate device memory when they apply the operator (a
-stream under graph capture, a fixed device-memory budget, a process whose
-memory belongs to another allocator) use this variant of the K*u kernel; its
+loop with a device-memory budget fixed at start-up, a process whose memory
+belongs to another allocator) use this variant of the K*u kernel; its
 per-CTA scratch is a static device array instead of context memory.  This
 test calls it through the C ABI twice in a row (the shared scratch keeps the
 previous call's contents) and checks y and u.y against the existing entry

@@ -493,11 +493,15 @@ __global__ void __launch_bounds__(32) k_block_inverse(const float2 *__restrict__
 //   2. M[i0:i0+32, group] = D_blk (E - S) with the block's precomputed
 //      inverse, E the identity columns of the group.
 // Writes M in FP64 (hi + lo) and in FP32 (the FP32 V-cycle's copy).
-constexpr int TI_G = 16, TI_KC = 64, TI_THREADS = 256;
+// A group is TI_G = 16 columns (8 warps) when the ring fits in shared memory,
+// else 8, 4 or 2 (wide coarsest bands, e.g. the reference's default hierarchy).
+constexpr int TI_KC = 64;
 
-__global__ void __launch_bounds__(TI_THREADS) k_trinv_tiles(const float2 *__restrict__ LB,
-                                                            const float2 *__restrict__ D, int n, int b, int R,
-                                                            double *__restrict__ M, float *__restrict__ M32) {
+template <int TI_G>
+__global__ void __launch_bounds__(16 * TI_G) k_trinv_tiles(const float2 *__restrict__ LB,
+                                                           const float2 *__restrict__ D, int n, int b, int R,
+                                                           double *__restrict__ M, float *__restrict__ M32) {
+    constexpr int TI_THREADS = 16 * TI_G;
     extern __shared__ float2 tsm[];
     float2 *ring = tsm;                       // [R][TI_G]
     float2 *Lt = ring + (int64_t)R * TI_G;    // [32][TI_KC + 1]
@@ -578,7 +582,7 @@ __global__ void __launch_bounds__(TI_THREADS) k_trinv_tiles(const float2 *__rest
     }
 }
 
-size_t trinv_smem_bytes(int R) { return sizeof(float2) * ((size_t)R * TI_G + 32 * (TI_KC + 1) + 32 * TI_G); }
+size_t trinv_smem_bytes(int R, int G) { return sizeof(float2) * ((size_t)R * G + 32 * (TI_KC + 1) + 32 * G); }
 
 // The same column sweep in FP32 (the hi words of the double-float band and
 // block inverses, FP32 FMA accumulation), writing only the FP32 copy M32 that
@@ -586,9 +590,11 @@ size_t trinv_smem_bytes(int R) { return sizeof(float2) * ((size_t)R * TI_G + 32 
 // only perturbs that preconditioner: the coarse apply M32' (M32 r) stays
 // symmetric positive semi-definite for any M32, and the outer solve still
 // converges on the FP64 residual.
-__global__ void __launch_bounds__(TI_THREADS) k_trinv_tiles32(const float2 *__restrict__ LB,
-                                                              const float2 *__restrict__ D, int n, int b, int R,
-                                                              float *__restrict__ M32) {
+template <int TI_G>
+__global__ void __launch_bounds__(16 * TI_G) k_trinv_tiles32(const float2 *__restrict__ LB,
+                                                             const float2 *__restrict__ D, int n, int b, int R,
+                                                             float *__restrict__ M32) {
+    constexpr int TI_THREADS = 16 * TI_G;
     extern __shared__ float tsm32[];
     float *ring = tsm32;                      // [R][TI_G]
     float *Lt = ring + (int64_t)R * TI_G;     // [32][TI_KC + 1]
@@ -654,7 +660,25 @@ __global__ void __launch_bounds__(TI_THREADS) k_trinv_tiles32(const float2 *__re
     }
 }
 
-size_t trinv32_smem_bytes(int R) { return sizeof(float) * ((size_t)R * TI_G + 32 * (TI_KC + 1) + 32 * TI_G); }
+size_t trinv32_smem_bytes(int R, int G) { return sizeof(float) * ((size_t)R * G + 32 * (TI_KC + 1) + 32 * G); }
+
+// launches of the two sweeps for the context's column-group width
+template <int G>
+static void trinv32_launch(const Ctx &c, const float2 *LB, const float2 *D, int n, int b) {
+    k_trinv_tiles32<G><<<(n + G - 1) / G, 16 * G, trinv32_smem_bytes(c.trinv_ring, G), c.stream>>>(
+        LB, D, n, b, c.trinv_ring, c.d_Ainv32);
+}
+template <int G>
+static void trinv64_launch(const Ctx &c, const float2 *LB, const float2 *D, int n, int b) {
+    k_trinv_tiles<G><<<(n + G - 1) / G, 16 * G, trinv_smem_bytes(c.trinv_ring, G), c.stream>>>(
+        LB, D, n, b, c.trinv_ring, c.d_Ainv, nullptr);
+}
+template <int G>
+static void trinv_attributes(int R) {
+    cudaFuncSetAttribute(k_trinv_tiles<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trinv_smem_bytes(R, G));
+    cudaFuncSetAttribute(k_trinv_tiles32<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)trinv32_smem_bytes(R, G));
+}
 
 // Enqueues the whole factorization (band Cholesky, L^-1, FP32 copy); no host
 // synchronisation, so the sequence is captured once into a CUDA graph.
@@ -688,8 +712,12 @@ static void factor_enqueue(Ctx &c, int *d_info) {
     k_block_inverse<<<nblk, 32, 0, c.stream>>>(LB, rd, n, b, D);
     cudaMemsetAsync(c.d_Ainv32, 0, sizeof(float) * (size_t)n * n, c.stream);
     ++g_launches;
-    k_trinv_tiles32<<<(n + TI_G - 1) / TI_G, TI_THREADS, trinv32_smem_bytes(c.trinv_ring), c.stream>>>(
-        LB, D, n, b, c.trinv_ring, c.d_Ainv32);
+    switch (c.trinv_g) {
+        case 16: trinv32_launch<16>(c, LB, D, n, b); break;
+        case 8: trinv32_launch<8>(c, LB, D, n, b); break;
+        case 4: trinv32_launch<4>(c, LB, D, n, b); break;
+        default: trinv32_launch<2>(c, LB, D, n, b); break;
+    }
 }
 
 // The FP64 copy M of L^-1 (double-float sweep), for the FP64 V-cycle; made on
@@ -702,8 +730,12 @@ int ensure_coarse_m64(Ctx &c) {
     (void)nblk;
     if (cudaMemsetAsync(c.d_Ainv, 0, sizeof(double) * (size_t)n * n, c.stream) != cudaSuccess) return -1;
     ++g_launches;
-    k_trinv_tiles<<<(n + TI_G - 1) / TI_G, TI_THREADS, c.trinv_smem, c.stream>>>(LB, D, n, b, c.trinv_ring,
-                                                                                 c.d_Ainv, nullptr);
+    switch (c.trinv_g) {
+        case 16: trinv64_launch<16>(c, LB, D, n, b); break;
+        case 8: trinv64_launch<8>(c, LB, D, n, b); break;
+        case 4: trinv64_launch<4>(c, LB, D, n, b); break;
+        default: trinv64_launch<2>(c, LB, D, n, b); break;
+    }
     if (cudaGetLastError() != cudaSuccess) return -1;
     c.m64_valid = true;
     return 0;
@@ -719,12 +751,18 @@ int coarse_factor_invert(Ctx &c) {
     if (!c.factor_graph) {
         int R = 32;
         while (R < c.cband + 32) R <<= 1;
-        const size_t smem = trinv_smem_bytes(R);
+        int G = 16;   // the widest column group whose ring fits
+        while (G > 2 && trinv_smem_bytes(R, G) > 220 * 1024) G >>= 1;
+        const size_t smem = trinv_smem_bytes(R, G);
         if (smem > 220 * 1024) return -2;
-        cudaFuncSetAttribute(k_trinv_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_trinv_tiles32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)trinv32_smem_bytes(R));
+        switch (G) {
+            case 16: trinv_attributes<16>(R); break;
+            case 8: trinv_attributes<8>(R); break;
+            case 4: trinv_attributes<4>(R); break;
+            default: trinv_attributes<2>(R); break;
+        }
         c.trinv_ring = R;
+        c.trinv_g = G;
         c.trinv_smem = smem;
         const int64_t before = g_launches;
         cudaGraph_t g = nullptr;

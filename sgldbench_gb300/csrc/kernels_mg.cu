@@ -61,14 +61,22 @@ __global__ void k_restrict(const T *__restrict__ rf, T *__restrict__ rc, int nyc
 // (2S-1)^3 taps unroll, the weights are constants and the indices stay 32-bit
 // (grids below 2^31 / 3 nodes).  Lanes hold consecutive coarse y, so for one
 // (dx, dz) a warp's taps cover a contiguous run of fine nodes.
+// A coarse node outside the active domain (cflag) gets 0 without reading the
+// fine grid: all 8 coarse elements around it are empty, so every fine node
+// strictly inside their union -- the tent's support -- is inactive and holds 0.
 template <typename T, int S>
-__global__ void __launch_bounds__(128) k_restrict_s(const T *__restrict__ rf, T *__restrict__ rc, int nyc, int nxc,
-                                                    int nzc) {
+__global__ void __launch_bounds__(128) k_restrict_s(const T *__restrict__ rf, T *__restrict__ rc,
+                                                    const uint8_t *__restrict__ cflag, int nyc, int nxc, int nzc) {
     const int NYc = nyc + 1, NXc = nxc + 1;
     const int NYf = S * nyc + 1, NXf = S * nxc + 1, NZf = S * nzc + 1;
     const int pl = blockIdx.x * blockDim.x + threadIdx.x;
     if (pl >= NYc * NXc) return;
     const int I = pl % NYc, J = pl / NYc, Kz = blockIdx.y;
+    if (!(cflag[pl + NYc * NXc * Kz] & NF_ACTIVE)) {
+        const int n = 3 * (pl + NYc * NXc * Kz);
+        rc[n] = rc[n + 1] = rc[n + 2] = T(0);
+        return;
+    }
     const T inv = T(1) / T(S);
     T a0 = T(0), a1 = T(0), a2 = T(0);
 #pragma unroll
@@ -106,9 +114,9 @@ void launch_restrict(const Level &fine, const Level &coarse, const T *rf, T *rc,
     const dim3 g((unsigned)(((coarse.ny + 1) * (coarse.nx + 1) + 127) / 128), (unsigned)(coarse.nz + 1));
     const bool small = 3 * (int64_t)fine.nnode < (int64_t)INT32_MAX;
     if (small && coarse.span == 2)
-        k_restrict_s<T, 2><<<g, 128, 0, st>>>(rf, rc, coarse.ny, coarse.nx, coarse.nz);
+        k_restrict_s<T, 2><<<g, 128, 0, st>>>(rf, rc, coarse.nflag, coarse.ny, coarse.nx, coarse.nz);
     else if (small && coarse.span == 4)
-        k_restrict_s<T, 4><<<g, 128, 0, st>>>(rf, rc, coarse.ny, coarse.nx, coarse.nz);
+        k_restrict_s<T, 4><<<g, 128, 0, st>>>(rf, rc, coarse.nflag, coarse.ny, coarse.nx, coarse.nz);
     else
         k_restrict<T><<<g, 128, 0, st>>>(rf, rc, coarse.ny, coarse.nx, coarse.nz, coarse.span);
 }
@@ -202,17 +210,38 @@ __global__ void k_prolong_smooth(const T *__restrict__ xc, const T *__restrict__
 // done axis by axis (z, then x, then y).  Span S is a compile-time constant,
 // indices are 32-bit.  Same result as k_prolong_smooth up to the order of the
 // interpolation sums.
+// With cflag (the coarse node flags; passed for the FP32 V-cycle, whose output
+// vectors are zeroed when allocated), a thread whose 8 coarse corners are all
+// inactive writes nothing: every fine element touching one of its fine nodes
+// lies in a coarse element sharing a corner with the cell, and an active
+// coarse element makes all 8 of its corners active, so those fine nodes are
+// inactive and already hold 0.
 template <typename T, int S, bool FINAL>
 __global__ void __launch_bounds__(128) k_prolong_cells(const T *__restrict__ xc, const T *__restrict__ rf,
                                                        const T *__restrict__ D, const uint8_t *__restrict__ nflag,
-                                                       T omega, T *__restrict__ xf, int nyc, int nxc, int nzc,
+                                                       const uint8_t *__restrict__ cflag, T omega,
+                                                       T *__restrict__ xf, int nyc, int nxc, int nzc,
                                                        double *__restrict__ partial) {
     const int NYc = nyc + 1, NXc = nxc + 1;
     const int NYf = S * nyc + 1, NXf = S * nxc + 1;
     const int pl = blockIdx.x * blockDim.x + threadIdx.x;
     const int K = blockIdx.y;
     T dot = T(0);
-    if (pl < NYc * NXc) {
+    bool live = pl < NYc * NXc;
+    if (live && cflag) {
+        const int I = pl % NYc, J = pl / NYc;
+        bool any = false;
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+                    if (!((a && I == nyc) || (b && J == nxc) || (c && K == nzc)))
+                        any |= (cflag[(I + a) + NYc * ((J + b) + NXc * (K + c))] & NF_ACTIVE) != 0;
+        live = any;
+    }
+    if (live) {
         const int I = pl % NYc, J = pl / NYc;
         const int ly = I < nyc ? S : 1, lx = J < nxc ? S : 1, lz = K < nzc ? S : 1;
         T cv[2][2][2][3];   // [c (z)][b (x)][a (y)][component]
@@ -288,13 +317,16 @@ template <typename T>
 void launch_prolong_smooth(const Level &fine, const Level &coarse, const T *xc, const T *rf, const T *diag, T omega,
                            T *xf, bool final_level, double *partial_dot, int *nblocks_out, cudaStream_t st) {
     const bool small = 3 * (int64_t)fine.nnode < (int64_t)INT32_MAX;
+    // empty cells are skipped in FP32 only: the FP32 V-cycle's outputs (d_z32 and the
+    // levels' x32) are zeroed at allocation, so their inactive nodes hold 0 throughout
+    const bool skip_inactive = sizeof(T) == sizeof(float);
     if (small && (coarse.span == 2 || coarse.span == 4)) {
         const dim3 g((unsigned)(((coarse.ny + 1) * (coarse.nx + 1) + 127) / 128), (unsigned)(coarse.nz + 1));
         if (nblocks_out) *nblocks_out = (int)(g.x * g.y);
         ++g_launches;
 #define PCELLS(S, F)                                                                                              \
-    k_prolong_cells<T, S, F><<<g, 128, 0, st>>>(xc, rf, diag, fine.nflag, omega, xf, coarse.ny, coarse.nx, coarse.nz, \
-                                                F ? partial_dot : nullptr)
+    k_prolong_cells<T, S, F><<<g, 128, 0, st>>>(xc, rf, diag, fine.nflag, skip_inactive ? coarse.nflag : nullptr, \
+                                                omega, xf, coarse.ny, coarse.nx, coarse.nz, F ? partial_dot : nullptr)
         if (coarse.span == 2) {
             if (final_level)
                 PCELLS(2, true);

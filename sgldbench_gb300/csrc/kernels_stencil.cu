@@ -15,6 +15,9 @@
 // butterflies (72 adds), 45 FMAs, E scaling, inverse butterflies (72 adds).
 // FP64 arithmetic is the scarce resource on GB300, so this is the form that
 // matters for the FP64 operator.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "sgld_internal.cuh"
 
 namespace sgld {
@@ -331,42 +334,101 @@ __global__ void __launch_bounds__(KT_THREADS) k_kbyu(const T *__restrict__ u, T 
     }
 }
 
-// ---- FP32 K*u on packed pairs of element layers -------------------------------
+// ---- paired FP32 arithmetic -----------------------------------------------------
 // Blackwell executes FP32 add / multiply / FMA on register pairs (f32x2) at the
-// issue cost of one scalar instruction.  k_kbyu_x2 gives every thread two
-// elements, (ez, ez+1) of the same (y, x) column, packed as float2 lanes, so
-// the Hadamard butterflies, the Kh blocks and the modulus scaling all run as
-// paired instructions; the shared-memory exchange moves float2 as well.
-// Pair p of a CTA covers element layers z0-1+2p and z0+2p and completes node
-// layers z0-1+2p and z0+2p: node layer ez takes the lower corners of element
-// ez plus the upper corners of element ez-1 (carried from the previous pair).
-// The corner sums are gathered in two steps: along y inside the warp (lanes
-// are consecutive y, so the neighbour's corner arrives by a shuffle), then
-// along x through shared memory (the next warp is the next x column), which
-// leaves 6 float2 per thread in shared memory instead of 24.
-// The tile is 32 (y) x TX (x) elements; a CTA owns 31 x (TX-1) node columns,
-// so a wider tile recomputes fewer halo elements (15 % at TX = 8, 9 % at 16)
-// and stages fewer halo nodes, at the same 1024 threads per SM.
+// issue cost of one scalar instruction; the FP32 K*u runs all its element
+// arithmetic on such pairs.
 __device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 __device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 kh2(int i) { return make_float2(c_Kh32[i], c_Kh32[i]); }
 
-__device__ __forceinline__ void hex_apply_x2(float2 (&u)[24], float2 e) {
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax)
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            if (k & (1 << ax)) continue;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float2 lo = u[3 * k + c], hi = u[3 * (k | (1 << ax)) + c];
-                u[3 * k + c] = f2add(lo, hi);
-                u[3 * (k | (1 << ax)) + c] = f2sub(hi, lo);
-            }
-        }
-    float2 g[24];
+// ---- FP32 K*u in sum-factorised Hadamard form, node rows staged by TMA -------
+// The Hadamard transform of an element's 8 corners is a product of three
+// 2-point butterflies (x, y, z), and neighbouring elements share most of
+// them: the y butterfly of a node pair (an edge along y) serves the 4
+// elements around that edge, and the x butterfly of two such edges (an element
+// face in a node layer) serves the 2 elements above and below the face.
+// k_kbyu_tma forms each of them once.  Per node layer a thread forms the 12
+// face coefficients of its element column from 4 node columns; per element
+// layer it forms the 24 Hadamard coefficients from the faces below and above
+// (12 z butterflies), applies E*Kh and undoes the z butterfly.  The transposed
+// transform is shared the same way: the two elements of a face add their face
+// contributions before the x butterfly is undone, the two faces of an edge
+// add before the y butterfly is undone, and the two edges of a node add last.
+// Per element that is 12 staged words read instead of 24, about 110 paired
+// FP32 operations instead of 170, and an exchange of 6 float2 through shared
+// memory (x) and 3 warp shuffles (y) instead of 12 shuffles and 6 float2.
+//
+// Every thread carries two independent z streams in the lanes of its float2
+// registers: node layers [zA, zA+zc) and [zA+zc, zA+2zc) of the CTA's chunk.
+// So all arithmetic runs as paired f32x2 instructions with no lane shuffling.
+//
+// Staging: a node row (33 nodes x 3 words of one x column in one node layer)
+// arrives in a ring slot of shared memory by cp.async.bulk.tensor over a
+// rank-1 tensor map of the whole vector, one copy per row, completed on the
+// slot's mbarrier.  A rank-1 map is used because the rows of a node layer lie
+// 12*NY bytes apart, which is not a multiple of 16 bytes as a tensor map's
+// strides must be.  Each copy starts at the 16-byte boundary at or below its
+// row (the row's first word lands 0..3 words into the slot row), and words
+// outside the vector read as zeros (halo rows and layers past the grid).
+// Halo values feed only elements outside the grid, whose modulus is 0.
+namespace tk {
+constexpr int RING = 4;       // ring slots; loads run up to 3 element layers ahead
+constexpr int ROWW = 104;     // words per row copy: up to 3 lead words + 99, a multiple of 4
+constexpr int ROWP = 128;     // words per slot row: every copy lands on a 128-byte boundary
+constexpr unsigned WAIT_LIMIT = 1u << 22;   // mbarrier tries before a CTA gives up
+}  // namespace tk
+
+template <int TX>
+struct TkTile {
+    static constexpr int THREADS = KT_Y * TX;
+    static constexpr int ROWS = TX + 1;                     // node x columns staged per layer
+    static constexpr int SLOT_WORDS = 2 * ROWS * tk::ROWP;  // both streams
+    static constexpr size_t RING_BYTES = sizeof(float) * tk::RING * SLOT_WORDS;
+    static constexpr size_t EXCH_BYTES = sizeof(float2) * 2 * 6 * THREADS;   // double-buffered
+    static constexpr size_t SMEM = 128 + RING_BYTES + EXCH_BYTES + sizeof(uint64_t) * tk::RING;
+    static constexpr uint32_t SLOT_TX_BYTES = 2 * ROWS * tk::ROWW * sizeof(float);
+    static_assert(2 * ROWS <= THREADS, "one producer thread per row");
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for the completion of phase `parity`; false after WAIT_LIMIT tries
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (unsigned i = 0; i < tk::WAIT_LIMIT; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_load_1d(uint32_t dst, const CUtensorMap *map, int c0, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.1d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2}], [%3];" ::"r"(
+            dst),
+        "l"((uint64_t)map), "r"(c0), "r"(bar)
+        : "memory");
+}
+
+// g = Kh h (g[0..2] = 0: the rigid translations), the 11 blocks of the
+// Hadamard-basis element matrix on paired lanes
+__device__ __forceinline__ void kh_apply_x2(const float2 (&u)[24], float2 (&g)[24]) {
     g[0] = g[1] = g[2] = make_float2(0.f, 0.f);
 #define X3(i, j, k, o)                                                                    \
     {                                                                                     \
@@ -394,207 +456,254 @@ __device__ __forceinline__ void hex_apply_x2(float2 (&u)[24], float2 e) {
     g[23] = f2mul(kh2(44), u[23]);
 #undef X3
 #undef X2
-#pragma unroll
-    for (int i = 3; i < 24; ++i) g[i] = f2mul(g[i], e);
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax)
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            if (k & (1 << ax)) continue;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float2 a = g[3 * k + c], d = g[3 * (k | (1 << ax)) + c];
-                g[3 * k + c] = f2sub(a, d);
-                g[3 * (k | (1 << ax)) + c] = f2add(a, d);
-            }
-        }
-#pragma unroll
-    for (int i = 0; i < 24; ++i) u[i] = g[i];
 }
 
-constexpr int KX_RING = 5;   // node-layer slots: 3 in use + 2 in flight
-
-// geometry of the 32 x TX tile
-template <int TX>
-struct KxTile {
-    static constexpr int THREADS = KT_Y * TX;
-    static constexpr int NL = (KT_Y + 1) * (TX + 1);             // staged nodes per layer
-    static constexpr int SV = (NL * 3 + THREADS - 1) / THREADS;  // staged words per thread and layer
-    // floats of the ring, rounded up to 16 bytes so that the float2 exchange
-    // area behind it is aligned (5 * 891 floats alone would leave it 4 bytes off)
-    static constexpr int RING_FLOATS = ((KX_RING * NL * 3 + 3) / 4) * 4;
-    static constexpr size_t SMEM = sizeof(float) * RING_FLOATS + sizeof(float2) * 6 * THREADS;
-    static_assert((RING_FLOATS * sizeof(float)) % 16 == 0, "float2 exchange area must be aligned");
-};
-
-__device__ __forceinline__ int xslot(int z) { return (z + KX_RING) % KX_RING; }
-
 template <int TX, bool DOT>
-__global__ void __launch_bounds__(KT_Y * TX, 1024 / (KT_Y * TX))
-    k_kbyu_x2(const float *__restrict__ u, float *__restrict__ y, const float *__restrict__ E,
-              const uint8_t *__restrict__ nflag, int ny, int nx, int nz, int zc, double *__restrict__ partial,
-              const uint8_t *__restrict__ tiles) {
-    using G = KxTile<TX>;
-    constexpr int KT_X = TX, KT_THREADS = G::THREADS, KT_NL = G::NL, KT_SV = G::SV;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *su = reinterpret_cast<float *>(smem_raw);                  // [KX_RING][KT_NL*3]
-    float2 *so = reinterpret_cast<float2 *>(su + G::RING_FLOATS);   // [6][KT_THREADS]
+__global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
+    k_kbyu_tma(const __grid_constant__ CUtensorMap umap, float *__restrict__ y, const float *__restrict__ E,
+               const uint8_t *__restrict__ nflag, int ny, int nx, int nz, int zc, double *__restrict__ partial,
+               const uint8_t *__restrict__ tiles, int *__restrict__ err) {
+    using G = TkTile<TX>;
+    constexpr int THREADS = G::THREADS, ROWS = G::ROWS;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *base = smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u);
+    float *ring = reinterpret_cast<float *>(base);
+    float2 *exch = reinterpret_cast<float2 *>(base + G::RING_BYTES);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(base + G::RING_BYTES + G::EXCH_BYTES);
+    __shared__ int s_abort;
     const int tid = threadIdx.x;
     const int ty = tid % KT_Y, tx = tid / KT_Y;
     const int NY = ny + 1, NX = nx + 1, NZ = nz + 1;
-    const int y0 = blockIdx.x * (KT_Y - 1), x0 = blockIdx.y * (KT_X - 1), z0 = blockIdx.z * zc;
-    const int zend = min(z0 + zc, NZ);
-    const int npair = (zend - z0 + 2) / 2;   // element layers z0-1 .. zend-1
-    const int zlast = z0 + 2 * npair - 1;    // highest node layer the pairs read
+    const int y0 = blockIdx.x * (KT_Y - 1), x0 = blockIdx.y * (TX - 1);
+    const int zA = blockIdx.z * 2 * zc, zB = zA + zc;
     const int gny = y0 + ty, gnx = x0 + tx;
-    const bool owner = (ty < KT_Y - 1) && (tx < KT_X - 1) && gny < NY && gnx < NX;
-    const int ey = y0 - 1 + ty, ex = x0 - 1 + tx;
-    const bool ein = ey >= 0 && ey < ny && ex >= 0 && ex < nx;
+    const bool owner = ty < KT_Y - 1 && tx < TX - 1 && gny < NY && gnx < NX;
     if (tiles && !tiles[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)]) {
-        skip_tile(y, owner, gny, gnx, NY, NX, z0, zend, DOT ? partial : nullptr);
+        skip_tile(y, owner, gny, gnx, NY, NX, zA, min(zA + 2 * zc, NZ), DOT ? partial : nullptr);
         return;
     }
-    int soff[KT_SV];
-#pragma unroll
-    for (int k = 0; k < KT_SV; ++k) {
-        const int i = tid + k * KT_THREADS;
-        soff[k] = -2;
-        if (i < KT_NL * 3) {
-            const int node = i / 3, c = i - 3 * node;
-            const int ly = node % (KT_Y + 1), lx = node / (KT_Y + 1);
-            const int gy = y0 - 1 + ly, gx = x0 - 1 + lx;
-            soff[k] = (gy >= 0 && gy < NY && gx >= 0 && gx < NX) ? 3 * (gy + NY * gx) + c : -1;
-        }
+    const int ey = y0 - 1 + ty, ex = x0 - 1 + tx;
+    const bool ein = ey >= 0 && ey < ny && ex >= 0 && ex < nx;
+    const int nload = zc + 2;   // node layers zs-1 .. zs+zc of each stream
+    const int64_t lwords = 3 * (int64_t)NY * NX;
+    if (tid == 0) {
+        for (int i = 0; i < tk::RING; ++i) mbar_init(smem_addr(bars + i), 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    const int64_t lstride = 3 * (int64_t)NY * NX;
-    auto stage = [&](int z) {
-        float *dst = su + xslot(z) * KT_NL * 3;
-        const bool zin = z >= 0 && z < NZ;
-#pragma unroll
-        for (int k = 0; k < KT_SV; ++k) {
-            const int i = tid + k * KT_THREADS;
-            if (soff[k] == -2) continue;
-            if (zin && soff[k] >= 0)
-                async_copy(dst + i, u + ((int64_t)z * lstride + soff[k]));
-            else
-                dst[i] = 0.f;
+    __syncthreads();
+    // producer threads 0 .. 2*ROWS-1: thread p copies row p % ROWS of stream p / ROWS
+    const bool producer = tid < 2 * ROWS;
+    int64_t pw = 0;   // word index of the row's first node (y0-1, x0-1+row) in the stream's layer zs-1
+    if (producer) {
+        const int zs = tid < ROWS ? zA : zB;
+        pw = 3 * ((int64_t)(y0 - 1) + (int64_t)NY * (x0 - 1 + tid % ROWS)) + lwords * (zs - 1);
+    }
+    auto issue = [&](int i) {   // load i: node layer zs-1+i of both streams into slot i % RING
+        const int slot = i % tk::RING;
+        const uint32_t bar = smem_addr(bars + slot);
+        if (tid == 0) mbar_expect_tx(bar, G::SLOT_TX_BYTES);
+        if (producer) {
+            const int64_t w = pw + lwords * i;
+            tma_load_1d(smem_addr(ring + slot * G::SLOT_WORDS + tid * tk::ROWP), &umap,
+                        (int)(w & ~(int64_t)3), bar);
         }
     };
-    stage(z0 - 1);
-    stage(z0);
-    stage(z0 + 1);
-    async_commit();
-    async_wait_all();
-    __syncthreads();
-    float carry[3] = {0.f, 0.f, 0.f};
-    float dot = 0.f;
-    const int64_t eplane = (int64_t)ny * nx;
-    const int64_t ecol = (int64_t)ey + (int64_t)ny * ex;
-    // moduli of the next pair are loaded one step ahead (register double buffer)
-    auto emod = [&](int z) -> float { return (ein && z >= 0 && z < nz) ? E[ecol + eplane * z] : 0.f; };
-    float en0 = emod(z0 - 1), en1 = emod(z0);
-    for (int p = 0; p < npair; ++p) {
-        const int ez = z0 - 1 + 2 * p;
-        if (ez + 3 <= zlast) stage(ez + 3);
-        if (ez + 4 <= zlast) stage(ez + 4);
-        async_commit();
-        const float e0 = en0, e1 = en1;
-        en0 = emod(ez + 2);
-        en1 = emod(ez + 3);
-        float2 ue[24];
-        if (e0 != 0.f || e1 != 0.f) {
-            const float *l0 = su + xslot(ez) * KT_NL * 3, *l1 = su + xslot(ez + 1) * KT_NL * 3,
-                        *l2 = su + xslot(ez + 2) * KT_NL * 3;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const int dx = k & 1, dy = 1 - ((k >> 1) & 1), kp = k >> 2;
-                const int o = 3 * ((ty + dy) + (KT_Y + 1) * (tx + dx));
-                const float *a = kp ? l1 : l0, *b = kp ? l2 : l1;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) ue[3 * k + c] = make_float2(a[o + c], b[o + c]);
-            }
-            hex_apply_x2(ue, make_float2(e0, e1));
-        } else {
-#pragma unroll
-            for (int i = 0; i < 24; ++i) ue[i] = make_float2(0.f, 0.f);
+    int issued = 0, waited = 0;   // loads issued; loads whose completion thread 0 has seen
+    for (; issued < min(tk::RING, nload); ++issued) issue(issued);
+    auto wait_load = [&](int i) -> bool {   // thread 0
+        const bool ok = mbar_wait(smem_addr(bars + i % tk::RING), (uint32_t)((i / tk::RING) & 1));
+        waited = i + 1;
+        return ok;
+    };
+    // after a wait that gave up: thread 0 lets the copies in flight land and flags the
+    // error; the CTA's nodes (and dot partial) read NaN, so that a solve using this
+    // product stops and falls back instead of going on with a wrong one
+    auto bail = [&]() {
+        if (tid == 0) {
+            for (int i = waited; i < issued; ++i) wait_load(i);
+            if (err) atomicExch(err, 1);
+            if (DOT) partial[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = __longlong_as_double(0x7ff8000000000000ll);
         }
-        // y step: Y_dx = corner (dx, dy=1) of this element + corner (dx, dy=0)
-        // of the element one lane up (corner k = dx | (1-dy) << 1 | kp << 2)
-        float2 y1[2][3];   // dx = 1: stays in this thread (the owner's own column)
+        if (owner)
+            for (int z = zA; z < min(zA + 2 * zc, NZ); ++z) {
+                float *o = y + 3 * ((int64_t)gny + (int64_t)NY * (gnx + (int64_t)NX * z));
+                o[0] = o[1] = o[2] = __int_as_float(0x7fc00000);
+            }
+    };
+    if (tid == 0 && !(wait_load(0) && wait_load(1))) s_abort = 1;
+    __syncthreads();
+    if (s_abort) {
+        bail();
+        return;
+    }
+    // this thread reads node rows tx and tx+1 of each stream at words 3*ty + lead, where the
+    // lead (0..3 words) follows the row's start address modulo 16 bytes
+    int roff[2][2], lead0[2][2];
 #pragma unroll
-        for (int kp = 0; kp < 2; ++kp)
+    for (int s = 0; s < 2; ++s)
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int zs = s ? zB : zA;
+            const int64_t w = 3 * ((int64_t)(y0 - 1) + (int64_t)NY * (x0 - 1 + tx + r)) + lwords * (zs - 1);
+            lead0[s][r] = (int)(w & 3);
+            roff[s][r] = (s * ROWS + tx + r) * tk::ROWP + 3 * ty;
+        }
+    const int lstep = (int)(lwords & 3);
+    // the 12 face coefficients (x, y Hadamard) of node layer zs-1+i, both streams; also the
+    // values of node (ey+1, ex+1) in that layer
+    auto faces = [&](int i, float2 (&F)[12], float2 (&un)[3]) {
+        const float *sl = ring + (i % tk::RING) * G::SLOT_WORDS;
+        float2 v[2][2][3];   // [row][node ey, ey+1][c]
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const float *pa = sl + roff[0][r] + ((lead0[0][r] + lstep * i) & 3);
+            const float *pb = sl + roff[1][r] + ((lead0[1][r] + lstep * i) & 3);
+#pragma unroll
+            for (int n = 0; n < 2; ++n)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) v[r][n][c] = make_float2(pa[3 * n + c], pb[3 * n + c]);
+        }
+        // y butterfly (bit 1 = node ey): sum and u(ey) - u(ey+1); then x butterfly
+        // (bit 0 = column ex+1): sum and v(ex+1) - v(ex)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float2 s0 = f2add(v[0][0][c], v[0][1][c]), d0 = f2sub(v[0][0][c], v[0][1][c]);
+            const float2 s1 = f2add(v[1][0][c], v[1][1][c]), d1 = f2sub(v[1][0][c], v[1][1][c]);
+            F[c] = f2add(s0, s1);
+            F[3 + c] = f2sub(s1, s0);
+            F[6 + c] = f2add(d0, d1);
+            F[9 + c] = f2sub(d1, d0);
+            un[c] = v[1][1][c];
+        }
+    };
+    float2 Fp[12], carry[12], uo[3];
+    faces(0, Fp, uo);
+#pragma unroll
+    for (int i = 0; i < 12; ++i) carry[i] = make_float2(0.f, 0.f);
+    float dot = 0.f;
+    // moduli of element layer zs-1+j and flags of node layer zs-1+j, loaded a step ahead
+    // through pointers that advance one layer per step
+    // (32-bit offsets: the launcher keeps every word index of the vector below 2^31)
+    const int eplane = ny * nx, nplane = NY * NX;
+    int eoA = (ey + ny * ex) + eplane * (zA - 1), eoB = eoA + eplane * zc;
+    int noA = (gny + NY * gnx) + nplane * (zA - 1), noB = noA + nplane * zc;
+    auto emod = [&](int o, int k) -> float { return (ein && k >= 0 && k < nz) ? E[o] : 0.f; };
+    auto flag = [&](int o, int z) -> int { return (owner && z >= 0 && z < NZ) ? (int)nflag[o] : -1; };
+    float2 en = make_float2(emod(eoA, zA - 1), emod(eoB, zB - 1));
+    int fnA = -1, fnB = -1;   // -1: node not written (not owned, or past the grid)
+#pragma unroll 2
+    for (int j = 0; j <= zc; ++j) {
+        // element layer zs-1+j: faces of node layers zs-1+j (Fp) and zs+j (Ft)
+        const float2 ev = en;
+        const int fA = fnA, fB = fnB;
+        eoA += eplane;
+        eoB += eplane;
+        if (j < zc) {
+            en = make_float2(emod(eoA, zA + j), emod(eoB, zB + j));
+            fnA = flag(noA + nplane, zA + j);
+            fnB = flag(noB + nplane, zB + j);
+        }
+        float2 Ft[12], un[3];
+        faces(j + 1, Ft, un);
+        float2 h[24];
+#pragma unroll
+        for (int i = 0; i < 12; ++i) {
+            h[i] = f2add(Fp[i], Ft[i]);
+            h[12 + i] = f2sub(Ft[i], Fp[i]);
+            Fp[i] = Ft[i];
+        }
+        float2 g[24];
+        kh_apply_x2(h, g);
+        // E scale, z butterfly undone: the face below gets (a - d), the face above (a + d);
+        // the face below also takes the carried contribution of the element layer under it
+        float2 Lm[6], Rp[6];
+#pragma unroll
+        for (int by = 0; by < 2; ++by)
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const float2 a1 = ue[3 * (1 | (kp << 2)) + c], b1 = ue[3 * (1 | 2 | (kp << 2)) + c];
-                const float2 a0 = ue[3 * (kp << 2) + c], b0 = ue[3 * (2 | (kp << 2)) + c];
-                y1[kp][c] = f2add(a1, make_float2(__shfl_down_sync(0xffffffffu, b1.x, 1),
-                                                  __shfl_down_sync(0xffffffffu, b1.y, 1)));
-                so[(3 * kp + c) * KT_THREADS + tid] =
-                    f2add(a0, make_float2(__shfl_down_sync(0xffffffffu, b0.x, 1),
-                                          __shfl_down_sync(0xffffffffu, b0.y, 1)));
+                float2 phi[2];
+#pragma unroll
+                for (int bx = 0; bx < 2; ++bx) {
+                    const int i = 3 * (bx | (by << 1)) + c;
+                    phi[bx] = f2fma(ev, f2sub(g[i], g[12 + i]), carry[i]);
+                    carry[i] = f2mul(ev, f2add(g[i], g[12 + i]));
+                }
+                // x butterfly undone: column ex gets phi0 - phi1, column ex+1 gets phi0 + phi1
+                Lm[3 * by + c] = f2sub(phi[0], phi[1]);
+                Rp[3 * by + c] = f2add(phi[0], phi[1]);
             }
+        float2 *xb = exch + (j & 1) * 6 * THREADS;
+#pragma unroll
+        for (int v = 0; v < 6; ++v) xb[v * THREADS + tid] = Lm[v];
+        if (tid == 0 && j + 2 < nload && !wait_load(j + 2)) s_abort = 1;
         __syncthreads();
-        if (owner) {
-            // x step: dx = 0 comes from the next column (the next warp)
-            float2 lo[3], up[3];
+        if (s_abort) {
+            bail();
+            return;
+        }
+        // slots whose loads are consumed take the next ones
+        while (issued < nload && issued <= j + 1 + tk::RING) issue(issued++);
+        if (j >= 1 && tx < TX - 1) {
+            // edge of column ex+1 along y: this element's right face part + the next column's left part;
+            // y butterfly undone: node ey+1 gets T0 - T1, node ey gets T0 + T1
+            float2 o[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                lo[c] = f2add(y1[0][c], so[c * KT_THREADS + tid + KT_Y]);
-                up[c] = f2add(y1[1][c], so[(3 + c) * KT_THREADS + tid + KT_Y]);
+                const float2 t0 = f2add(Rp[c], xb[c * THREADS + tid + KT_Y]);
+                const float2 t1 = f2add(Rp[3 + c], xb[(3 + c) * THREADS + tid + KT_Y]);
+                const float2 up = f2add(t0, t1);
+                o[c] = f2add(f2sub(t0, t1), make_float2(__shfl_down_sync(0xffffffffu, up.x, 1),
+                                                        __shfl_down_sync(0xffffffffu, up.y, 1)));
             }
-            const int64_t node0 = (int64_t)gny + (int64_t)NY * gnx;
-            const int on = 3 * ((ty + 1) + (KT_Y + 1) * (tx + 1));
+            // node layer zs-1+j of each stream is complete
+            if (fA >= 0) {
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int z = ez + h;
-                float o[3];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) o[c] = h == 0 ? carry[c] + lo[c].x : lo[c].y + up[c].x;
-                if (z >= z0 && z < zend) {
-                    const int64_t node = node0 + (int64_t)NY * NX * z;
-                    const uint8_t f = nflag[node];
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        if (f & (NF_FIXX << c)) o[c] = 0.f;
-                        y[3 * node + c] = o[c];
-                    }
-                    if (DOT) {
-                        const float *un = su + xslot(z) * KT_NL * 3 + on;
-                        dot += un[0] * o[0] + un[1] * o[1] + un[2] * o[2];
-                    }
+                for (int c = 0; c < 3; ++c) {
+                    const float oc = (fA & (NF_FIXX << c)) ? 0.f : o[c].x;
+                    y[3 * noA + c] = oc;
+                    if (DOT) dot = fmaf(uo[c].x, oc, dot);
                 }
             }
+            if (fB >= 0) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) carry[c] = up[c].y;
+                for (int c = 0; c < 3; ++c) {
+                    const float oc = (fB & (NF_FIXX << c)) ? 0.f : o[c].y;
+                    y[3 * noB + c] = oc;
+                    if (DOT) dot = fmaf(uo[c].y, oc, dot);
+                }
+            }
         }
-        async_wait_all();
-        __syncthreads();
+        noA += nplane;
+        noB += nplane;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) uo[c] = un[c];
     }
     if (DOT) {
-        __shared__ double red[KT_THREADS / 32];
+        __shared__ double red[THREADS / 32];
         const double s = block_sum_to_double<float>(dot, red);
         if (tid == 0) partial[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s;
     }
 }
 
-// node layers per CTA of k_kbyu_x2: an odd count (so that the element layers
-// z0-1 .. z0+zc-1 form whole pairs).  Default: near 15, balanced over the z
-// extent; sgld_assemble's tuner (tune_kbyu_f32) may set another per level.
-static int kbyu_x2_zc(int NZ) {
-    const int chunks = (NZ + 14) / 15;
-    int zc = (NZ + chunks - 1) / chunks;
-    if (!(zc & 1)) ++zc;
-    return zc;
+// node layers per stream of k_kbyu_tma (a CTA covers two streams): about 32
+// node layers per CTA, balanced over the z extent
+static int kbyu_tma_zc(int NZ) {
+    const int chunks = (NZ + 31) / 32;
+    return (NZ + 2 * chunks - 1) / (2 * chunks);
 }
 
-int kbyu_f32_zc(const Level &l) { return l.kx_zc > 0 ? l.kx_zc : kbyu_x2_zc(l.nz + 1); }
+// sgld_assemble's tuner (tune_kbyu_f32) may set another chunk per level
+int kbyu_f32_zc(const Level &l) { return l.kx_zc > 0 ? l.kx_zc : kbyu_tma_zc(l.nz + 1); }
 // tile width in x: 8 unless the tuner chose 16
 int kbyu_f32_tx(const Level &l) { return l.kx_tx == 16 ? 16 : 8; }
+// node layers one CTA of the FP32 K*u covers (two streams)
+int kbyu_f32_cta_layers(const Level &l) { return 2 * kbyu_f32_zc(l); }
 
-static dim3 kbyu_x2_grid(const Level &l) {
+static dim3 kbyu_f32_grid(const Level &l) {
     const int NZ = l.nz + 1;
-    const int zc = kbyu_f32_zc(l), tx = kbyu_f32_tx(l);
-    return dim3((l.ny + 1 + KT_Y - 2) / (KT_Y - 1), (l.nx + 1 + tx - 2) / (tx - 1), (NZ + zc - 1) / zc);
+    const int zl = kbyu_f32_cta_layers(l), tx = kbyu_f32_tx(l);
+    return dim3((l.ny + 1 + KT_Y - 2) / (KT_Y - 1), (l.nx + 1 + tx - 2) / (tx - 1), (NZ + zl - 1) / zl);
 }
 
 static dim3 kbyu_grid(const Level &l) {
@@ -611,10 +720,40 @@ static constexpr size_t kbyu_smem() {
 void init_kernel_attributes() {
     cudaFuncSetAttribute(k_kbyu<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<double>());
     cudaFuncSetAttribute(k_kbyu<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<double>());
-    cudaFuncSetAttribute(k_kbyu_x2<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KxTile<8>::SMEM);
-    cudaFuncSetAttribute(k_kbyu_x2<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KxTile<8>::SMEM);
-    cudaFuncSetAttribute(k_kbyu_x2<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KxTile<16>::SMEM);
-    cudaFuncSetAttribute(k_kbyu_x2<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KxTile<16>::SMEM);
+    cudaFuncSetAttribute(k_kbyu_tma<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TkTile<8>::SMEM);
+    cudaFuncSetAttribute(k_kbyu_tma<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TkTile<8>::SMEM);
+    cudaFuncSetAttribute(k_kbyu_tma<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TkTile<16>::SMEM);
+    cudaFuncSetAttribute(k_kbyu_tma<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TkTile<16>::SMEM);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); null when the driver does not provide it
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// Rank-1 tensor map of the n FP32 words at u with boxes of tk::ROWW words;
+// words outside [0, n) read as zeros.  TMA coordinates are 32-bit, so n is
+// limited to 2^31 - 1 words.
+static int vector_tensor_map(CUtensorMap *m, const float *u, int64_t n) {
+    const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc || n <= 0 || n > (int64_t)INT32_MAX || (reinterpret_cast<uintptr_t>(u) & 15)) return -1;
+    const cuuint64_t dim[1] = {(cuuint64_t)n};
+    const cuuint64_t stride[1] = {(cuuint64_t)sizeof(float)};   // no strides at rank 1
+    const cuuint32_t box[1] = {(cuuint32_t)tk::ROWW}, estride[1] = {1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 1, const_cast<float *>(u), dim, stride, box, estride,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? 0 : -1;
 }
 
 template <typename T, bool DOT>
@@ -634,31 +773,37 @@ void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *
         kbyu_launch<double, false>(l0, E, u, y, nullptr, nblocks_out, s);
 }
 
-void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
-                     int *nblocks_out, cudaStream_t s) {
-    const dim3 g = kbyu_x2_grid(l0);
+int launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
+                    int *nblocks_out, cudaStream_t s) {
+    const dim3 g = kbyu_f32_grid(l0);
     const int zc = kbyu_f32_zc(l0), tx = kbyu_f32_tx(l0);
     if (nblocks_out) *nblocks_out = (int)(g.x * g.y * g.z);
-    ++g_launches;
     // the tile map only when it was made for this tile
-    const uint8_t *tiles = (l0.tiles_x2 && l0.tiles_x2_tx == tx && l0.tiles_x2_zc == zc) ? l0.tiles_x2 : nullptr;
+    const uint8_t *tiles = (l0.tiles_f32 && l0.tiles_f32_tx == tx && l0.tiles_f32_zc == zc) ? l0.tiles_f32 : nullptr;
+    // every row coordinate the CTAs form (up to 2 zc + 2 layers past the grid) must fit 32 bits
+    const int64_t lw = 3 * (int64_t)(l0.ny + 1) * (l0.nx + 1);
+    if (3 * l0.nnode + lw * (2 * (int64_t)zc + 2) >= (int64_t)INT32_MAX) return (int)cudaErrorInvalidValue;
+    CUtensorMap m;
+    if (vector_tensor_map(&m, u, 3 * l0.nnode)) return (int)cudaErrorInvalidValue;
+    ++g_launches;
     if (tx == 8) {
-        using G = KxTile<8>;
+        using G = TkTile<8>;
         if (partial_dot)
-            k_kbyu_x2<8, true><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, partial_dot,
-                                                              tiles);
+            k_kbyu_tma<8, true><<<g, G::THREADS, G::SMEM, s>>>(m, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, partial_dot,
+                                                              tiles, l0.kerr);
         else
-            k_kbyu_x2<8, false><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr,
-                                                               tiles);
+            k_kbyu_tma<8, false><<<g, G::THREADS, G::SMEM, s>>>(m, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr,
+                                                               tiles, l0.kerr);
     } else {
-        using G = KxTile<16>;
+        using G = TkTile<16>;
         if (partial_dot)
-            k_kbyu_x2<16, true><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc,
-                                                               partial_dot, tiles);
+            k_kbyu_tma<16, true><<<g, G::THREADS, G::SMEM, s>>>(m, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc,
+                                                               partial_dot, tiles, l0.kerr);
         else
-            k_kbyu_x2<16, false><<<g, G::THREADS, G::SMEM, s>>>(u, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr,
-                                                                tiles);
+            k_kbyu_tma<16, false><<<g, G::THREADS, G::SMEM, s>>>(m, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr,
+                                                                tiles, l0.kerr);
     }
+    return 0;
 }
 
 int update_kbyu_tiles(Level &l0, cudaStream_t s) {
@@ -669,21 +814,27 @@ int update_kbyu_tiles(Level &l0, cudaStream_t s) {
         if (e != cudaSuccess) return (int)e;
         make_tile_map(l0, KT_Y, KT_X, KT_ZC, g16, l0.tiles16, s);
     }
-    const int tx = kbyu_f32_tx(l0), zc = kbyu_f32_zc(l0);
-    if (l0.tiles_x2 && l0.tiles_x2_tx == tx && l0.tiles_x2_zc == zc) return 0;
-    const dim3 g = kbyu_x2_grid(l0);
-    const int64_t n = (int64_t)g.x * g.y * g.z;
-    if (n > l0.tiles_x2_cap) {
-        if (l0.tiles_x2) cudaFree(l0.tiles_x2);
-        l0.tiles_x2 = nullptr;
-        l0.tiles_x2_cap = 0;
-        e = cudaMalloc((void **)&l0.tiles_x2, (size_t)n);
+    if (!l0.kerr) {
+        e = cudaMalloc((void **)&l0.kerr, sizeof(int));
         if (e != cudaSuccess) return (int)e;
-        l0.tiles_x2_cap = n;
+        e = cudaMemsetAsync(l0.kerr, 0, sizeof(int), s);
+        if (e != cudaSuccess) return (int)e;
     }
-    make_tile_map(l0, KT_Y, tx, zc, g, l0.tiles_x2, s);
-    l0.tiles_x2_tx = tx;
-    l0.tiles_x2_zc = zc;
+    const int tx = kbyu_f32_tx(l0), zc = kbyu_f32_zc(l0);
+    if (l0.tiles_f32 && l0.tiles_f32_tx == tx && l0.tiles_f32_zc == zc) return 0;
+    const dim3 g = kbyu_f32_grid(l0);
+    const int64_t n = (int64_t)g.x * g.y * g.z;
+    if (n > l0.tiles_f32_cap) {
+        if (l0.tiles_f32) cudaFree(l0.tiles_f32);
+        l0.tiles_f32 = nullptr;
+        l0.tiles_f32_cap = 0;
+        e = cudaMalloc((void **)&l0.tiles_f32, (size_t)n);
+        if (e != cudaSuccess) return (int)e;
+        l0.tiles_f32_cap = n;
+    }
+    make_tile_map(l0, KT_Y, tx, kbyu_f32_cta_layers(l0), g, l0.tiles_f32, s);
+    l0.tiles_f32_tx = tx;
+    l0.tiles_f32_zc = zc;
     return (int)cudaGetLastError();
 }
 

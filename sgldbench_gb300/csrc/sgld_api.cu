@@ -862,6 +862,8 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
             CK(dalloc(&lv.x, 3 * lv.nnode));
             CK(dalloc(&lv.r32, 3 * lv.nnode));
             CK(dalloc(&lv.x32, 3 * lv.nnode));
+            // the FP32 prolongation skips empty cells and relies on zeros at inactive nodes
+            CK(cudaMemset(lv.x32, 0, sizeof(float) * 3 * lv.nnode));
         }
     }
     if (c.lv[0].nel_active == 0) return fail(ctx, SGLD_ERR_ARG, "the voxel grid has no solid voxel");
@@ -880,6 +882,7 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
     for (double **p : {&c.d_b, &c.d_x, &c.d_r, &c.d_z, &c.d_p, &c.d_q, &c.d_tmp}) CK(dalloc(p, nv));
     CK(dalloc(&c.d_r32, nv));
     CK(dalloc(&c.d_z32, nv));
+    CK(cudaMemset(c.d_z32, 0, sizeof(float) * nv));   // see lv.x32
     for (float **p : {&c.d_e32, &c.d_s32, &c.d_d32, &c.d_t32}) CK(dalloc(p, nv));
     CK(dalloc(&c.d_isc, 16));
     init_kernel_attributes();
@@ -908,8 +911,8 @@ void sgld_destroy(sgld_ctx *ctx) {
         cudaSetDevice(c.device);
     for (Level &l : c.lv) {
         for (void *p : {(void *)l.eact, (void *)l.nflag, (void *)l.diag, (void *)l.idiag, (void *)l.idiag32, (void *)l.Ks, (void *)l.r,
-                        (void *)l.x, (void *)l.r32, (void *)l.x32, (void *)l.tiles16, (void *)l.tiles_x2,
-                        (void *)l.runs})
+                        (void *)l.x, (void *)l.r32, (void *)l.x32, (void *)l.tiles16, (void *)l.tiles_f32,
+                        (void *)l.runs, (void *)l.kerr})
             if (p) cudaFree(p);
     }
     for (void *p : {(void *)c.d_nodemap, (void *)c.d_elemap, (void *)c.E, (void *)c.d_E32, (void *)c.d_b,
@@ -954,7 +957,7 @@ int sgld_kbyu_tile(const sgld_ctx *ctx, int *tile_x, int *z_chunk) {
     if (!ctx || ctx->c.L < 1) return SGLD_ERR_ARG;
     const Level &l0 = ctx->c.lv[0];
     if (tile_x) *tile_x = kbyu_f32_tx(l0);
-    if (z_chunk) *z_chunk = kbyu_f32_zc(l0);
+    if (z_chunk) *z_chunk = kbyu_f32_cta_layers(l0);
     return SGLD_OK;
 }
 
@@ -1153,8 +1156,8 @@ static int tune_kbyu_f32(sgld_ctx *ctx) {
     }
     const int NZ = l0.nz + 1;
     std::vector<int> cand;
-    for (int zc : {7, 9, 11, 15, 21, 31, 47})
-        if (zc <= NZ) cand.push_back(zc);
+    for (int zc : {4, 6, 8, 12, 16, 24})   // node layers per stream, two streams per CTA
+        if (2 * zc <= NZ + 1) cand.push_back(zc);
     cand.push_back(0);   // the default rule
     CK(cudaMemsetAsync(c.d_r32, 0, sizeof(float) * 3 * (size_t)l0.nnode, c.stream));
     cudaEvent_t a, b;
@@ -1167,7 +1170,8 @@ static int tune_kbyu_f32(sgld_ctx *ctx) {
             l0.kx_tx = tx;
             l0.kx_zc = zc;
             if (update_kbyu_tiles(l0, c.stream)) return fail(ctx, SGLD_ERR_CUDA, "K*u tile maps");
-            launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, c.stream);
+            if (launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, c.stream))
+                return fail(ctx, SGLD_ERR_CUDA, "FP32 K*u: the vector's tensor map could not be made");
             CK(cudaEventRecord(a, c.stream));
             for (int r = 0; r < 3; ++r) launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, c.stream);
             CK(cudaEventRecord(b, c.stream));

@@ -40,7 +40,8 @@ constexpr int KH_NNZ = 45;
 struct Level {
     int nx = 0, ny = 0, nz = 0;   // elements
     int span = 1;                 // coarsening factor from the next finer level
-    int kx_zc = 0;                // node layers per CTA of the FP32 K*u (0 = default rule; set by the tuner)
+    int kx_zc = 0;                // node layers per z stream of the FP32 K*u, two streams per CTA
+                                  // (0 = default rule; set by the tuner)
     int kx_tx = 0;                // x width of the FP32 K*u tile, 8 or 16 (0 = 8; set by the tuner)
     int64_t nel = 0, nnode = 0;   // full-grid counts
     int64_t nel_active = 0, nnode_active = 0;
@@ -49,15 +50,18 @@ struct Level {
     // 0 = no active element in the CTA's element box, so every node it owns
     // is inactive and its result is zero): the 32 x 8 x 16-layer grid of the
     // FP64 and double-float kernels, and the FP32 kernel's grid for the tile
-    // (tiles_x2_tx, tiles_x2_zc) it was made for
-    uint8_t *tiles16 = nullptr, *tiles_x2 = nullptr;
+    // (tiles_f32_tx, tiles_f32_zc) it was made for
+    uint8_t *tiles16 = nullptr, *tiles_f32 = nullptr;
     // finest level: the y-runs of the active bricks (32 y x 8 x x 8 z nodes
     // holding an active node), each first DOF | floats << 40, in address order;
     // empty when nearly every brick is active (then the flat kernels run)
     int64_t *runs = nullptr;
     int64_t nruns = 0;
-    int tiles_x2_tx = 0, tiles_x2_zc = 0;
-    int64_t tiles_x2_cap = 0;
+    int tiles_f32_tx = 0, tiles_f32_zc = 0;
+    // finest level: set to 1 by an FP32 K*u CTA that gave up waiting for its
+    // staged node rows (the CTA writes NaN to the nodes it owns)
+    int *kerr = nullptr;
+    int64_t tiles_f32_cap = 0;
     uint8_t *nflag = nullptr;     // [nnode] NF_* bits
     double *diag = nullptr;       // [3*nnode] Jacobi diagonal (levels 1..L-1)
     double *idiag = nullptr;      // [3*nnode] 1 / diag on active nodes, 0 elsewhere
@@ -102,6 +106,7 @@ struct Ctx {
     cudaGraphExec_t factor_graph = nullptr;   // captured factorization of the coarsest matrix
     int64_t factor_graph_launches = 0;
     int trinv_ring = 0;
+    int trinv_g = 16;               // columns per CTA of the L^-1 sweeps (narrower for wide bands)
     size_t trinv_smem = 0;
     bool m64_valid = false;         // d_Ainv holds L^-1 of the current factorization (made on first use)
     double *d_cpart = nullptr;      // [CSPLIT*ncf] GEMV partials
@@ -177,11 +182,13 @@ void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *
                      int *nblocks_out, cudaStream_t s);
 // (re)makes l0's active-tile maps for its current FP32 tile; 0 or a CUDA error
 int update_kbyu_tiles(Level &l0, cudaStream_t s);
-void launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
-                     int *nblocks_out, cudaStream_t s);
+// 0, or a CUDA error code when the launch could not be set up (the input's tensor map)
+int launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
+                    int *nblocks_out, cudaStream_t s);
 void init_kernel_attributes();
 int kbyu_f32_zc(const Level &l0);   // node layers per CTA the FP32 K*u uses on this level
 int kbyu_f32_tx(const Level &l0);   // x width (elements) of the FP32 K*u tile on this level
+int kbyu_f32_cta_layers(const Level &l0);   // node layers one CTA of the FP32 K*u covers
 // double-float K*u (kernels_df.cu)
 void upload_kh_df(const double *Kh, cudaStream_t s);
 void init_kbyu_df_attributes();

@@ -1,5 +1,5 @@
 """Roofline figures of the solve's dominant kernel, the FP32 K*u of the inner
-CG (k_kbyu_x2), for bench.py and kernel_bench.py.
+CG (k_kbyu_tma), for bench.py and kernel_bench.py.
 
 Algorithmic bytes per launch follow the operator's own data (per active node:
 u read and y written, 3 FP32 values each, plus one flag byte; per active
@@ -18,7 +18,7 @@ import os
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
-# ncu DRAM bytes per full-grid node of one k_kbyu_x2 launch, by workload kind
+# ncu DRAM bytes per full-grid node of one k_kbyu_tma launch, by workload kind
 # (filled from the captures summarised under profiles/)
 DRAM_BYTES_PER_GRID_NODE: dict = {}
 
@@ -37,7 +37,7 @@ def kbyu_f32_bytes(active_nodes: int, active_elements: int) -> int:
 
 
 def kbyu_f32_roofline(s, voxels=None, reps: int = 20, kind: str = "blobs") -> dict:
-    """Roofline record of k_kbyu_x2 on solver s (assembled)."""
+    """Roofline record of k_kbyu_tma on solver s (assembled)."""
     nn, ne = s.numNodes, s.numElements
     alg = kbyu_f32_bytes(nn, ne)
     ms = s.time_op("kbyu32", reps)
@@ -48,7 +48,7 @@ def kbyu_f32_roofline(s, voxels=None, reps: int = 20, kind: str = "blobs") -> di
     per = DRAM_BYTES_PER_GRID_NODE.get(kind)
     return {"bound": "hbm", "achieved": achieved, "peak": p["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / p["hbm_gbs"], "traffic": None if per is None else per * grid_nodes,
-            "kernel": "k_kbyu_x2 (FP32 K*u of the inner CG)", "avg_launch_ms": ms,
+            "kernel": "k_kbyu_tma (FP32 K*u of the inner CG)", "avg_launch_ms": ms,
             "launch_timing": f"CUDA events around {reps} back-to-back launches on the library stream "
                              "(sgld_time_op) after the timed region; inside it the kernel runs in the inner CG's "
                              "graph", "algorithmic_bytes_per_launch": alg,

@@ -12,8 +12,9 @@
 * The real model data/part_R256.TopVoxel (1.85 M voxels): FP64 and mixed
   solves against the oracle's FP64 solve of the same system, on 5 dyadic
   levels and on the reference's own default hierarchy (coarsestResolution-
-  Control_ = 50000 and nonDyadic_ = 1, Data_GlobalVariables.m:13-15: 4 levels,
-  a 4:1 first step, a 10 x 16 x 7-element coarsest grid).
+  Control_ = 50000 and nonDyadic_ = 1, Data_GlobalVariables.m:13-15: the
+  grid padded to multiples of 8, a 4:1 first step and a 2:1 second one, so
+  3 levels with a 32 x 20 x 14-element coarsest grid).
 
 The oracle (C + numpy restatement of the reference) takes about half a
 minute of host time per solve at these sizes.
@@ -140,7 +141,8 @@ def part_default(built_lib):
     s = VoxelSolver(tv.voxels, omega=0.6)   # num_levels from the reference rule, non_dyadic = 1
     fixed, F = T.boundary_conditions(tv, s)
     m = G.build_model_fixed(s.voxels, fixed, omega=0.6)
-    assert m.numLevels == s.numLevels == 4
+    assert m.numLevels == s.numLevels == 3
+    assert (s.levels[-1]["resX"], s.levels[-1]["resY"], s.levels[-1]["resZ"]) == (32, 20, 14)
     for i, lv in enumerate(m.levels, 1):
         info = s.levels[i - 1]
         assert (info["resX"], info["resY"], info["resZ"]) == (lv.resX, lv.resY, lv.resZ)

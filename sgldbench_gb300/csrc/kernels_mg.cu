@@ -220,13 +220,14 @@ template <typename T, int S, bool FINAL>
 __global__ void __launch_bounds__(128) k_prolong_cells(const T *__restrict__ xc, const T *__restrict__ rf,
                                                        const T *__restrict__ D, const uint8_t *__restrict__ nflag,
                                                        const uint8_t *__restrict__ cflag, T omega,
-                                                       T *__restrict__ xf, int nyc, int nxc, int nzc,
+                                                       T *__restrict__ xf, int nyc, int nxc, int nzc, int zp,
                                                        double *__restrict__ partial) {
     const int NYc = nyc + 1, NXc = nxc + 1;
     const int NYf = S * nyc + 1, NXf = S * nxc + 1;
     const int pl = blockIdx.x * blockDim.x + threadIdx.x;
-    const int K = blockIdx.y;
     T dot = T(0);
+    // coarse planes K = blockIdx.y * zp .. + zp - 1 (fewer CTAs, so fewer partial sums)
+    for (int K = blockIdx.y * zp; K < min(nzc + 1, (int)(blockIdx.y + 1) * zp); ++K) {
     bool live = pl < NYc * NXc;
     if (live && cflag) {
         const int I = pl % NYc, J = pl / NYc;
@@ -284,27 +285,34 @@ __global__ void __launch_bounds__(128) k_prolong_cells(const T *__restrict__ xc,
                     const T wy1 = T(ry) * inv, wy0 = T(S - ry) * inv;
                     const int f = rowbase + ry;
                     const uint8_t fl = nflag[f];
-                    T o[3] = {T(0), T(0), T(0)};
-                    if (fl & NF_ACTIVE) {
-                        T r[3];
+                    const bool act = (fl & NF_ACTIVE) != 0;
+                    // loads as selects (predicated, issued together) rather than under a branch
+                    T r[3], dg[3], o[3];
 #pragma unroll
-                        for (int q = 0; q < 3; ++q) {
-                            r[q] = rf[3 * f + q];
-                            const T t = (omega * r[q]) * D[3 * f + q];
-                            o[q] = (t + (wy0 * qx[0][q] + wy1 * qx[1][q])) + t;
-                        }
-                        if (FINAL) {
-#pragma unroll
-                            for (int q = 0; q < 3; ++q)
-                                if (fl & (NF_FIXX << q)) o[q] = T(0);
-                            dot += o[0] * r[0] + o[1] * r[1] + o[2] * r[2];
-                        }
+                    for (int q = 0; q < 3; ++q) {
+                        r[q] = act ? rf[3 * f + q] : T(0);
+                        dg[q] = act ? D[3 * f + q] : T(0);
                     }
 #pragma unroll
-                    for (int q = 0; q < 3; ++q) xf[3 * f + q] = o[q];
+                    for (int q = 0; q < 3; ++q) {
+                        const T t = (omega * r[q]) * dg[q];
+                        o[q] = act ? (t + (wy0 * qx[0][q] + wy1 * qx[1][q])) + t : T(0);
+                    }
+                    if (FINAL) {
+#pragma unroll
+                        for (int q = 0; q < 3; ++q)
+                            if (fl & (NF_FIXX << q)) o[q] = T(0);
+                        dot += o[0] * r[0] + o[1] * r[1] + o[2] * r[2];
+                    }
+                    // inactive nodes of an output that keeps zeros there (cflag set) are not rewritten
+                    if (act || !cflag) {
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) xf[3 * f + q] = o[q];
+                    }
                 }
             }
         }
+    }
     }
     if (FINAL && partial) {
         __shared__ double red[4];
@@ -321,12 +329,17 @@ void launch_prolong_smooth(const Level &fine, const Level &coarse, const T *xc, 
     // levels' x32) are zeroed at allocation, so their inactive nodes hold 0 throughout
     const bool skip_inactive = sizeof(T) == sizeof(float);
     if (small && (coarse.span == 2 || coarse.span == 4)) {
-        const dim3 g((unsigned)(((coarse.ny + 1) * (coarse.nx + 1) + 127) / 128), (unsigned)(coarse.nz + 1));
+        // 8 (else 4) coarse planes per CTA while that keeps at least 8 CTAs per SM
+        const int64_t plane_ctas = ((coarse.ny + 1) * (int64_t)(coarse.nx + 1) + 127) / 128;
+        int zp = 8;
+        while (zp > 1 && plane_ctas * ((coarse.nz + zp) / zp) < 152 * 8) zp >>= 1;
+        const dim3 g((unsigned)plane_ctas, (unsigned)((coarse.nz + zp) / zp));
         if (nblocks_out) *nblocks_out = (int)(g.x * g.y);
         ++g_launches;
 #define PCELLS(S, F)                                                                                              \
     k_prolong_cells<T, S, F><<<g, 128, 0, st>>>(xc, rf, diag, fine.nflag, skip_inactive ? coarse.nflag : nullptr, \
-                                                omega, xf, coarse.ny, coarse.nx, coarse.nz, F ? partial_dot : nullptr)
+                                                omega, xf, coarse.ny, coarse.nx, coarse.nz, zp,                  \
+                                                F ? partial_dot : nullptr)
         if (coarse.span == 2) {
             if (final_level)
                 PCELLS(2, true);

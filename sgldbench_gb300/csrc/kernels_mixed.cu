@@ -26,10 +26,19 @@ __device__ __forceinline__ double mblock_reduce(double v) {
     return s;
 }
 
+// four independent accumulators per thread, so that four loads are in flight
+// (a K*u launch on a large grid leaves tens of thousands of partials)
 __device__ double msum_partials(const double *__restrict__ part, int nb) {
-    double s = 0.0;
-    for (int i = threadIdx.x; i < nb; i += MB) s += part[i];
-    return mblock_reduce(s);
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int i = threadIdx.x;
+    for (; i + 3 * MB < nb; i += 4 * MB) {
+        s0 += part[i];
+        s1 += part[i + MB];
+        s2 += part[i + 2 * MB];
+        s3 += part[i + 3 * MB];
+    }
+    for (; i < nb; i += MB) s0 += part[i];
+    return mblock_reduce((s0 + s1) + (s2 + s3));
 }
 
 // inner scalars (FP64 storage): rho = z.s of the last iteration, alpha, beta,
@@ -272,14 +281,33 @@ void launch_icg_dupdate(float *e, float *d, const float *w, int64_t n, const dou
 }
 
 // ---- the same two updates over the active runs only -------------------------
-// On a grid with inactive regions the inner CG's vectors are exactly zero
-// outside the active bricks (32 y x 8 x x 8 z nodes holding an active node):
-// the inner solve's entry kernel and the K*u write every node, and these
-// updates keep zeros zero.  So the updates may visit only the bricks'
-// y-runs (runs[i] = first DOF | floats << 40, at most 96 floats each): a
-// warp per run, lanes over its floats.  Sums visit the runs in a fixed order.
+// On a grid with inactive regions the inner CG's vectors are exactly zero at
+// inactive nodes: the inner solve's entry kernel writes every node, K*u and
+// the V-cycle leave zeros there, and these updates keep zeros zero.  So the
+// updates may visit only the active nodes' words.
+// The active y-runs (merged where they touch or lie a few nodes apart) are
+// cut into chunks of at most 2048 floats, each cut on a 16-byte boundary
+// (runs[i] = first DOF | floats << 40).  A warp takes a chunk: the words up to
+// the first 16-byte boundary one by one, then float4 groups, then the last
+// words.  Sums visit the chunks in a fixed order.
 constexpr int RUN_SHIFT = 40;
 constexpr int64_t RUN_MASK = (int64_t(1) << RUN_SHIFT) - 1;
+
+// the chunk's words [b, b + len): head words before a 16-byte boundary, the
+// float4 groups of the body, tail words; f(i) for single words, f4(i4) for a
+// float4 group at float index 4 * i4
+template <typename F1, typename F4>
+__device__ __forceinline__ void run_chunk(int64_t b, int len, int lane, F1 f1, F4 f4) {
+    const int head = min((int)((4 - (b & 3)) & 3), len);
+    if (lane < head) f1(b + lane);
+    const int64_t a4 = (b + head) >> 2;
+    const int n4 = (len - head) >> 2;
+    // unrolled so that several groups' loads are in flight at once
+#pragma unroll 4
+    for (int k = lane; k < n4; k += 32) f4(a4 + k);
+    const int rest = len - head - 4 * n4;
+    if (lane < rest) f1(b + head + 4 * (int64_t)n4 + lane);
+}
 
 __global__ void __launch_bounds__(MB) k_icg_update_runs(float *__restrict__ s, const float *__restrict__ t,
                                                         const int64_t *__restrict__ runs, int64_t nruns,
@@ -287,20 +315,23 @@ __global__ void __launch_bounds__(MB) k_icg_update_runs(float *__restrict__ s, c
     const float a = (float)sc[IS_ALPHA];
     const int lane = threadIdx.x & 31;
     const int64_t w0 = (int64_t)blockIdx.x * (MB / 32) + (threadIdx.x >> 5), nw = (int64_t)gridDim.x * (MB / 32);
+    float4 *s4 = reinterpret_cast<float4 *>(s);
+    const float4 *t4 = reinterpret_cast<const float4 *>(t);
     float acc = 0.f;
     for (int64_t r = w0; r < nruns; r += nw) {
         const int64_t rv = runs[r];
-        const int64_t b = rv & RUN_MASK;
-        const int len = (int)(rv >> RUN_SHIFT);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const int j = lane + 32 * k;
-            if (j < len) {
-                const float v = fmaf(-a, t[b + j], s[b + j]);
-                s[b + j] = v;
+        run_chunk(
+            rv & RUN_MASK, (int)(rv >> RUN_SHIFT), lane,
+            [&](int64_t i) {
+                const float v = fmaf(-a, t[i], s[i]);
+                s[i] = v;
                 acc = fmaf(v, v, acc);
-            }
-        }
+            },
+            [&](int64_t i4) {
+                const float4 v = fma4(-a, t4[i4], s4[i4]);
+                s4[i4] = v;
+                acc = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, acc))));
+            });
     }
     if (part) {
 #pragma unroll
@@ -323,19 +354,22 @@ __global__ void __launch_bounds__(MB) k_icg_dupdate_runs(float *__restrict__ e, 
     const float a = (float)sc[IS_ALPHA], bt = (float)sc[IS_BETA];
     const int lane = threadIdx.x & 31;
     const int64_t w0 = (int64_t)blockIdx.x * (MB / 32) + (threadIdx.x >> 5), nw = (int64_t)gridDim.x * (MB / 32);
+    float4 *e4 = reinterpret_cast<float4 *>(e), *d4 = reinterpret_cast<float4 *>(d);
+    const float4 *w4 = reinterpret_cast<const float4 *>(w);
     for (int64_t r = w0; r < nruns; r += nw) {
         const int64_t rv = runs[r];
-        const int64_t b = rv & RUN_MASK;
-        const int len = (int)(rv >> RUN_SHIFT);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const int j = lane + 32 * k;
-            if (j < len) {
-                const float dv = d[b + j];
-                e[b + j] = fmaf(a, dv, e[b + j]);
-                d[b + j] = fmaf(bt, dv, w[b + j]);
-            }
-        }
+        run_chunk(
+            rv & RUN_MASK, (int)(rv >> RUN_SHIFT), lane,
+            [&](int64_t i) {
+                const float dv = d[i];
+                e[i] = fmaf(a, dv, e[i]);
+                d[i] = fmaf(bt, dv, w[i]);
+            },
+            [&](int64_t i4) {
+                const float4 dv = d4[i4];
+                e4[i4] = fma4(a, dv, e4[i4]);
+                d4[i4] = fma4(bt, dv, w4[i4]);
+            });
     }
 }
 

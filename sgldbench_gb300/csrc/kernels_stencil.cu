@@ -492,12 +492,15 @@ __global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    // producer threads 0 .. 2*ROWS-1: thread p copies row p % ROWS of stream p / ROWS
-    const bool producer = tid < 2 * ROWS;
+    // row p (row p % ROWS of stream p / ROWS) is copied by lane p / NW of warp p % NW, so that
+    // every warp issues 2 or 3 copies
+    constexpr int NW = THREADS / 32;
+    const int prow = (tid & 31) * NW + (tid >> 5);
+    const bool producer = prow < 2 * ROWS;
     int64_t pw = 0;   // word index of the row's first node (y0-1, x0-1+row) in the stream's layer zs-1
     if (producer) {
-        const int zs = tid < ROWS ? zA : zB;
-        pw = 3 * ((int64_t)(y0 - 1) + (int64_t)NY * (x0 - 1 + tid % ROWS)) + lwords * (zs - 1);
+        const int zs = prow < ROWS ? zA : zB;
+        pw = 3 * ((int64_t)(y0 - 1) + (int64_t)NY * (x0 - 1 + prow % ROWS)) + lwords * (zs - 1);
     }
     auto issue = [&](int i) {   // load i: node layer zs-1+i of both streams into slot i % RING
         const int slot = i % tk::RING;
@@ -505,13 +508,15 @@ __global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
         if (tid == 0) mbar_expect_tx(bar, G::SLOT_TX_BYTES);
         if (producer) {
             const int64_t w = pw + lwords * i;
-            tma_load_1d(smem_addr(ring + slot * G::SLOT_WORDS + tid * tk::ROWP), &umap,
+            tma_load_1d(smem_addr(ring + slot * G::SLOT_WORDS + prow * tk::ROWP), &umap,
                         (int)(w & ~(int64_t)3), bar);
         }
     };
-    int issued = 0, waited = 0;   // loads issued; loads whose completion thread 0 has seen
+    int issued = 0, waited = 0;   // loads issued; loads this thread has waited for
     for (; issued < min(tk::RING, nload); ++issued) issue(issued);
-    auto wait_load = [&](int i) -> bool {   // thread 0
+    // every thread waits for a load right before reading it; a wait that gives up raises
+    // s_abort, which the CTA acts on after its next barrier
+    auto wait_load = [&](int i) -> bool {
         const bool ok = mbar_wait(smem_addr(bars + i % tk::RING), (uint32_t)((i / tk::RING) & 1));
         waited = i + 1;
         return ok;
@@ -531,34 +536,26 @@ __global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
                 o[0] = o[1] = o[2] = __int_as_float(0x7fc00000);
             }
     };
-    if (tid == 0 && !(wait_load(0) && wait_load(1))) s_abort = 1;
-    __syncthreads();
-    if (s_abort) {
-        bail();
-        return;
-    }
     // this thread reads node rows tx and tx+1 of each stream at words 3*ty + lead, where the
     // lead (0..3 words) follows the row's start address modulo 16 bytes
-    int roff[2][2], lead0[2][2];
-#pragma unroll
-    for (int s = 0; s < 2; ++s)
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const int zs = s ? zB : zA;
-            const int64_t w = 3 * ((int64_t)(y0 - 1) + (int64_t)NY * (x0 - 1 + tx + r)) + lwords * (zs - 1);
-            lead0[s][r] = (int)(w & 3);
-            roff[s][r] = (s * ROWS + tx + r) * tk::ROWP + 3 * ty;
-        }
-    const int lstep = (int)(lwords & 3);
+    // (the other rows and the other stream sit at fixed offsets from row tx of stream A, and
+    // their leads differ from its lead by per-CTA constants)
+    const int roff = tx * tk::ROWP + 3 * ty;
+    const int64_t w00 = 3 * ((int64_t)(y0 - 1) + (int64_t)NY * (x0 - 1 + tx)) + lwords * (zA - 1);
+    const int lead00 = (int)(w00 & 3);
+    const int dr = (3 * NY) & 3, ds = (int)((lwords * zc) & 3);   // lead steps: next row, stream B
+    const int lstep = (int)(lwords & 3);                          // lead step: next layer
     // the 12 face coefficients (x, y Hadamard) of node layer zs-1+i, both streams; also the
     // values of node (ey+1, ex+1) in that layer
     auto faces = [&](int i, float2 (&F)[12], float2 (&un)[3]) {
-        const float *sl = ring + (i % tk::RING) * G::SLOT_WORDS;
+        if (!wait_load(i)) s_abort = 1;
+        const float *sl = ring + (i % tk::RING) * G::SLOT_WORDS + roff;
+        const int li = lead00 + lstep * i;
         float2 v[2][2][3];   // [row][node ey, ey+1][c]
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
-            const float *pa = sl + roff[0][r] + ((lead0[0][r] + lstep * i) & 3);
-            const float *pb = sl + roff[1][r] + ((lead0[1][r] + lstep * i) & 3);
+            const float *pa = sl + r * tk::ROWP + ((li + r * dr) & 3);
+            const float *pb = sl + (ROWS + r) * tk::ROWP + ((li + r * dr + ds) & 3);
 #pragma unroll
             for (int n = 0; n < 2; ++n)
 #pragma unroll
@@ -578,7 +575,7 @@ __global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
         }
     };
     float2 Fp[12], carry[12], uo[3];
-    faces(0, Fp, uo);
+    faces(0, Fp, uo);   // a wait that gave up here is acted on after step 0's barrier
 #pragma unroll
     for (int i = 0; i < 12; ++i) carry[i] = make_float2(0.f, 0.f);
     float dot = 0.f;
@@ -636,7 +633,6 @@ __global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
         float2 *xb = exch + (j & 1) * 6 * THREADS;
 #pragma unroll
         for (int v = 0; v < 6; ++v) xb[v * THREADS + tid] = Lm[v];
-        if (tid == 0 && j + 2 < nload && !wait_load(j + 2)) s_abort = 1;
         __syncthreads();
         if (s_abort) {
             bail();

@@ -257,28 +257,44 @@ int fail(sgld_ctx *ctx, int code, const std::string &msg) {
 int build_active_runs(sgld_ctx *ctx) {
     Level &l0 = ctx->c.lv[0];
     const int NY = l0.ny + 1, NX = l0.nx + 1, NZ = l0.nz + 1;
-    const int by = (NY + 31) / 32, bx = (NX + 7) / 8, bz = (NZ + 7) / 8;
-    std::vector<uint8_t> brick((size_t)by * bx * bz, 0);
-    for (int z = 0; z < NZ; ++z)
-        for (int x = 0; x < NX; ++x) {
-            const uint8_t *f = l0.h_nflag.data() + (size_t)NY * (x + (size_t)NX * z);
-            for (int y = 0; y < NY; ++y)
-                if (f[y] & NF_ACTIVE) brick[(size_t)(y / 32) + by * ((size_t)(x / 8) + (size_t)bx * (z / 8))] = 1;
-        }
-    size_t nact = 0;
-    for (uint8_t b : brick) nact += b;
-    if (nact > 0.85 * (double)brick.size()) return SGLD_OK;
+    const int64_t nn = (int64_t)NY * NX * NZ;
+    if ((double)l0.nnode_active > 0.85 * (double)nn) return SGLD_OK;   // nearly full: the flat kernels run
+    // the maximal y-runs of active nodes in address order, merged where they touch or lie
+    // at most kRunGap floats apart, cut into chunks of at most kRunChunk floats on 16-byte
+    // boundaries (kernels_mixed.cu)
+    constexpr int64_t kRunChunk = 2048, kRunGap = 48;
     std::vector<int64_t> runs;
-    runs.reserve(nact * 64);
-    for (int z = 0; z < NZ; ++z)
-        for (int x = 0; x < NX; ++x)
-            for (int yb = 0; yb < by; ++yb) {
-                if (!brick[(size_t)yb + by * ((size_t)(x / 8) + (size_t)bx * (z / 8))]) continue;
-                const int y0 = 32 * yb, len = 3 * std::min(32, NY - y0);
-                const int64_t first = 3 * ((int64_t)y0 + (int64_t)NY * (x + (int64_t)NX * z));
-                runs.push_back(first | ((int64_t)len << 40));
-            }
-    l0.nruns = (int64_t)runs.size();
+    runs.reserve((size_t)NX * NZ * 2);
+    int64_t sb = -1, se = -1;   // current span [sb, se) in floats
+    auto flush = [&]() {
+        for (int64_t p = sb; p < se;) {
+            int64_t q = std::min(se, p + kRunChunk);
+            if (q < se) q &= ~(int64_t)3;   // interior cuts on 16-byte boundaries
+            runs.push_back(p | ((q - p) << 40));
+            p = q;
+        }
+    };
+    const uint8_t *f = l0.h_nflag.data();
+    for (int64_t n = 0; n < nn;) {
+        if (!(f[n] & NF_ACTIVE)) {
+            ++n;
+            continue;
+        }
+        int64_t m = n + 1;   // the run ends at the column's end at the latest
+        const int64_t col_end = (n / NY + 1) * NY;
+        while (m < col_end && (f[m] & NF_ACTIVE)) ++m;
+        // a gap of a few inactive nodes is bridged (their words are zero in every vector of
+        // the inner solve, and the updates keep zeros zero): longer runs, fewer partial groups
+        if (se >= 0 && 3 * n - se <= kRunGap) {
+            se = 3 * m;
+        } else {
+            if (sb >= 0) flush();
+            sb = 3 * n;
+            se = 3 * m;
+        }
+        n = m;
+    }
+    if (sb >= 0) flush();    l0.nruns = (int64_t)runs.size();
     CK(dalloc(&l0.runs, runs.size()));
     CK(cudaMemcpy(l0.runs, runs.data(), sizeof(int64_t) * runs.size(), cudaMemcpyHostToDevice));
     return SGLD_OK;

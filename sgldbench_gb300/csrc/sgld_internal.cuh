@@ -52,9 +52,10 @@ struct Level {
     // FP64 and double-float kernels, and the FP32 kernel's grid for the tile
     // (tiles_f32_tx, tiles_f32_zc) it was made for
     uint8_t *tiles16 = nullptr, *tiles_f32 = nullptr;
-    // finest level: the y-runs of the active bricks (32 y x 8 x x 8 z nodes
-    // holding an active node), each first DOF | floats << 40, in address order;
-    // empty when nearly every brick is active (then the flat kernels run)
+    // finest level: the words of the active nodes as chunks of contiguous
+    // floats (runs of active nodes along y, gaps of a few nodes bridged), each
+    // first DOF | floats << 40, in address order; empty when nearly every node
+    // is active (then the flat kernels run)
     int64_t *runs = nullptr;
     int64_t nruns = 0;
     int tiles_f32_tx = 0, tiles_f32_zc = 0;

@@ -478,8 +478,10 @@ __global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
     const int zA = blockIdx.z * 2 * zc, zB = zA + zc;
     const int gny = y0 + ty, gnx = x0 + tx;
     const bool owner = ty < KT_Y - 1 && tx < TX - 1 && gny < NY && gnx < NX;
+    // the output keeps exact zeros at inactive nodes (it is zeroed when allocated and no
+    // launch writes there): a tile without active elements writes nothing
     if (tiles && !tiles[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)]) {
-        skip_tile(y, owner, gny, gnx, NY, NX, zA, min(zA + 2 * zc, NZ), DOT ? partial : nullptr);
+        if (DOT && tid == 0) partial[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = 0.0;
         return;
     }
     const int ey = y0 - 1 + ty, ex = x0 - 1 + tx;
@@ -532,7 +534,9 @@ __global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
         }
         if (owner)
             for (int z = zA; z < min(zA + 2 * zc, NZ); ++z) {
-                float *o = y + 3 * ((int64_t)gny + (int64_t)NY * (gnx + (int64_t)NX * z));
+                const int64_t node = (int64_t)gny + (int64_t)NY * (gnx + (int64_t)NX * z);
+                if (!(nflag[node] & NF_ACTIVE)) continue;
+                float *o = y + 3 * node;
                 o[0] = o[1] = o[2] = __int_as_float(0x7fc00000);
             }
     };
@@ -586,9 +590,11 @@ __global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
     int eoA = (ey + ny * ex) + eplane * (zA - 1), eoB = eoA + eplane * zc;
     int noA = (gny + NY * gnx) + nplane * (zA - 1), noB = noA + nplane * zc;
     auto emod = [&](int o, int k) -> float { return (ein && k >= 0 && k < nz) ? E[o] : 0.f; };
+    // the raw flag byte, or -1 (not owned, past the grid); nothing uses the loaded byte
+    // until the next step, so the load's latency stays hidden
     auto flag = [&](int o, int z) -> int { return (owner && z >= 0 && z < NZ) ? (int)nflag[o] : -1; };
     float2 en = make_float2(emod(eoA, zA - 1), emod(eoB, zB - 1));
-    int fnA = -1, fnB = -1;   // -1: node not written (not owned, or past the grid)
+    int fnA = -1, fnB = -1;
 #pragma unroll 2
     for (int j = 0; j <= zc; ++j) {
         // element layer zs-1+j: faces of node layers zs-1+j (Fp) and zs+j (Ft)
@@ -653,7 +659,7 @@ __global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
                                                         __shfl_down_sync(0xffffffffu, up.y, 1)));
             }
             // node layer zs-1+j of each stream is complete
-            if (fA >= 0) {
+            if (fA >= 0 && (fA & NF_ACTIVE)) {   // inactive nodes are never written
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     const float oc = (fA & (NF_FIXX << c)) ? 0.f : o[c].x;
@@ -661,7 +667,7 @@ __global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
                     if (DOT) dot = fmaf(uo[c].x, oc, dot);
                 }
             }
-            if (fB >= 0) {
+            if (fB >= 0 && (fB & NF_ACTIVE)) {
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     const float oc = (fB & (NF_FIXX << c)) ? 0.f : o[c].y;

@@ -900,6 +900,8 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
     CK(dalloc(&c.d_z32, nv));
     CK(cudaMemset(c.d_z32, 0, sizeof(float) * nv));   // see lv.x32
     for (float **p : {&c.d_e32, &c.d_s32, &c.d_d32, &c.d_t32}) CK(dalloc(p, nv));
+    // the FP32 K*u (whose output is always d_t32) never writes inactive nodes
+    CK(cudaMemset(c.d_t32, 0, sizeof(float) * nv));
     CK(dalloc(&c.d_isc, 16));
     init_kernel_attributes();
     init_kbyu_df_attributes();

@@ -183,7 +183,9 @@ void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *
                      int *nblocks_out, cudaStream_t s);
 // (re)makes l0's active-tile maps for its current FP32 tile; 0 or a CUDA error
 int update_kbyu_tiles(Level &l0, cudaStream_t s);
-// 0, or a CUDA error code when the launch could not be set up (the input's tensor map)
+// 0, or a CUDA error code when the launch could not be set up (the input's tensor map).
+// y is written at active nodes only: its inactive nodes must already hold zeros
+// (every caller passes the context's d_t32, zeroed when allocated)
 int launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
                     int *nblocks_out, cudaStream_t s);
 void init_kernel_attributes();

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsgld_gb300.so")
-SOURCES = ["kernels_stencil.cu", "kernels_mg.cu", "kernels_asm.cu", "kernels_vec.cu", "kernels_mixed.cu", "kernels_topopt.cu", "kernels_df.cu", "kernels_principal.cu", "kernels_pde.cu", "kernels_mma.cu", "kernels_net.cu", "sgld_net.cu", "sgld_learned.cu", "noalloc.cu", "kernels_cases.cu", "sgld_cases.cu",
+SOURCES = ["kernels_stencil.cu", "kernels_mg.cu", "kernels_asm.cu", "kernels_vec.cu", "kernels_mixed.cu", "kernels_topopt.cu", "kernels_df.cu", "kernels_principal.cu", "kernels_pde.cu", "kernels_mma.cu", "kernels_net.cu", "kernels_net_tc.cu", "sgld_net.cu", "sgld_learned.cu", "noalloc.cu", "kernels_cases.cu", "sgld_cases.cu",
            "sgld_api.cu", "sgld_topopt_api.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

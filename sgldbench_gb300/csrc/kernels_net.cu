@@ -13,11 +13,14 @@
 //   * every product accumulates in FP32.
 // A 3x3x3 convolution ("same", zero padding) is an implicit GEMM: output
 // voxels x output channels, reduced over 27 taps x input channels.  The work
-// is small (about 4 GFLOP forward at 65x33x33 nodes), so it runs on the FP32
-// pipes with shared-memory operand tiles rather than on the tensor cores.
+// is small (about 4 GFLOP forward at 65x33x33 nodes).  The forward and data-
+// gradient convolutions run on the tensor cores (kernels_net_tc.cu); k_conv
+// below is their FP32-pipe form (SGLD_NET_CUDA_CORES=1, and channel counts
+// above 64), and the weight gradient stays on the FP32 pipes.
 #include <cuda_bf16.h>
 
 #include "sgld_internal.cuh"
+#include "sgld_net.cuh"
 
 namespace sgld {
 
@@ -394,14 +397,29 @@ static size_t conv_smem(int cin, int cout) { return sizeof(float) * (size_t)cin 
 
 // opt-in shared memory of the convolution (64 x 64 channels need 49 KB)
 void net_init_attributes() {
+    net_tc_init_attributes();
     const int mx = (int)conv_smem(CV_CMAX, CV_CMAX);
     cudaFuncSetAttribute(k_conv<bf16, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_conv<bf16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_conv<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 }
 
+// the CUDA-core convolutions instead of the tensor-core ones (environment
+// SGLD_NET_CUDA_CORES=1, read once; for comparisons)
+static bool net_cuda_cores() {
+    static const bool v = [] {
+        const char *e = getenv("SGLD_NET_CUDA_CORES");
+        return e && e[0] == '1';
+    }();
+    return v;
+}
+
 void net_conv_fwd(const bf16 *in, int cin, const bf16 *w, const float *b, int cout, int taps, int ny, int nx, int nz,
-                  bool relu_bf16_out, void *out, cudaStream_t s) {
+                  bool relu_bf16_out, void *out, bf16 *wimg, int *err, cudaStream_t s) {
+    if (wimg && net_conv_tc_fits(cin, cout) && !net_cuda_cores()) {
+        net_conv_fwd_tc(in, cin, w, b, cout, taps, ny, nx, nz, relu_bf16_out, out, wimg, err, s);
+        return;
+    }
     const int64_t V = (int64_t)ny * nx * nz;
     const int threads = 32 * (((cout + 3) & ~3) / 4);
     ++g_launches;
@@ -415,11 +433,16 @@ void net_conv_fwd(const bf16 *in, int cin, const bf16 *w, const float *b, int co
 
 // data gradient: gin (=/+=) mask(conv(gout, flipped w)); wt is scratch of taps*cin*cout
 void net_conv_bwd_data(const float *gout, int cout, const bf16 *w, bf16 *wt, int cin, int taps, int ny, int nx,
-                       int nz, const bf16 *mask, float *gin, bool accumulate, cudaStream_t s) {
+                       int nz, const bf16 *mask, float *gin, bool accumulate, bf16 *wimg, int *err, cudaStream_t s) {
     const int64_t V = (int64_t)ny * nx * nz;
     const int64_t nw = (int64_t)taps * cin * cout;
-    g_launches += 2;
+    ++g_launches;
     k_wflip<<<nblk(nw), 256, 0, s>>>(w, taps, cin, cout, wt);
+    if (wimg && net_conv_tc_fits(cout, cin) && !net_cuda_cores()) {
+        net_conv_bwd_data_tc(gout, cout, wt, cin, taps, ny, nx, nz, mask, gin, accumulate, wimg, err, s);
+        return;
+    }
+    ++g_launches;
     const int threads = 32 * (((cin + 3) & ~3) / 4);
     k_conv<float, 2><<<nblk(V, CV_BM), threads, conv_smem(cout, cin), s>>>(gout, cout, wt, nullptr, cin, taps, ny, nx,
                                                                            nz, gin, mask, accumulate ? 1 : 0);

@@ -42,7 +42,8 @@ const int *dim3_of(const Net &n, int l) { return n.dims[l]; }
 void conv_fwd(Net &n, int k, const bf16 *in, void *out, bool relu) {
     const NetConv &c = n.conv[k];
     const int *d = dim3_of(n, c.level);
-    net_conv_fwd(in, c.cin, n.wb + c.w, n.w + c.b, c.cout, c.taps, d[0], d[1], d[2], relu, out, n.s);
+    net_conv_fwd(in, c.cin, n.wb + c.w, n.w + c.b, c.cout, c.taps, d[0], d[1], d[2], relu, out, n.wimg, n.tc_err,
+                 n.s);
 }
 
 // dW, db of convolution k from its input activation and the gradient of its output
@@ -56,7 +57,8 @@ void conv_wgrad(Net &n, int k, const bf16 *in, const float *gout) {
 void conv_bwd(Net &n, int k, const float *gout, const bf16 *mask, float *gin, bool acc) {
     const NetConv &c = n.conv[k];
     const int *d = dim3_of(n, c.level);
-    net_conv_bwd_data(gout, c.cout, n.wb + c.w, n.wt, c.cin, c.taps, d[0], d[1], d[2], mask, gin, acc, n.s);
+    net_conv_bwd_data(gout, c.cout, n.wb + c.w, n.wt, c.cin, c.taps, d[0], d[1], d[2], mask, gin, acc, n.wimg,
+                      n.tc_err, n.s);
 }
 
 int conv_a(int l) { return 2 * l; }
@@ -109,10 +111,11 @@ int net_init(Net &n, int ny, int nx, int nz, int cin, int cout, int L, const int
         add(n.width[l], n.width[l], 27, l);
     }
     add(n.width[0], cout, 1, 0);
-    int64_t wmax = 0, pmax = 0;
+    int64_t wmax = 0, pmax = 0, imax = 0;
     for (const NetConv &c : n.conv) {
         const int64_t nw = (int64_t)c.taps * c.cin * c.cout;
         wmax = std::max(wmax, nw);
+        imax = std::max(imax, (int64_t)c.taps * ((c.cin + 15) & ~15) * ((c.cout + 15) & ~15));
         pmax = std::max(pmax, (int64_t)net_wgrad_splits(n.V[c.level]) * (nw + c.cout));
     }
     cudaError_t e = cudaSuccess;
@@ -124,6 +127,9 @@ int net_init(Net &n, int ny, int nx, int nz, int cin, int cout, int L, const int
     NA(&n.g, n.nparam);
     NA(&n.wb, n.nparam);
     NA(&n.wt, wmax);
+    NA(&n.wimg, imax);
+    NA(&n.tc_err, 1);
+    if (e == cudaSuccess) e = cudaMemsetAsync(n.tc_err, 0, sizeof(int), s);
     NA(&n.wpart, pmax);
     NA(&n.x_own, n.V[0] * cin);
     n.X.level = 0;

@@ -46,6 +46,8 @@ struct Net {
     int64_t nparam = 0;
     float *w = nullptr, *m = nullptr, *v = nullptr, *g = nullptr, *wpart = nullptr;
     bf16 *wb = nullptr, *wt = nullptr;
+    bf16 *wimg = nullptr;   // one convolution's weights as tensor-core operand images (all taps)
+    int *tc_err = nullptr;  // set by a tensor-core convolution whose MMA wait gave up
     NetAct X, Ea[NET_MAXL], E[NET_MAXL], P[NET_MAXL], Du[NET_MAXL], S[NET_MAXL], D[NET_MAXL];
     bf16 *x_own = nullptr;   // the network's own input buffer (X.a may point elsewhere)
     float *Y = nullptr, *gY = nullptr, *T = nullptr, *M = nullptr;
@@ -65,10 +67,19 @@ void net_adam_step(Net &n, float lr);                            // n.g -> n.w, 
 
 // kernels_net.cu
 void net_init_attributes();
+// wimg: scratch for the weight images of the tensor-core path (taps x pad16(cin) x
+// pad16(cout) BF16); err: device flag of that path
 void net_conv_fwd(const bf16 *in, int cin, const bf16 *w, const float *b, int cout, int taps, int ny, int nx, int nz,
-                  bool relu_bf16_out, void *out, cudaStream_t s);
+                  bool relu_bf16_out, void *out, bf16 *wimg, int *err, cudaStream_t s);
 void net_conv_bwd_data(const float *gout, int cout, const bf16 *w, bf16 *wt, int cin, int taps, int ny, int nx,
-                       int nz, const bf16 *mask, float *gin, bool accumulate, cudaStream_t s);
+                       int nz, const bf16 *mask, float *gin, bool accumulate, bf16 *wimg, int *err, cudaStream_t s);
+// kernels_net_tc.cu: the same two convolutions on the tensor cores (tcgen05)
+bool net_conv_tc_fits(int cin, int cout);
+void net_tc_init_attributes();
+void net_conv_fwd_tc(const bf16 *in, int cin, const bf16 *w, const float *b, int cout, int taps, int ny, int nx,
+                     int nz, bool relu_bf16_out, void *out, bf16 *wimg, int *err, cudaStream_t s);
+void net_conv_bwd_data_tc(const float *gout, int cout, const bf16 *wt, int cin, int taps, int ny, int nx, int nz,
+                          const bf16 *mask, float *gin, bool accumulate, bf16 *wimg, int *err, cudaStream_t s);
 int net_wgrad_splits(int64_t V);
 void net_conv_wgrad(const bf16 *in, int cin, const float *gout, int cout, int taps, int ny, int nx, int nz,
                     float *part, float *gw, float *gb, cudaStream_t s);

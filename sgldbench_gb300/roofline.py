@@ -18,9 +18,18 @@ import os
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
-# ncu DRAM bytes per full-grid node of one k_kbyu_tma launch, by workload kind
-# (filled from the captures summarised under profiles/)
-DRAM_BYTES_PER_GRID_NODE: dict = {}
+# ncu DRAM bytes per full-grid node of one k_kbyu_tma launch, by workload kind.
+# "blobs": dram__bytes_read.sum + dram__bytes_write.sum = 160,872,448 + 31,981,824
+# bytes for one launch on the 384 x 192 x 192 thresholded-blob shape (30 % solid,
+# 385 * 193 * 193 = 14,340,865 grid nodes; default tile 32 x 8 x 26 layers) on a
+# GB300, from
+#   SGLD_AUTOTUNE=0 ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
+#       --clock-control none -k regex:k_kbyu_tma -c 1 --csv python -m sgldbench_gb300.kernel_bench
+#       --domain blobs --size 384 192 192 --levels 6 --ops kbyu32 --reps 3
+# The same shape family at 1024 x 512 x 512 is too large for a capture; its
+# traffic is scaled by the grid nodes (the launch reads the rows of the tiles
+# that hold active elements and writes the active nodes, both in proportion).
+DRAM_BYTES_PER_GRID_NODE: dict = {"blobs": (160872448 + 31981824) / 14340865}
 
 
 def peaks() -> dict:

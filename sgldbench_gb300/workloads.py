@@ -9,7 +9,11 @@ oracle's in the parity tests -- is recorded here with its provenance.
 from __future__ import annotations
 
 # (nx, ny, nz, levels, fill, blobs) -> (iterations, provenance)
-FP64_ITERATIONS: dict = {}
+FP64_ITERATIONS: dict = {
+    (1024, 512, 512, 7, 0.3, 64): (
+        507, "measured: the reference-form FP64 PCG of held-out case 0 on a GB300 (bench.py plain_fp64, "
+             "two runs, 507 iterations each)"),
+}
 
 # used when no measurement is recorded for a workload
 DEFAULT_ITERATIONS = 500

@@ -2135,6 +2135,10 @@ int sgld::vcycle_f64(sgld_ctx *ctx, const double *r, double *z, double *partial,
     return vcycle_dev(ctx, r, z, partial, nb);
 }
 
+int sgld::vcycle_f32(sgld_ctx *ctx, const float *r, float *z, double *partial, int *nb) {
+    return vcycle_dev32(ctx, r, z, partial, nb);
+}
+
 int sgld::solve_on_device(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *info) {
     int rc = check_assembled(ctx);
     if (rc) return rc;

@@ -15,8 +15,10 @@
 // For a new load F the start is
 //   x_b = sum_i (W_i' F) W_i       the energy-optimal start in span(W), and
 //   x   = x_b + beta P net(.)      beta = v'r0 / v'Kv for v = P net(.),
-// kept only if it lowers r'Mr (M = the FP64 V-cycle, an SPD approximation of
-// K^-1, so r'Mr tracks the energy norm of the error).  The solve then runs to
+// kept only if it lowers r'Mr (M = the FP32 V-cycle, an SPD approximation of
+// K^-1, so r'Mr tracks the energy norm of the error; the start's residual and
+// the correction's energy come from the FP32 K*u, since they only choose
+// between two starts).  The solve then runs to
 // its tolerance on the true residual as any other, so the start changes the
 // iteration count and never the converged answer.
 #include <math.h>
@@ -107,6 +109,29 @@ int mnorm_into(sgld_ctx *ctx, const double *r, double *out) {
     if (rc) return rc;
     launch_finalize_sum(c.d_part2, nb, out, c.stream);
     return SGLD_OK;
+}
+
+// The choice between two starts only compares r'Mr values, so it runs on the FP32
+// operators (the solve itself forms its true residual with the double-float K*u):
+// r'Mr with the FP32 V-cycle, r narrowed to FP32, into *out (device)
+int mnorm32_into(sgld_ctx *ctx, const double *r, double *out) {
+    Ctx &c = ctx->c;
+    launch_narrow(r, c.d_r32, 3 * c.lv[0].nnode, c.stream);
+    int nb = 0;
+    const int rc = vcycle_f32(ctx, c.d_r32, c.d_z32, c.d_part2, &nb);
+    if (rc) return rc;
+    launch_finalize_sum(c.d_part2, nb, out, c.stream);
+    return SGLD_OK;
+}
+
+// y = K x with the FP32 operator (x narrowed, the product widened); 0 or a CUDA error
+int kbyu32_into(Ctx &c, const double *x, double *y, cudaStream_t s) {
+    const Level &l0 = c.lv[0];
+    const int64_t nv = 3 * l0.nnode;
+    launch_narrow(x, c.d_r32, nv, s);
+    if (int e = launch_kbyu_f32(l0, c.d_E32, c.d_r32, c.d_t32, nullptr, nullptr, s)) return e;
+    launch_widen(c.d_t32, y, nv, s);
+    return 0;
 }
 
 // the network's level: the finest one with at most 110K nodes (MATLAB level
@@ -202,7 +227,7 @@ int net_correction(sgld_cases *cs, sgld_cases_stats *st) {
                                       nullptr, nullptr, s);
     }
     launch_mask_fixed(l0, c.d_p, s);
-    launch_kbyu_df(l0, c.E, c.d_p, c.d_q, nullptr, nullptr, s);
+    if (kbyu32_into(c, c.d_p, c.d_q, s)) return cfail(ctx, SGLD_ERR_CUDA, "FP32 K*u of the network's correction");
     dot_into(c, c.d_p, cs->d_r0, nv, cs->d_sc + 0, s);
     dot_into(c, c.d_p, c.d_q, nv, cs->d_sc + 1, s);
     double h[2];
@@ -211,10 +236,10 @@ int net_correction(sgld_cases *cs, sgld_cases_stats *st) {
     if (!(h[1] > 0.0) || !isfinite(h[0]) || !isfinite(h[1])) return SGLD_OK;
     const double beta = h[0] / h[1];
     int rc;
-    if ((rc = mnorm_into(ctx, cs->d_r0, cs->d_sc + 2))) return rc;
+    if ((rc = mnorm32_into(ctx, cs->d_r0, cs->d_sc + 2))) return rc;
     CCK(cudaMemcpyAsync(cs->d_w, cs->d_r0, sizeof(double) * nv, cudaMemcpyDeviceToDevice, s));
     net_axpby(cs->d_w, c.d_q, -beta, 1.0, nv, s);
-    if ((rc = mnorm_into(ctx, cs->d_w, cs->d_sc + 3))) return rc;
+    if ((rc = mnorm32_into(ctx, cs->d_w, cs->d_sc + 3))) return rc;
     double m[2];
     CCK(cudaMemcpyAsync(m, cs->d_sc + 2, sizeof m, cudaMemcpyDeviceToHost, s));
     CCK(cudaStreamSynchronize(s));
@@ -302,8 +327,9 @@ int cases_run(sgld_cases *cs, const sgld_solve_opts *o, int mode, int train, sgl
     else CCK(cudaMemsetAsync(c.d_x, 0, sizeof(double) * nv, s));
     const bool want_net = mode == 2 && cs->net_ok;
     if (want_net || st->diagnostics) {
+        // r0 = F - K x_b for the network's features and the choice of start (FP32 K*u)
         CCK(cudaMemcpyAsync(cs->d_xb, c.d_x, sizeof(double) * nv, cudaMemcpyDeviceToDevice, s));
-        launch_kbyu_df(l0, c.E, c.d_x, c.d_q, nullptr, nullptr, s);
+        if (kbyu32_into(c, c.d_x, c.d_q, s)) return cfail(ctx, SGLD_ERR_CUDA, "FP32 K*u of the basis start");
         launch_residual(cs->d_r0, c.d_b, c.d_q, nv, s);
         launch_mask_fixed(l0, cs->d_r0, s);
     }

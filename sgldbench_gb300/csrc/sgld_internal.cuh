@@ -253,6 +253,8 @@ int solve_on_device(sgld_ctx *ctx, const sgld_solve_opts *o, sgld_solve_info *in
 // FP64 additive V-cycle z = M r on full-grid vectors; with partial, the CTA
 // partials of z.r (nb of them) for launch_finalize_sum
 int vcycle_f64(sgld_ctx *ctx, const double *r, double *z, double *partial, int *nb);
+// the FP32 V-cycle on FP32 full-grid vectors (z: the context's d_z32, whose inactive nodes hold 0)
+int vcycle_f32(sgld_ctx *ctx, const float *r, float *z, double *partial, int *nb);
 // SIMP loop (kernels_topopt.cu)
 void upload_filter_weights(double rmin, int *radius, double *d_w, cudaStream_t s);
 void launch_density_filter(const Level &l0, const double *x, int r, const double *fw, double *y, cudaStream_t s);

@@ -4,7 +4,7 @@ and as the small driver of kernel-level profiler captures.
   python -m sgldbench_gb300.kernel_bench [--size NX NY NZ] [--levels L]
                                          [--ops kbyu64 kbyu32 kbyu_df vcycle64 vcycle32 assemble]
                                          [--reps N] [--domain graded|blobs] [--fill F]
-                                         [--solve PRECISION]
+                                         [--solve PRECISION] [--net NY NX NZ]
 
 Builds the SIMP-graded cantilever of the given size (or, with --domain blobs,
 the thresholded Gaussian-blob shape of the large stress analysis with its
@@ -15,6 +15,12 @@ runs one solve to relative residual 1e-6 in the given precision (the
 cantilever load, or one patch load of the blob shape) and prints its
 iterations and device time; with SGLD_INNER_LOOP=host its inner loop runs
 from the host, so that a profiler's launch list shows every kernel.
+
+--net NY NX NZ times the learned start's U-Net alone (8 input channels, 3
+outputs, 4 levels of widths 16/32/48/64) on that node grid instead: forward
+passes and training steps (host copies of its small inputs included); with
+SGLD_NET_CUDA_CORES=1 its convolutions run on the FP32 pipes instead of the
+tensor cores.
 """
 from __future__ import annotations
 
@@ -35,6 +41,34 @@ def bytes_and_flops(op: str, nn: int, ne: int) -> tuple[int, float]:
     return 0, 0.0
 
 
+def net_bench(dims, reps: int):
+    import os
+    import time
+
+    from .net import UNet
+
+    cin = 8
+    net = UNet(tuple(dims), cin, 3, levels=4, widths=[16, 32, 48, 64], seed=0)
+    V = int(np.prod(dims))
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((V, cin)).astype(np.float32)
+    t = rng.standard_normal((V, 3)).astype(np.float32)
+    for _ in range(3):
+        net.forward(x)
+        net.train_step(x, t, lr=1e-4)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        net.forward(x)
+    t1 = time.perf_counter()
+    for _ in range(reps):
+        net.train_step(x, t, lr=1e-4)
+    t2 = time.perf_counter()
+    print(json.dumps({"net": list(dims), "convolutions": "fp32 pipes" if os.environ.get("SGLD_NET_CUDA_CORES") == "1"
+                      else "tensor cores", "forward_ms": (t1 - t0) / reps * 1e3,
+                      "train_step_ms": (t2 - t1) / reps * 1e3}), flush=True)
+    net.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--size", type=int, nargs=3, default=[256, 128, 128])
@@ -44,7 +78,11 @@ def main():
     ap.add_argument("--domain", choices=["graded", "blobs"], default="graded")
     ap.add_argument("--fill", type=float, default=0.3)
     ap.add_argument("--solve", choices=["fp64", "mixed", "mixed_df"], default=None)
+    ap.add_argument("--net", type=int, nargs=3, default=None, metavar=("NY", "NX", "NZ"))
     args = ap.parse_args()
+    if args.net:
+        net_bench(args.net, args.reps)
+        return
     nx, ny, nz = args.size
     if args.domain == "blobs":
         vox = D.gaussian_blobs(nx, ny, nz, seed=0, n_blobs=64, fill=args.fill)

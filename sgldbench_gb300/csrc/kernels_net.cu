@@ -455,14 +455,19 @@ int net_wgrad_splits(int64_t V) {
 
 // gw = dL/dw [taps][cin][cout], gb = dL/db [cout]; part holds S*(taps*cin*cout + cout) floats
 void net_conv_wgrad(const bf16 *in, int cin, const float *gout, int cout, int taps, int ny, int nx, int nz,
-                    float *part, float *gw, float *gb, cudaStream_t s) {
+                    float *part, float *gw, float *gb, int *err, cudaStream_t s) {
     const int64_t V = (int64_t)ny * nx * nz;
     const int S = net_wgrad_splits(V);
     const int64_t vchunk = (V + S - 1) / S;
     const int64_t nw = (int64_t)taps * cin * cout;
     float *bpart = part + (int64_t)S * nw;
-    g_launches += 3;
-    k_conv_wgrad<bf16><<<dim3(taps, S), 256, 0, s>>>(in, cin, gout, cout, taps, ny, nx, nz, vchunk, part, bpart);
+    g_launches += 2;
+    if (err && net_wgrad_tc_fits(cin, cout) && !net_cuda_cores()) {
+        net_conv_wgrad_tc(in, cin, gout, cout, taps, ny, nx, nz, S, vchunk, part, bpart, err, s);
+    } else {
+        ++g_launches;
+        k_conv_wgrad<bf16><<<dim3(taps, S), 256, 0, s>>>(in, cin, gout, cout, taps, ny, nx, nz, vchunk, part, bpart);
+    }
     k_sum_parts<<<nblk(nw), 256, 0, s>>>(part, nw, S, gw);
     k_sum_parts<<<nblk(cout), 256, 0, s>>>(bpart, cout, S, gb);
 }

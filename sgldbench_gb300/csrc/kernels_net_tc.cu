@@ -1,5 +1,5 @@
-// The U-Net's 3x3x3 convolutions (forward and data gradient) on the tensor
-// cores: an implicit GEMM per CTA of 128 output voxels x all output channels,
+// The U-Net's 3x3x3 convolutions (forward, data gradient and weight gradient)
+// on the tensor cores; the forward and data gradient are an implicit GEMM per CTA of 128 output voxels x all output channels,
 // reduced over 27 taps x input channels with tcgen05.mma (BF16 operands, FP32
 // accumulation in tensor memory).  Same operands and epilogues as the
 // CUDA-core convolution k_conv (kernels_net.cu): BF16 activations, FP32
@@ -163,13 +163,158 @@ __global__ void __launch_bounds__(TC_BM) k_conv_tc(const TIn *__restrict__ in, i
     if (warp == 0) tc::tmem_dealloc(taddr, ncols);
 }
 
+// Weight and bias gradients of one convolution on the tensor cores, split over
+// voxel ranges like the FP32-pipe k_conv_wgrad:
+//   part[s][t][ci][co] = sum_{v in range s} in[nb(v,t)][ci] * g[v][co]
+//   bpart[s][co]       = sum_{v in range s} g[v][co]     (centre tap only)
+// as D = A B^T with A = 128 channel rows (ci, zero-padded; for the centre tap
+// row cin holds ones, so that D's row cin is the bias sum) x 128 voxels, B = cout
+// rows x the same voxels, K = the voxels of the CTA's range, 128 per block, all
+// accumulated in one TMEM tile.  Operands are BF16 (g rounded as in k_conv_wgrad).
+template <typename TIn>
+__global__ void __launch_bounds__(TC_BM) k_conv_wgrad_tc(const TIn *__restrict__ in, int cin,
+                                                         const float *__restrict__ g, int cout, int NP, int taps,
+                                                         int ny, int nx, int nz, int64_t vchunk,
+                                                         float *__restrict__ part, float *__restrict__ bpart,
+                                                         int *__restrict__ err) {
+    extern __shared__ __align__(128) unsigned char tsm[];
+    constexpr int KB = TC_BM;                     // voxels per block (the K of 8 MMAs)
+    const int abytes = TC_BM * KB * 2, bbytes = NP * KB * 2;
+    unsigned char *Abuf = tsm, *Bbuf = tsm + 2 * abytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(tsm + 2 * abytes + 2 * bbytes);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int t = blockIdx.x, s = blockIdx.y;
+    const bool centre = taps == 1 || t == 13;
+    const uint32_t ncols = NP <= 32 ? 32u : 64u;
+    // padding rows stay zero: clear both buffers once
+    for (int i = tid; i < (2 * abytes + 2 * bbytes) / 16; i += TC_BM) reinterpret_cast<uint4 *>(tsm)[i] = make_uint4(0, 0, 0, 0);
+    if (warp == 0) {
+        tc::tmem_alloc(tc::saddr(tslot), ncols);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) {
+        tc::mbar_init(tc::saddr(bars), 1);
+        tc::mbar_init(tc::saddr(bars + 1), 1);
+        tc::mbar_init_fence();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t taddr = *tslot;
+    const int64_t V = (int64_t)ny * nx * nz;
+    const int64_t vb = (int64_t)s * vchunk, ve = min(V, vb + vchunk);
+    const int nblk = ve > vb ? (int)((ve - vb + KB - 1) / KB) : 0;
+    const uint32_t idesc = tc::idesc_bf16(TC_BM, NP);
+    const uint32_t lbo = 128, sbo = (KB / 8) * 128;
+    const uint16_t one = __bfloat16_as_ushort(__float2bfloat16_rn(1.f));
+    // 16-byte loads of 8 activation channels / 4 gradient channels where rows allow them
+    const bool vec_in = (cin & 7) == 0 && (reinterpret_cast<uintptr_t>(in) & 15) == 0;
+    const bool vec_g = (cout & 3) == 0 && (reinterpret_cast<uintptr_t>(g) & 15) == 0;
+    bool ok = true;
+    for (int b = 0; b < nblk; ++b) {
+        const int buf = b & 1;
+        if (b >= 2) ok = tc::mbar_wait(tc::saddr(bars + buf), (uint32_t)(((b - 2) >> 1) & 1)) && ok;
+        unsigned char *A = Abuf + buf * abytes, *B = Bbuf + buf * bbytes;
+        const int64_t v = vb + (int64_t)b * KB + tid;   // this thread's voxel = column tid
+        const bool valid = v < ve;
+        int64_t nb = -1;
+        if (valid) {
+            const int y = (int)(v % ny), x = (int)((v / ny) % nx), z = (int)(v / ((int64_t)ny * nx));
+            nb = tc_tap_nb(y, x, z, t, taps, ny, nx, nz);
+        }
+        // column tid of A (channels of the neighbour) and of B (gradient channels)
+        if (vec_in) {
+            for (int c8 = 0; c8 < cin; c8 += 8) {
+                const uint4 q = nb >= 0 ? *reinterpret_cast<const uint4 *>(in + nb * cin + c8) : make_uint4(0, 0, 0, 0);
+                const uint32_t w4[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    *reinterpret_cast<uint16_t *>(A + tc::canon_off(c8 + j, tid, KB)) =
+                        (uint16_t)(w4[j >> 1] >> (16 * (j & 1)));
+            }
+        } else {
+            for (int ci = 0; ci < cin; ++ci)
+                *reinterpret_cast<uint16_t *>(A + tc::canon_off(ci, tid, KB)) =
+                    nb >= 0 ? bf16_bits(in[nb * cin + ci]) : (uint16_t)0;
+        }
+        if (centre) *reinterpret_cast<uint16_t *>(A + tc::canon_off(cin, tid, KB)) = valid ? one : (uint16_t)0;
+        if (vec_g) {
+            for (int c4 = 0; c4 < cout; c4 += 4) {
+                const float4 q = valid ? *reinterpret_cast<const float4 *>(g + v * cout + c4) : make_float4(0, 0, 0, 0);
+                const float f4[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    *reinterpret_cast<uint16_t *>(B + tc::canon_off(c4 + j, tid, KB)) = bf16_bits(f4[j]);
+            }
+        } else {
+            for (int co = 0; co < cout; ++co)
+                *reinterpret_cast<uint16_t *>(B + tc::canon_off(co, tid, KB)) =
+                    valid ? bf16_bits(g[v * cout + co]) : (uint16_t)0;
+        }
+        tc::fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            tc::tc_fence_after();
+            const uint32_t a0 = tc::saddr(A), b0 = tc::saddr(B);
+            for (int kk = 0; kk < KB / 16; ++kk)
+                tc::mma_bf16(taddr, tc::smem_desc(a0 + 256 * kk, lbo, sbo), tc::smem_desc(b0 + 256 * kk, lbo, sbo),
+                             idesc, (b > 0 || kk > 0) ? 1u : 0u);
+            tc::mma_commit(tc::saddr(bars + buf));
+        }
+    }
+    if (nblk > 0) ok = tc::mbar_wait(tc::saddr(bars + ((nblk - 1) & 1)), (uint32_t)(((nblk - 1) >> 1) & 1)) && ok;
+    tc::tc_fence_after();
+    if (__syncthreads_or(!ok)) {
+        if (nblk > 0) tc::mbar_wait(tc::saddr(bars + ((nblk - 1) & 1)), (uint32_t)(((nblk - 1) >> 1) & 1));
+        tc::tc_fence_before();
+        __syncthreads();
+        if (warp == 0) tc::tmem_dealloc(taddr, ncols);
+        if (tid == 0 && err) atomicExch(err, 1);
+        return;
+    }
+    const int row = tid;   // TMEM lane = channel row (warp w holds rows 32w .. 32w+31)
+    float *outw = part + ((int64_t)s * taps + t) * cin * cout;
+    for (int c0 = 0; c0 < NP; c0 += 16) {
+        float r[16];
+        tc::tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int co = c0 + j;
+            if (co >= cout) continue;
+            const float val = nblk > 0 ? r[j] : 0.f;
+            if (row < cin)
+                outw[row * cout + co] = val;
+            else if (centre && row == cin)
+                bpart[(int64_t)s * cout + co] = val;
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(taddr, ncols);
+}
+
 static inline int pad16(int c) { return (c + 15) & ~15; }
 static inline int nblk_tc(int64_t n, int b) { return (int)((n + b - 1) / b); }
 static size_t tc_smem(int KP, int NP) { return 2 * (size_t)TC_BM * KP * 2 + 2 * (size_t)NP * KP * 2 + 32; }
 
 bool net_conv_tc_fits(int cin, int cout) { return cin <= TC_CMAX && cout <= TC_CMAX; }
 
+static size_t tc_wgrad_smem(int NP) { return 2 * (size_t)TC_BM * TC_BM * 2 + 2 * (size_t)NP * TC_BM * 2 + 32; }
+
+bool net_wgrad_tc_fits(int cin, int cout) { return cin < TC_BM && cout <= TC_CMAX; }
+
+void net_conv_wgrad_tc(const bf16 *in, int cin, const float *gout, int cout, int taps, int ny, int nx, int nz, int S,
+                       int64_t vchunk, float *part, float *bpart, int *err, cudaStream_t s) {
+    const int NP = pad16(cout);
+    ++g_launches;
+    k_conv_wgrad_tc<bf16><<<dim3(taps, S), TC_BM, tc_wgrad_smem(NP), s>>>(in, cin, gout, cout, NP, taps, ny, nx, nz,
+                                                                          vchunk, part, bpart, err);
+}
+
 void net_tc_init_attributes() {
+    cudaFuncSetAttribute(k_conv_wgrad_tc<bf16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tc_wgrad_smem(TC_CMAX));
     const int mx = (int)tc_smem(TC_CMAX, TC_CMAX);
     cudaFuncSetAttribute(k_conv_tc<bf16, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_conv_tc<bf16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);

@@ -233,6 +233,10 @@ int net_correction(sgld_cases *cs, sgld_cases_stats *st) {
     double h[2];
     CCK(cudaMemcpyAsync(h, cs->d_sc, sizeof h, cudaMemcpyDeviceToHost, s));
     CCK(cudaStreamSynchronize(s));
+    if (net_take_error(cs->net)) {
+        cs->ready = false;
+        return cfail(ctx, SGLD_ERR_CUDA, "a tensor-core convolution's MMA wait gave up in the network's forward pass");
+    }
     if (!(h[1] > 0.0) || !isfinite(h[0]) || !isfinite(h[1])) return SGLD_OK;
     const double beta = h[0] / h[1];
     int rc;
@@ -295,6 +299,10 @@ int net_train(sgld_cases *cs, int steps, float lr, sgld_cases_stats *st) {
     CCK(cudaGetLastError());
     CCK(cudaMemcpyAsync(&st->net_loss, cs->net.d_loss, sizeof(double), cudaMemcpyDeviceToHost, s));
     CCK(cudaStreamSynchronize(s));
+    if (net_take_error(cs->net)) {
+        cs->ready = false;
+        return cfail(ctx, SGLD_ERR_CUDA, "a tensor-core convolution's MMA wait gave up while training the network");
+    }
     return SGLD_OK;
 }
 

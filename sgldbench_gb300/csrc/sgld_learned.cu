@@ -233,6 +233,10 @@ int learned_before_solve(sgld_ctx *ctx, LearnedWS *w, int mode, double E0, int *
     double q[5] = {0, 0, 0, 0, 0};
     LCK(cudaMemcpyAsync(q, w->d_sc + 2, (net_in ? 5 : 2) * sizeof(double), cudaMemcpyDeviceToHost, s));
     LCK(cudaStreamSynchronize(s));
+    if (net_in && net_take_error(w->net)) {
+        w->ready = false;
+        return lfail(ctx, SGLD_ERR_CUDA, "a tensor-core convolution's MMA wait gave up in the network's forward pass");
+    }
     const double g1 = q[0], h11 = q[1], g2 = q[2], h12 = q[3], h22 = q[4];
     if (!(h11 > 0.0) || !isfinite(g1) || !isfinite(h11)) return SGLD_OK;
     // r'Mr of r0, of the extrapolation alone, and of the subspace step
@@ -304,6 +308,10 @@ int learned_after_solve(sgld_ctx *ctx, LearnedWS *w, int mode, int steps, float 
     LCK(cudaGetLastError());
     LCK(cudaMemcpyAsync(loss, w->net.d_loss, sizeof(double), cudaMemcpyDeviceToHost, s));
     LCK(cudaStreamSynchronize(s));
+    if (net_take_error(w->net)) {
+        w->ready = false;
+        return lfail(ctx, SGLD_ERR_CUDA, "a tensor-core convolution's MMA wait gave up while training the network");
+    }
     return SGLD_OK;
 }
 

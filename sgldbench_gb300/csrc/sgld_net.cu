@@ -50,7 +50,8 @@ void conv_fwd(Net &n, int k, const bf16 *in, void *out, bool relu) {
 void conv_wgrad(Net &n, int k, const bf16 *in, const float *gout) {
     const NetConv &c = n.conv[k];
     const int *d = dim3_of(n, c.level);
-    net_conv_wgrad(in, c.cin, gout, c.cout, c.taps, d[0], d[1], d[2], n.wpart, n.g + c.w, n.g + c.b, n.s);
+    net_conv_wgrad(in, c.cin, gout, c.cout, c.taps, d[0], d[1], d[2], n.wpart, n.g + c.w, n.g + c.b, n.tc_err,
+                   n.s);
 }
 
 // gradient of convolution k's input: gin (=/+=) mask(conv^T(gout))
@@ -248,6 +249,14 @@ void net_adam_step(Net &n, float lr) {
     net_adam(n.w, n.m, n.v, n.g, n.wb, n.nparam, lr, b1, b2, eps, c1, c2, n.s);
 }
 
+bool net_take_error(Net &n) {
+    int h = 0;
+    if (cudaMemcpyAsync(&h, n.tc_err, sizeof h, cudaMemcpyDeviceToHost, n.s) != cudaSuccess) return true;
+    if (cudaStreamSynchronize(n.s) != cudaSuccess) return true;
+    if (h && cudaMemsetAsync(n.tc_err, 0, sizeof(int), n.s) != cudaSuccess) return true;
+    return h != 0;
+}
+
 }  // namespace sgld
 
 // ---- C ABI ------------------------------------------------------------------
@@ -380,6 +389,7 @@ int sgld_net_forward(sgld_net *h, const float *x, float *y) {
     NCK(cudaGetLastError());
     NCK(cudaMemcpyAsync(y, n.Y, sizeof(float) * n.V[0] * n.cout, cudaMemcpyDeviceToHost, n.s));
     NCK(cudaStreamSynchronize(n.s));
+    if (net_take_error(n)) return nfail(h, SGLD_ERR_CUDA, "a tensor-core convolution's MMA wait gave up");
     return SGLD_OK;
 }
 
@@ -397,6 +407,7 @@ int sgld_net_grad(sgld_net *h, const float *x, const float *target, const float 
     if (loss) NCK(cudaMemcpyAsync(loss, n.d_loss, sizeof(double), cudaMemcpyDeviceToHost, n.s));
     if (grad) NCK(cudaMemcpyAsync(grad, n.g, sizeof(float) * n.nparam, cudaMemcpyDeviceToHost, n.s));
     NCK(cudaStreamSynchronize(n.s));
+    if (net_take_error(n)) return nfail(h, SGLD_ERR_CUDA, "a tensor-core convolution's MMA wait gave up");
     return SGLD_OK;
 }
 
@@ -415,6 +426,7 @@ int sgld_net_train_step(sgld_net *h, const float *x, const float *target, const 
     NCK(cudaGetLastError());
     if (loss) NCK(cudaMemcpyAsync(loss, n.d_loss, sizeof(double), cudaMemcpyDeviceToHost, n.s));
     NCK(cudaStreamSynchronize(n.s));
+    if (net_take_error(n)) return nfail(h, SGLD_ERR_CUDA, "a tensor-core convolution's MMA wait gave up");
     return SGLD_OK;
 }
 

@@ -64,6 +64,9 @@ void net_forward(Net &n);                                        // n.X.a -> n.Y
 void net_loss(Net &n, const float *T, const float *M);           // n.Y -> n.gY, *n.d_loss
 void net_backward(Net &n);                                       // n.gY -> n.g
 void net_adam_step(Net &n, float lr);                            // n.g -> n.w, n.wb
+// after the work queued on n.s: true when a tensor-core convolution's bounded
+// MMA wait gave up (its output is then invalid); clears the flag
+bool net_take_error(Net &n);
 
 // kernels_net.cu
 void net_init_attributes();
@@ -73,8 +76,11 @@ void net_conv_fwd(const bf16 *in, int cin, const bf16 *w, const float *b, int co
                   bool relu_bf16_out, void *out, bf16 *wimg, int *err, cudaStream_t s);
 void net_conv_bwd_data(const float *gout, int cout, const bf16 *w, bf16 *wt, int cin, int taps, int ny, int nx,
                        int nz, const bf16 *mask, float *gin, bool accumulate, bf16 *wimg, int *err, cudaStream_t s);
-// kernels_net_tc.cu: the same two convolutions on the tensor cores (tcgen05)
+// kernels_net_tc.cu: the same convolutions on the tensor cores (tcgen05)
 bool net_conv_tc_fits(int cin, int cout);
+bool net_wgrad_tc_fits(int cin, int cout);
+void net_conv_wgrad_tc(const bf16 *in, int cin, const float *gout, int cout, int taps, int ny, int nx, int nz, int S,
+                       int64_t vchunk, float *part, float *bpart, int *err, cudaStream_t s);
 void net_tc_init_attributes();
 void net_conv_fwd_tc(const bf16 *in, int cin, const bf16 *w, const float *b, int cout, int taps, int ny, int nx,
                      int nz, bool relu_bf16_out, void *out, bf16 *wimg, int *err, cudaStream_t s);
@@ -82,7 +88,7 @@ void net_conv_bwd_data_tc(const float *gout, int cout, const bf16 *wt, int cin, 
                           const bf16 *mask, float *gin, bool accumulate, bf16 *wimg, int *err, cudaStream_t s);
 int net_wgrad_splits(int64_t V);
 void net_conv_wgrad(const bf16 *in, int cin, const float *gout, int cout, int taps, int ny, int nx, int nz,
-                    float *part, float *gw, float *gb, cudaStream_t s);
+                    float *part, float *gw, float *gb, int *err, cudaStream_t s);
 void net_pool(const bf16 *f, int C, const int fd[3], const int cd[3], bf16 *c, cudaStream_t s);
 void net_pool_bwd(const float *gc, int C, const int fd[3], const int cd[3], const bf16 *maskf, float *gf,
                   bool accumulate, cudaStream_t s);

@@ -8,8 +8,10 @@ test calls it through the C ABI twice in a row (the shared scratch keeps the
 previous call's contents) and checks y and u.y against the existing entry
 point sgld_kbyu, with the tolerance of the other K*u parity tests (1e-13
 relative for y, 1e-12 for the dot product), and that it refuses to run while
-the device holds another context's element matrix.  It is collected last so that a
-run that stops at the first failure has run every other test first.
+the device holds another context's element matrix; that an eager call leaves
+the device's free memory unchanged; and that the call captured into a CUDA
+graph and replayed with new inputs meets the same references.  It is collected
+last so that a run that stops at the first failure has run every other test first.
 """
 import ctypes
 
@@ -83,4 +85,32 @@ def test_kbyu_dot_noalloc_matches_kbyu(built_lib):
     torch.cuda.synchronize()
     assert _rel(y_full[idx].cpu().numpy(), y_ref) <= 1e-13
     other.close()
+
+    # the eager call takes no device memory; then the use the entry point
+    # exists for: the call captured into a CUDA graph and replayed with new
+    # inputs (graph instantiation itself may take memory, so that is not checked)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(dev)[0]
+    assert call() == _lib.SGLD_OK
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(dev)[0] == free0
+    side = torch.cuda.Stream(dev)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side):
+        rc = lib.sgld_kbyu_dot_noalloc(s.ctx, ctypes.c_void_p(u_full.data_ptr()), ctypes.c_void_p(y_full.data_ptr()),
+                                       ctypes.c_void_p(dot.data_ptr()), ctypes.c_void_p(side.cuda_stream))
+    assert rc == _lib.SGLD_OK, lib.sgld_last_error(s.ctx)
+    for _ in range(2):
+        u = rng.standard_normal(s.numDOFs)
+        y_ref = s.Solving_KbyU_MatrixFree(u)
+        u_full[idx] = torch.from_numpy(u).to(dev)
+        y_full.fill_(float("nan"))
+        dot.fill_(float("nan"))
+        torch.cuda.synchronize()
+        graph.replay()
+        torch.cuda.synchronize()
+        assert _rel(y_full[idx].cpu().numpy(), y_ref) <= 1e-13
+        d_ref = float(u @ y_ref)
+        assert abs(dot.item() - d_ref) <= 1e-12 * abs(d_ref)
+    del graph
     s.close()

@@ -24,13 +24,58 @@ namespace sgld {
 
 __constant__ double c_Kh[KH_NNZ];
 __constant__ float c_Kh32[KH_NNZ];
+// the 8-value form of an element matrix with cubic symmetry (kh_cubic):
+// A-B, B, C, D, E, F-G, G, H (KH_CLASS below)
+__constant__ float c_Kc32[8];
 __constant__ double c_M[48 * 24];   // stress: corner stresses = M * u_e (reference corner order)
+
+// Under the symmetries of the cube (axis permutations and reflections) an
+// isotropic hexahedron's Hadamard-basis blocks take 8 values:
+//   {3, 7, 14} and {11, 16, 18}: A / F on the diagonal, B / G off it;
+//   {4, 6}, {5, 12}, {8, 13}: C in every entry;
+//   {9, 20}, {10, 17}, {15, 19}: D on the diagonal, E off it;
+//   21, 22, 23: H.
+// KH_CLASS gives each of the 45 stored values its letter (A = 0 .. H = 7).
+constexpr int KH_CLASS[KH_NNZ] = {0, 1, 1, 1, 0, 1, 1, 1, 0,   // {3, 7, 14}
+                                  2, 2, 2, 2,                  // {4, 6}
+                                  2, 2, 2, 2,                  // {5, 12}
+                                  2, 2, 2, 2,                  // {8, 13}
+                                  3, 4, 4, 3,                  // {9, 20}
+                                  3, 4, 4, 3,                  // {10, 17}
+                                  5, 6, 6, 6, 5, 6, 6, 6, 5,   // {11, 16, 18}
+                                  3, 4, 4, 3,                  // {15, 19}
+                                  7, 7, 7};                    // 21, 22, 23
+
+bool kh_cubic(const double *Kh) {
+    double rep[8], mx = 0.0;
+    for (int i = KH_NNZ - 1; i >= 0; --i) {
+        rep[KH_CLASS[i]] = Kh[i];   // ends with each letter's first entry
+        mx = fmax(mx, fabs(Kh[i]));
+    }
+    for (int i = 0; i < KH_NNZ; ++i)
+        if (fabs(Kh[i] - rep[KH_CLASS[i]]) > 1e-12 * mx) return false;
+    return true;
+}
 
 void upload_kh(const double *Kh, cudaStream_t s) {
     float f[KH_NNZ];
     for (int i = 0; i < KH_NNZ; ++i) f[i] = (float)Kh[i];
     cudaMemcpyToSymbolAsync(c_Kh, Kh, sizeof(double) * KH_NNZ, 0, cudaMemcpyHostToDevice, s);
     cudaMemcpyToSymbolAsync(c_Kh32, f, sizeof(float) * KH_NNZ, 0, cudaMemcpyHostToDevice, s);
+    // A-B, B, C, D, E, F-G, G, H from the letters' first entries (zeros when not cubic;
+    // the 8-value kernels then never run)
+    float kc[8] = {};
+    if (kh_cubic(Kh)) {
+        kc[0] = (float)(Kh[0] - Kh[1]);
+        kc[1] = (float)Kh[1];
+        kc[2] = (float)Kh[9];
+        kc[3] = (float)Kh[21];
+        kc[4] = (float)Kh[22];
+        kc[5] = (float)(Kh[29] - Kh[30]);
+        kc[6] = (float)Kh[30];
+        kc[7] = (float)Kh[42];
+    }
+    cudaMemcpyToSymbolAsync(c_Kc32, kc, sizeof kc, 0, cudaMemcpyHostToDevice, s);
     cudaStreamSynchronize(s);
 }
 
@@ -458,7 +503,47 @@ __device__ __forceinline__ void kh_apply_x2(const float2 (&u)[24], float2 (&g)[2
 #undef X2
 }
 
-template <int TX, bool DOT>
+// the same product for an element matrix with cubic symmetry, from its 8 values
+// k = (A-B, B, C, D, E, F-G, G, H): a 3-block [[A,B,B],[B,A,B],[B,B,A]] is
+// (A-B) u_i + B (u_i + u_j + u_k), a C-block maps both entries to C (u_i + u_j);
+// 33 paired operations instead of 49, on 8 constants the thread keeps in registers
+__device__ __forceinline__ void kh_apply_cubic_x2(const float2 (&u)[24], float2 (&g)[24], const float2 (&k)[8]) {
+    g[0] = g[1] = g[2] = make_float2(0.f, 0.f);
+#define Y3(i, j, l, a, b)                                           \
+    {                                                               \
+        const float2 t = f2mul(k[b], f2add(f2add(u[i], u[j]), u[l])); \
+        g[i] = f2fma(k[a], u[i], t);                                \
+        g[j] = f2fma(k[a], u[j], t);                                \
+        g[l] = f2fma(k[a], u[l], t);                                \
+    }
+#define YC(i, j)                                   \
+    {                                              \
+        const float2 t = f2mul(k[2], f2add(u[i], u[j])); \
+        g[i] = t;                                  \
+        g[j] = t;                                  \
+    }
+#define YD(i, j)                                        \
+    {                                                   \
+        g[i] = f2fma(k[4], u[j], f2mul(k[3], u[i]));    \
+        g[j] = f2fma(k[4], u[i], f2mul(k[3], u[j]));    \
+    }
+    Y3(3, 7, 14, 0, 1)
+    YC(4, 6)
+    YC(5, 12)
+    YC(8, 13)
+    YD(9, 20)
+    YD(10, 17)
+    Y3(11, 16, 18, 5, 6)
+    YD(15, 19)
+    g[21] = f2mul(k[7], u[21]);
+    g[22] = f2mul(k[7], u[22]);
+    g[23] = f2mul(k[7], u[23]);
+#undef Y3
+#undef YC
+#undef YD
+}
+
+template <int TX, bool DOT, bool CUBIC>
 __global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
     k_kbyu_tma(const __grid_constant__ CUtensorMap umap, float *__restrict__ y, const float *__restrict__ E,
                const uint8_t *__restrict__ nflag, int ny, int nx, int nz, int zc, double *__restrict__ partial,
@@ -578,6 +663,9 @@ __global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
             un[c] = v[1][1][c];
         }
     };
+    float2 kc[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) kc[i] = CUBIC ? make_float2(c_Kc32[i], c_Kc32[i]) : make_float2(0.f, 0.f);
     float2 Fp[12], carry[12], uo[3];
     faces(0, Fp, uo);   // a wait that gave up here is acted on after step 0's barrier
 #pragma unroll
@@ -617,7 +705,10 @@ __global__ void __launch_bounds__(KT_Y * TX, TX == 8 ? 2 : 1)
             Fp[i] = Ft[i];
         }
         float2 g[24];
-        kh_apply_x2(h, g);
+        if constexpr (CUBIC)
+            kh_apply_cubic_x2(h, g, kc);
+        else
+            kh_apply_x2(h, g);
         // E scale, z butterfly undone: the face below gets (a - d), the face above (a + d);
         // the face below also takes the carried contribution of the element layer under it
         float2 Lm[6], Rp[6];
@@ -717,15 +808,25 @@ static constexpr size_t kbyu_smem() {
     return sizeof(T) * (3 * KT_NL * 3 + 24 * KT_THREADS);
 }
 
+template <int TX, bool DOT, bool CUBIC>
+static void tma_attributes() {
+    cudaFuncSetAttribute(k_kbyu_tma<TX, DOT, CUBIC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)TkTile<TX>::SMEM);
+}
+
 // opt-in shared memory sizes; called once per context before any launch or
 // graph capture
 void init_kernel_attributes() {
     cudaFuncSetAttribute(k_kbyu<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<double>());
     cudaFuncSetAttribute(k_kbyu<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kbyu_smem<double>());
-    cudaFuncSetAttribute(k_kbyu_tma<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TkTile<8>::SMEM);
-    cudaFuncSetAttribute(k_kbyu_tma<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TkTile<8>::SMEM);
-    cudaFuncSetAttribute(k_kbyu_tma<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TkTile<16>::SMEM);
-    cudaFuncSetAttribute(k_kbyu_tma<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TkTile<16>::SMEM);
+    tma_attributes<8, true, false>();
+    tma_attributes<8, false, false>();
+    tma_attributes<16, true, false>();
+    tma_attributes<16, false, false>();
+    tma_attributes<8, true, true>();
+    tma_attributes<8, false, true>();
+    tma_attributes<16, true, true>();
+    tma_attributes<16, false, true>();
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
@@ -775,6 +876,14 @@ void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *
         kbyu_launch<double, false>(l0, E, u, y, nullptr, nblocks_out, s);
 }
 
+template <int TX, bool DOT, bool CUBIC>
+static void tma_launch(dim3 g, const CUtensorMap &m, float *y, const float *E, const Level &l0, int zc,
+                       double *partial_dot, const uint8_t *tiles, cudaStream_t s) {
+    using G = TkTile<TX>;
+    k_kbyu_tma<TX, DOT, CUBIC><<<g, G::THREADS, G::SMEM, s>>>(m, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, partial_dot,
+                                                              tiles, l0.kerr);
+}
+
 int launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, double *partial_dot,
                     int *nblocks_out, cudaStream_t s) {
     const dim3 g = kbyu_f32_grid(l0);
@@ -788,22 +897,21 @@ int launch_kbyu_f32(const Level &l0, const float *E, const float *u, float *y, d
     CUtensorMap m;
     if (vector_tensor_map(&m, u, 3 * l0.nnode)) return (int)cudaErrorInvalidValue;
     ++g_launches;
+    const bool cubic = l0.kh_cubic;
     if (tx == 8) {
-        using G = TkTile<8>;
         if (partial_dot)
-            k_kbyu_tma<8, true><<<g, G::THREADS, G::SMEM, s>>>(m, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, partial_dot,
-                                                              tiles, l0.kerr);
+            cubic ? tma_launch<8, true, true>(g, m, y, E, l0, zc, partial_dot, tiles, s)
+                  : tma_launch<8, true, false>(g, m, y, E, l0, zc, partial_dot, tiles, s);
         else
-            k_kbyu_tma<8, false><<<g, G::THREADS, G::SMEM, s>>>(m, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr,
-                                                               tiles, l0.kerr);
+            cubic ? tma_launch<8, false, true>(g, m, y, E, l0, zc, nullptr, tiles, s)
+                  : tma_launch<8, false, false>(g, m, y, E, l0, zc, nullptr, tiles, s);
     } else {
-        using G = TkTile<16>;
         if (partial_dot)
-            k_kbyu_tma<16, true><<<g, G::THREADS, G::SMEM, s>>>(m, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc,
-                                                               partial_dot, tiles, l0.kerr);
+            cubic ? tma_launch<16, true, true>(g, m, y, E, l0, zc, partial_dot, tiles, s)
+                  : tma_launch<16, true, false>(g, m, y, E, l0, zc, partial_dot, tiles, s);
         else
-            k_kbyu_tma<16, false><<<g, G::THREADS, G::SMEM, s>>>(m, y, E, l0.nflag, l0.ny, l0.nx, l0.nz, zc, nullptr,
-                                                                tiles, l0.kerr);
+            cubic ? tma_launch<16, false, true>(g, m, y, E, l0, zc, nullptr, tiles, s)
+                  : tma_launch<16, false, false>(g, m, y, E, l0, zc, nullptr, tiles, s);
     }
     return 0;
 }

@@ -708,11 +708,22 @@ bool g_kh_stale[kMaxDevices] = {};      // upload again even if the record match
 double g_kh_held[kMaxDevices][KH_NNZ];   // the element matrix in each device's constants
 }  // namespace
 
+// the FP32 K*u's 45-value form even for a cubic element matrix (environment
+// SGLD_KH_GENERAL=1, read once; for comparisons)
+static bool kh_general_forced() {
+    static const bool v = [] {
+        const char *e = getenv("SGLD_KH_GENERAL");
+        return e && e[0] == '1';
+    }();
+    return v;
+}
+
 int bind_ctx(sgld_ctx *ctx) {
     Ctx &c = ctx->c;
     int dev = -1;
     CK(cudaGetDevice(&dev));
     if (dev != c.device) CK(cudaSetDevice(c.device));
+    if (!c.lv.empty()) c.lv[0].kh_cubic = !kh_general_forced() && kh_cubic(c.Kh);
     std::lock_guard<std::mutex> lock(g_bind_mu);
     const bool same = g_kh_valid[c.device] && memcmp(g_kh_held[c.device], c.Kh, sizeof c.Kh) == 0;
     if (same && !g_kh_stale[c.device]) return SGLD_OK;

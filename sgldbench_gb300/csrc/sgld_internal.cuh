@@ -43,6 +43,8 @@ struct Level {
     int kx_zc = 0;                // node layers per z stream of the FP32 K*u, two streams per CTA
                                   // (0 = default rule; set by the tuner)
     int kx_tx = 0;                // x width of the FP32 K*u tile, 8 or 16 (0 = 8; set by the tuner)
+    bool kh_cubic = false;        // finest level: the bound element matrix has the hexahedron's
+                                  // cubic symmetry (kh_cubic), so the FP32 K*u takes its 8-value form
     int64_t nel = 0, nnode = 0;   // full-grid counts
     int64_t nel_active = 0, nnode_active = 0;
     uint8_t *eact = nullptr;      // [nel] element non-empty
@@ -179,6 +181,9 @@ extern thread_local int64_t g_launches;
 
 // ---- launchers (kernels_*.cu) ------------------------------------------------
 void upload_kh(const double *Kh, cudaStream_t s);
+// true when the 45 Hadamard-basis values take the 8 distinct values that the cubic
+// symmetry of an isotropic hexahedral element gives them (to 1e-12 of the largest)
+bool kh_cubic(const double *Kh);
 void launch_kbyu_f64(const Level &l0, const double *E, const double *u, double *y, double *partial_dot,
                      int *nblocks_out, cudaStream_t s);
 // (re)makes l0's active-tile maps for its current FP32 tile; 0 or a CUDA error

@@ -4,6 +4,7 @@ compiled MEX kernels by the CPU tests).
 
 Tolerances (relative, max-norm unless stated):
   K*u, restriction, interpolation, Jacobi diagonals   1e-13
+  FP32 K*u of the mixed solve's inner loop              1e-5
   Galerkin element matrices Ks                          1e-12
   V-cycle (coarsest solve through an explicit inverse)  1e-9
   PCG: iteration count equal to the oracle's (+-1); displacement relative L2
@@ -74,6 +75,62 @@ def test_kbyu(pair):
     m, s = pair
     u = np.random.default_rng(1).standard_normal(m.levels[0].numDOFs)
     assert _rel(s.Solving_KbyU_MatrixFree(u), G.kbyu(m, u)) <= 1e-13
+
+
+def test_kbyu_fp32(pair):
+    """The FP32 K*u of the inner solve (its 8-value form: the reference's
+    isotropic element matrix has the cube's symmetry): FP32 u, moduli and sums,
+    so 1e-5."""
+    m, s = pair
+    u = np.random.default_rng(11).standard_normal(m.levels[0].numDOFs)
+    assert _rel(s.Solving_KbyU_MatrixFree(u, "mixed"), G.kbyu(m, u)) <= 1e-5
+
+
+def _hadamard_to_ke(Ke, scale_blocks):
+    """Ke with some of its Hadamard-basis blocks scaled: the transform of
+    sgld_set_ke's check (corner order k = ks | kt<<1 | kp<<2, H the 8-point
+    Hadamard matrix), applied, scaled blockwise and undone.  Scaling a whole
+    diagonal block keeps the block pattern and the symmetry but, for unequal
+    factors, breaks the cube's symmetry."""
+    kmap = [0, 1, 3, 2, 4, 5, 7, 6]
+    P = np.zeros((24, 24))
+    for j in range(8):
+        for c in range(3):
+            P[3 * kmap[j] + c, 3 * j + c] = 1.0
+    H = np.array([[np.prod([(1.0 if (k >> a) & 1 else -1.0) if (mm >> a) & 1 else 1.0 for a in range(3)])
+                   for k in range(8)] for mm in range(8)])
+    HH = np.kron(H, np.eye(3))
+    Kh = HH @ (P @ Ke @ P.T) @ HH.T / 64.0
+    for idx, f in scale_blocks:
+        ix = np.ix_(idx, idx)
+        Kh[ix] *= f
+    return P.T @ (HH.T @ Kh @ HH) @ P
+
+
+def test_kbyu_fp32_general_element_matrix(built_lib):
+    """An element matrix with the Hadamard block pattern but without the
+    cube's symmetry takes the FP32 K*u's 45-value form; both forms against the
+    oracle with that matrix."""
+    from oracle import kernels as OK
+
+    rng = np.random.default_rng(12)
+    vox = rng.random((12, 20, 10)) < 0.8
+    m, s = make_pair(vox, non_dyadic=0, seed=6)
+    l1 = m.levels[0]
+    Ke2 = _hadamard_to_ke(m.Ke, [([9, 20], 1.2), ([11, 16, 18], 0.9)])
+    assert np.allclose(Ke2, Ke2.T) and not np.allclose(Ke2, m.Ke)
+    u = rng.standard_normal(l1.numDOFs)
+    y_iso = G.kbyu(m, u)
+    assert _rel(s.Solving_KbyU_MatrixFree(u, "mixed"), y_iso) <= 1e-5
+    s.set_ke(Ke2)
+    y2 = OK.kbyu(u, l1.eNodMat, Ke2, l1.eleModulus, l1.colors)
+    y2[l1.fixedDOFs] = 0.0
+    assert _rel(y2, y_iso) > 1e-3
+    assert _rel(s.Solving_KbyU_MatrixFree(u, "mixed"), y2) <= 1e-5
+    assert _rel(s.Solving_KbyU_MatrixFree(u), y2) <= 1e-13
+    s.set_ke(m.Ke)
+    assert _rel(s.Solving_KbyU_MatrixFree(u, "mixed"), y_iso) <= 1e-5
+    s.close()
 
 
 def test_restrict_interpolate(pair):

@@ -257,6 +257,10 @@ int sgld_vcycle(sgld_ctx *ctx, const double *r, double *z);
  * V-cycle.  Inputs and outputs stay FP64 compact vectors. */
 int sgld_kbyu_prec(sgld_ctx *ctx, const double *u, double *y, int precision);
 int sgld_vcycle_prec(sgld_ctx *ctx, const double *r, double *z, int precision);
+/* The restriction the FP32 V-cycle applies (SGLD_PREC_MIXED / _MIXED_DF: FP32
+ * copy of r_fine, FP32 sums) or sgld_restrict (SGLD_PREC_FP64); level index ii
+ * as sgld_restrict. */
+int sgld_restrict_prec(sgld_ctx *ctx, int ii, const double *r_fine, double *r_coarse, int precision);
 
 /* Solving_PreconditionedConjugateGradientSolver.m:1-37 with AtX = KbyU and
  * PtV = Vcycle (as Solving_CG_GMGS.m:7 binds them).  x: in = initial guess when

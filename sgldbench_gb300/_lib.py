@@ -91,6 +91,7 @@ SIGNATURES = {
     "sgld_build_hierarchy": (i32, [vp, i32, i32]),
     "sgld_kbyu_device": (i32, [vp, vp, vp]),
     "sgld_restrict": (i32, [vp, i32, vp, vp]),
+    "sgld_restrict_prec": (i32, [vp, i32, vp, vp, i32]),
     "sgld_interpolate": (i32, [vp, i32, vp, vp]),
     "sgld_vcycle": (i32, [vp, vp, vp]),
     "sgld_pcg": (i32, [vp, vp, vp, vp, vp]),

@@ -64,15 +64,19 @@ __global__ void k_restrict(const T *__restrict__ rf, T *__restrict__ rc, int nyc
 // A coarse node outside the active domain (cflag) gets 0 without reading the
 // fine grid: all 8 coarse elements around it are empty, so every fine node
 // strictly inside their union -- the tent's support -- is inactive and holds 0.
+// With keep_zeros (the FP32 V-cycle, whose coarse vectors are zeroed when
+// allocated) an inactive coarse node is not written at all: it holds 0 already.
 template <typename T, int S>
 __global__ void __launch_bounds__(128) k_restrict_s(const T *__restrict__ rf, T *__restrict__ rc,
-                                                    const uint8_t *__restrict__ cflag, int nyc, int nxc, int nzc) {
+                                                    const uint8_t *__restrict__ cflag, int nyc, int nxc, int nzc,
+                                                    int keep_zeros) {
     const int NYc = nyc + 1, NXc = nxc + 1;
     const int NYf = S * nyc + 1, NXf = S * nxc + 1, NZf = S * nzc + 1;
     const int pl = blockIdx.x * blockDim.x + threadIdx.x;
     if (pl >= NYc * NXc) return;
     const int I = pl % NYc, J = pl / NYc, Kz = blockIdx.y;
     if (!(cflag[pl + NYc * NXc * Kz] & NF_ACTIVE)) {
+        if (keep_zeros) return;
         const int n = 3 * (pl + NYc * NXc * Kz);
         rc[n] = rc[n + 1] = rc[n + 2] = T(0);
         return;
@@ -113,10 +117,13 @@ void launch_restrict(const Level &fine, const Level &coarse, const T *rf, T *rc,
     ++g_launches;
     const dim3 g((unsigned)(((coarse.ny + 1) * (coarse.nx + 1) + 127) / 128), (unsigned)(coarse.nz + 1));
     const bool small = 3 * (int64_t)fine.nnode < (int64_t)INT32_MAX;
+    // FP32: the coarse vectors (the levels' r32) are zeroed at allocation and keep zeros at
+    // inactive nodes
+    const int keep = sizeof(T) == sizeof(float) && static_cast<const void *>(rc) == coarse.r32;
     if (small && coarse.span == 2)
-        k_restrict_s<T, 2><<<g, 128, 0, st>>>(rf, rc, coarse.nflag, coarse.ny, coarse.nx, coarse.nz);
+        k_restrict_s<T, 2><<<g, 128, 0, st>>>(rf, rc, coarse.nflag, coarse.ny, coarse.nx, coarse.nz, keep);
     else if (small && coarse.span == 4)
-        k_restrict_s<T, 4><<<g, 128, 0, st>>>(rf, rc, coarse.nflag, coarse.ny, coarse.nx, coarse.nz);
+        k_restrict_s<T, 4><<<g, 128, 0, st>>>(rf, rc, coarse.nflag, coarse.ny, coarse.nx, coarse.nz, keep);
     else
         k_restrict<T><<<g, 128, 0, st>>>(rf, rc, coarse.ny, coarse.nx, coarse.nz, coarse.span);
 }
@@ -286,12 +293,14 @@ __global__ void __launch_bounds__(128) k_prolong_cells(const T *__restrict__ xc,
                     const int f = rowbase + ry;
                     const uint8_t fl = nflag[f];
                     const bool act = (fl & NF_ACTIVE) != 0;
-                    // loads as selects (predicated, issued together) rather than under a branch
+                    // r and D are loaded whatever the flag says, so that these loads do not
+                    // wait for the flag load (one round trip per fine node, not two); what
+                    // an inactive node holds is discarded by the selects below
                     T r[3], dg[3], o[3];
 #pragma unroll
                     for (int q = 0; q < 3; ++q) {
-                        r[q] = act ? rf[3 * f + q] : T(0);
-                        dg[q] = act ? D[3 * f + q] : T(0);
+                        r[q] = rf[3 * f + q];
+                        dg[q] = D[3 * f + q];
                     }
 #pragma unroll
                     for (int q = 0; q < 3; ++q) {
@@ -302,7 +311,7 @@ __global__ void __launch_bounds__(128) k_prolong_cells(const T *__restrict__ xc,
 #pragma unroll
                         for (int q = 0; q < 3; ++q)
                             if (fl & (NF_FIXX << q)) o[q] = T(0);
-                        dot += o[0] * r[0] + o[1] * r[1] + o[2] * r[2];
+                        if (act) dot += o[0] * r[0] + o[1] * r[1] + o[2] * r[2];
                     }
                     // inactive nodes of an output that keeps zeros there (cflag set) are not rewritten
                     if (act || !cflag) {

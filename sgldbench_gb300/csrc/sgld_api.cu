@@ -889,8 +889,10 @@ int sgld_create(int resY, int resX, int resZ, const uint8_t *solid, const sgld_o
             CK(dalloc(&lv.x, 3 * lv.nnode));
             CK(dalloc(&lv.r32, 3 * lv.nnode));
             CK(dalloc(&lv.x32, 3 * lv.nnode));
-            // the FP32 prolongation skips empty cells and relies on zeros at inactive nodes
+            // the FP32 prolongation skips empty cells and the FP32 restriction inactive
+            // nodes: both rely on zeros at inactive nodes
             CK(cudaMemset(lv.x32, 0, sizeof(float) * 3 * lv.nnode));
+            CK(cudaMemset(lv.r32, 0, sizeof(float) * 3 * lv.nnode));
         }
     }
     if (c.lv[0].nel_active == 0) return fail(ctx, SGLD_ERR_ARG, "the voxel grid has no solid voxel");
@@ -1366,6 +1368,29 @@ int sgld_restrict(sgld_ctx *ctx, int ii, const double *rf, double *rc_out) {
     double *fin = (l - 1 == 0) ? c.d_r : c.lv[l - 1].x;
     if ((rc = level_vec_to_dev(ctx, l - 1, rf, fin))) return rc;
     launch_restrict<double>(c.lv[l - 1], c.lv[l], fin, c.lv[l].r, c.stream);
+    CKL();
+    return level_vec_to_host(ctx, l, c.lv[l].r, rc_out);
+}
+
+int sgld_restrict_prec(sgld_ctx *ctx, int ii, const double *rf, double *rc_out, int precision) {
+    if (precision == SGLD_PREC_FP64) return sgld_restrict(ctx, ii, rf, rc_out);
+    if (precision != SGLD_PREC_MIXED && precision != SGLD_PREC_MIXED_DF) {
+        if (ctx) ctx->c.err = "unknown precision mode";
+        return SGLD_ERR_ARG;
+    }
+    if (!ctx || !rf || !rc_out || ii < 2 || ii > ctx->c.L) return SGLD_ERR_ARG;
+    if (int rc = bind_ctx(ctx)) return rc;
+    Ctx &c = ctx->c;
+    const int l = ii - 1;
+    int rc;
+    // the fine vector in FP64 (zeros at inactive nodes), narrowed into the FP32 vector the
+    // V-cycle restricts from at that level
+    double *fin = (l - 1 == 0) ? c.d_r : c.lv[l - 1].x;
+    if ((rc = level_vec_to_dev(ctx, l - 1, rf, fin))) return rc;
+    float *fin32 = (l - 1 == 0) ? c.d_r32 : c.lv[l - 1].r32;
+    launch_narrow(fin, fin32, 3 * c.lv[l - 1].nnode, c.stream);
+    launch_restrict<float>(c.lv[l - 1], c.lv[l], fin32, c.lv[l].r32, c.stream);
+    launch_widen(c.lv[l].r32, c.lv[l].r, 3 * c.lv[l].nnode, c.stream);
     CKL();
     return level_vec_to_host(ctx, l, c.lv[l].r, rc_out);
 }

@@ -226,10 +226,15 @@ class VoxelSolver:
         self._check(self.lib.sgld_kbyu_df(self.ctx, _p(u), _p(y)))
         return y
 
-    def Solving_RestrictResidual(self, rFiner, ii: int) -> np.ndarray:
+    def Solving_RestrictResidual(self, rFiner, ii: int, precision: str = "fp64") -> np.ndarray:
+        """R r; ``precision`` 'mixed' / 'mixed_df' applies the FP32 restriction
+        of the inner solve's V-cycle (sgld_restrict_prec)."""
         r = self._vec(rFiner, self.levels[ii - 2]["numDOFs"])
         out = np.zeros(self.levels[ii - 1]["numDOFs"])
-        self._check(self.lib.sgld_restrict(self.ctx, ii, _p(r), _p(out)))
+        if precision == "fp64":
+            self._check(self.lib.sgld_restrict(self.ctx, ii, _p(r), _p(out)))
+        else:
+            self._check(self.lib.sgld_restrict_prec(self.ctx, ii, _p(r), _p(out), _precision(precision)))
         return out
 
     def Solving_InterpolationDeviation(self, xCoarser, ii: int) -> np.ndarray:

@@ -5,6 +5,7 @@ compiled MEX kernels by the CPU tests).
 Tolerances (relative, max-norm unless stated):
   K*u, restriction, interpolation, Jacobi diagonals   1e-13
   FP32 K*u of the mixed solve's inner loop              1e-5
+  FP32 restriction of the inner V-cycle                 1e-6
   Galerkin element matrices Ks                          1e-12
   V-cycle (coarsest solve through an explicit inverse)  1e-9
   PCG: iteration count equal to the oracle's (+-1); displacement relative L2
@@ -141,6 +142,16 @@ def test_restrict_interpolate(pair):
         assert _rel(s.Solving_RestrictResidual(rf, ii), G.restrict(m.levels, rf, ii)) <= 1e-13
         xc = rng.standard_normal(m.levels[ii - 1].numDOFs)
         assert _rel(s.Solving_InterpolationDeviation(xc, ii), G.interpolate(m.levels, xc, ii)) <= 1e-13
+
+
+def test_restrict_fp32(pair):
+    """The FP32 restriction of the inner V-cycle against the oracle's: FP32
+    input and sums of up to 27 taps, so 1e-6."""
+    m, s = pair
+    rng = np.random.default_rng(13)
+    for ii in range(2, m.numLevels + 1):
+        rf = rng.standard_normal(m.levels[ii - 2].numDOFs)
+        assert _rel(s.Solving_RestrictResidual(rf, ii, "mixed"), G.restrict(m.levels, rf, ii)) <= 1e-6
 
 
 def test_diag_and_stencils(pair):

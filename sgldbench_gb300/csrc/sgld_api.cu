@@ -1034,6 +1034,16 @@ int sgld_set_ke(sgld_ctx *ctx, const double *Ke) {
     memcpy(ctx->c.Ke, Ke, sizeof(double) * 576);
     memcpy(ctx->c.Kh, Kh, sizeof Kh);
     ctx->c.assembled = false;
+    // the captured solve graphs hold the FP32 K*u form chosen for the old matrix (kh_cubic)
+    Ctx &c = ctx->c;
+    if (c.solve_graph) {
+        cudaGraphExecDestroy(c.solve_graph);
+        c.solve_graph = nullptr;
+    }
+    if (c.inner_graph) {
+        cudaGraphExecDestroy(c.inner_graph);
+        c.inner_graph = nullptr;
+    }
     return setup_templates(ctx);
 }
 

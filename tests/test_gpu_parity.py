@@ -134,6 +134,34 @@ def test_kbyu_fp32_general_element_matrix(built_lib):
     s.close()
 
 
+def test_mixed_solve_after_element_matrix_change(built_lib):
+    """The captured solve graphs hold the FP32 K*u form chosen for the element
+    matrix they were built with (the 8-value form for the reference's
+    isotropic Ke).  After sgld_set_ke with a matrix without the cube's symmetry
+    a mixed solve runs the general form: it converges without the FP64
+    fallback, to the FP64 solve of the new system (displacement 1e-5)."""
+    from sgldbench_gb300 import VoxelSolver
+    from sgldbench_gb300 import domains as D
+
+    vox = D.cuboid(32, 16, 16)
+    s = VoxelSolver(vox, num_levels=3, non_dyadic=0, omega=0.6, pad=False)
+    F, fixed = D.cantilever3(vox, s.nodMapBack(1))
+    s.set_fixed_dofs(fixed)
+    s.set_modulus(np.random.default_rng(4).uniform(0.2, 1.0, s.numElements))
+    s.Solving_AssembleFEAstencil()
+    for prec in ("mixed", "mixed_df"):
+        _, info = s.pcg(F, tol=1e-6, maxIT=500, precision=prec)
+        assert info["converged"] and not info["fallback"], info
+    s.set_ke(_hadamard_to_ke(s.Ke, [([9, 20], 1.2), ([11, 16, 18], 0.9)]))
+    s.Solving_AssembleFEAstencil()
+    U64, _ = s.pcg(F, tol=1e-10, maxIT=2000, precision="fp64")
+    for prec in ("mixed", "mixed_df"):
+        U, info = s.pcg(F, tol=1e-6, maxIT=500, precision=prec)
+        assert info["converged"] and not info["fallback"], info
+        assert np.linalg.norm(U - U64) <= 1e-5 * np.linalg.norm(U64)
+    s.close()
+
+
 def test_restrict_interpolate(pair):
     m, s = pair
     rng = np.random.default_rng(2)

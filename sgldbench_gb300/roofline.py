@@ -45,16 +45,26 @@ def kbyu_f32_bytes(active_nodes: int, active_elements: int) -> int:
     return active_nodes * (3 * 4 * 2 + 1) + active_elements * 4
 
 
-def kbyu_f32_roofline(s, voxels=None, reps: int = 20, kind: str = "blobs") -> dict:
-    """Roofline record of k_kbyu_tma on solver s (assembled)."""
-    nn, ne = s.numNodes, s.numElements
+# The reference's K*u applies the dense 24 x 24 Ke to each element (576 multiply-adds,
+# src/MEXfuncs/Solving_KbyU_MatrixFree_mex.cpp:105-138) and scales by its modulus: 1152 + 24
+# flops per active element.  The FP32 CUDA-core peak is nominal: 152 SMs x 128 FP32 lanes x 2
+# flops per FMA at the maximum SM clock of 2070 MHz (no measured figure exists for it).
+KBYU_FLOPS_PER_ELEMENT = 1152 + 24
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12
+
+
+def kbyu_f32_record(nn: int, ne: int, ms: float, grid_nodes: int, reps: int, tile=None, kind: str = "blobs") -> dict:
+    """Roofline record of one k_kbyu_tma launch of `ms` milliseconds on nn active nodes and ne
+    active elements.  The binding roof reported is HBM (algorithmic bytes / time against the
+    measured copy bandwidth).  `fp32_dense_equivalent` adds the compute view: the reference
+    algorithm's flops for the same product / time against the nominal FP32 CUDA-core peak.  The
+    sum-factorised kernel executes about a fifth of those flops, so that fraction says how fast
+    the product is, not how busy the FP32 pipes are (ncu: FMA pipe active 46 % of cycles)."""
     alg = kbyu_f32_bytes(nn, ne)
-    ms = s.time_op("kbyu32", reps)
     p = peaks()
     achieved = alg / (ms * 1e-3) / 1e9
-    ry, rx, rz = s.resY, s.resX, s.resZ
-    grid_nodes = (ry + 1) * (rx + 1) * (rz + 1)
     per = DRAM_BYTES_PER_GRID_NODE.get(kind)
+    tflops = KBYU_FLOPS_PER_ELEMENT * ne / (ms * 1e-3) / 1e12
     return {"bound": "hbm", "achieved": achieved, "peak": p["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / p["hbm_gbs"], "traffic": None if per is None else per * grid_nodes,
             "kernel": "k_kbyu_tma (FP32 K*u of the inner CG)", "avg_launch_ms": ms,
@@ -63,4 +73,17 @@ def kbyu_f32_roofline(s, voxels=None, reps: int = 20, kind: str = "blobs") -> di
                              "graph", "algorithmic_bytes_per_launch": alg,
             "algorithmic_bytes": "active nodes x (3 x 4 B in + 3 x 4 B out + 1 B flags) + active elements x 4 B",
             "active_nodes": nn, "active_elements": ne, "grid_nodes": grid_nodes,
-            "peak_source": p["source"], "tile": s.kbyu_tile()}
+            "peak_source": p["source"], "tile": tile,
+            "fp32_dense_equivalent": {
+                "flops_per_element": KBYU_FLOPS_PER_ELEMENT, "achieved_tflops": tflops,
+                "peak_tflops": FP32_NOMINAL_TFLOPS, "frac": tflops / FP32_NOMINAL_TFLOPS,
+                "peak_source": "nominal (152 SMs x 128 FP32 lanes x 2 flops x 2070 MHz)",
+                "note": "flops of the reference's dense per-element product; the sum-factorised kernel "
+                        "executes about a fifth of them"}}
+
+
+def kbyu_f32_roofline(s, voxels=None, reps: int = 20, kind: str = "blobs") -> dict:
+    """Roofline record of k_kbyu_tma on solver s (assembled)."""
+    ms = s.time_op("kbyu32", reps)
+    grid_nodes = (s.resY + 1) * (s.resX + 1) * (s.resZ + 1)
+    return kbyu_f32_record(s.numNodes, s.numElements, ms, grid_nodes, reps, s.kbyu_tile(), kind)

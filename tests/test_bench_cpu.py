@@ -5,7 +5,9 @@ cores, no GPU) keeps the JSON-line contract, on a small grid.
   describing the run;
 * e2e equal to the line's value with no host<->device bytes;
 * the per-iteration split into K*u, V-cycle and the rest adds up;
-* under a launcher, ranks other than 0 print nothing and exit 0.
+* under a launcher, ranks other than 0 print nothing and exit 0;
+* the GPU arm's roofline record (bytes and the FP32 dense-equivalent view) is
+  consistent for a given launch time (a stand-in solver object, no GPU).
 """
 import json
 import os
@@ -43,3 +45,31 @@ def test_reference_arm_other_ranks_silent():
     out = _run({"RANK": "1", "WORLD_SIZE": "2"})
     assert out.returncode == 0, out.stderr[-2000:]
     assert out.stdout.strip() == ""
+
+
+def test_roofline_record_consistent():
+    sys.path.insert(0, ROOT)
+    from sgldbench_gb300 import roofline as R
+
+    class Stub:
+        numNodes, numElements = 77105356, 75736061
+        resY, resX, resZ = 512, 1024, 512
+
+        def time_op(self, op, reps):
+            assert op == "kbyu32" and reps == 20
+            return 1.19
+
+        def kbyu_tile(self):
+            return {"tile_x": 8, "z_chunk": 24}
+
+    rec = R.kbyu_f32_roofline(Stub(), reps=20)
+    assert rec["bound"] == "hbm" and rec["unit"] == "GB/s"
+    assert rec["algorithmic_bytes_per_launch"] == Stub.numNodes * 25 + Stub.numElements * 4
+    assert abs(rec["achieved"] - rec["algorithmic_bytes_per_launch"] / 1.19e-3 / 1e9) <= 1e-6 * rec["achieved"]
+    assert abs(rec["frac"] - rec["achieved"] / rec["peak"]) <= 1e-12
+    assert rec["grid_nodes"] == 513 * 1025 * 513 and rec["traffic"] > rec["algorithmic_bytes_per_launch"]
+    fp = rec["fp32_dense_equivalent"]
+    assert fp["flops_per_element"] == 1176
+    assert abs(fp["achieved_tflops"] - 1176 * Stub.numElements / 1.19e-3 / 1e12) <= 1e-9 * fp["achieved_tflops"]
+    assert abs(fp["peak_tflops"] - 80.54784) <= 1e-6 and 0 < fp["frac"] < 1.5
+    json.dumps(rec)

@@ -582,7 +582,7 @@ static int ensure_block_buffers(sgld_ctx *ctx, int nrhs);
 // ||b|| <= tol.  One that did not converge, met a non-finite residual or whose
 // true residual stays above tol after its residual replacements is not
 // trusted: the reference-form FP64 solve reruns from the same start and its
-// answer is returned (info->fallback = 1).  Plain FP64 MGPCG stays the judge.
+// answer is returned (info->fallback = 1).  Plain FP64 MGPCG stays the arbiter.
 bool mixed_failed(const sgld_solve_info &i, double tol) {
     return !i.converged || !std::isfinite(i.true_relres) || !std::isfinite(i.relres) || i.true_relres > tol;
 }

@@ -17,13 +17,23 @@ def dist_env() -> tuple[int, int, int]:
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def init(backend: str) -> None:
+def init(backend: str, timeout_s: float | None = None) -> None:
+    """Joins the process group.  A rank that dies or stops between steps must not
+    leave the others waiting forever in their next collective: the group's
+    timeout (`timeout_s`, else SGLD_PG_TIMEOUT_S, else 600 s) bounds every wait,
+    after which the waiting ranks' collective raises.  (A peer whose process has
+    exited usually ends the wait sooner: its connections close.)"""
+    import datetime
+
     import torch.distributed as dist
 
     os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
     rank, world, _ = dist_env()
     if world > 1 and not dist.is_initialized():
-        dist.init_process_group(backend, rank=rank, world_size=world)
+        if timeout_s is None:
+            timeout_s = float(os.environ.get("SGLD_PG_TIMEOUT_S", "600"))
+        dist.init_process_group(backend, rank=rank, world_size=world,
+                                timeout=datetime.timedelta(seconds=timeout_s))
 
 
 def barrier() -> None:
